@@ -1,0 +1,382 @@
+"""Benchmark of the DEM step: particle-steps/s at 1,048,576 polydisperse spheres.
+
+Workload: the settling box -- 1,048,576 spheres, radii lognormal (median
+5 mm, sigma 0.25) clipped to [2.5, 10] mm, random sequential addition in a
+walled 1 x 1 x 2 m box, linear spring-dashpot kn = 1e5, restitution 0.5,
+Coulomb mu = 0.3, gravity, dt = 5e-6 s, hash cell 2 x max radius (50 x 50 x
+100 cells), cell keys radix sorted every step.  Synthetic, seeded.
+
+One step = contact gather + integration, (cell key, slot) onesweep sort,
+reorder + cell_start.  Timings:
+
+  value      device time per step (CUDA events on the engine's stream, one
+             event pair per step, the L2 flushed by a 256 MB write before
+             every timed step), whole job over ranks;
+  e2e        the same steps through the public C ABI with host buffers:
+             per step, upload positions + velocities from pinned host memory
+             (sd_engine_set_state), step, read positions back
+             (sd_engine_get_state);
+  roofline   the dominant kernel (contact + integrate) timed alone on the
+             same stream, its algorithmic bytes / duration against the
+             measured HBM peak;
+  cpu_baseline  the CPU oracle (the restated step, OpenMP on the host cores)
+             on a bounded sample of the same scene.
+
+``--impl reference`` times the reference path on the host cores.  The
+reference has no CPU DEM path (its Device::CPU is never read), so this arm
+runs the CPU restatement of the step (oracle/) with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s @1M spheres"
+UNIT = "particle-steps/s"
+N_FULL = 1 << 20
+# algorithmic HBM bytes per sphere of one launch of the contact+integrate
+# kernel: read own position/velocity/spin (48), write next position/velocity/
+# spin (48) + cell key + slot (8); the cell_start table (250,001 words for
+# 1,048,576 spheres) adds ~1 B/sphere
+CONTACT_BYTES_PER_SPHERE = 48 + 48 + 8
+# algorithmic HBM bytes per sphere-step of the whole step (2 sort passes of
+# 18-bit keys):  contact 104 + histogram 4 + 2 x (8 read + 8 write) + reorder
+# (slot 4 + key 4 + gather 48 + write 48)
+STEP_BYTES_PER_SPHERE = 104 + 4 + 32 + 104
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_scene(n: int, seed: int):
+    from stardust_gb300 import scenes
+    box = (1.0, 1.0, 2.0) if n == N_FULL else scenes.scaled_box(n)
+    t0 = time.time()
+    pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=box, seed=seed)
+    log(f"scene: {n} spheres, volume fraction {phi:.4f}, generated in {time.time() - t0:.1f}s")
+    return pos, vel, cfg, dt, phi
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            d = json.loads(f.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def recorded_traffic():
+    """Per-launch DRAM bytes of the contact kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "roofline_traffic.json"
+    if f.exists():
+        try:
+            d = json.loads(f.read_text())
+            return d.get("contact_integrate_bytes_per_sphere")
+        except Exception:
+            return None
+    return None
+
+
+def cpu_oracle_rate(pos, vel, cfg, dt, seconds: float, threads: int | None):
+    """Oracle steps on the host cores until ~`seconds` of work: particle-steps/s."""
+    from oracle import oracle as orc
+    from stardust_gb300 import DEMEngine
+    # the engine's derived parameters (host-only, no GPU call)
+    eng = DEMEngine(cfg)
+    eng.add_spheres(pos, vel)
+    p = orc.params_from_engine(eng.params(), dt)
+    eng.close()
+    if threads:
+        orc.lib().sdo_set_num_threads(threads)
+    used = orc.lib().sdo_num_threads()
+    n = len(pos)
+    omg = orc.with_ids(np.zeros_like(pos), np.arange(n))
+    sp, sv, sw, _, cs = orc.prepare(p, pos, vel, omg)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        pn, vn, wn, keys, _, _, _ = orc.contact_integrate(p, sp, sv, sw, cs, record=False)
+        sp, sv, sw, _, cs = orc.sort_reorder(p, pn, vn, wn, keys)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return n * steps / el, used, steps, el
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    n = args.n
+    pos, vel, cfg, dt, phi = build_scene(n, args.seed)
+    from oracle import oracle as orc
+    from stardust_gb300 import DEMEngine
+    eng = DEMEngine(cfg)
+    eng.add_spheres(pos, vel)
+    p = orc.params_from_engine(eng.params(), dt)
+    eng.close()
+    used = orc.lib().sdo_num_threads()
+    omg = orc.with_ids(np.zeros_like(pos), np.arange(n))
+    sp, sv, sw, _, cs = orc.prepare(p, pos, vel, omg)
+    for _ in range(args.warmup):
+        pn, vn, wn, keys, _, _, _ = orc.contact_integrate(p, sp, sv, sw, cs, record=False)
+        sp, sv, sw, _, cs = orc.sort_reorder(p, pn, vn, wn, keys)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pn, vn, wn, keys, _, _, _ = orc.contact_integrate(p, sp, sv, sw, cs, record=False)
+        sp, sv, sw, _, cs = orc.sort_reorder(p, pn, vn, wn, keys)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s",
+                   "n_spheres": n, "volume_fraction": round(phi, 4), "l2": "n/a (host cores)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": f"{args.steps} full steps of the {n}-sphere scene, CPU restatement of the "
+                                   "step (the reference has no CPU DEM path), OpenMP on all host threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+    import stardust_gb300 as sd
+    from stardust_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl")
+    n = args.n
+    pos, vel, cfg, dt, phi = build_scene(n, args.seed + rank)
+    cfg.cuda_device = local
+    cfg.flags = 0
+    eng = sd.DEMEngine(cfg)
+    eng.add_spheres(pos, vel)
+    eng.prepare()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    # warm-up (graph capture happens on the first step)
+    eng.step(dt, args.warmup)
+    eng.sync()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-timed steps (value)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+            eng.step(dt, 1)
+            ends[k].record(stream)
+        barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    clocks = clk.summary()
+    eng.sync()
+    total_ms = sum(step_ms)
+    t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms * 1e-3)
+
+    # ---- dominant kernel alone: contact + integrate (idempotent stage)
+    kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage_ms = {}
+    for name, stage in (("contact_integrate", _abi.SD_STAGE_CONTACT), ("sort", _abi.SD_STAGE_SORT),
+                        ("reorder", _abi.SD_STAGE_REORDER)):
+        ms = []
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            kstarts[k].record(stream)
+            _abi.call("sd_engine_launch_stage", eng._h, stage, dt, h=eng._h)
+            kends[k].record(stream)
+        torch.cuda.synchronize()
+        ms = [s.elapsed_time(e) for s, e in zip(kstarts, kends)]
+        stage_ms[name] = sum(ms) / len(ms)
+    eng.sync()
+    contact_ms = stage_ms["contact_integrate"]
+    peak, peak_kind = measured_peak()
+    achieved = n * CONTACT_BYTES_PER_SPHERE / (contact_ms * 1e-3) / 1e9
+    traffic_ps = recorded_traffic()
+
+    # ---- end to end through the C ABI with host buffers
+    hpos = torch.from_numpy(eng.positions()).pin_memory()
+    hvel = torch.from_numpy(eng.velocities()).pin_memory()
+    hout = torch.empty_like(hpos).pin_memory()
+    import ctypes as C
+    lib = _abi.lib()
+    nbytes = hpos.numel() * 4
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _abi.check(lib.sd_engine_set_state(eng._h, _abi.SD_FIELD_POSITION, C.c_void_p(hpos.data_ptr()), nbytes),
+                   "set_state", eng._h)
+        _abi.check(lib.sd_engine_set_state(eng._h, _abi.SD_FIELD_VELOCITY, C.c_void_p(hvel.data_ptr()), nbytes),
+                   "set_state", eng._h)
+        _abi.check(lib.sd_engine_step(eng._h, dt, 1), "step", eng._h)
+        _abi.check(lib.sd_engine_get_state(eng._h, _abi.SD_FIELD_POSITION, C.c_void_p(hout.data_ptr()), nbytes),
+                   "get_state", eng._h)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e = world * n * args.steps / float(t.item())
+    st = eng.stats()
+    eng.close()
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        n_cpu = min(n, args.cpu_n)
+        if n_cpu == n:
+            cp, cv, ccfg, cdt = pos, vel, cfg, dt
+        else:
+            cp, cv, ccfg, cdt, _ = build_scene(n_cpu, args.seed)
+        rate, used, csteps, cel = cpu_oracle_rate(cp, cv, ccfg, cdt, args.cpu_seconds, None)
+        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"{csteps} steps of the {n_cpu}-sphere scene in {cel:.1f}s, CPU restatement of the step "
+                         f"(oracle/, OpenMP, {used} threads)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s",
+                       "n_spheres": n, "volume_fraction": round(phi, 4), "cells": st["n_cells"],
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": None if traffic_ps is None else traffic_ps * n,
+                         "algorithmic_bytes": CONTACT_BYTES_PER_SPHERE * n,
+                         "launch_ms": contact_ms},
+            "stages_ms": stage_ms,
+            "step_bytes_per_sphere": STEP_BYTES_PER_SPHERE,
+            "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": 5 * args.steps,
+            "contacts": st["contacts"],
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_FULL)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-n", type=int, default=N_FULL)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warm-up raised to 3 steps (timing rule)")
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

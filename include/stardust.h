@@ -1,0 +1,294 @@
+/*
+ * stardust.h -- C ABI of stardust-gb300, a GB300-native (sm_103a) DEM step.
+ *
+ * The reference engine (spacesuit825/stardust) exposes its per-step DEM path
+ * as C++ classes: STARDUST::DEMEngine (src/engine/engine.hpp:37-447) and the
+ * static operator class STARDUST::SpatialPartition
+ * (src/engine/cuda/collision_detection.cuh:30-66).  This header is the drop-in
+ * boundary for that path: plain C, opaque handles, pointers and sizes, int
+ * status codes instead of exit() (src/engine/cuda/cuda_utils.hpp:8-14).
+ *
+ * Conventions
+ *   - Every function returns an sd_status; 0 is success.  sd_last_error()
+ *     gives a message for the last failure on a handle (or globally for
+ *     handle-less calls when h is NULL).
+ *   - Ownership: an engine owns all device memory it allocates; raw operator
+ *     calls (sd_hash_*, sd_sort_*) use caller-owned device memory only.
+ *   - Threading: calls on one engine handle must be serialised.  Different
+ *     handles may be used from different host threads.  `stream` arguments
+ *     are cudaStream_t values passed as void* (NULL = legacy default stream).
+ *   - Layouts: float4 arrays are 16-byte aligned, 4 floats per element.
+ *     Sphere position = (x, y, z, radius); velocity = (vx, vy, vz, mass);
+ *     angular velocity = (wx, wy, wz, 0).
+ */
+#ifndef STARDUST_GB300_H
+#define STARDUST_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SD_ABI_VERSION 1
+
+typedef enum sd_status {
+    SD_OK = 0,
+    SD_ERR_INVALID_ARG = 1, /* bad pointer, size or option */
+    SD_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    SD_ERR_JSON = 3,        /* scene file unreadable or not the expected schema */
+    SD_ERR_CAPACITY = 4,    /* an output or pair buffer was too small */
+    SD_ERR_ITER_LIMIT = 5,  /* a bounded device wait or iteration gave up */
+    SD_ERR_STATE = 6,       /* call not valid in the engine's current state */
+    SD_ERR_IO = 7,          /* file read/write failed */
+    SD_ERR_NOMEM = 8,       /* host or device allocation failed */
+    SD_ERR_UNSUPPORTED = 9  /* feature not available in this build/config */
+} sd_status;
+
+/* Collision engine selector; mirrors STARDUST::CollisionEngine
+ * (src/engine/engine.hpp:21-24).  SD_ENGINE_SAP is accepted for source
+ * compatibility and runs the spatial-hash pipeline (the reference's SAP
+ * step is not a correct broad phase). */
+typedef enum sd_collision_engine {
+    SD_ENGINE_SAP = 0,
+    SD_ENGINE_SHP = 1 /* spatial hash */
+} sd_collision_engine;
+
+/* Mirrors STARDUST::Device (engine.hpp:26-29).  Only SD_DEVICE_GPU runs;
+ * the reference never implemented its CPU device either. */
+typedef enum sd_device { SD_DEVICE_CPU = 0, SD_DEVICE_GPU = 1 } sd_device;
+
+typedef struct sd_config {
+    uint32_t struct_size;     /* sizeof(sd_config), set by sd_config_default */
+    int32_t collision_engine; /* sd_collision_engine */
+    int32_t device;           /* sd_device */
+    int32_t cuda_device;      /* CUDA ordinal */
+    float domain;             /* reference m_domain (engine.hpp:43); used as the box edge
+                                 when box_hi is left at 0 */
+    float box_lo[3], box_hi[3];
+    int32_t walls;            /* bit 2*axis+side: wall on that face (0x3f = closed box) */
+    float cell;               /* hash cell edge; 0 = 2 * largest radius */
+    float kn;                 /* normal stiffness N/m */
+    float restitution;        /* normal restitution coefficient (0, 1] */
+    float mu;                 /* Coulomb friction coefficient */
+    float gravity[3];
+    uint64_t pair_capacity;   /* capacity of the contact-pair validation buffer */
+    uint32_t flags;           /* SD_FLAG_* */
+    uint32_t reserved;        /* must be 0 (keeps the struct free of padding) */
+} sd_config;
+
+/* Record per-sphere force/torque and the contact count at every step
+ * (needed for SD_FIELD_FORCE/TORQUE; costs 32 B per sphere-step). */
+#define SD_FLAG_RECORD 0x1u
+
+typedef struct sd_stats {
+    uint64_t n_spheres;
+    uint64_t steps;           /* steps taken since prepare */
+    uint64_t contacts;        /* particle-particle contacts at the last step (pairs) */
+    double kinetic_energy;    /* translational + rotational, J */
+    double momentum[3];
+    uint32_t device_errors;   /* OR of device error bits (see SD_DEVERR_*) */
+    uint32_t n_cells;
+} sd_stats;
+
+#define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
+#define SD_DEVERR_PAIR_OVERFLOW 0x2u
+#define SD_DEVERR_BAD_INPUT 0x4u
+
+typedef enum sd_field {
+    SD_FIELD_POSITION = 0, /* float4 (x, y, z, r) */
+    SD_FIELD_VELOCITY = 1, /* float4 (vx, vy, vz, m) */
+    SD_FIELD_OMEGA = 2,    /* float4 (wx, wy, wz, 0) */
+    SD_FIELD_FORCE = 3,    /* float4 contact + wall force of the last step (fx, fy, fz, 0) */
+    SD_FIELD_TORQUE = 4,   /* float4 contact torque of the last step */
+    SD_FIELD_IDS = 5       /* uint32 original sphere id of each sorted slot (device ptr only) */
+} sd_field;
+
+/* Derived step parameters (box, grid, contact-law constants).  Cell key of
+ * a position: ix = clamp(trunc((x - lo[0]) / cell), 0, nx-1) (same for y, z),
+ * key = (ix*ny + iy)*nz + iz.  Normal damping gamma_n = damp * sqrt(m_eff). */
+typedef struct sd_params {
+    float lo[3], hi[3];
+    float cell;
+    int32_t nx, ny, nz;
+    float kn, damp, mu;
+    float gravity[3];
+    float dt;        /* dt of the captured step graph (0 before the first step) */
+    int32_t walls;
+} sd_params;
+
+typedef struct sd_engine sd_engine;
+
+/* ------------------------------------------------------------ engine API */
+
+/* Fills the defaults: GPU, spatial hash, unit box with all walls, kn 1e5,
+ * restitution 0.5, mu 0.3, gravity (0, 0, -9.81). */
+sd_status sd_config_default(sd_config* cfg);
+
+/* DEMEngine(engineConfig, Scalar domain): engine.hpp:43-166. */
+sd_status sd_engine_create(const sd_config* cfg, sd_engine** out);
+/* ~DEMEngine: engine.hpp:192-296 (frees every device buffer). */
+sd_status sd_engine_destroy(sd_engine* h);
+/* Copies the last error message of h (or of handle-less calls when h is
+ * NULL) into buf; always NUL-terminates when len > 0. */
+sd_status sd_last_error(const sd_engine* h, char* buf, size_t len);
+
+/* Adds n free spheres.  pos4 = (x, y, z, r), vel4 = (vx, vy, vz, m) host
+ * arrays; omega4 may be NULL (zero spin).  Replaces the bulk of
+ * DEMEngine::add(DEMParticle) for one-sphere entities
+ * (engine.cpp:601-603, entity_handler.cpp:101-107). */
+sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4,
+                                const float* vel4, const float* omega4);
+
+/* DEMEngine::add(DEMParticle(id, grid_resolution, size, diameter, mass,
+ * position, velocity)) (entity.cpp:9-59, entity.hpp:24-32) for one-sphere
+ * entities (grid_resolution 1): a free sphere of radius diameter/2 and the
+ * given mass at `position`.  Multi-sphere entities return
+ * SD_ERR_UNSUPPORTED. */
+sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float size,
+                                 float diameter, float mass, const float position[3],
+                                 const float velocity[3]);
+
+/* DEMEngine::loadJSONSetup (engine.cpp:65-108, schema of
+ * setup/star_test.json): scene.domain, scene.gravity (magnitude, along -z),
+ * scene.entities[] of {type: "generic", position[3], size, mass,
+ * velocity[3]}; a generic entity becomes one sphere of diameter `size`.  Extension keys (all optional): scene.box {lo[3], hi[3]},
+ * scene.walls (int mask), scene.cell, scene.material {kn, restitution, mu},
+ * scene.spheres[] of {position[3], radius, mass, velocity[3]}.  Unknown keys
+ * are rejected with SD_ERR_JSON. */
+sd_status sd_engine_load_scene_json(sd_engine* h, const char* path);
+
+/* prep() + transfer(): engine.cpp:605-614.  Allocates device state, uploads
+ * it and sorts it into cell order. */
+sd_status sd_engine_prepare(sd_engine* h);
+
+/* Runs n_steps steps of length dt on the engine's stream (captured once as a
+ * CUDA graph).  Returns after enqueueing; use sd_engine_sync to wait. */
+sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps);
+/* DEMEngine::update(float dt): simulation_kernel.cu:52-153 -- one step. */
+sd_status sd_engine_update(sd_engine* h, float dt);
+
+/* Stages of one step, for profiling: launching CONTACT, SORT, REORDER in
+ * that order is one step.  CONTACT alone is idempotent (it reads the
+ * current state and writes the next-state buffers). */
+#define SD_STAGE_CONTACT 0
+#define SD_STAGE_SORT 1
+#define SD_STAGE_REORDER 2
+sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt);
+/* Waits for queued work and reports device error bits as SD_ERR_ITER_LIMIT /
+ * SD_ERR_CAPACITY. */
+sd_status sd_engine_sync(sd_engine* h);
+
+/* Copies a field in ORIGINAL sphere order (the order spheres were added)
+ * into host memory; bytes must be n_spheres * 16. */
+sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+/* Overwrites a field (POSITION, VELOCITY, OMEGA) from host memory in
+ * original sphere order.  The engine re-sorts before the next step. */
+sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src, size_t bytes);
+/* Device pointer of a field in current SORTED slot order (headless
+ * replacement of the GL VBO interop, engine.hpp:165-168). */
+sd_status sd_engine_device_ptr(sd_engine* h, int32_t field, void** out);
+/* The engine's CUDA stream (cudaStream_t as void*). */
+sd_status sd_engine_stream(sd_engine* h, void** out);
+
+/* Contact pairs of the current state: u64 (min_id << 32 | max_id), sorted
+ * ascending, original ids.  *n receives the total; SD_ERR_CAPACITY if it
+ * exceeds cap (the first cap are not guaranteed to be the smallest). */
+sd_status sd_engine_get_pairs(sd_engine* h, uint64_t* dst, uint64_t cap, uint64_t* n);
+
+sd_status sd_engine_stats(sd_engine* h, sd_stats* out);
+
+/* The step parameters derived from the config and the sphere set (valid
+ * before prepare once spheres are added). */
+sd_status sd_engine_params(sd_engine* h, sd_params* out);
+
+/* Binary snapshot of the engine state (config, step count, all sphere
+ * fields in sorted order).  Loading it into an engine created with the
+ * same config resumes bit-exactly. */
+sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path);
+sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
+
+/* --------------------------------------------------- raw operator API ---
+ * Device pointers, caller-owned memory, asynchronous on `stream`. */
+
+/* SpatialPartition::constructCollisionList (sh_collision_detection.cu:285-306,
+ * kernel :27-127): writes 9*n (cell, sphere) entries -- home entry, phantom
+ * entries, padding -- and the number of non-padding entries into *d_count
+ * (device u32, overwritten).  Bit-exact with the reference's rule,
+ * including its phantom-offset behaviour. */
+sd_status sd_hash_construct_collision_list(uint32_t n, float cell_dim, uint32_t* d_cells,
+                                           uint32_t* d_spheres, const float* d_sizes,
+                                           const float* d_pos4, uint32_t* d_count,
+                                           void* stream);
+
+/* Bytes of device scratch sd_sort_pairs / sd_hash_sort_collision_list need
+ * for n keys of key_bits bits. */
+sd_status sd_sort_scratch_bytes(uint64_t n, int32_t key_bits, uint64_t* bytes);
+
+/* Stable LSD radix sort of (key, value) u32 pairs by key bits
+ * [0, key_bits), onesweep style (one histogram pass + one pass per digit
+ * with decoupled look-back).  The sorted result is left in d_keys/d_vals;
+ * d_keys_tmp/d_vals_tmp are n-element ping-pong buffers.  The first 16
+ * bytes of scratch hold a status word (see sd_sort_status); the caller
+ * zeroes it once. */
+sd_status sd_sort_pairs(uint32_t* d_keys, uint32_t* d_vals, uint32_t* d_keys_tmp,
+                        uint32_t* d_vals_tmp, uint64_t n, int32_t key_bits, void* d_scratch,
+                        uint64_t scratch_bytes, void* stream);
+
+/* SpatialPartition::sortCollisionList (sh_collision_detection.cu:310-360):
+ * sorts the first n (cell, sphere) entries by the full 32-bit cell word,
+ * result back in d_cells/d_spheres, like the reference's four-pass
+ * ping-pong. */
+sd_status sd_hash_sort_collision_list(uint32_t* d_cells, uint32_t* d_spheres,
+                                      uint32_t* d_cells_tmp, uint32_t* d_spheres_tmp,
+                                      uint64_t n, void* d_scratch, uint64_t scratch_bytes,
+                                      void* stream);
+
+/* Reads the sort status word (synchronises the stream): *errors receives
+ * the device error bits accumulated since the caller last zeroed it. */
+sd_status sd_sort_status(const void* d_scratch, void* stream, uint32_t* errors);
+
+/* Candidate pairs of SpatialPartition::tranverseAndResolveCollisionList
+ * (collision_resolution.cu:100-199): over the first *d_count sorted
+ * entries, every home entry pairs with every later entry of its cell run;
+ * pairs within one rigid body (d_body_of, may be NULL) are skipped
+ * (collision_resolution.cu:69).  Writes (home, other) sphere ids in the
+ * reference's traversal order to d_pair_a/d_pair_b and the total into
+ * *d_npairs (device u64).  Pairs beyond cap are counted, not written. */
+sd_status sd_hash_candidate_pairs(const uint32_t* d_cells, const uint32_t* d_spheres,
+                                  const uint32_t* d_count, uint32_t n_entries,
+                                  const int32_t* d_body_of, uint32_t* d_pair_a,
+                                  uint32_t* d_pair_b, uint64_t cap, uint64_t* d_npairs,
+                                  void* d_scratch, uint64_t scratch_bytes, void* stream);
+
+/* Bytes of device scratch sd_hash_candidate_pairs needs for n_entries. */
+sd_status sd_hash_pairs_scratch_bytes(uint64_t n_entries, uint64_t* bytes);
+
+/* ------------------------------------------------------ scene generators
+ * Seeded, deterministic host-side scene builders (the reference builds its
+ * scenes in sandbox/testDEM.cpp:60-98 with unseeded rand()). */
+
+/* nx*ny*nz spheres on a cubic lattice of the given spacing starting at
+ * origin (first centre = origin), each coordinate jittered by
+ * U[-jitter, jitter]; velocities U[-vmax, vmax] per axis.  Writes pos4/vel4
+ * (n*4 floats each), sphere i = (ix*ny + iy)*nz + iz. */
+sd_status sd_scene_lattice(int32_t nx, int32_t ny, int32_t nz, float spacing, float jitter,
+                           const float origin[3], float radius, float mass, float vmax,
+                           uint64_t seed, float* pos4, float* vel4);
+
+/* Random sequential addition of n non-overlapping spheres in the box
+ * [lo, hi], radii lognormal(r_median, r_sigma) clipped to [r_min, r_max],
+ * inserted largest first; mass = density * 4/3 pi r^3; velocities
+ * U[-vmax, vmax].  Gives up with SD_ERR_CAPACITY after max_attempts
+ * placements attempts for one sphere.  *volume_fraction (may be NULL)
+ * receives the packed fraction. */
+sd_status sd_scene_rsa(uint64_t n, const float lo[3], const float hi[3], float r_median,
+                       float r_sigma, float r_min, float r_max, float density, float vmax,
+                       uint64_t seed, uint64_t max_attempts, float* pos4, float* vel4,
+                       double* volume_fraction);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STARDUST_GB300_H */

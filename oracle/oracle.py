@@ -1,0 +1,232 @@
+"""ctypes front end of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU legs, as the checker or as the timed CPU restatement.  The
+product library never loads it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_lib = None
+
+
+class Params(C.Structure):
+    """sdo_params (oracle/sd_oracle.h)."""
+    _fields_ = [
+        ("lo", C.c_float * 3), ("hi", C.c_float * 3), ("cell", C.c_float),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("kn", C.c_float), ("damp", C.c_float), ("mu", C.c_float),
+        ("g", C.c_float * 3), ("dt", C.c_float), ("walls", C.c_int32),
+    ]
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        from . import build as _build  # noqa: F401  (package-relative when imported as oracle.oracle)
+        path = HERE / "liboracle.so"
+        if not path.exists():
+            _build.build()
+        l = C.CDLL(str(path))
+        P = C.c_void_p
+        sig = {
+            "sdo_ref_hash_build": (C.c_uint32, [C.c_uint32, C.c_float, P, P, P, P]),
+            "sdo_radix_sort_pairs": (None, [P, P, C.c_uint32, C.c_int, P, P]),
+            "sdo_ref_candidate_pairs": (C.c_uint64, [P, P, C.c_uint32, P, P, P, C.c_uint64]),
+            "sdo_ref_resolve_forces": (None, [P, P, C.c_uint32, P, P, P, P]),
+            "sdo_ref_update_spheres": (None, [C.c_int, P, P, P, P, P, P, P, P, P]),
+            "sdo_ref_body_forces": (None, [C.c_int, P, P, P, P, P, P, P]),
+            "sdo_ref_advect": (None, [C.c_int, C.c_float, P, P, P, P, P, P, P, P, P, P]),
+            "sdo_cell_key": (C.c_uint32, [P, C.c_float, C.c_float, C.c_float]),
+            "sdo_cell_keys": (None, [P, C.c_uint32, P, P]),
+            "sdo_sort_reorder": (None, [P, C.c_uint32, P, P, P, P, P, P, P, P, P]),
+            "sdo_contact_integrate": (C.c_uint64, [P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]),
+            "sdo_contact_integrate_f64": (C.c_uint64, [P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]),
+            "sdo_contact_pairs": (C.c_uint64, [P, C.c_uint32, P, P, P, P, C.c_uint64]),
+            "sdo_run": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_int]),
+            "sdo_num_threads": (C.c_int, []),
+            "sdo_set_num_threads": (None, [C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+# ---------------------------------------------------------------- ref_compat
+def ref_hash_build(pos4: np.ndarray, sizes: np.ndarray, cell_dim: float):
+    n = len(pos4)
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    sizes = np.ascontiguousarray(sizes, np.float32)
+    cells = np.empty(9 * n, np.uint32)
+    spheres = np.empty(9 * n, np.uint32)
+    count = lib().sdo_ref_hash_build(n, cell_dim, _p(pos4), _p(sizes), _p(cells), _p(spheres))
+    return cells, spheres, int(count)
+
+
+def radix_sort_pairs(keys: np.ndarray, vals: np.ndarray, nbits: int = 32):
+    k = np.array(keys, np.uint32, copy=True)
+    v = np.array(vals, np.uint32, copy=True)
+    tk = np.empty_like(k)
+    tv = np.empty_like(v)
+    lib().sdo_radix_sort_pairs(_p(k), _p(v), len(k), nbits, _p(tk), _p(tv))
+    return k, v
+
+
+def ref_candidate_pairs(cells, spheres, count, body_of=None):
+    cells = np.ascontiguousarray(cells, np.uint32)
+    spheres = np.ascontiguousarray(spheres, np.uint32)
+    bo = None if body_of is None else np.ascontiguousarray(body_of, np.int32)
+    n = lib().sdo_ref_candidate_pairs(_p(cells), _p(spheres), count, _p(bo), None, None, 0)
+    a = np.empty(max(n, 1), np.uint32)
+    b = np.empty(max(n, 1), np.uint32)
+    lib().sdo_ref_candidate_pairs(_p(cells), _p(spheres), count, _p(bo), _p(a), _p(b), n)
+    return a[:n], b[:n]
+
+
+def ref_resolve_forces(cells, spheres, count, pos4, vel4, body_of=None):
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    vel4 = np.ascontiguousarray(vel4, np.float32)
+    f = np.zeros_like(pos4)
+    bo = None if body_of is None else np.ascontiguousarray(body_of, np.int32)
+    lib().sdo_ref_resolve_forces(_p(np.ascontiguousarray(cells, np.uint32)),
+                                 _p(np.ascontiguousarray(spheres, np.uint32)), count, _p(bo), _p(pos4),
+                                 _p(vel4), _p(f))
+    return f
+
+
+# ------------------------------------------------------------------- physics
+def params_from_engine(ep: dict, dt: float) -> Params:
+    """Oracle parameters equal to the engine's derived ones (sd_engine_params)."""
+    p = Params()
+    for a in range(3):
+        p.lo[a] = ep["lo"][a]
+        p.hi[a] = ep["hi"][a]
+        p.g[a] = ep["gravity"][a]
+    p.cell = ep["cell"]
+    p.nx, p.ny, p.nz = ep["dims"]
+    p.kn = ep["kn"]
+    p.damp = ep["damp"]
+    p.mu = ep["mu"]
+    p.dt = dt
+    p.walls = ep["walls"]
+    return p
+
+
+def make_params(lo, hi, cell, kn, damp, mu, g, dt, walls) -> Params:
+    p = Params()
+    for a in range(3):
+        p.lo[a] = lo[a]
+        p.hi[a] = hi[a]
+        p.g[a] = g[a]
+    p.cell = cell
+    dims = [max(1, int(np.ceil((np.float64(np.float32(hi[a])) - np.float64(np.float32(lo[a])))
+                               / np.float64(np.float32(cell))))) for a in range(3)]
+    p.nx, p.ny, p.nz = dims
+    p.kn = kn
+    p.damp = damp
+    p.mu = mu
+    p.dt = dt
+    p.walls = walls
+    return p
+
+
+def damp_from(kn: float, e: float) -> float:
+    le = np.log(np.float64(np.float32(e)))
+    beta = -le / np.sqrt(np.pi ** 2 + le * le)
+    return float(np.float32(2.0 * beta * np.sqrt(np.float64(np.float32(kn)))))
+
+
+def ncells(p: Params) -> int:
+    return p.nx * p.ny * p.nz
+
+
+def with_ids(omg: np.ndarray, ids: np.ndarray) -> np.ndarray:
+    o = np.array(omg, np.float32, copy=True)
+    o.view(np.uint32)[:, 3] = np.asarray(ids, np.uint32) & 0x7FFFFFFF
+    return o
+
+
+def ids_of(omg: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(omg, np.float32).view(np.uint32)[:, 3] & 0x7FFFFFFF
+
+
+def cell_keys(p: Params, pos4: np.ndarray) -> np.ndarray:
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    keys = np.empty(len(pos4), np.uint32)
+    lib().sdo_cell_keys(C.byref(p), len(pos4), _p(pos4), _p(keys))
+    return keys
+
+
+def sort_reorder(p: Params, pos_n, vel_n, omg_n, keys):
+    n = len(pos_n)
+    pos = np.empty((n, 4), np.float32)
+    vel = np.empty((n, 4), np.float32)
+    omg = np.empty((n, 4), np.float32)
+    ks = np.empty(n, np.uint32)
+    cs = np.empty(ncells(p) + 1, np.uint32)
+    lib().sdo_sort_reorder(C.byref(p), n, _p(np.ascontiguousarray(pos_n, np.float32)),
+                           _p(np.ascontiguousarray(vel_n, np.float32)), _p(np.ascontiguousarray(omg_n, np.float32)),
+                           _p(np.ascontiguousarray(keys, np.uint32)), _p(ks), _p(pos), _p(vel), _p(omg), _p(cs))
+    return pos, vel, omg, ks, cs
+
+
+def prepare(p: Params, pos4, vel4, omg4):
+    """Initial cell sort of a state given in insertion order (ids in omg.w)."""
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    return sort_reorder(p, pos4, vel4, omg4, cell_keys(p, pos4))
+
+
+def contact_integrate(p: Params, pos, vel, omg, cs, record=True, f64=False):
+    n = len(pos)
+    dt = np.float64 if f64 else np.float32
+    pos_n = np.empty((n, 4), dt)
+    vel_n = np.empty((n, 4), dt)
+    omg_n = np.empty((n, 4), dt)
+    keys = np.empty(n, np.uint32)
+    f = np.empty((n, 4), dt) if record else None
+    t = np.empty((n, 4), dt) if record else None
+    fn = lib().sdo_contact_integrate_f64 if f64 else lib().sdo_contact_integrate
+    c = fn(C.byref(p), n, _p(np.ascontiguousarray(pos, dt)), _p(np.ascontiguousarray(vel, dt)),
+           _p(np.ascontiguousarray(omg, dt)), _p(np.ascontiguousarray(cs, np.uint32)), _p(pos_n), _p(vel_n),
+           _p(omg_n), _p(keys), _p(f), _p(t))
+    return pos_n, vel_n, omg_n, keys, f, t, int(c)
+
+
+def contact_pairs(p: Params, pos, omg, cs, cap=1 << 22):
+    out = np.empty(cap, np.uint64)
+    n = lib().sdo_contact_pairs(C.byref(p), len(pos), _p(np.ascontiguousarray(pos, np.float32)),
+                                _p(np.ascontiguousarray(omg, np.float32)), _p(np.ascontiguousarray(cs, np.uint32)),
+                                _p(out), cap)
+    if n > cap:
+        raise RuntimeError("pair capacity")
+    return out[:n].copy()
+
+
+def run(p: Params, pos, vel, omg, steps: int, prepare_first: bool = True):
+    """sdo_run: returns the cell-sorted state after `steps` steps."""
+    pos = np.array(pos, np.float32, copy=True)
+    vel = np.array(vel, np.float32, copy=True)
+    omg = np.array(omg, np.float32, copy=True)
+    rc = lib().sdo_run(C.byref(p), len(pos), _p(pos), _p(vel), _p(omg), steps, 1 if prepare_first else 0)
+    if rc != 0:
+        raise RuntimeError("oracle run failed")
+    return pos, vel, omg
+
+
+def unsort(arr: np.ndarray, omg: np.ndarray) -> np.ndarray:
+    """Back to insertion order by the ids in omg.w."""
+    out = np.empty_like(arr)
+    out[ids_of(omg)] = arr
+    return out

@@ -1,0 +1,12 @@
+"""stardust-gb300: a GB300-native (sm_103a) DEM step behind a C ABI.
+
+The product is ``libstardust_gb300.so`` (C ABI: include/stardust.h).  This
+package builds it (``stardust_gb300.build``) and mirrors the reference's
+engine and operator classes over it (``stardust_gb300.engine``).
+"""
+from . import _abi
+from ._abi import SdError, lib
+from .engine import DEMEngine, EngineConfig, SpatialPartition, scene_lattice, scene_rsa
+
+__all__ = ["DEMEngine", "EngineConfig", "SpatialPartition", "SdError", "lib", "scene_lattice",
+           "scene_rsa", "_abi"]

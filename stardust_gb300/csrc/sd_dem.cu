@@ -1,0 +1,412 @@
+// sd_dem.cu -- the per-step DEM pipeline on a cell-sorted sphere state.
+//
+// One step is three stages (plus the sort between them):
+//
+//   contact_integrate   thread per sorted slot i: gather every sphere in the
+//                       3x3 columns of cells z-1..z+1 around i (each column a
+//                       contiguous slot range because keys are z-fastest),
+//                       accumulate spring-dashpot + Coulomb contact forces and
+//                       box-wall forces, integrate (symplectic Euler), write
+//                       the next state at slot i and its new cell key.  No
+//                       atomics: every pair is evaluated from both sides, so
+//                       the result does not depend on thread timing.
+//   sort                (key, slot) onesweep radix sort, sd_sort.cu
+//   reorder             gather the next state into sorted order and fill
+//                       cell_start (lower-bound of every cell, empty cells
+//                       included) block-cooperatively -- no memset needed.
+//
+// Replaces the reference's step (simulation_kernel.cu:52-153:
+// updateSphereData -> cleanBuffers -> broad phase -> reactCollisions ->
+// computeForcesAndTorques -> advect) for free spheres.  The reference's
+// force law (collision_resolution.cu:79-95: forces multiplied by velocity
+// signs, partner force assigned non-atomically) is replaced by the linear
+// spring-dashpot law with restitution damping and Coulomb friction, walls
+// and gravity.  The operation order here is the specification the CPU
+// oracle restates; the file is compiled with -fmad=false so nothing is
+// contracted.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sd_common.cuh"
+#include "sd_internal.h"
+
+namespace sd {
+
+constexpr uint32_t kIdMask = 0x7fffffffu;
+
+__device__ __forceinline__ int32_t axis_cell(float x, float lo, float cell, int32_t n) {
+    float t = (x - lo) / cell;
+    if (!(t >= 0.0f)) return 0;
+    if (t >= (float)n) return n - 1;
+    return (int32_t)t;
+}
+
+__device__ __forceinline__ uint32_t cell_key(const DemParams& p, float x, float y, float z) {
+    int32_t ix = axis_cell(x, p.lo[0], p.cell, p.nx);
+    int32_t iy = axis_cell(y, p.lo[1], p.cell, p.ny);
+    int32_t iz = axis_cell(z, p.lo[2], p.cell, p.nz);
+    return (uint32_t)((ix * p.ny + iy) * p.nz + iz);
+}
+
+// Linear spring-dashpot normal force with restitution damping
+// (gamma_n = damp * sqrt(m_eff), damp = 2*beta*sqrt(kn),
+// beta = -ln e / sqrt(pi^2 + ln^2 e)) -- not clipped at zero, so a binary
+// collision restores exactly the configured restitution -- and
+// viscous-regularised Coulomb friction |Ft| = min(mu*max(Fn,0), gamma_n*|vt|).  n points from the
+// partner to this sphere; (dv, ws) give the relative contact velocity
+// v_rel = dv - ws x n with ws = ri*wi + rj*wj.
+__device__ __forceinline__ void contact_response(const DemParams& p, float nx, float ny, float nz,
+                                                 float delta, float dvx, float dvy, float dvz,
+                                                 float wsx, float wsy, float wsz, float meff, float ri,
+                                                 float3& f, float3& t) {
+    float cx = wsy * nz - wsz * ny;
+    float cy = wsz * nx - wsx * nz;
+    float cz = wsx * ny - wsy * nx;
+    float vrx = dvx - cx, vry = dvy - cy, vrz = dvz - cz;
+    float vn = (vrx * nx + vry * ny) + vrz * nz;
+    float gn = p.damp * sqrtf(meff);
+    float fn = p.kn * delta - gn * vn;
+    const float fc = fn > 0.0f ? fn : 0.0f;
+    float vtx = vrx - vn * nx, vty = vry - vn * ny, vtz = vrz - vn * nz;
+    float vt2 = (vtx * vtx + vty * vty) + vtz * vtz;
+    f.x += fn * nx;
+    f.y += fn * ny;
+    f.z += fn * nz;
+    if (vt2 > 0.0f) {
+        float vt = sqrtf(vt2);
+        float ftm = fminf(p.mu * fc, gn * vt);
+        float s = ftm / vt;
+        float ftx = -(s * vtx), fty = -(s * vty), ftz = -(s * vtz);
+        f.x += ftx;
+        f.y += fty;
+        f.z += ftz;
+        float qx = ny * ftz - nz * fty;
+        float qy = nz * ftx - nx * ftz;
+        float qz = nx * fty - ny * ftx;
+        t.x -= ri * qx;
+        t.y -= ri * qy;
+        t.z -= ri * qz;
+    }
+}
+
+template <bool RECORD>
+__global__ void __launch_bounds__(256)
+dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                             const float4* __restrict__ vel, const float4* __restrict__ omg,
+                             const uint32_t* __restrict__ cell_start, float4* __restrict__ pos_n,
+                             float4* __restrict__ vel_n, float4* __restrict__ omg_n,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                             float4* __restrict__ force, float4* __restrict__ torque,
+                             uint32_t* __restrict__ status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t contacts = 0;
+    if (i < n) {
+        const float4 pi = pos[i], vi = vel[i], wi = omg[i];
+        const float ri = pi.w, mi = vi.w;
+        float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
+        const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
+        const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
+        const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
+        const int32_t z0 = cz > 0 ? cz - 1 : 0;
+        const int32_t z1 = cz + 1 < p.nz ? cz + 1 : p.nz - 1;
+        for (int32_t ddx = -1; ddx <= 1; ++ddx) {
+            const int32_t X = cx + ddx;
+            if (X < 0 || X >= p.nx) continue;
+            for (int32_t ddy = -1; ddy <= 1; ++ddy) {
+                const int32_t Y = cy + ddy;
+                if (Y < 0 || Y >= p.ny) continue;
+                const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+                const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
+                const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+                for (uint32_t s = s0; s < s1; ++s) {
+                    if (s == i) continue;
+                    const float4 pj = __ldg(&pos[s]);
+                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    const float d2 = (dx * dx + dy * dy) + dz * dz;
+                    const float rs = ri + pj.w;
+                    if (!(d2 < rs * rs) || d2 == 0.0f) continue;
+                    ++contacts;
+                    const float4 vj = __ldg(&vel[s]);
+                    const float4 wj = __ldg(&omg[s]);
+                    const float rj = pj.w, mj = vj.w;
+                    const float dist = sqrtf(d2);
+                    const float inv = 1.0f / dist;
+                    const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+                    const float wsx = ri * wi.x + rj * wj.x;
+                    const float wsy = ri * wi.y + rj * wj.y;
+                    const float wsz = ri * wi.z + rj * wj.z;
+                    const float meff = (mi * mj) / (mi + mj);
+                    contact_response(p, nx, ny, nz, rs - dist, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, wsx,
+                                     wsy, wsz, meff, ri, f, t);
+                }
+            }
+        }
+        if (p.walls) {
+            const float wsx = ri * wi.x, wsy = ri * wi.y, wsz = ri * wi.z;
+            const float xs[3] = {pi.x, pi.y, pi.z};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+#pragma unroll
+                for (int side = 0; side < 2; ++side) {
+                    if (!(p.walls & (1 << (2 * a + side)))) continue;
+                    const float gap = side == 0 ? xs[a] - p.lo[a] : p.hi[a] - xs[a];
+                    if (!(gap < ri)) continue;
+                    float nn[3] = {0.f, 0.f, 0.f};
+                    nn[a] = side == 0 ? 1.0f : -1.0f;
+                    contact_response(p, nn[0], nn[1], nn[2], ri - gap, vi.x, vi.y, vi.z, wsx, wsy, wsz, mi,
+                                     ri, f, t);
+                }
+            }
+        }
+        if (RECORD) {
+            force[i] = make_float4(f.x, f.y, f.z, 0.0f);
+            torque[i] = make_float4(t.x, t.y, t.z, 0.0f);
+        }
+        const float dt = p.dt;
+        const float nvx = vi.x + dt * (f.x / mi + p.g[0]);
+        const float nvy = vi.y + dt * (f.y / mi + p.g[1]);
+        const float nvz = vi.z + dt * (f.z / mi + p.g[2]);
+        const float nxp = pi.x + dt * nvx, nyp = pi.y + dt * nvy, nzp = pi.z + dt * nvz;
+        const float inertia = ((0.4f * mi) * ri) * ri;
+        pos_n[i] = make_float4(nxp, nyp, nzp, ri);
+        vel_n[i] = make_float4(nvx, nvy, nvz, mi);
+        omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia),
+                               wi.z + dt * (t.z / inertia), wi.w);
+        keys[i] = cell_key(p, nxp, nyp, nzp);
+        vals[i] = i;
+    }
+    if (RECORD) {
+        uint32_t v = contacts;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane_id() == 0 && v)
+            atomicAdd(reinterpret_cast<unsigned long long*>(status + 2), (unsigned long long)v);
+    }
+}
+
+__global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                                uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 q = pos[i];
+    keys[i] = cell_key(p, q.x, q.y, q.z);
+    vals[i] = i;
+}
+
+constexpr int kReorderThreads = 256;
+
+// Gather the next state into sorted order and write cell_start.  Block b
+// owns slots [b0, b1) and the cells (key[b0-1], key[b1-1]] (the first block
+// starts at cell 0, the last ends at ncells), so every cell's lower bound is
+// written exactly once, by binary search over the block's keys in shared
+// memory.
+__global__ void __launch_bounds__(kReorderThreads)
+dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
+                   const uint32_t* __restrict__ vals, const float4* __restrict__ pos_n,
+                   const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
+                   float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
+                   uint32_t* __restrict__ cell_start) {
+    __shared__ uint32_t s_keys[kReorderThreads + 1];
+    const uint32_t b0 = blockIdx.x * kReorderThreads;
+    const uint32_t b1 = min(b0 + kReorderThreads, n);
+    const uint32_t k = b0 + threadIdx.x;
+    if (k < n) {
+        const uint32_t src = vals[k];
+        if (src < n) {  // always true for a valid permutation
+            pos[k] = pos_n[src];
+            vel[k] = vel_n[src];
+            omg[k] = omg_n[src];
+        }
+        s_keys[threadIdx.x + 1] = keys[k];
+    }
+    if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
+    __syncthreads();
+    const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
+    const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
+    const uint32_t cnt = b1 - b0;
+    for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += kReorderThreads) {
+        uint32_t a = 0, z = cnt;  // first index in [0, cnt) with key >= c, else cnt
+        while (a < z) {
+            uint32_t m = (a + z) >> 1;
+            if ((int64_t)s_keys[m + 1] < c) a = m + 1;
+            else z = m;
+        }
+        cell_start[c] = b0 + a;
+    }
+}
+
+__global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                                 const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
+                                 unsigned long long* __restrict__ pairs, unsigned long long* __restrict__ npairs,
+                                 uint64_t cap, uint32_t* __restrict__ status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 pi = pos[i];
+    const uint32_t idi = __float_as_uint(omg[i].w) & kIdMask;
+    const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
+    const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
+    const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
+    const int32_t z0 = cz > 0 ? cz - 1 : 0;
+    const int32_t z1 = cz + 1 < p.nz ? cz + 1 : p.nz - 1;
+    for (int32_t ddx = -1; ddx <= 1; ++ddx) {
+        const int32_t X = cx + ddx;
+        if (X < 0 || X >= p.nx) continue;
+        for (int32_t ddy = -1; ddy <= 1; ++ddy) {
+            const int32_t Y = cy + ddy;
+            if (Y < 0 || Y >= p.ny) continue;
+            const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+            const uint32_t s1 = min(cell_start[col + (uint32_t)z1 + 1], n);
+            for (uint32_t s = cell_start[col + (uint32_t)z0]; s < s1; ++s) {
+                if (s == i) continue;
+                const float4 pj = pos[s];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float d2 = (dx * dx + dy * dy) + dz * dz;
+                const float rs = pi.w + pj.w;
+                if (!(d2 < rs * rs) || d2 == 0.0f) continue;
+                const uint32_t idj = __float_as_uint(omg[s].w) & kIdMask;
+                if (idi < idj) {
+                    unsigned long long slot = atomicAdd(npairs, 1ull);
+                    if (slot < cap) pairs[slot] = ((unsigned long long)idi << 32) | idj;
+                    else atomicOr(status, kErrPairOverflow);
+                }
+            }
+        }
+    }
+}
+
+// dst[id] = src[slot]: back to the order spheres were added.
+__global__ void dem_unsort_kernel(const float4* __restrict__ src, const float4* __restrict__ omg,
+                                  float4* __restrict__ dst, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t id = __float_as_uint(omg[i].w) & kIdMask;
+    if (id < n) dst[id] = src[i];
+}
+
+// dst[slot] = src_by_id[id], keeping the w lane of dst when keep_w (the id
+// lane of the omega array).
+__global__ void dem_scatter_in_kernel(const float4* __restrict__ src, const float4* __restrict__ omg,
+                                      float4* __restrict__ dst, uint32_t n, bool keep_w) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t id = __float_as_uint(omg[i].w) & kIdMask;
+    if (id >= n) return;
+    float4 v = src[id];
+    if (keep_w) v.w = dst[i].w;
+    dst[i] = v;
+}
+
+// Kinetic energy (translational + rotational, solid spheres) and linear
+// momentum, accumulated in double.
+__global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                  const float4* __restrict__ omg, double* __restrict__ out) {
+    double e = 0, px = 0, py = 0, pz = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i], w = omg[i], q = pos[i];
+        double m = v.w, r = q.w;
+        double I = 0.4 * m * r * r;
+        e += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z) +
+             0.5 * I * ((double)w.x * w.x + (double)w.y * w.y + (double)w.z * w.z);
+        px += m * v.x;
+        py += m * v.y;
+        pz += m * v.z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e += __shfl_down_sync(0xffffffffu, e, o);
+        px += __shfl_down_sync(0xffffffffu, px, o);
+        py += __shfl_down_sync(0xffffffffu, py, o);
+        pz += __shfl_down_sync(0xffffffffu, pz, o);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&out[0], e);
+        atomicAdd(&out[1], px);
+        atomicAdd(&out[2], py);
+        atomicAdd(&out[3], pz);
+    }
+}
+
+static inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1) / threads; }
+
+cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    dem_keys_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos_n, b.keys, b.vals);
+    return cudaGetLastError();
+}
+
+int dem_key_bits(uint32_t ncells) {
+    int bits = 1;
+    while (bits < 32 && (1ull << bits) < (unsigned long long)ncells) ++bits;
+    return bits;
+}
+
+cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
+    b.sorted_in_tmp = false;
+    if (b.n == 0) return cudaSuccess;
+    return sort_pairs_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, dem_key_bits(b.ncells), b.sort_scratch,
+                            st, &b.sorted_in_tmp);
+}
+
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
+    if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
+    const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
+    const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
+    dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
+        b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
+    (void)p;
+    cudaError_t e = dem_sort_async(b, st);
+    if (e != cudaSuccess) return e;
+    return dem_reorder_async(b, st);
+}
+
+cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    if (record) {
+        cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+        dem_contact_integrate_kernel<true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.force,
+            b.torque, b.dev_status);
+    } else {
+        dem_contact_integrate_kernel<false><<<grid_for(b.n, 256), 256, 0, st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, nullptr,
+            nullptr, b.dev_status);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(b.npairs, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess || b.n == 0) return e;
+    dem_pairs_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.omg, b.cell_start, b.pairs, b.npairs,
+                                                         b.pair_cap, b.dev_status);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dem_unsort_kernel<<<grid_for(n, 256), 256, 0, st>>>(src, omg, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_scatter_in_async(const float4* src_by_id, const float4* omg, float4* dst, uint32_t n, bool keep_w,
+                                 cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dem_scatter_in_kernel<<<grid_for(n, 256), 256, 0, st>>>(src_by_id, omg, dst, n, keep_w);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_energy_async(const DemBuffers& b, double* d_out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(d_out, 0, 4 * sizeof(double), st);
+    if (e != cudaSuccess || b.n == 0) return e;
+    unsigned g = grid_for(b.n, 256);
+    if (g > 152 * 4) g = 152 * 4;
+    dem_energy_kernel<<<g, 256, 0, st>>>(b.n, b.pos, b.vel, b.omg, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace sd

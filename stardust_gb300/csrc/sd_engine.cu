@@ -1,0 +1,959 @@
+// sd_engine.cu -- host side of stardust-gb300: the C ABI of include/stardust.h.
+//
+// The engine replaces STARDUST::DEMEngine + EntityHandler
+// (src/engine/engine.hpp:37-447, src/engine/entities/entity_handler.cpp) for
+// the per-step DEM path.  Design differences from the reference, each for a
+// GB300 reason:
+//   * one structure-of-float4 sphere state kept in cell-sorted order on the
+//     device (x,y,z,r | vx,vy,vz,m | wx,wy,wz,id) and re-sorted every step,
+//     instead of ~30 separately cudaMalloc'd SoA arrays (engine.cpp:243-599);
+//   * the whole step is captured once as a CUDA graph and replayed, instead
+//     of a host loop of launches with a device-wide sync (simulation_kernel.cu:31);
+//   * errors are status codes plus a per-handle message, not exit();
+//   * all device memory is owned by the handle and freed by sd_engine_destroy.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/stardust.h"
+#include "sd_internal.h"
+#include "sd_json.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct CudaBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sd_engine {
+    sd_config cfg{};
+    std::string err;
+
+    // host sphere set in insertion order; omega.w carries the id bits
+    std::vector<float4> h_pos, h_vel, h_omg;
+
+    bool prepared = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    sd::DemParams P{};
+    sd::DemBuffers B{};
+    std::vector<void*> allocations;
+    double* d_energy = nullptr;
+    float4* d_tmp = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.0f;
+    bool graph_valid = false;
+    uint64_t steps = 0;
+    bool need_resort = false;
+};
+
+namespace {
+
+sd_status fail(sd_engine* h, sd_status code, const std::string& msg) {
+    if (h) h->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+sd_status cuda_fail(sd_engine* h, cudaError_t e, const char* where) {
+    return fail(h, SD_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define SD_CUDA(h, call)                                          \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_fail((h), _e, #call);  \
+    } while (0)
+
+inline float4 f4(const float* p) { return make_float4(p[0], p[1], p[2], p[3]); }
+
+uint32_t id_bits(uint32_t id) { return id & 0x7fffffffu; }
+
+float id_as_float(uint32_t id) {
+    float f;
+    uint32_t b = id_bits(id);
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// damping coefficient prefactor: gamma_n = damp * sqrt(m_eff) with
+// damp = 2 * beta * sqrt(kn), beta = -ln(e) / sqrt(pi^2 + ln^2(e))
+float damp_from(float kn, float e) {
+    double le = std::log((double)e);
+    double beta = -le / std::sqrt(M_PI * M_PI + le * le);
+    return (float)(2.0 * beta * std::sqrt((double)kn));
+}
+
+template <typename T>
+sd_status dev_alloc(sd_engine* h, T** p, size_t count) {
+    void* q = nullptr;
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(h, SD_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    h->allocations.push_back(q);
+    *p = static_cast<T*>(q);
+    return SD_OK;
+}
+
+void release_device(sd_engine* h) {
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    h->graph_valid = false;
+    for (void* p : h->allocations) cudaFree(p);
+    h->allocations.clear();
+    h->B = sd::DemBuffers{};
+    h->d_energy = nullptr;
+    h->d_tmp = nullptr;
+    if (h->stream) cudaStreamDestroy(h->stream);
+    h->stream = nullptr;
+    h->prepared = false;
+}
+
+sd_status derive_params(sd_engine* h) {
+    const sd_config& c = h->cfg;
+    sd::DemParams& P = h->P;
+    bool box_given = c.box_hi[0] != 0.f || c.box_hi[1] != 0.f || c.box_hi[2] != 0.f;
+    for (int a = 0; a < 3; ++a) {
+        P.lo[a] = box_given ? c.box_lo[a] : 0.0f;
+        P.hi[a] = box_given ? c.box_hi[a] : c.domain;
+        if (!(P.hi[a] > P.lo[a])) return fail(h, SD_ERR_INVALID_ARG, "box: hi must exceed lo on every axis");
+    }
+    float rmax = 0.0f;
+    for (auto& p : h->h_pos) rmax = std::max(rmax, p.w);
+    float cell = c.cell > 0.0f ? c.cell : 2.0f * rmax;
+    if (!(cell > 0.0f)) cell = (P.hi[0] - P.lo[0]);
+    // a sphere must fit within the 3x3x3 cell neighbourhood: every contact
+    // partner is then found in the adjacent cells
+    if (cell < 2.0f * rmax) return fail(h, SD_ERR_INVALID_ARG, "cell must be >= 2 * largest radius");
+    P.cell = cell;
+    uint64_t ncells = 1;
+    int32_t* dims[3] = {&P.nx, &P.ny, &P.nz};
+    for (int a = 0; a < 3; ++a) {
+        double nd = std::ceil(((double)P.hi[a] - (double)P.lo[a]) / (double)cell);
+        if (nd < 1) nd = 1;
+        if (nd > (1 << 20)) return fail(h, SD_ERR_INVALID_ARG, "grid too fine (> 2^20 cells per axis)");
+        *dims[a] = (int32_t)nd;
+        ncells *= (uint64_t)nd;
+    }
+    if (ncells > (1ull << 30)) return fail(h, SD_ERR_INVALID_ARG, "grid has more than 2^30 cells");
+    if (!(c.restitution > 0.0f && c.restitution <= 1.0f))
+        return fail(h, SD_ERR_INVALID_ARG, "restitution must be in (0, 1]");
+    if (!(c.kn > 0.0f)) return fail(h, SD_ERR_INVALID_ARG, "kn must be > 0");
+    if (!(c.mu >= 0.0f)) return fail(h, SD_ERR_INVALID_ARG, "mu must be >= 0");
+    P.kn = c.kn;
+    P.damp = damp_from(c.kn, c.restitution);
+    P.mu = c.mu;
+    for (int a = 0; a < 3; ++a) P.g[a] = c.gravity[a];
+    P.walls = c.walls;
+    P.dt = 0.0f;
+    return SD_OK;
+}
+
+// Uploads `n` spheres (device order given by the host arrays) into the
+// next-state buffers and sorts them into cell order.
+sd_status upload_and_sort(sd_engine* h, const float4* pos, const float4* vel, const float4* omg, uint32_t n) {
+    sd::DemBuffers& B = h->B;
+    if (n) {
+        SD_CUDA(h, cudaMemcpyAsync(B.pos_n, pos, sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.vel_n, vel, sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.omg_n, omg, sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
+    }
+    SD_CUDA(h, sd::dem_keys_from_state_async(h->P, B, h->stream));
+    SD_CUDA(h, sd::dem_sort_reorder_async(h->P, B, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SD_OK;
+}
+
+sd_status allocate(sd_engine* h, uint32_t n) {
+    sd::DemBuffers& B = h->B;
+    B.n = n;
+    B.ncells = (uint32_t)((uint64_t)h->P.nx * h->P.ny * h->P.nz);
+    int bits = 1;
+    while (bits < 32 && (1ull << bits) < (unsigned long long)B.ncells) ++bits;
+    sd_status s;
+    if ((s = dev_alloc(h, &B.pos, n)) || (s = dev_alloc(h, &B.vel, n)) || (s = dev_alloc(h, &B.omg, n)) ||
+        (s = dev_alloc(h, &B.pos_n, n)) || (s = dev_alloc(h, &B.vel_n, n)) || (s = dev_alloc(h, &B.omg_n, n)) ||
+        (s = dev_alloc(h, &B.keys, n)) || (s = dev_alloc(h, &B.vals, n)) || (s = dev_alloc(h, &B.keys_tmp, n)) ||
+        (s = dev_alloc(h, &B.vals_tmp, n)) || (s = dev_alloc(h, &B.cell_start, (size_t)B.ncells + 1)) ||
+        (s = dev_alloc(h, &B.sort_scratch, sd::sort_scratch_words(n, bits))) ||
+        (s = dev_alloc(h, &B.dev_status, 8)) || (s = dev_alloc(h, &h->d_energy, 4)) ||
+        (s = dev_alloc(h, &h->d_tmp, n)))
+        return s;
+    if (h->cfg.flags & SD_FLAG_RECORD) {
+        if ((s = dev_alloc(h, &B.force, n)) || (s = dev_alloc(h, &B.torque, n))) return s;
+        SD_CUDA(h, cudaMemsetAsync(B.force, 0, sizeof(float4) * std::max<uint32_t>(n, 1), h->stream));
+        SD_CUDA(h, cudaMemsetAsync(B.torque, 0, sizeof(float4) * std::max<uint32_t>(n, 1), h->stream));
+    }
+    B.pair_cap = h->cfg.pair_capacity;
+    if ((s = dev_alloc(h, &B.pairs, (size_t)B.pair_cap)) || (s = dev_alloc(h, &B.npairs, 1))) return s;
+    SD_CUDA(h, cudaMemsetAsync(B.dev_status, 0, 8 * sizeof(uint32_t), h->stream));
+    SD_CUDA(h, cudaMemsetAsync(B.sort_scratch, 0, 16 * sizeof(uint32_t), h->stream));
+    return SD_OK;
+}
+
+sd_status prepare_with(sd_engine* h, const float4* pos, const float4* vel, const float4* omg, uint32_t n) {
+    sd_status s = derive_params(h);
+    if (s) return s;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(h, SD_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (h->device >= ndev) return fail(h, SD_ERR_INVALID_ARG, "cuda_device out of range");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    SD_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    if ((s = allocate(h, n))) {
+        release_device(h);
+        return s;
+    }
+    if ((s = upload_and_sort(h, pos, vel, omg, n))) {
+        release_device(h);
+        return s;
+    }
+    h->prepared = true;
+    h->steps = 0;
+    return SD_OK;
+}
+
+sd_status build_graph(sd_engine* h, float dt) {
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->P.dt = dt;
+    bool record = (h->cfg.flags & SD_FLAG_RECORD) != 0;
+    cudaGraph_t g = nullptr;
+    SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = sd::dem_contact_integrate_async(h->P, h->B, record, h->stream);
+    cudaError_t e2 = e1 == cudaSuccess ? sd::dem_sort_reorder_async(h->P, h->B, h->stream) : e1;
+    cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
+    if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
+    if (e3 != cudaSuccess) return cuda_fail(h, e3, "cudaStreamEndCapture");
+    cudaError_t e4 = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e4 != cudaSuccess) return cuda_fail(h, e4, "cudaGraphInstantiate");
+    h->graph_dt = dt;
+    h->graph_valid = true;
+    return SD_OK;
+}
+
+sd_status resort_if_needed(sd_engine* h) {
+    if (!h->need_resort) return SD_OK;
+    sd::DemBuffers& B = h->B;
+    if (B.n) {
+        SD_CUDA(h, cudaMemcpyAsync(B.pos_n, B.pos, sizeof(float4) * B.n, cudaMemcpyDeviceToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.vel_n, B.vel, sizeof(float4) * B.n, cudaMemcpyDeviceToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.omg_n, B.omg, sizeof(float4) * B.n, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    SD_CUDA(h, sd::dem_keys_from_state_async(h->P, B, h->stream));
+    SD_CUDA(h, sd::dem_sort_reorder_async(h->P, B, h->stream));
+    h->need_resort = false;
+    return SD_OK;
+}
+
+sd_status read_device_errors(sd_engine* h, uint32_t* bits) {
+    uint32_t a = 0, b = 0;
+    SD_CUDA(h, cudaMemcpyAsync(&a, h->B.dev_status, 4, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaMemcpyAsync(&b, h->B.sort_scratch, 4, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    *bits = a | b;
+    return SD_OK;
+}
+
+sd_status errors_to_status(sd_engine* h, uint32_t bits) {
+    if (bits & sd::kErrLookbackTimeout)
+        return fail(h, SD_ERR_ITER_LIMIT, "device: a decoupled look-back wait hit its spin limit");
+    if (bits & sd::kErrPairOverflow) return fail(h, SD_ERR_CAPACITY, "device: contact-pair buffer overflow");
+    return SD_OK;
+}
+
+// ------------------------------------------------------------ RNG + scenes
+struct SplitMix {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+    double u01() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+sd_status sd_config_default(sd_config* cfg) {
+    if (!cfg) return fail(nullptr, SD_ERR_INVALID_ARG, "cfg is NULL");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->struct_size = sizeof(sd_config);
+    cfg->collision_engine = SD_ENGINE_SHP;
+    cfg->device = SD_DEVICE_GPU;
+    cfg->cuda_device = 0;
+    cfg->domain = 1.0f;
+    cfg->walls = 0x3f;
+    cfg->cell = 0.0f;
+    cfg->kn = 1e5f;
+    cfg->restitution = 0.5f;
+    cfg->mu = 0.3f;
+    cfg->gravity[2] = -9.81f;
+    cfg->pair_capacity = 1u << 20;
+    cfg->flags = 0;
+    return SD_OK;
+}
+
+sd_status sd_engine_create(const sd_config* cfg, sd_engine** out) {
+    if (!cfg || !out) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL argument");
+    if (cfg->struct_size != sizeof(sd_config))
+        return fail(nullptr, SD_ERR_INVALID_ARG, "sd_config.struct_size mismatch (use sd_config_default)");
+    if (cfg->device != SD_DEVICE_GPU)
+        return fail(nullptr, SD_ERR_UNSUPPORTED, "only SD_DEVICE_GPU is implemented");
+    if (cfg->collision_engine != SD_ENGINE_SHP && cfg->collision_engine != SD_ENGINE_SAP)
+        return fail(nullptr, SD_ERR_INVALID_ARG, "unknown collision engine");
+    if (cfg->cuda_device < 0) return fail(nullptr, SD_ERR_INVALID_ARG, "cuda_device < 0");
+    sd_engine* h = new (std::nothrow) sd_engine();
+    if (!h) return fail(nullptr, SD_ERR_NOMEM, "out of host memory");
+    h->cfg = *cfg;
+    h->device = cfg->cuda_device;
+    *out = h;
+    return SD_OK;
+}
+
+sd_status sd_engine_destroy(sd_engine* h) {
+    if (!h) return SD_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release_device(h);
+    delete h;
+    return SD_OK;
+}
+
+sd_status sd_last_error(const sd_engine* h, char* buf, size_t len) {
+    if (!buf || len == 0) return SD_ERR_INVALID_ARG;
+    const std::string& m = h ? h->err : g_last_error;
+    size_t k = std::min(len - 1, m.size());
+    std::memcpy(buf, m.data(), k);
+    buf[k] = 0;
+    return SD_OK;
+}
+
+sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, const float* vel4,
+                                const float* omega4) {
+    if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "spheres cannot be added after prepare (reference: addEntityRuntime is a stub)");
+    if (n && (!pos4 || !vel4)) return fail(h, SD_ERR_INVALID_ARG, "pos4/vel4 NULL");
+    if (h->h_pos.size() + n >= 0x7fffffffull) return fail(h, SD_ERR_CAPACITY, "more than 2^31-1 spheres");
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* p = pos4 + 4 * i;
+        const float* v = vel4 + 4 * i;
+        if (!(p[3] > 0.0f) || !(v[3] > 0.0f) || !std::isfinite(p[0]) || !std::isfinite(p[1]) ||
+            !std::isfinite(p[2]) || !std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2]))
+            return fail(h, SD_ERR_INVALID_ARG, "sphere " + std::to_string(i) + ": radius and mass must be > 0 and values finite");
+    }
+    h->h_pos.reserve(h->h_pos.size() + n);
+    for (uint64_t i = 0; i < n; ++i) {
+        uint32_t id = (uint32_t)h->h_pos.size();
+        h->h_pos.push_back(f4(pos4 + 4 * i));
+        h->h_vel.push_back(f4(vel4 + 4 * i));
+        float4 w = omega4 ? f4(omega4 + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        w.w = id_as_float(id);
+        h->h_omg.push_back(w);
+    }
+    return SD_OK;
+}
+
+sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float size, float diameter, float mass,
+                                 const float position[3], const float velocity[3]) {
+    if (!h || !position || !velocity) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    (void)size;
+    if (grid_resolution != 1)
+        return fail(h, SD_ERR_UNSUPPORTED, "multi-sphere entities (grid_resolution > 1) are not supported by this engine");
+    float p[4] = {position[0], position[1], position[2], 0.5f * diameter};
+    float v[4] = {velocity[0], velocity[1], velocity[2], mass};
+    return sd_engine_add_spheres(h, 1, p, v, nullptr);
+}
+
+static bool json_vec3(const sd::JsonValue* v, float out[3]) {
+    if (!v || v->kind != sd::JsonValue::Array || v->arr.size() != 3) return false;
+    for (int k = 0; k < 3; ++k) {
+        if (v->arr[k].kind != sd::JsonValue::Number) return false;
+        out[k] = (float)v->arr[k].num;
+    }
+    return true;
+}
+
+static bool json_num(const sd::JsonValue* v, float* out) {
+    if (!v || v->kind != sd::JsonValue::Number) return false;
+    *out = (float)v->num;
+    return true;
+}
+
+static bool keys_subset(const sd::JsonValue& o, std::initializer_list<const char*> allowed, std::string* bad) {
+    for (auto& kv : o.obj) {
+        bool ok = false;
+        for (const char* a : allowed) ok = ok || kv.first == a;
+        if (!ok) {
+            *bad = kv.first;
+            return false;
+        }
+    }
+    return true;
+}
+
+sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
+    if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "scene must be loaded before prepare");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(h, SD_ERR_IO, std::string("cannot open ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string text = ss.str();
+    sd::JsonValue root;
+    std::string perr;
+    if (!sd::JsonParser(text).parse(&root, &perr)) return fail(h, SD_ERR_JSON, perr);
+    std::string bad;
+    if (root.kind != sd::JsonValue::Object) return fail(h, SD_ERR_JSON, "top level must be an object");
+    if (!keys_subset(root, {"scene"}, &bad)) return fail(h, SD_ERR_JSON, "unknown top-level key \"" + bad + "\"");
+    const sd::JsonValue* scene = root.get("scene");
+    if (!scene || scene->kind != sd::JsonValue::Object) return fail(h, SD_ERR_JSON, "missing object \"scene\"");
+    if (!keys_subset(*scene, {"domain", "entities", "gravity", "box", "walls", "cell", "material", "spheres"}, &bad))
+        return fail(h, SD_ERR_JSON, "unknown key scene." + bad);
+    sd_config c = h->cfg;
+    float tmp;
+    if (const sd::JsonValue* d = scene->get("domain")) {
+        if (!json_num(d, &tmp) || !(tmp > 0)) return fail(h, SD_ERR_JSON, "scene.domain must be a positive number");
+        c.domain = tmp;
+    }
+    if (const sd::JsonValue* g = scene->get("gravity")) {
+        if (!json_num(g, &tmp)) return fail(h, SD_ERR_JSON, "scene.gravity must be a number (magnitude along -z)");
+        c.gravity[0] = 0.f;
+        c.gravity[1] = 0.f;
+        c.gravity[2] = -tmp;
+    }
+    if (const sd::JsonValue* b = scene->get("box")) {
+        if (b->kind != sd::JsonValue::Object || !keys_subset(*b, {"lo", "hi"}, &bad) || !json_vec3(b->get("lo"), c.box_lo) ||
+            !json_vec3(b->get("hi"), c.box_hi))
+            return fail(h, SD_ERR_JSON, "scene.box must be {lo:[3], hi:[3]}");
+    }
+    if (const sd::JsonValue* w = scene->get("walls")) {
+        if (!json_num(w, &tmp) || tmp < 0 || tmp > 63 || tmp != std::floor(tmp))
+            return fail(h, SD_ERR_JSON, "scene.walls must be an integer mask 0..63");
+        c.walls = (int32_t)tmp;
+    }
+    if (const sd::JsonValue* ce = scene->get("cell")) {
+        if (!json_num(ce, &tmp) || !(tmp > 0)) return fail(h, SD_ERR_JSON, "scene.cell must be a positive number");
+        c.cell = tmp;
+    }
+    if (const sd::JsonValue* m = scene->get("material")) {
+        if (m->kind != sd::JsonValue::Object || !keys_subset(*m, {"kn", "restitution", "mu"}, &bad))
+            return fail(h, SD_ERR_JSON, "scene.material may hold kn, restitution, mu");
+        if (m->get("kn") && !json_num(m->get("kn"), &c.kn)) return fail(h, SD_ERR_JSON, "material.kn");
+        if (m->get("restitution") && !json_num(m->get("restitution"), &c.restitution))
+            return fail(h, SD_ERR_JSON, "material.restitution");
+        if (m->get("mu") && !json_num(m->get("mu"), &c.mu)) return fail(h, SD_ERR_JSON, "material.mu");
+    }
+    std::vector<float> pos, vel;
+    if (const sd::JsonValue* ents = scene->get("entities")) {
+        if (ents->kind != sd::JsonValue::Array) return fail(h, SD_ERR_JSON, "scene.entities must be an array");
+        for (size_t i = 0; i < ents->arr.size(); ++i) {
+            const sd::JsonValue& e = ents->arr[i];
+            std::string where = "scene.entities[" + std::to_string(i) + "]";
+            if (e.kind != sd::JsonValue::Object) return fail(h, SD_ERR_JSON, where + " must be an object");
+            if (!keys_subset(e, {"type", "position", "size", "mass", "velocity"}, &bad))
+                return fail(h, SD_ERR_JSON, "unknown key " + where + "." + bad);
+            const sd::JsonValue* t = e.get("type");
+            if (!t || t->kind != sd::JsonValue::String || t->str != "generic")
+                return fail(h, SD_ERR_JSON, where + ".type must be \"generic\"");
+            float p3[3], v3[3] = {0, 0, 0}, size, mass;
+            if (!json_vec3(e.get("position"), p3)) return fail(h, SD_ERR_JSON, where + ".position must be [x,y,z]");
+            if (e.get("velocity") && !json_vec3(e.get("velocity"), v3))
+                return fail(h, SD_ERR_JSON, where + ".velocity must be [vx,vy,vz]");
+            if (!json_num(e.get("size"), &size) || !(size > 0)) return fail(h, SD_ERR_JSON, where + ".size must be > 0");
+            if (!json_num(e.get("mass"), &mass) || !(mass > 0)) return fail(h, SD_ERR_JSON, where + ".mass must be > 0");
+            float p4[4] = {p3[0], p3[1], p3[2], 0.5f * size}, v4[4] = {v3[0], v3[1], v3[2], mass};
+            pos.insert(pos.end(), p4, p4 + 4);
+            vel.insert(vel.end(), v4, v4 + 4);
+        }
+    }
+    if (const sd::JsonValue* sph = scene->get("spheres")) {
+        if (sph->kind != sd::JsonValue::Array) return fail(h, SD_ERR_JSON, "scene.spheres must be an array");
+        for (size_t i = 0; i < sph->arr.size(); ++i) {
+            const sd::JsonValue& e = sph->arr[i];
+            std::string where = "scene.spheres[" + std::to_string(i) + "]";
+            if (e.kind != sd::JsonValue::Object || !keys_subset(e, {"position", "radius", "mass", "velocity"}, &bad))
+                return fail(h, SD_ERR_JSON, where + ": expected {position, radius, mass, velocity}");
+            float p3[3], v3[3] = {0, 0, 0}, r, m;
+            if (!json_vec3(e.get("position"), p3) || !json_num(e.get("radius"), &r) || !json_num(e.get("mass"), &m) ||
+                !(r > 0) || !(m > 0) || (e.get("velocity") && !json_vec3(e.get("velocity"), v3)))
+                return fail(h, SD_ERR_JSON, where + ": bad position/radius/mass/velocity");
+            float p4[4] = {p3[0], p3[1], p3[2], r}, v4[4] = {v3[0], v3[1], v3[2], m};
+            pos.insert(pos.end(), p4, p4 + 4);
+            vel.insert(vel.end(), v4, v4 + 4);
+        }
+    }
+    h->cfg = c;
+    return sd_engine_add_spheres(h, pos.size() / 4, pos.data(), vel.data(), nullptr);
+}
+
+sd_status sd_engine_prepare(sd_engine* h) {
+    if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "already prepared");
+    return prepare_with(h, h->h_pos.data(), h->h_vel.data(), h->h_omg.data(), (uint32_t)h->h_pos.size());
+}
+
+sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
+    if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(h, SD_ERR_INVALID_ARG, "dt must be positive and finite");
+    if (n_steps < 0) return fail(h, SD_ERR_INVALID_ARG, "n_steps < 0");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    if (!h->graph_valid || h->graph_dt != dt) {
+        if ((s = build_graph(h, dt))) return s;
+    }
+    for (int32_t i = 0; i < n_steps; ++i) SD_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+    h->steps += (uint64_t)n_steps;
+    return SD_OK;
+}
+
+sd_status sd_engine_update(sd_engine* h, float dt) { return sd_engine_step(h, dt, 1); }
+
+sd_status sd_engine_sync(sd_engine* h) {
+    if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (!h->prepared) return SD_OK;
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    uint32_t bits = 0;
+    sd_status s = read_device_errors(h, &bits);
+    if (s) return s;
+    return errors_to_status(h, bits);
+}
+
+static const float4* field_ptr(sd_engine* h, int32_t field) {
+    switch (field) {
+        case SD_FIELD_POSITION: return h->B.pos;
+        case SD_FIELD_VELOCITY: return h->B.vel;
+        case SD_FIELD_OMEGA: return h->B.omg;
+        case SD_FIELD_FORCE: return h->B.force;
+        case SD_FIELD_TORQUE: return h->B.torque;
+        default: return nullptr;
+    }
+}
+
+sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes) {
+    if (!h || !host_dst) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    uint32_t n = h->B.n;
+    if (bytes != (size_t)n * sizeof(float4)) return fail(h, SD_ERR_INVALID_ARG, "bytes must be n_spheres * 16");
+    if (field == SD_FIELD_IDS) return fail(h, SD_ERR_INVALID_ARG, "SD_FIELD_IDS is a device-pointer field");
+    if ((field == SD_FIELD_FORCE || field == SD_FIELD_TORQUE) && !(h->cfg.flags & SD_FLAG_RECORD))
+        return fail(h, SD_ERR_STATE, "force/torque need SD_FLAG_RECORD");
+    const float4* src = field_ptr(h, field);
+    if (!src) return fail(h, SD_ERR_INVALID_ARG, "unknown field");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    SD_CUDA(h, sd::dem_unsort_async(src, h->B.omg, h->d_tmp, n, h->stream));
+    SD_CUDA(h, cudaMemcpyAsync(host_dst, h->d_tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (field == SD_FIELD_OMEGA) {
+        float4* o = static_cast<float4*>(host_dst);
+        for (uint32_t i = 0; i < n; ++i) o[i].w = 0.0f;
+    }
+    return SD_OK;
+}
+
+sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src, size_t bytes) {
+    if (!h || !host_src) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    uint32_t n = h->B.n;
+    if (bytes != (size_t)n * sizeof(float4)) return fail(h, SD_ERR_INVALID_ARG, "bytes must be n_spheres * 16");
+    if (field != SD_FIELD_POSITION && field != SD_FIELD_VELOCITY && field != SD_FIELD_OMEGA)
+        return fail(h, SD_ERR_INVALID_ARG, "only POSITION, VELOCITY, OMEGA can be set");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    SD_CUDA(h, cudaMemcpyAsync(h->d_tmp, host_src, bytes, cudaMemcpyHostToDevice, h->stream));
+    float4* dst = const_cast<float4*>(field_ptr(h, field));
+    // the omega array's w lane holds the slot's sphere id: keep it
+    SD_CUDA(h, sd::dem_scatter_in_async(h->d_tmp, h->B.omg, dst, n, field == SD_FIELD_OMEGA, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    // only a position change can change cell keys
+    if (field == SD_FIELD_POSITION) h->need_resort = true;
+    return SD_OK;
+}
+
+sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
+    if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    switch (stage) {
+        case SD_STAGE_CONTACT: {
+            if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(h, SD_ERR_INVALID_ARG, "dt must be positive");
+            sd::DemParams p = h->P;
+            p.dt = dt;
+            SD_CUDA(h, sd::dem_contact_integrate_async(p, h->B, (h->cfg.flags & SD_FLAG_RECORD) != 0, h->stream));
+            return SD_OK;
+        }
+        case SD_STAGE_SORT: SD_CUDA(h, sd::dem_sort_async(h->B, h->stream)); return SD_OK;
+        case SD_STAGE_REORDER: SD_CUDA(h, sd::dem_reorder_async(h->B, h->stream)); return SD_OK;
+        default: return fail(h, SD_ERR_INVALID_ARG, "unknown stage");
+    }
+}
+
+sd_status sd_engine_device_ptr(sd_engine* h, int32_t field, void** out) {
+    if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (field == SD_FIELD_IDS) {
+        // ids live in the w lane of the omega array
+        *out = reinterpret_cast<char*>(h->B.omg) + 12;
+        return SD_OK;
+    }
+    const float4* p = field_ptr(h, field);
+    if (!p) return fail(h, SD_ERR_INVALID_ARG, "field not available");
+    *out = const_cast<float4*>(p);
+    return SD_OK;
+}
+
+sd_status sd_engine_stream(sd_engine* h, void** out) {
+    if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    *out = h->stream;
+    return SD_OK;
+}
+
+sd_status sd_engine_get_pairs(sd_engine* h, uint64_t* dst, uint64_t cap, uint64_t* n) {
+    if (!h || !n) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    SD_CUDA(h, sd::dem_pairs_async(h->P, h->B, h->stream));
+    unsigned long long total = 0;
+    SD_CUDA(h, cudaMemcpyAsync(&total, h->B.npairs, 8, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    *n = total;
+    if (total > h->B.pair_cap) {
+        uint32_t zero = 0;
+        SD_CUDA(h, cudaMemcpy(h->B.dev_status, &zero, 4, cudaMemcpyHostToDevice));
+        return fail(h, SD_ERR_CAPACITY, "engine pair_capacity too small for " + std::to_string(total) + " pairs");
+    }
+    if (total > cap) return fail(h, SD_ERR_CAPACITY, "dst too small for " + std::to_string(total) + " pairs");
+    if (total) {
+        if (!dst) return fail(h, SD_ERR_INVALID_ARG, "dst NULL");
+        SD_CUDA(h, cudaMemcpy(dst, h->B.pairs, total * 8, cudaMemcpyDeviceToHost));
+        std::sort(dst, dst + total);
+    }
+    return SD_OK;
+}
+
+sd_status sd_engine_params(sd_engine* h, sd_params* out) {
+    if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    sd_status s = derive_params(h);
+    if (s) return s;
+    static_assert(sizeof(sd_params) == sizeof(sd::DemParams), "sd_params mirrors DemParams");
+    std::memcpy(out, &h->P, sizeof(sd_params));
+    out->dt = h->graph_valid ? h->graph_dt : 0.0f;
+    return SD_OK;
+}
+
+sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
+    if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->n_spheres = h->prepared ? h->B.n : h->h_pos.size();
+    out->steps = h->steps;
+    if (!h->prepared) return SD_OK;
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    SD_CUDA(h, sd::dem_energy_async(h->B, h->d_energy, h->stream));
+    double e[4];
+    SD_CUDA(h, cudaMemcpyAsync(e, h->d_energy, sizeof e, cudaMemcpyDeviceToHost, h->stream));
+    // contacts of the current state (count of overlapping pairs)
+    SD_CUDA(h, sd::dem_pairs_async(h->P, h->B, h->stream));
+    unsigned long long np = 0;
+    SD_CUDA(h, cudaMemcpyAsync(&np, h->B.npairs, 8, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    out->kinetic_energy = e[0];
+    out->momentum[0] = e[1];
+    out->momentum[1] = e[2];
+    out->momentum[2] = e[3];
+    out->contacts = np;
+    out->n_cells = h->B.ncells;
+    uint32_t bits = 0;
+    if ((s = read_device_errors(h, &bits))) return s;
+    // a pair overflow from this stats pass is not an error of the run
+    if (np > h->B.pair_cap) {
+        bits &= ~sd::kErrPairOverflow;
+        uint32_t clear = bits;
+        SD_CUDA(h, cudaMemcpy(h->B.dev_status, &clear, 4, cudaMemcpyHostToDevice));
+    }
+    out->device_errors = bits;
+    return SD_OK;
+}
+
+static const char kCkptMagic[8] = {'S', 'D', 'G', 'B', 'C', 'K', 'P', '1'};
+
+sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
+    if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    SD_CUDA(h, cudaSetDevice(h->device));
+    sd_status s = resort_if_needed(h);
+    if (s) return s;
+    uint32_t n = h->B.n;
+    std::vector<float4> buf(3 * (size_t)n);
+    if (n) {
+        SD_CUDA(h, cudaMemcpyAsync(buf.data(), h->B.pos, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(buf.data() + n, h->B.vel, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(buf.data() + 2 * (size_t)n, h->B.omg, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    }
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(h, SD_ERR_IO, std::string("cannot write ") + path);
+    uint32_t ver = 1;
+    f.write(kCkptMagic, 8);
+    f.write(reinterpret_cast<const char*>(&ver), 4);
+    f.write(reinterpret_cast<const char*>(&n), 4);
+    f.write(reinterpret_cast<const char*>(&h->steps), 8);
+    f.write(reinterpret_cast<const char*>(&h->cfg), sizeof(sd_config));
+    f.write(reinterpret_cast<const char*>(&h->P), sizeof(sd::DemParams));
+    f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(float4)));
+    if (!f) return fail(h, SD_ERR_IO, "write failed");
+    return SD_OK;
+}
+
+sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
+    if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(h, SD_ERR_IO, std::string("cannot open ") + path);
+    char magic[8];
+    uint32_t ver = 0, n = 0;
+    uint64_t steps = 0;
+    sd_config cfg;
+    sd::DemParams P;
+    f.read(magic, 8);
+    f.read(reinterpret_cast<char*>(&ver), 4);
+    f.read(reinterpret_cast<char*>(&n), 4);
+    f.read(reinterpret_cast<char*>(&steps), 8);
+    f.read(reinterpret_cast<char*>(&cfg), sizeof cfg);
+    f.read(reinterpret_cast<char*>(&P), sizeof P);
+    if (!f || std::memcmp(magic, kCkptMagic, 8) != 0 || ver != 1)
+        return fail(h, SD_ERR_IO, "not a stardust-gb300 checkpoint");
+    std::vector<float4> buf(3 * (size_t)n);
+    f.read(reinterpret_cast<char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(float4)));
+    if (!f) return fail(h, SD_ERR_IO, "truncated checkpoint");
+    if (std::memcmp(&cfg, &h->cfg, sizeof cfg) != 0)
+        return fail(h, SD_ERR_STATE, "checkpoint was written by an engine with a different config");
+    release_device(h);
+    // host copy in original id order
+    h->h_pos.assign(n, float4{});
+    h->h_vel.assign(n, float4{});
+    h->h_omg.assign(n, float4{});
+    for (uint32_t s = 0; s < n; ++s) {
+        uint32_t id;
+        std::memcpy(&id, &buf[2 * (size_t)n + s].w, 4);
+        id &= 0x7fffffffu;
+        if (id >= n) return fail(h, SD_ERR_IO, "corrupt checkpoint ids");
+        h->h_pos[id] = buf[s];
+        h->h_vel[id] = buf[n + s];
+        h->h_omg[id] = buf[2 * (size_t)n + s];
+    }
+    // upload in the saved (sorted) slot order: a stable re-sort of a sorted
+    // state is the identity, so slot order -- and with it every summation
+    // order -- is exactly that of the run that wrote the checkpoint
+    sd_status s = prepare_with(h, buf.data(), buf.data() + n, buf.data() + 2 * (size_t)n, n);
+    if (s) return s;
+    if (std::memcmp(&P.cell, &h->P.cell, sizeof(float)) != 0)
+        return fail(h, SD_ERR_STATE, "checkpoint grid differs from the derived grid");
+    h->steps = steps;
+    return SD_OK;
+}
+
+// ------------------------------------------------------------- raw operators
+sd_status sd_hash_construct_collision_list(uint32_t n, float cell_dim, uint32_t* d_cells, uint32_t* d_spheres,
+                                           const float* d_sizes, const float* d_pos4, uint32_t* d_count,
+                                           void* stream) {
+    if (n && (!d_cells || !d_spheres || !d_sizes || !d_pos4)) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL pointer");
+    if (!d_count) return fail(nullptr, SD_ERR_INVALID_ARG, "d_count NULL");
+    if (n > 0x7fffffffu / 9) return fail(nullptr, SD_ERR_CAPACITY, "n too large for 9n entries");
+    if (!(cell_dim > 0.0f)) return fail(nullptr, SD_ERR_INVALID_ARG, "cell_dim must be > 0");
+    if (reinterpret_cast<uintptr_t>(d_pos4) & 15u) return fail(nullptr, SD_ERR_INVALID_ARG, "d_pos4 must be 16-byte aligned");
+    cudaError_t e = sd::ref_hash_build_async(n, cell_dim, d_cells, d_spheres, d_sizes,
+                                             reinterpret_cast<const float4*>(d_pos4), d_count,
+                                             static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "ref_hash_build");
+    return SD_OK;
+}
+
+sd_status sd_sort_scratch_bytes(uint64_t n, int32_t key_bits, uint64_t* bytes) {
+    if (!bytes) return fail(nullptr, SD_ERR_INVALID_ARG, "bytes NULL");
+    if (key_bits < 1 || key_bits > 32) return fail(nullptr, SD_ERR_INVALID_ARG, "key_bits must be 1..32");
+    if (n >= (1ull << 30)) return fail(nullptr, SD_ERR_CAPACITY, "n must be < 2^30");
+    *bytes = sd::sort_scratch_words(n, key_bits) * sizeof(uint32_t);
+    return SD_OK;
+}
+
+sd_status sd_sort_pairs(uint32_t* d_keys, uint32_t* d_vals, uint32_t* d_keys_tmp, uint32_t* d_vals_tmp, uint64_t n,
+                        int32_t key_bits, void* d_scratch, uint64_t scratch_bytes, void* stream) {
+    if (key_bits < 1 || key_bits > 32) return fail(nullptr, SD_ERR_INVALID_ARG, "key_bits must be 1..32");
+    if (n >= (1ull << 30)) return fail(nullptr, SD_ERR_CAPACITY, "n must be < 2^30");
+    if (n && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp || !d_scratch))
+        return fail(nullptr, SD_ERR_INVALID_ARG, "NULL pointer");
+    if (scratch_bytes < sd::sort_scratch_words(n, key_bits) * sizeof(uint32_t))
+        return fail(nullptr, SD_ERR_CAPACITY, "scratch smaller than sd_sort_scratch_bytes");
+    if (n == 0) return SD_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    bool in_tmp = false;
+    cudaError_t e = sd::sort_pairs_async(d_keys, d_vals, d_keys_tmp, d_vals_tmp, (uint32_t)n, key_bits,
+                                         static_cast<uint32_t*>(d_scratch), st, &in_tmp);
+    if (e == cudaSuccess && in_tmp) {
+        e = cudaMemcpyAsync(d_keys, d_keys_tmp, 4 * n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_vals, d_vals_tmp, 4 * n, cudaMemcpyDeviceToDevice, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "sort_pairs");
+    return SD_OK;
+}
+
+sd_status sd_hash_sort_collision_list(uint32_t* d_cells, uint32_t* d_spheres, uint32_t* d_cells_tmp,
+                                      uint32_t* d_spheres_tmp, uint64_t n, void* d_scratch, uint64_t scratch_bytes,
+                                      void* stream) {
+    return sd_sort_pairs(d_cells, d_spheres, d_cells_tmp, d_spheres_tmp, n, 32, d_scratch, scratch_bytes, stream);
+}
+
+sd_status sd_sort_status(const void* d_scratch, void* stream, uint32_t* errors) {
+    if (!d_scratch || !errors) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(errors, d_scratch, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "sort_status");
+    return SD_OK;
+}
+
+sd_status sd_hash_pairs_scratch_bytes(uint64_t n_entries, uint64_t* bytes) {
+    if (!bytes) return fail(nullptr, SD_ERR_INVALID_ARG, "bytes NULL");
+    *bytes = sd::ref_pairs_scratch_words(n_entries) * sizeof(uint32_t);
+    return SD_OK;
+}
+
+sd_status sd_hash_candidate_pairs(const uint32_t* d_cells, const uint32_t* d_spheres, const uint32_t* d_count,
+                                  uint32_t n_entries, const int32_t* d_body_of, uint32_t* d_pair_a,
+                                  uint32_t* d_pair_b, uint64_t cap, uint64_t* d_npairs, void* d_scratch,
+                                  uint64_t scratch_bytes, void* stream) {
+    if (!d_count || !d_npairs || !d_scratch) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL pointer");
+    if (n_entries && (!d_cells || !d_spheres)) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL pointer");
+    if (cap && (!d_pair_a || !d_pair_b)) return fail(nullptr, SD_ERR_INVALID_ARG, "pair buffers NULL");
+    if (reinterpret_cast<uintptr_t>(d_npairs) & 7u) return fail(nullptr, SD_ERR_INVALID_ARG, "d_npairs must be 8-byte aligned");
+    if (scratch_bytes < sd::ref_pairs_scratch_words(n_entries) * sizeof(uint32_t))
+        return fail(nullptr, SD_ERR_CAPACITY, "scratch smaller than sd_hash_pairs_scratch_bytes");
+    cudaError_t e = sd::ref_candidate_pairs_async(d_cells, d_spheres, d_count, n_entries, d_body_of, d_pair_a,
+                                                  d_pair_b, cap, reinterpret_cast<unsigned long long*>(d_npairs),
+                                                  static_cast<uint32_t*>(d_scratch), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "candidate_pairs");
+    return SD_OK;
+}
+
+// ------------------------------------------------------------ scene builders
+sd_status sd_scene_lattice(int32_t nx, int32_t ny, int32_t nz, float spacing, float jitter, const float origin[3],
+                           float radius, float mass, float vmax, uint64_t seed, float* pos4, float* vel4) {
+    if (nx < 0 || ny < 0 || nz < 0 || !origin || !pos4 || !vel4)
+        return fail(nullptr, SD_ERR_INVALID_ARG, "bad lattice arguments");
+    SplitMix rng{seed};
+    size_t i = 0;
+    for (int32_t x = 0; x < nx; ++x)
+        for (int32_t y = 0; y < ny; ++y)
+            for (int32_t z = 0; z < nz; ++z, ++i) {
+                int32_t idx[3] = {x, y, z};
+                for (int a = 0; a < 3; ++a) {
+                    double j = (2.0 * rng.u01() - 1.0) * jitter;
+                    pos4[4 * i + a] = (float)((double)origin[a] + (double)idx[a] * spacing + j);
+                }
+                pos4[4 * i + 3] = radius;
+                for (int a = 0; a < 3; ++a) vel4[4 * i + a] = (float)((2.0 * rng.u01() - 1.0) * vmax);
+                vel4[4 * i + 3] = mass;
+            }
+    return SD_OK;
+}
+
+sd_status sd_scene_rsa(uint64_t n, const float lo[3], const float hi[3], float r_median, float r_sigma, float r_min,
+                       float r_max, float density, float vmax, uint64_t seed, uint64_t max_attempts, float* pos4,
+                       float* vel4, double* volume_fraction) {
+    if (!lo || !hi || (n && (!pos4 || !vel4)) || !(r_min > 0) || !(r_max >= r_min) || !(density > 0))
+        return fail(nullptr, SD_ERR_INVALID_ARG, "bad RSA arguments");
+    for (int a = 0; a < 3; ++a)
+        if (!(hi[a] - lo[a] > 2 * r_max)) return fail(nullptr, SD_ERR_INVALID_ARG, "box smaller than a sphere");
+    SplitMix rng{seed};
+    std::vector<double> r(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        double u1 = rng.u01(), u2 = rng.u01();
+        double g = std::sqrt(-2.0 * std::log(u1 + 1e-300)) * std::cos(2.0 * M_PI * u2);
+        double x = (double)r_median * std::exp((double)r_sigma * g);
+        r[i] = std::min<double>(std::max<double>(x, r_min), r_max);
+    }
+    std::sort(r.begin(), r.end(), [](double a, double b) { return a > b; });
+    const double c = 2.0 * r_max;
+    int dims[3];
+    for (int a = 0; a < 3; ++a) dims[a] = std::max(1, (int)std::ceil((hi[a] - lo[a]) / c));
+    size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+    // cell-binned occupancy; a cell of edge 2*r_max holds few spheres
+    std::vector<std::vector<uint32_t>> bins(ncell);
+    std::vector<double> P(3 * n);
+    double vol = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        double ri = r[i];
+        bool placed = false;
+        for (uint64_t att = 0; att < max_attempts && !placed; ++att) {
+            double x[3];
+            for (int a = 0; a < 3; ++a) x[a] = lo[a] + ri + rng.u01() * ((double)hi[a] - lo[a] - 2 * ri);
+            int ci[3];
+            for (int a = 0; a < 3; ++a) ci[a] = std::min(dims[a] - 1, (int)((x[a] - lo[a]) / c));
+            bool clash = false;
+            for (int dx = -1; dx <= 1 && !clash; ++dx)
+                for (int dy = -1; dy <= 1 && !clash; ++dy)
+                    for (int dz = -1; dz <= 1 && !clash; ++dz) {
+                        int X = ci[0] + dx, Y = ci[1] + dy, Z = ci[2] + dz;
+                        if (X < 0 || Y < 0 || Z < 0 || X >= dims[0] || Y >= dims[1] || Z >= dims[2]) continue;
+                        for (uint32_t j : bins[((size_t)X * dims[1] + Y) * dims[2] + Z]) {
+                            double ex = x[0] - P[3 * j], ey = x[1] - P[3 * j + 1], ez = x[2] - P[3 * j + 2];
+                            double rr = ri + r[j];
+                            if (ex * ex + ey * ey + ez * ez < rr * rr) {
+                                clash = true;
+                                break;
+                            }
+                        }
+                    }
+            if (clash) continue;
+            for (int a = 0; a < 3; ++a) P[3 * i + a] = x[a];
+            bins[((size_t)ci[0] * dims[1] + ci[1]) * dims[2] + ci[2]].push_back((uint32_t)i);
+            placed = true;
+        }
+        if (!placed)
+            return fail(nullptr, SD_ERR_CAPACITY, "RSA could not place sphere " + std::to_string(i) + " within max_attempts");
+        double vi = 4.0 / 3.0 * M_PI * ri * ri * ri;
+        vol += vi;
+        for (int a = 0; a < 3; ++a) {
+            pos4[4 * i + a] = (float)P[3 * i + a];
+            vel4[4 * i + a] = (float)((2.0 * rng.u01() - 1.0) * vmax);
+        }
+        pos4[4 * i + 3] = (float)ri;
+        vel4[4 * i + 3] = (float)(density * vi);
+    }
+    if (volume_fraction)
+        *volume_fraction = vol / (((double)hi[0] - lo[0]) * ((double)hi[1] - lo[1]) * ((double)hi[2] - lo[2]));
+    return SD_OK;
+}
+
+}  // extern "C"

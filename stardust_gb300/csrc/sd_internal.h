@@ -1,0 +1,77 @@
+// sd_internal.h -- declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sd {
+
+// Device-side error word bits (read back by the host through sd_engine_stats
+// or the raw API's status word); equal to the public SD_DEVERR_* values.
+enum : uint32_t {
+    kErrLookbackTimeout = 1u << 0,  // a decoupled look-back spin hit its limit
+    kErrPairOverflow = 1u << 1,     // a pair buffer was too small
+    kErrBadInput = 1u << 2,         // non-finite or out-of-range input seen
+};
+
+// ---- radix sort (sd_sort.cu)
+uint64_t sort_scratch_words(uint64_t n, int key_bits);
+int sort_num_passes(int key_bits);
+cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                             uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
+                             bool* in_tmp);
+
+// ---- reference-compatible spatial hash (sd_hash_ref.cu)
+cudaError_t ref_hash_build_async(uint32_t n, float cell_dim, uint32_t* cells, uint32_t* spheres,
+                                 const float* sizes, const float4* pos, uint32_t* d_count,
+                                 cudaStream_t st);
+uint64_t ref_pairs_scratch_words(uint64_t n_entries);
+cudaError_t ref_candidate_pairs_async(const uint32_t* cells, const uint32_t* spheres,
+                                      const uint32_t* d_count, uint32_t n_entries,
+                                      const int32_t* body_of, uint32_t* pair_a, uint32_t* pair_b,
+                                      uint64_t cap, unsigned long long* d_npairs, uint32_t* scratch,
+                                      cudaStream_t st);
+
+// ---- physics pipeline (sd_dem.cu)
+struct DemParams {
+    float lo[3], hi[3];
+    float cell;
+    int32_t nx, ny, nz;
+    float kn, damp, mu;
+    float g[3];
+    float dt;
+    int32_t walls;
+};
+
+struct DemBuffers {
+    uint32_t n;
+    uint32_t ncells;
+    float4 *pos, *vel, *omg;        // current state, cell-sorted
+    float4 *pos_n, *vel_n, *omg_n;  // next state, slot order of the current
+    uint32_t *keys, *vals;          // sort keys / slot indices
+    uint32_t *keys_tmp, *vals_tmp;  // sort ping-pong
+    uint32_t* cell_start;           // ncells + 1
+    uint32_t* sort_scratch;
+    uint32_t* dev_status;           // [0] error bits, [1] contacts lo, [2] contacts hi
+    float4 *force, *torque;         // optional per-slot outputs (may be null)
+    unsigned long long* pairs;      // optional contact pairs (may be null)
+    unsigned long long* npairs;
+    uint64_t pair_cap;
+    bool sorted_in_tmp;             // set by dem_sort_async: result in the *_tmp buffers
+};
+
+int dem_key_bits(uint32_t ncells);
+cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
+cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
+cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
+cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record,
+                                        cudaStream_t st);
+cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
+cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n,
+                             cudaStream_t st);
+cudaError_t dem_scatter_in_async(const float4* src_by_id, const float4* omg, float4* dst, uint32_t n, bool keep_w,
+                                 cudaStream_t st);
+cudaError_t dem_energy_async(const DemBuffers& b, double* d_out, cudaStream_t st);
+
+}  // namespace sd

@@ -1,0 +1,309 @@
+// sd_sort.cu -- stable onesweep LSD radix sort of (u32 key, u32 value) pairs.
+//
+// Replaces the reference's three-kernel, 16-CTA radix sort
+// (RadixTabulateCUDA / RadixSumCUDA / RadixReorderCUDA,
+// src/engine/cuda/sh_collision_detection.cu:129-283, driven by
+// sortCollisionList :310-360).  Its intended semantics -- a stable LSD sort
+// of 32-bit cell words carrying 32-bit sphere words -- are kept; the
+// algorithm is the single-pass-per-digit "onesweep" scheme:
+//
+//   1. one histogram kernel reads every key once and builds the digit
+//      histograms of all passes (warp-aggregated shared atomics);
+//   2. per digit pass, one kernel: each CTA takes the next tile index from an
+//      atomic counter, ranks its keys per digit with __match_any_sync (stable
+//      within warp, warp-ordered across the tile), publishes its per-digit
+//      tile count, resolves its global digit offset by decoupled look-back
+//      over the predecessors' published counts, stages the tile in shared
+//      memory in digit order and writes it out in coalesced runs.
+//
+// Digits are up to 9 bits wide: a key range of `key_bits` bits takes
+// ceil(key_bits / 9) passes (18-bit cell keys: 2 passes; 32-bit: 4 of 8).
+// Look-back waits are bounded (kSpinLimit) and report through the status
+// word instead of hanging.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sd_common.cuh"
+#include "sd_internal.h"
+
+namespace sd {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / kWarp;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1;
+
+// Scratch layout (u32 words):
+//   [0]                 status word (error bits; never cleared by the sort)
+//   [4 .. 8)            per-pass tile counters
+//   [16 .. 16+4*512)    per-pass global digit histograms
+//   [kStatusOff ..)     per-pass tile status [pass][tile][512] (only the
+//                       pass's digit bins are used)
+constexpr uint64_t kHistOff = 16;
+constexpr uint64_t kStatusOff = kHistOff + 4 * 512;
+
+struct SortPlan {
+    int passes;
+    int shift[4];
+    int bits[4];
+};
+
+static SortPlan make_plan(int key_bits) {
+    SortPlan p{};
+    if (key_bits < 1) key_bits = 1;
+    if (key_bits > 32) key_bits = 32;
+    p.passes = (key_bits + 8) / 9;
+    int base = key_bits / p.passes, extra = key_bits % p.passes, sh = 0;
+    for (int i = 0; i < p.passes; ++i) {
+        p.bits[i] = base + (i < extra ? 1 : 0);
+        p.shift[i] = sh;
+        sh += p.bits[i];
+    }
+    return p;
+}
+
+template <int ITEMS>
+constexpr uint32_t tile_keys() { return kSortThreads * ITEMS; }
+
+// --------------------------------------------------------------- histogram
+__global__ void __launch_bounds__(kSortThreads)
+sort_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan plan,
+                      uint32_t* __restrict__ scratch) {
+    __shared__ uint32_t hist[4][512];
+    for (int i = threadIdx.x; i < 4 * 512; i += blockDim.x) (&hist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        uint32_t i = base + threadIdx.x;
+        bool valid = i < n;
+        uint32_t k = valid ? keys[i] : 0u;
+        uint32_t active = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            if (p >= plan.passes) break;
+            uint32_t d = (k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1u);
+            uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
+            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&hist[p][d], __popc(peers & active));
+        }
+    }
+    __syncthreads();
+    for (int p = 0; p < plan.passes; ++p) {
+        uint32_t nb = 1u << plan.bits[p];
+        for (uint32_t d = threadIdx.x; d < nb; d += blockDim.x)
+            if (hist[p][d]) atomicAdd(&scratch[kHistOff + p * 512 + d], hist[p][d]);
+    }
+}
+
+// ------------------------------------------------------------ onesweep pass
+// BINS: 256 or 512 digit bins (template so the 8-bit passes do half the
+// per-digit work).  ITEMS: keys per thread (tile = 256 * ITEMS keys).
+template <int BINS, int ITEMS>
+__global__ void __launch_bounds__(kSortThreads)
+sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                 uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+                 int shift, int bits, int pass, uint32_t num_tiles, uint32_t* __restrict__ scratch) {
+    constexpr int TILE = kSortThreads * ITEMS;
+    constexpr int DPT = BINS / kSortThreads;  // digits per thread (1 or 2)
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* s_keys = smem;                            // TILE
+    uint32_t* s_vals = s_keys + TILE;                   // TILE
+    uint32_t* s_whist = s_vals + TILE;                  // kSortWarps * BINS
+    uint32_t* s_tile_start = s_whist + kSortWarps * BINS;  // BINS
+    uint32_t* s_gbase = s_tile_start + BINS;            // BINS
+    uint32_t* s_ws = s_gbase + BINS;                    // 40 (scan scratch + tile id)
+
+    const uint32_t mask = (1u << bits) - 1u;
+    const int w = threadIdx.x / kWarp;
+    const uint32_t lane = lane_id();
+
+    if (threadIdx.x == 0) s_ws[36] = atomicAdd(&scratch[4 + pass], 1u);
+    for (int i = threadIdx.x; i < kSortWarps * BINS; i += kSortThreads) s_whist[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_ws[36];
+    const uint32_t tile_base = tile * TILE;
+
+    // load + warp-local stable ranking
+    uint32_t key[ITEMS], val[ITEMS], rank[ITEMS];
+    uint32_t* wh = s_whist + w * BINS;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = tile_base + w * (ITEMS * kWarp) + j * kWarp + lane;
+        bool valid = idx < n;
+        key[j] = valid ? keys_in[idx] : 0xffffffffu;
+        val[j] = valid ? vals_in[idx] : 0u;
+        uint32_t d = valid ? ((key[j] >> shift) & mask) : 0xffffffffu;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t before = __popc(peers & lanemask_lt());
+        uint32_t base = valid ? wh[d] : 0u;
+        __syncwarp();
+        if (valid && before == 0) wh[d] = base + __popc(peers);
+        __syncwarp();
+        rank[j] = base + before;
+    }
+    __syncthreads();
+
+    // per-digit warp offsets and tile counts
+    uint32_t cnt[DPT];
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        uint32_t d = threadIdx.x + q * kSortThreads, run = 0;
+#pragma unroll
+        for (int ww = 0; ww < kSortWarps; ++ww) {
+            uint32_t c = s_whist[ww * BINS + d];
+            s_whist[ww * BINS + d] = run;
+            run += c;
+        }
+        cnt[q] = run;
+    }
+    // publish this tile's aggregate before anything else so successors can
+    // make progress
+    uint32_t* status = scratch + kStatusOff + ((uint64_t)pass * num_tiles + tile) * 512;
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        uint32_t d = threadIdx.x + q * kSortThreads;
+        st_relaxed(&status[d], (tile == 0 ? kFlagInc : kFlagAgg) | cnt[q]);
+    }
+
+    // tile-local digit starts and global digit starts (exclusive scans over
+    // digits; digit d = threadIdx.x + q*256)
+    const uint32_t* ghist = scratch + kHistOff + pass * 512;
+    uint32_t carry_t = 0, carry_g = 0;
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        uint32_t d = threadIdx.x + q * kSortThreads;
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan(cnt[q], s_ws, &tot);
+        s_tile_start[d] = carry_t + ex;
+        carry_t += tot;
+        uint32_t gv = ghist[d];
+        uint32_t gex = block_exclusive_scan(gv, s_ws, &tot);
+        s_gbase[d] = carry_g + gex;
+        carry_g += tot;
+    }
+
+    // decoupled look-back, one digit per thread per q
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        uint32_t d = threadIdx.x + q * kSortThreads;
+        uint32_t excl = 0;
+        if (tile > 0) {
+            int64_t p = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (p >= 0) {
+                const uint32_t* ps = scratch + kStatusOff + ((uint64_t)pass * num_tiles + (uint64_t)p) * 512;
+                uint32_t v = ld_relaxed(&ps[d]);
+                if ((v & ~kCountMask) == 0u) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(&scratch[0], kErrLookbackTimeout);
+                        break;
+                    }
+                    if (spins > 64) __nanosleep(32);
+                    continue;
+                }
+                excl += v & kCountMask;
+                if (v & kFlagInc) break;
+                --p;
+            }
+            st_relaxed(&status[d], kFlagInc | ((excl + cnt[q]) & kCountMask));
+        }
+        s_gbase[d] += excl;
+    }
+    __syncthreads();
+
+    // stage the tile in digit order
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = tile_base + w * (ITEMS * kWarp) + j * kWarp + lane;
+        if (idx < n) {
+            uint32_t d = (key[j] >> shift) & mask;
+            uint32_t pos = s_tile_start[d] + s_whist[w * BINS + d] + rank[j];
+            s_keys[pos] = key[j];
+            s_vals[pos] = val[j];
+        }
+    }
+    __syncthreads();
+
+    // coalesced write-out: consecutive staged keys of one digit go to
+    // consecutive global positions
+    uint32_t valid_in_tile = n - tile_base < (uint32_t)TILE ? n - tile_base : (uint32_t)TILE;
+    for (uint32_t s = threadIdx.x; s < valid_in_tile; s += kSortThreads) {
+        uint32_t k = s_keys[s];
+        uint32_t d = (k >> shift) & mask;
+        uint32_t o = s_gbase[d] + (s - s_tile_start[d]);
+        // o < n whenever the histogram and look-back are consistent; the
+        // check keeps a timed-out look-back from writing out of bounds
+        if (o < n) {
+            keys_out[o] = k;
+            vals_out[o] = s_vals[s];
+        }
+    }
+}
+
+template <int BINS, int ITEMS>
+static size_t pass_smem_bytes() {
+    return sizeof(uint32_t) * (2 * (size_t)kSortThreads * ITEMS + (size_t)kSortWarps * BINS + 2 * BINS + 40);
+}
+
+constexpr int kSortItems = 8;
+
+uint64_t sort_scratch_words(uint64_t n, int key_bits) {
+    SortPlan p = make_plan(key_bits);
+    uint64_t tiles = (n + tile_keys<kSortItems>() - 1) / tile_keys<kSortItems>();
+    if (tiles == 0) tiles = 1;
+    return kStatusOff + (uint64_t)p.passes * tiles * 512;
+}
+
+template <int BINS, int ITEMS>
+static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t* ko, uint32_t* vo,
+                               uint32_t n, int shift, int bits, int pass, uint32_t tiles,
+                               uint32_t* scratch, cudaStream_t st) {
+    static bool configured = false;
+    size_t sm = pass_smem_bytes<BINS, ITEMS>();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel<BINS, ITEMS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    sort_pass_kernel<BINS, ITEMS><<<tiles, kSortThreads, sm, st>>>(ki, vi, ko, vo, n, shift, bits,
+                                                                   pass, tiles, scratch);
+    return cudaGetLastError();
+}
+
+// Sorts (keys, vals) by bits [0, key_bits).  Returns via *in_tmp whether
+// the result ended in the tmp buffers (odd pass count).
+cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                             uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
+                             bool* in_tmp) {
+    SortPlan plan = make_plan(key_bits);
+    *in_tmp = false;
+    if (n == 0) return cudaSuccess;
+    uint32_t tiles = (n + tile_keys<kSortItems>() - 1) / tile_keys<kSortItems>();
+    // clear counters, histograms and this sort's tile status (not the status word)
+    size_t clear_words = kStatusOff - 4 + (size_t)plan.passes * tiles * 512;
+    cudaError_t e = cudaMemsetAsync(scratch + 4, 0, clear_words * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    int hist_blocks = (int)((n + kSortThreads * 16 - 1) / (kSortThreads * 16));
+    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
+    if (hist_blocks < 1) hist_blocks = 1;
+    sort_histogram_kernel<<<hist_blocks, kSortThreads, 0, st>>>(keys, n, plan, scratch);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
+    for (int p = 0; p < plan.passes; ++p) {
+        if (plan.bits[p] <= 8)
+            e = launch_pass<256, kSortItems>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+        else
+            e = launch_pass<512, kSortItems>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+        if (e != cudaSuccess) return e;
+        uint32_t* t;
+        t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+    }
+    *in_tmp = (plan.passes & 1) != 0;
+    return cudaSuccess;
+}
+
+int sort_num_passes(int key_bits) { return make_plan(key_bits).passes; }
+
+}  // namespace sd

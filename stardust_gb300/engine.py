@@ -1,0 +1,286 @@
+"""Python mirror of the reference engine surface, over the C ABI.
+
+``DEMEngine`` follows STARDUST::DEMEngine (src/engine/engine.hpp:37-447):
+``add`` / ``prep`` / ``transfer`` / ``update(dt)`` keep their meaning;
+``add_spheres`` and ``step(dt, n)`` are the bulk forms.  ``SpatialPartition``
+follows the static operator class of the same name
+(src/engine/cuda/collision_detection.cuh:30-66) and works on CUDA tensors.
+Every call goes to libstardust_gb300.so; nothing runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import call, lib
+
+
+@dataclass
+class EngineConfig:
+    """sd_config: defaults are the 4,096-sphere box config's material."""
+    collision_engine: int = _abi.SD_ENGINE_SHP
+    device: int = _abi.SD_DEVICE_GPU
+    cuda_device: int = 0
+    domain: float = 1.0
+    box_lo: tuple = (0.0, 0.0, 0.0)
+    box_hi: tuple = (0.0, 0.0, 0.0)
+    walls: int = 0x3F
+    cell: float = 0.0
+    kn: float = 1e5
+    restitution: float = 0.5
+    mu: float = 0.3
+    gravity: tuple = (0.0, 0.0, -9.81)
+    pair_capacity: int = 1 << 20
+    flags: int = 0
+
+    def to_c(self) -> _abi.SdConfig:
+        c = _abi.SdConfig()
+        call("sd_config_default", C.byref(c))
+        c.collision_engine = self.collision_engine
+        c.device = self.device
+        c.cuda_device = self.cuda_device
+        c.domain = self.domain
+        for a in range(3):
+            c.box_lo[a] = self.box_lo[a]
+            c.box_hi[a] = self.box_hi[a]
+            c.gravity[a] = self.gravity[a]
+        c.walls = self.walls
+        c.cell = self.cell
+        c.kn = self.kn
+        c.restitution = self.restitution
+        c.mu = self.mu
+        c.pair_capacity = self.pair_capacity
+        c.flags = self.flags
+        return c
+
+
+def _f32(a, cols=4) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != cols:
+        raise ValueError(f"expected an (n, {cols}) float32 array, got {a.shape}")
+    return a
+
+
+class DEMEngine:
+    """Owning handle over one sd_engine."""
+
+    def __init__(self, config: EngineConfig | None = None):
+        self.config = config or EngineConfig()
+        self._c = self.config.to_c()
+        h = C.c_void_p()
+        call("sd_engine_create", C.byref(self._c), C.byref(h))
+        self._h = h
+        self._n = 0
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sd_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        call(name, self._h, *args, h=self._h)
+
+    # -- scene (engine.hpp:187-190)
+    def add_spheres(self, pos4, vel4, omega4=None) -> None:
+        p = _f32(pos4)
+        v = _f32(vel4)
+        if len(p) != len(v):
+            raise ValueError("pos4 and vel4 lengths differ")
+        w = None if omega4 is None else _f32(omega4)
+        self._call("sd_engine_add_spheres", len(p), p.ctypes.data, v.ctypes.data,
+                   None if w is None else w.ctypes.data)
+        self._n += len(p)
+
+    def add(self, grid_resolution: int, size: float, diameter: float, mass: float, position, velocity) -> None:
+        """DEMEngine::add(DEMParticle(...)) for one-sphere entities."""
+        p = (C.c_float * 3)(*position)
+        v = (C.c_float * 3)(*velocity)
+        self._call("sd_engine_add_particle", grid_resolution, size, diameter, mass, p, v)
+        self._n += 1
+
+    def load_scene_json(self, path: str) -> None:
+        self._call("sd_engine_load_scene_json", str(path).encode())
+        st = self.stats()
+        self._n = int(st["n_spheres"])
+
+    def prepare(self) -> None:
+        self._call("sd_engine_prepare")
+
+    # reference names: prep() builds host arrays, transfer() uploads
+    def prep(self) -> None:
+        pass
+
+    def transfer(self) -> None:
+        self.prepare()
+
+    # -- stepping
+    def step(self, dt: float, n_steps: int = 1) -> None:
+        self._call("sd_engine_step", dt, n_steps)
+
+    def update(self, dt: float) -> None:
+        self._call("sd_engine_update", dt)
+
+    def sync(self) -> None:
+        self._call("sd_engine_sync")
+
+    # -- state
+    @property
+    def n(self) -> int:
+        return self._n
+
+    def get(self, field: int) -> np.ndarray:
+        out = np.empty((self._n, 4), dtype=np.float32)
+        self._call("sd_engine_get_state", field, out.ctypes.data, out.nbytes)
+        return out
+
+    def set(self, field: int, arr) -> None:
+        a = _f32(arr)
+        self._call("sd_engine_set_state", field, a.ctypes.data, a.nbytes)
+
+    def positions(self) -> np.ndarray:
+        return self.get(_abi.SD_FIELD_POSITION)
+
+    def velocities(self) -> np.ndarray:
+        return self.get(_abi.SD_FIELD_VELOCITY)
+
+    def omegas(self) -> np.ndarray:
+        return self.get(_abi.SD_FIELD_OMEGA)
+
+    def forces(self) -> np.ndarray:
+        return self.get(_abi.SD_FIELD_FORCE)
+
+    def torques(self) -> np.ndarray:
+        return self.get(_abi.SD_FIELD_TORQUE)
+
+    def device_ptr(self, field: int) -> int:
+        p = C.c_void_p()
+        self._call("sd_engine_device_ptr", field, C.byref(p))
+        return p.value
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._call("sd_engine_stream", C.byref(p))
+        return p.value or 0
+
+    def pairs(self, cap: int | None = None) -> np.ndarray:
+        n = C.c_uint64()
+        cap = self.config.pair_capacity if cap is None else cap
+        out = np.empty(max(cap, 1), dtype=np.uint64)
+        self._call("sd_engine_get_pairs", out.ctypes.data, cap, C.byref(n))
+        return out[: n.value].copy()
+
+    def stats(self) -> dict:
+        s = _abi.SdStats()
+        self._call("sd_engine_stats", C.byref(s))
+        return {
+            "n_spheres": s.n_spheres, "steps": s.steps, "contacts": s.contacts,
+            "kinetic_energy": s.kinetic_energy, "momentum": tuple(s.momentum),
+            "device_errors": s.device_errors, "n_cells": s.n_cells,
+        }
+
+    def params(self) -> dict:
+        p = _abi.SdParams()
+        self._call("sd_engine_params", C.byref(p))
+        return {"lo": tuple(p.lo), "hi": tuple(p.hi), "cell": p.cell, "dims": (p.nx, p.ny, p.nz),
+                "kn": p.kn, "damp": p.damp, "mu": p.mu, "gravity": tuple(p.gravity), "dt": p.dt,
+                "walls": p.walls}
+
+    def save_checkpoint(self, path: str) -> None:
+        self._call("sd_engine_save_checkpoint", str(path).encode())
+
+    def load_checkpoint(self, path: str) -> None:
+        self._call("sd_engine_load_checkpoint", str(path).encode())
+
+
+def scene_lattice(nx, ny, nz, spacing, jitter, origin, radius, mass, vmax, seed):
+    """Seeded jittered cubic lattice (sd_scene_lattice)."""
+    n = nx * ny * nz
+    pos = np.empty((n, 4), np.float32)
+    vel = np.empty((n, 4), np.float32)
+    o = (C.c_float * 3)(*origin)
+    call("sd_scene_lattice", nx, ny, nz, spacing, jitter, o, radius, mass, vmax, seed,
+         pos.ctypes.data, vel.ctypes.data)
+    return pos, vel
+
+
+def scene_rsa(n, lo, hi, r_median, r_sigma, r_min, r_max, density, vmax, seed, max_attempts=50_000_000):
+    """Seeded random-sequential-addition packing (sd_scene_rsa)."""
+    pos = np.empty((n, 4), np.float32)
+    vel = np.empty((n, 4), np.float32)
+    phi = C.c_double()
+    call("sd_scene_rsa", n, (C.c_float * 3)(*lo), (C.c_float * 3)(*hi), r_median, r_sigma, r_min, r_max,
+         density, vmax, seed, max_attempts, pos.ctypes.data, vel.ctypes.data, C.byref(phi))
+    return pos, vel, phi.value
+
+
+class SpatialPartition:
+    """Reference operator class over CUDA tensors (torch), bit-exact broad phase."""
+
+    @staticmethod
+    def _stream(stream):
+        if stream is None:
+            import torch
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        return C.c_void_p(stream)
+
+    @staticmethod
+    def construct_collision_list(n, cell_dim, cells, spheres, sizes, pos4, count, stream=None):
+        """constructCollisionList: 9n (cell, sphere) entries + valid count."""
+        call("sd_hash_construct_collision_list", n, cell_dim, cells.data_ptr(), spheres.data_ptr(),
+             sizes.data_ptr(), pos4.data_ptr(), count.data_ptr(), SpatialPartition._stream(stream))
+
+    @staticmethod
+    def sort_scratch_bytes(n, key_bits=32) -> int:
+        b = C.c_uint64()
+        call("sd_sort_scratch_bytes", n, key_bits, C.byref(b))
+        return b.value
+
+    @staticmethod
+    def sort_collision_list(cells, spheres, cells_tmp, spheres_tmp, n, scratch, stream=None):
+        """sortCollisionList: stable sort of the first n entries by cell word."""
+        call("sd_hash_sort_collision_list", cells.data_ptr(), spheres.data_ptr(), cells_tmp.data_ptr(),
+             spheres_tmp.data_ptr(), n, scratch.data_ptr(), scratch.numel() * scratch.element_size(),
+             SpatialPartition._stream(stream))
+
+    @staticmethod
+    def sort_pairs(keys, vals, keys_tmp, vals_tmp, n, key_bits, scratch, stream=None):
+        call("sd_sort_pairs", keys.data_ptr(), vals.data_ptr(), keys_tmp.data_ptr(), vals_tmp.data_ptr(), n,
+             key_bits, scratch.data_ptr(), scratch.numel() * scratch.element_size(),
+             SpatialPartition._stream(stream))
+
+    @staticmethod
+    def sort_status(scratch, stream=None) -> int:
+        v = C.c_uint32()
+        call("sd_sort_status", scratch.data_ptr(), SpatialPartition._stream(stream), C.byref(v))
+        return v.value
+
+    @staticmethod
+    def pairs_scratch_bytes(n_entries) -> int:
+        b = C.c_uint64()
+        call("sd_hash_pairs_scratch_bytes", n_entries, C.byref(b))
+        return b.value
+
+    @staticmethod
+    def candidate_pairs(cells, spheres, count, n_entries, body_of, pair_a, pair_b, cap, npairs, scratch,
+                        stream=None):
+        """Candidate pairs of tranverseAndResolveCollisionList's run traversal."""
+        call("sd_hash_candidate_pairs", cells.data_ptr(), spheres.data_ptr(), count.data_ptr(), n_entries,
+             None if body_of is None else body_of.data_ptr(), pair_a.data_ptr(), pair_b.data_ptr(), cap,
+             npairs.data_ptr(), scratch.data_ptr(), scratch.numel() * scratch.element_size(),
+             SpatialPartition._stream(stream))

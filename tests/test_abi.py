@@ -1,0 +1,184 @@
+"""The C-ABI library loads without a GPU, exports every declared symbol, and
+its host-only entry points (config, scene loading, generators, parameter
+derivation, error reporting) behave as documented."""
+import ctypes as C
+import json
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = []
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*sd_status\s+(sd_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported(sdlib):
+    names = declared_functions()
+    assert len(names) >= 25
+    lib = C.CDLL(str(sdlib._abi.LIB_PATH))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_every_declared_symbol_has_a_binding(sdlib):
+    assert set(declared_functions()) <= set(sdlib._abi.SIGNATURES)
+
+
+def test_config_default_and_bad_struct_size(sdlib):
+    c = sdlib._abi.SdConfig()
+    sdlib._abi.call("sd_config_default", C.byref(c))
+    assert c.struct_size == C.sizeof(sdlib._abi.SdConfig)
+    assert c.kn == pytest.approx(1e5) and c.restitution == pytest.approx(0.5) and c.mu == pytest.approx(0.3)
+    c.struct_size = 7
+    h = C.c_void_p()
+    st = sdlib.lib().sd_engine_create(C.byref(c), C.byref(h))
+    assert st == sdlib._abi.SD_ERR_INVALID_ARG
+    assert "struct_size" in sdlib._abi.last_error()
+
+
+def test_cpu_device_is_rejected(sdlib):
+    cfg = sdlib.EngineConfig(device=sdlib._abi.SD_DEVICE_CPU)
+    with pytest.raises(sdlib.SdError) as e:
+        sdlib.DEMEngine(cfg)
+    assert e.value.status == sdlib._abi.SD_ERR_UNSUPPORTED
+
+
+def test_add_spheres_validates(sdlib):
+    eng = sdlib.DEMEngine()
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add_spheres(np.array([[0.5, 0.5, 0.5, 0.0]], np.float32), np.array([[0, 0, 0, 1.0]], np.float32))
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    with pytest.raises(sdlib.SdError):
+        eng.add_spheres(np.array([[np.nan, 0.5, 0.5, 0.1]], np.float32), np.array([[0, 0, 0, 1.0]], np.float32))
+    eng.close()
+
+
+def test_multi_sphere_particle_unsupported(sdlib):
+    eng = sdlib.DEMEngine()
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add(2, 0.15, 0.15, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
+    assert e.value.status == sdlib._abi.SD_ERR_UNSUPPORTED
+    eng.add(1, 0.1, 0.1, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
+    assert eng.stats()["n_spheres"] == 1
+    eng.close()
+
+
+def test_params_derivation(sdlib):
+    from stardust_gb300 import scenes
+    pos, vel, cfg, dt = scenes.box_lattice(n_side=4)
+    eng = sdlib.DEMEngine(cfg)
+    eng.add_spheres(pos, vel)
+    p = eng.params()
+    assert p["dims"] == (32, 32, 32)
+    assert p["cell"] == pytest.approx(0.02)
+    # gamma_n = damp sqrt(m_eff); damp = 2 beta sqrt(kn), beta = -ln e / sqrt(pi^2 + ln^2 e)
+    le = np.log(0.5)
+    beta = -le / np.sqrt(np.pi ** 2 + le ** 2)
+    assert p["damp"] == pytest.approx(2 * beta * np.sqrt(1e5), rel=1e-6)
+    eng.close()
+
+
+def test_cell_smaller_than_diameter_rejected(sdlib):
+    cfg = sdlib.EngineConfig(box_hi=(1, 1, 1), cell=0.01)
+    eng = sdlib.DEMEngine(cfg)
+    eng.add_spheres(np.array([[0.5, 0.5, 0.5, 0.02]], np.float32), np.array([[0, 0, 0, 1.0]], np.float32))
+    with pytest.raises(sdlib.SdError) as e:
+        eng.params()
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    eng.close()
+
+
+def test_reference_scene_json_loads(sdlib, tmp_path):
+    # the schema of setup/star_test.json: scene.domain, entities[], gravity
+    scene = {"scene": {"domain": 4, "entities": [
+        {"type": "generic", "position": [0.5, 0.5, 0.5], "size": 0.15, "mass": 3, "velocity": [0, 0, 0]},
+        {"type": "generic", "position": [1, 1, 1], "size": 0.15, "mass": 3, "velocity": [0, 0, 0]}],
+        "gravity": 9.81}}
+    f = tmp_path / "star_test.json"
+    f.write_text(json.dumps(scene, indent=4))
+    eng = sdlib.DEMEngine()
+    eng.load_scene_json(f)
+    assert eng.n == 2
+    p = eng.params()
+    assert p["hi"] == pytest.approx((4, 4, 4)) and p["lo"] == pytest.approx((0, 0, 0))
+    assert p["gravity"] == pytest.approx((0, 0, -9.81))
+    assert p["cell"] == pytest.approx(0.15)  # 2 x radius (diameter = size)
+    eng.close()
+
+
+def test_scene_json_extensions_and_errors(sdlib, tmp_path):
+    ok = {"scene": {"box": {"lo": [0, 0, 0], "hi": [1, 1, 2]}, "walls": 63, "cell": 0.05,
+                    "material": {"kn": 2e5, "restitution": 0.8, "mu": 0.1},
+                    "spheres": [{"position": [0.5, 0.5, 0.5], "radius": 0.01, "mass": 0.001}]}}
+    f = tmp_path / "ok.json"
+    f.write_text(json.dumps(ok))
+    eng = sdlib.DEMEngine()
+    eng.load_scene_json(f)
+    p = eng.params()
+    assert p["dims"] == (20, 20, 40) and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
+    eng.close()
+    for bad, what in (({"scene": {"domain": 1, "colour": 3}}, "colour"),
+                      ({"scene": {"entities": [{"type": "mesh", "position": [0, 0, 0], "size": 1, "mass": 1}]}}, "generic"),
+                      ({"scene": {"entities": [{"type": "generic", "position": [0, 0], "size": 1, "mass": 1}]}}, "position"),
+                      ({"nope": {}}, "nope")):
+        g = tmp_path / "bad.json"
+        g.write_text(json.dumps(bad))
+        e2 = sdlib.DEMEngine()
+        with pytest.raises(sdlib.SdError) as e:
+            e2.load_scene_json(g)
+        assert e.value.status == sdlib._abi.SD_ERR_JSON and what in str(e.value)
+        e2.close()
+    g = tmp_path / "broken.json"
+    g.write_text('{"scene": {"domain": 1,}')
+    e3 = sdlib.DEMEngine()
+    with pytest.raises(sdlib.SdError) as e:
+        e3.load_scene_json(g)
+    assert e.value.status == sdlib._abi.SD_ERR_JSON
+    with pytest.raises(sdlib.SdError) as e:
+        e3.load_scene_json(tmp_path / "missing.json")
+    assert e.value.status == sdlib._abi.SD_ERR_IO
+    e3.close()
+
+
+def test_state_calls_before_prepare_are_errors(sdlib):
+    eng = sdlib.DEMEngine()
+    eng.add_spheres(np.array([[0.5, 0.5, 0.5, 0.1]], np.float32), np.array([[0, 0, 0, 1.0]], np.float32))
+    for fn in (lambda: eng.step(1e-5, 1), lambda: eng.positions(), lambda: eng.pairs()):
+        with pytest.raises(sdlib.SdError) as e:
+            fn()
+        assert e.value.status == sdlib._abi.SD_ERR_STATE
+    eng.close()
+
+
+def test_generators_are_seeded(sdlib):
+    from stardust_gb300 import scenes
+    a = scenes.box_lattice(n_side=6, seed=3)[0]
+    b = scenes.box_lattice(n_side=6, seed=3)[0]
+    c = scenes.box_lattice(n_side=6, seed=4)[0]
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    # jitter bound and spacing of the lattice
+    assert np.all(np.abs(np.diff(np.sort(np.unique(np.round(a[:, 0], 3))))) > 0.02)
+
+
+def test_rsa_is_non_overlapping(sdlib):
+    from stardust_gb300 import scenes
+    n = 3000
+    pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=scenes.scaled_box(n), seed=5)
+    assert 0.30 < phi < 0.40
+    d = pos[:, None, :3].astype(np.float64) - pos[None, :, :3]
+    dist = np.sqrt((d ** 2).sum(-1))
+    rs = pos[:, None, 3].astype(np.float64) + pos[None, :, 3]
+    np.fill_diagonal(dist, 1e9)
+    assert np.all(dist >= rs * (1 - 1e-6))
+    lo, hi = np.array(cfg.box_lo), np.array(cfg.box_hi)
+    assert np.all(pos[:, :3] - pos[:, 3:4] >= lo - 1e-7) and np.all(pos[:, :3] + pos[:, 3:4] <= hi + 1e-7)
+    assert np.all((pos[:, 3] >= 0.0025) & (pos[:, 3] <= 0.01))
+    assert np.allclose(vel[:, 3], scenes.DENSITY * 4 / 3 * np.pi * pos[:, 3].astype(np.float64) ** 3, rtol=1e-6)
