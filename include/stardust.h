@@ -100,8 +100,9 @@ typedef enum sd_field {
     SD_FIELD_POSITION = 0, /* float4 (x, y, z, r) */
     SD_FIELD_VELOCITY = 1, /* float4 (vx, vy, vz, m) */
     SD_FIELD_OMEGA = 2,    /* float4 (wx, wy, wz, 0) */
-    SD_FIELD_FORCE = 3,    /* float4 contact + wall force of the last step (fx, fy, fz, 0) */
-    SD_FIELD_TORQUE = 4,   /* float4 contact torque of the last step */
+    SD_FIELD_FORCE = 3,    /* float4 contact + wall force of the last step (fx, fy, fz, 0);
+                              with SD_FLAG_RECORD; the device array is indexed by sphere id */
+    SD_FIELD_TORQUE = 4,   /* float4 contact torque of the last step (indexed by sphere id) */
     SD_FIELD_IDS = 5       /* uint32 original sphere id of each sorted slot (device ptr only) */
 } sd_field;
 

@@ -159,8 +159,13 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
             }
         }
         if (RECORD) {
-            force[i] = make_float4(f.x, f.y, f.z, 0.0f);
-            torque[i] = make_float4(t.x, t.y, t.z, 0.0f);
+            // recorded by sphere id: the slot order changes in the reorder
+            // that ends the step
+            const uint32_t id = __float_as_uint(wi.w) & kIdMask;
+            if (id < n) {
+                force[id] = make_float4(f.x, f.y, f.z, 0.0f);
+                torque[id] = make_float4(t.x, t.y, t.z, 0.0f);
+            }
         }
         const float dt = p.dt;
         const float nvx = vi.x + dt * (f.x / mi + p.g[0]);

@@ -565,8 +565,13 @@ sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
-    SD_CUDA(h, sd::dem_unsort_async(src, h->B.omg, h->d_tmp, n, h->stream));
-    SD_CUDA(h, cudaMemcpyAsync(host_dst, h->d_tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (field == SD_FIELD_FORCE || field == SD_FIELD_TORQUE) {
+        // recorded by sphere id already
+        SD_CUDA(h, cudaMemcpyAsync(host_dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        SD_CUDA(h, sd::dem_unsort_async(src, h->B.omg, h->d_tmp, n, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(host_dst, h->d_tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    }
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     if (field == SD_FIELD_OMEGA) {
         float4* o = static_cast<float4*>(host_dst);
@@ -811,11 +816,11 @@ sd_status sd_sort_pairs(uint32_t* d_keys, uint32_t* d_vals, uint32_t* d_keys_tmp
                         int32_t key_bits, void* d_scratch, uint64_t scratch_bytes, void* stream) {
     if (key_bits < 1 || key_bits > 32) return fail(nullptr, SD_ERR_INVALID_ARG, "key_bits must be 1..32");
     if (n >= (1ull << 30)) return fail(nullptr, SD_ERR_CAPACITY, "n must be < 2^30");
-    if (n && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp || !d_scratch))
+    if (n == 0) return SD_OK;
+    if (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp || !d_scratch)
         return fail(nullptr, SD_ERR_INVALID_ARG, "NULL pointer");
     if (scratch_bytes < sd::sort_scratch_words(n, key_bits) * sizeof(uint32_t))
         return fail(nullptr, SD_ERR_CAPACITY, "scratch smaller than sd_sort_scratch_bytes");
-    if (n == 0) return SD_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     bool in_tmp = false;
     cudaError_t e = sd::sort_pairs_async(d_keys, d_vals, d_keys_tmp, d_vals_tmp, (uint32_t)n, key_bits,
