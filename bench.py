@@ -236,9 +236,15 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    # warm-up (graph capture happens on the first step)
+    # warm-up (graph capture happens on the first step), then the autotuner
+    # picks the launch knobs on this scene (its steps are warm-up too)
     eng.step(dt, args.warmup)
     eng.sync()
+    tuned = None
+    if not args.no_tune:
+        from stardust_gb300 import autotune
+        tuned = autotune.tune_engine(eng, dt, reps=5)
+        log(f"autotune: {tuned}")
 
     def barrier():
         torch.cuda.synchronize()
@@ -336,7 +342,9 @@ def run_ours(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s",
                        "n_spheres": n, "volume_fraction": round(phi, 4), "cells": st["n_cells"],
-                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}"},
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}",
+                       "knobs": {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items")}},
+            "autotune": tuned,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
             "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -368,6 +376,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")

@@ -117,6 +117,7 @@ typedef struct sd_params {
     float gravity[3];
     float dt;        /* dt of the captured step graph (0 before the first step) */
     int32_t walls;
+    float rmax;      /* largest sphere radius */
 } sd_params;
 
 typedef struct sd_engine sd_engine;
@@ -209,6 +210,16 @@ sd_status sd_engine_params(sd_engine* h, sd_params* out);
  * same config resumes bit-exactly. */
 sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path);
 sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
+
+/* ------------------------------------------------------------ launch knobs
+ * Process-wide kernel variants and tile sizes, set by the autotuner
+ * (stardust_gb300.autotune) in place of the reference's hand block sweeps
+ * (profiling/blocksweep*.txt).  Engines re-capture their step graph on the
+ * next step after a change.  Knobs:
+ *   "contact_mode"  0 = one-pass candidate scan, 1 = two-phase scan (default)
+ *   "sort_items"    keys per thread of the sort's digit pass: 8 (default) or 16 */
+sd_status sd_tune_set(const char* knob, int32_t value);
+sd_status sd_tune_get(const char* knob, int32_t* value);
 
 /* --------------------------------------------------- raw operator API ---
  * Device pointers, caller-owned memory, asynchronous on `stream`. */

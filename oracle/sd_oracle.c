@@ -489,7 +489,7 @@ void sdo_sort_reorder(const sdo_params* p, uint32_t n,
  * the specification the CUDA kernels follow; it is written once as a macro
  * template and instantiated for float (the parity oracle) and double (the
  * error statement). */
-#define SDO_DEFINE_STEP(REAL, SQRT, FMIN, SUFFIX)                                           \
+#define SDO_DEFINE_STEP(REAL, SQRT, FMIN, FMA, SUFFIX)                                           \
 static inline void contact_response##SUFFIX(                                                 \
     const sdo_params* p, REAL nx, REAL ny, REAL nz, REAL delta,                              \
     REAL dvx, REAL dvy, REAL dvz, REAL wsx, REAL wsy, REAL wsz, REAL meff, REAL ri,          \
@@ -546,7 +546,7 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
                     if ((int64_t)s == i) continue;                                           \
                     const REAL* pj = pos + 4 * (size_t)s;                                    \
                     REAL dx = xi - pj[0], dy = yi - pj[1], dz = zi - pj[2];                  \
-                    REAL d2 = (dx * dx + dy * dy) + dz * dz;                                 \
+                    REAL d2 = FMA(dz, dz, FMA(dy, dy, dx * dx));                             \
                     REAL rs = ri + pj[3];                                                    \
                     if (!(d2 < rs * rs) || d2 == (REAL)0) continue;                          \
                     ++contacts;                                                              \
@@ -603,8 +603,8 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
     return contacts;                                                                         \
 }
 
-SDO_DEFINE_STEP(float, sqrtf, fminf, _f32)
-SDO_DEFINE_STEP(double, sqrt, fmin, _f64)
+SDO_DEFINE_STEP(float, sqrtf, fminf, fmaf, _f32)
+SDO_DEFINE_STEP(double, sqrt, fmin, fma, _f64)
 
 uint64_t sdo_contact_integrate(const sdo_params* p, uint32_t n,
                                const float* pos, const float* vel, const float* omg,
@@ -652,7 +652,7 @@ uint64_t sdo_contact_pairs(const sdo_params* p, uint32_t n, const float* pos,
                     if (s == i) continue;
                     const float* pj = pos + 4 * (size_t)s;
                     float dx = pi[0] - pj[0], dy = pi[1] - pj[1], dz = pi[2] - pj[2];
-                    float d2 = (dx * dx + dy * dy) + dz * dz;
+                    float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     float rs = pi[3] + pj[3];
                     if (!(d2 < rs * rs) || d2 == 0.0f) continue;
                     uint32_t idj;

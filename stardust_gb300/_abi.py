@@ -91,6 +91,7 @@ class SdParams(C.Structure):
         ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
         ("kn", C.c_float), ("damp", C.c_float), ("mu", C.c_float),
         ("gravity", C.c_float * 3), ("dt", C.c_float), ("walls", C.c_int32),
+        ("rmax", C.c_float),
     ]
 
 
@@ -114,6 +115,8 @@ SIGNATURES = {
     "sd_engine_step": [P, F32, I32],
     "sd_engine_update": [P, F32],
     "sd_engine_launch_stage": [P, I32, F32],
+    "sd_tune_set": [C.c_char_p, I32],
+    "sd_tune_get": [C.c_char_p, C.POINTER(I32)],
     "sd_engine_sync": [P],
     "sd_engine_get_state": [P, I32, P, C.c_size_t],
     "sd_engine_set_state": [P, I32, P, C.c_size_t],
@@ -174,3 +177,14 @@ def check(status: int, where: str, h=None) -> None:
 
 def call(name: str, *args, h=None) -> None:
     check(getattr(lib(), name)(*args), name, h)
+
+
+def tune_set(knob: str, value: int) -> None:
+    """Set a process-wide launch knob (see sd_tune_set)."""
+    call("sd_tune_set", knob.encode(), value)
+
+
+def tune_get(knob: str) -> int:
+    v = C.c_int32()
+    call("sd_tune_get", knob.encode(), C.byref(v))
+    return v.value

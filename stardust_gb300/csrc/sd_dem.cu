@@ -89,7 +89,51 @@ __device__ __forceinline__ void contact_response(const DemParams& p, float nx, f
     }
 }
 
-template <bool RECORD>
+// |d|^2 as specified for the overlap test: dx*dx, then two fused
+// multiply-adds (the CPU restatement uses fmaf in the same order).
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+}
+
+// Sphere-sphere contact of i with slot s: (dx, dy, dz) = x_i - x_j,
+// d2 = |x_i - x_j|^2, rs = r_i + r_j.
+__device__ __forceinline__ void pair_contact(const DemParams& p, float dx, float dy, float dz, float d2, float rs,
+                                             float rj, float ri, float mi, const float4& vi, const float4& wi,
+                                             const float4* __restrict__ vel, const float4* __restrict__ omg,
+                                             uint32_t s, float3& f, float3& t) {
+    const float4 vj = __ldg(&vel[s]);
+    const float4 wj = __ldg(&omg[s]);
+    const float mj = vj.w;
+    const float dist = sqrtf(d2);
+    const float inv = 1.0f / dist;
+    const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+    const float wsx = ri * wi.x + rj * wj.x;
+    const float wsy = ri * wi.y + rj * wj.y;
+    const float wsz = ri * wi.z + rj * wj.z;
+    const float meff = (mi * mj) / (mi + mj);
+    contact_response(p, nx, ny, nz, rs - dist, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, wsx, wsy, wsz, meff, ri, f,
+                     t);
+}
+
+// Passes whose digit histograms the contact kernel can build (keys up to 27
+// bits, i.e. grids up to 2^27 cells); larger grids use the sort's own
+// histogram kernel.  The plan travels packed in one word: passes in bits
+// 0-1, then per pass q a 5-bit shift at 2+9q and a 4-bit width at 7+9q.
+constexpr int kFusedPasses = 3;
+
+static uint32_t pack_hist_spec(const SortPlan& plan) {
+    uint32_t v = (uint32_t)plan.passes & 3u;
+    for (int q = 0; q < plan.passes && q < kFusedPasses; ++q)
+        v |= ((uint32_t)plan.shift[q] & 31u) << (2 + 9 * q) | ((uint32_t)plan.bits[q] & 15u) << (7 + 9 * q);
+    return v;
+}
+
+// Per-thread contact list of the two-phase scan (shared memory, thread-major
+// columns so consecutive lanes hit consecutive banks).
+constexpr int kContactList = 16;
+constexpr int kListStride = 256;
+
+template <bool RECORD, int MODE>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -97,48 +141,97 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ vel_n, float4* __restrict__ omg_n,
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
-                             uint32_t* __restrict__ status) {
+                             uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t s_hist[kFusedPasses][512];
+    __shared__ uint32_t s_list[MODE == 0 ? 1 : kContactList][kListStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0;
+    uint32_t key = 0;
     if (i < n) {
         const float4 pi = pos[i], vi = vel[i], wi = omg[i];
         const float ri = pi.w, mi = vi.w;
         float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
+        // The candidate cells: the 3x3x3 block around i's cell, cut per axis
+        // to the cells a partner's centre can occupy, |x_j - x_i| < r_i + r_max
+        // (padded by 1e-5 against rounding).  Only non-contacts are dropped,
+        // and the surviving candidates keep the block's visiting order --
+        // columns (x outer, y inner), slots ascending -- so the force sums are
+        // identical to a full 27-cell scan.
+        const float reach = (ri + p.rmax) * 1.00001f;
         const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
         const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
         const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
-        const int32_t z0 = cz > 0 ? cz - 1 : 0;
-        const int32_t z1 = cz + 1 < p.nz ? cz + 1 : p.nz - 1;
-        for (int32_t ddx = -1; ddx <= 1; ++ddx) {
-            const int32_t X = cx + ddx;
-            if (X < 0 || X >= p.nx) continue;
-            for (int32_t ddy = -1; ddy <= 1; ++ddy) {
-                const int32_t Y = cy + ddy;
-                if (Y < 0 || Y >= p.ny) continue;
-                const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
-                const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
-                const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
-                for (uint32_t s = s0; s < s1; ++s) {
-                    if (s == i) continue;
-                    const float4 pj = __ldg(&pos[s]);
-                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                    const float d2 = (dx * dx + dy * dy) + dz * dz;
-                    const float rs = ri + pj.w;
-                    if (!(d2 < rs * rs) || d2 == 0.0f) continue;
-                    ++contacts;
-                    const float4 vj = __ldg(&vel[s]);
-                    const float4 wj = __ldg(&omg[s]);
-                    const float rj = pj.w, mj = vj.w;
-                    const float dist = sqrtf(d2);
-                    const float inv = 1.0f / dist;
-                    const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
-                    const float wsx = ri * wi.x + rj * wj.x;
-                    const float wsy = ri * wi.y + rj * wj.y;
-                    const float wsz = ri * wi.z + rj * wj.z;
-                    const float meff = (mi * mj) / (mi + mj);
-                    contact_response(p, nx, ny, nz, rs - dist, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, wsx,
-                                     wsy, wsz, meff, ri, f, t);
+        const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, p.lo[0], p.cell, p.nx));
+        const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, p.lo[0], p.cell, p.nx));
+        const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, p.lo[1], p.cell, p.ny));
+        const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, p.lo[1], p.cell, p.ny));
+        const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, p.lo[2], p.cell, p.nz));
+        const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, p.lo[2], p.cell, p.nz));
+        if (MODE == 0) {
+            // one pass: test and apply each candidate in the scan loop
+            for (int32_t X = x0; X <= x1; ++X) {
+                for (int32_t Y = y0; Y <= y1; ++Y) {
+                    const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+                    const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
+                    const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+                    for (uint32_t s = s0; s < s1; ++s) {
+                        const float4 pa = __ldg(&pos[s]);
+                        const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                        const float da = dist2(ax, ay, az);
+                        const float ra = ri + pa.w;
+                        if (da < ra * ra && da != 0.0f) {
+                            ++contacts;
+                            pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                        }
+                    }
                 }
+            }
+        } else {
+            // two phases: a tight scan that only tests overlap and appends the
+            // contact's slot to a per-thread list in shared memory, then the
+            // force evaluation over the list.  A full list is evaluated before
+            // the scan resumes, so contacts are applied in scan order.  The
+            // sphere itself has d2 == 0 and fails the contact test.
+            uint32_t* my = &s_list[0][threadIdx.x];
+            int32_t X = x0, Y = y0;
+            uint32_t s, s1;
+            {
+                const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+                s = __ldg(&cell_start[col + (uint32_t)z0]);
+                s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+            }
+            bool done = false;
+            while (true) {
+                int cnt = 0;
+                while (true) {
+                    for (; s < s1 && cnt < kContactList; ++s) {
+                        const float4 pa = __ldg(&pos[s]);
+                        const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                        const float da = dist2(ax, ay, az);
+                        const float ra = ri + pa.w;
+                        if (da < ra * ra && da != 0.0f) my[kListStride * cnt++] = s;
+                    }
+                    if (cnt == kContactList) break;
+                    if (++Y > y1) {
+                        Y = y0;
+                        if (++X > x1) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+                    s = __ldg(&cell_start[col + (uint32_t)z0]);
+                    s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+                }
+                for (int c = 0; c < cnt; ++c) {
+                    const uint32_t sj = my[kListStride * c];
+                    const float4 pa = __ldg(&pos[sj]);
+                    const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                    pair_contact(p, ax, ay, az, dist2(ax, ay, az), ri + pa.w, pa.w, ri, mi, vi, wi, vel, omg, sj,
+                                 f, t);
+                }
+                contacts += cnt;
+                if (done) break;
             }
         }
         if (p.walls) {
@@ -177,8 +270,32 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
         vel_n[i] = make_float4(nvx, nvy, nvz, mi);
         omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia),
                                wi.z + dt * (t.z / inertia), wi.w);
-        keys[i] = cell_key(p, nxp, nyp, nzp);
+        key = cell_key(p, nxp, nyp, nzp);
+        keys[i] = key;
         vals[i] = i;
+    }
+    if (ghist) {
+        // digit histograms of the keys just written, for the sort that
+        // follows: warp-aggregated into shared memory, then one global atomic
+        // per non-empty bin and block
+        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+        __syncthreads();
+        const bool valid = i < n;
+        const int passes = (int)(hist_spec & 3u);
+#pragma unroll
+        for (int q = 0; q < kFusedPasses; ++q) {
+            if (q >= passes) break;
+            const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
+            const uint32_t d = (key >> shift) & ((1u << bits) - 1u);
+            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
+            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[q][d], __popc(peers));
+        }
+        __syncthreads();
+        for (int q = 0; q < passes; ++q) {
+            const uint32_t bits = (hist_spec >> (7 + 9 * q)) & 15u;
+            for (uint32_t d = threadIdx.x; d < (1u << bits); d += blockDim.x)
+                if (s_hist[q][d]) atomicAdd(&ghist[q * 512 + d], s_hist[q][d]);
+        }
     }
     if (RECORD) {
         uint32_t v = contacts;
@@ -265,7 +382,7 @@ __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restri
                 if (s == i) continue;
                 const float4 pj = pos[s];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const float d2 = (dx * dx + dy * dy) + dz * dz;
+                const float d2 = dist2(dx, dy, dz);
                 const float rs = pi.w + pj.w;
                 if (!(d2 < rs * rs) || d2 == 0.0f) continue;
                 const uint32_t idj = __float_as_uint(omg[s].w) & kIdMask;
@@ -368,20 +485,55 @@ cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream
     return dem_reorder_async(b, st);
 }
 
-cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
+static int g_contact_mode = 1;  // 0: one-pass scan, 1: two-phase scan (default)
+
+void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
+int dem_contact_mode() { return g_contact_mode; }
+
+template <bool RECORD, int MODE>
+static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st) {
+    dem_contact_integrate_kernel<RECORD, MODE><<<grid_for(b.n, 256), 256, 0, st>>>(
+        p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals,
+        RECORD ? b.force : nullptr, RECORD ? b.torque : nullptr, b.dev_status, spec, ghist);
+}
+
+static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
+                                  uint32_t* ghist, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
+    const uint32_t spec = pack_hist_spec(plan);
     if (record) {
         cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        dem_contact_integrate_kernel<true><<<grid_for(b.n, 256), 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.force,
-            b.torque, b.dev_status);
+        if (g_contact_mode == 0) launch_contact_t<true, 0>(p, b, spec, ghist, st);
+        else launch_contact_t<true, 1>(p, b, spec, ghist, st);
     } else {
-        dem_contact_integrate_kernel<false><<<grid_for(b.n, 256), 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, nullptr,
-            nullptr, b.dev_status);
+        if (g_contact_mode == 0) launch_contact_t<false, 0>(p, b, spec, ghist, st);
+        else launch_contact_t<false, 1>(p, b, spec, ghist, st);
     }
     return cudaGetLastError();
+}
+
+cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
+    return launch_contact(p, b, record, SortPlan{}, nullptr, st);
+}
+
+// One whole step: clear the sort's scratch, contact + integrate (which also
+// builds the key histograms), the digit passes, reorder.
+cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    const SortPlan plan = sort_plan(dem_key_bits(b.ncells));
+    if (plan.passes > kFusedPasses) {
+        cudaError_t e = dem_contact_integrate_async(p, b, record, st);
+        if (e != cudaSuccess) return e;
+        return dem_sort_reorder_async(p, b, st);
+    }
+    cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
+    if (e != cudaSuccess) return e;
+    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
+    if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
+                               &b.sorted_in_tmp)) != cudaSuccess)
+        return e;
+    return dem_reorder_async(b, st);
 }
 
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {

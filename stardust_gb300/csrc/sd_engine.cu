@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -30,6 +31,10 @@
 namespace {
 
 thread_local std::string g_last_error;
+
+// Bumped by sd_tune_set: engines whose graph was captured under an older
+// epoch re-capture before their next step.
+std::atomic<uint64_t> g_tune_epoch{0};
 
 struct CudaBuf {
     void* p = nullptr;
@@ -58,6 +63,7 @@ struct sd_engine {
     bool graph_valid = false;
     uint64_t steps = 0;
     bool need_resort = false;
+    uint64_t graph_epoch = 0;
 };
 
 namespace {
@@ -142,7 +148,9 @@ sd_status derive_params(sd_engine* h) {
     uint64_t ncells = 1;
     int32_t* dims[3] = {&P.nx, &P.ny, &P.nz};
     for (int a = 0; a < 3; ++a) {
-        double nd = std::ceil(((double)P.hi[a] - (double)P.lo[a]) / (double)cell);
+        // the box edge over a float cell is an integer up to the cell's
+        // rounding (1 / 0.02f = 50.000001): do not let that add a cell layer
+        double nd = std::ceil(((double)P.hi[a] - (double)P.lo[a]) / (double)cell * (1.0 - 1e-6));
         if (nd < 1) nd = 1;
         if (nd > (1 << 20)) return fail(h, SD_ERR_INVALID_ARG, "grid too fine (> 2^20 cells per axis)");
         *dims[a] = (int32_t)nd;
@@ -158,6 +166,7 @@ sd_status derive_params(sd_engine* h) {
     P.mu = c.mu;
     for (int a = 0; a < 3; ++a) P.g[a] = c.gravity[a];
     P.walls = c.walls;
+    P.rmax = rmax;
     P.dt = 0.0f;
     return SD_OK;
 }
@@ -236,8 +245,7 @@ sd_status build_graph(sd_engine* h, float dt) {
     bool record = (h->cfg.flags & SD_FLAG_RECORD) != 0;
     cudaGraph_t g = nullptr;
     SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e1 = sd::dem_contact_integrate_async(h->P, h->B, record, h->stream);
-    cudaError_t e2 = e1 == cudaSuccess ? sd::dem_sort_reorder_async(h->P, h->B, h->stream) : e1;
+    cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
     cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
     if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
     if (e3 != cudaSuccess) return cuda_fail(h, e3, "cudaStreamEndCapture");
@@ -521,7 +529,8 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
-    if (!h->graph_valid || h->graph_dt != dt) {
+    if (!h->graph_valid || h->graph_dt != dt || h->graph_epoch != g_tune_epoch.load()) {
+        h->graph_epoch = g_tune_epoch.load();
         if ((s = build_graph(h, dt))) return s;
     }
     for (int32_t i = 0; i < n_steps; ++i) SD_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
@@ -530,6 +539,31 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
 }
 
 sd_status sd_engine_update(sd_engine* h, float dt) { return sd_engine_step(h, dt, 1); }
+
+sd_status sd_tune_set(const char* knob, int32_t value) {
+    if (!knob) return fail(nullptr, SD_ERR_INVALID_ARG, "knob NULL");
+    std::string k(knob);
+    if (k == "contact_mode") {
+        if (value != 0 && value != 1) return fail(nullptr, SD_ERR_INVALID_ARG, "contact_mode must be 0 or 1");
+        sd::dem_set_contact_mode(value);
+    } else if (k == "sort_items") {
+        if (value != 8 && value != 16) return fail(nullptr, SD_ERR_INVALID_ARG, "sort_items must be 8 or 16");
+        sd::sort_set_items(value);
+    } else {
+        return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
+    }
+    g_tune_epoch.fetch_add(1);
+    return SD_OK;
+}
+
+sd_status sd_tune_get(const char* knob, int32_t* value) {
+    if (!knob || !value) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL argument");
+    std::string k(knob);
+    if (k == "contact_mode") *value = sd::dem_contact_mode();
+    else if (k == "sort_items") *value = sd::sort_items();
+    else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
+    return SD_OK;
+}
 
 sd_status sd_engine_sync(sd_engine* h) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");

@@ -15,8 +15,25 @@ enum : uint32_t {
 };
 
 // ---- radix sort (sd_sort.cu)
+// Digit plan of an LSD sort over key bits [0, key_bits): up to 4 passes of
+// at most 9 bits, as even as possible.
+struct SortPlan {
+    int passes;
+    int shift[4];
+    int bits[4];
+};
+SortPlan sort_plan(int key_bits);
 uint64_t sort_scratch_words(uint64_t n, int key_bits);
 int sort_num_passes(int key_bits);
+void sort_set_items(int items);
+int sort_items();
+uint32_t* sort_hist_ptr(uint32_t* scratch);  // [4][512] global digit histograms
+cudaError_t sort_clear_async(uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st);
+cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPlan& plan, uint32_t* scratch,
+                                 cudaStream_t st);
+cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                              uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
+                              bool* in_tmp);
 cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                              uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
                              bool* in_tmp);
@@ -41,6 +58,7 @@ struct DemParams {
     float g[3];
     float dt;
     int32_t walls;
+    float rmax;  // largest sphere radius: bounds every contact partner's reach
 };
 
 struct DemBuffers {
@@ -67,6 +85,9 @@ cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record,
                                         cudaStream_t st);
+cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st);
+void dem_set_contact_mode(int mode);
+int dem_contact_mode();
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n,
                              cudaStream_t st);

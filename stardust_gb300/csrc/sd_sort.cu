@@ -43,13 +43,7 @@ constexpr uint32_t kCountMask = (1u << 30) - 1;
 constexpr uint64_t kHistOff = 16;
 constexpr uint64_t kStatusOff = kHistOff + 4 * 512;
 
-struct SortPlan {
-    int passes;
-    int shift[4];
-    int bits[4];
-};
-
-static SortPlan make_plan(int key_bits) {
+SortPlan sort_plan(int key_bits) {
     SortPlan p{};
     if (key_bits < 1) key_bits = 1;
     if (key_bits > 32) key_bits = 32;
@@ -245,56 +239,75 @@ static size_t pass_smem_bytes() {
     return sizeof(uint32_t) * (2 * (size_t)kSortThreads * ITEMS + (size_t)kSortWarps * BINS + 2 * BINS + 40);
 }
 
-constexpr int kSortItems = 8;
+// Smallest tile the pass kernel is instantiated with; sizes the status area.
+constexpr int kSortItemsMin = 8;
+static int g_sort_items = 8;  // keys per thread of the pass kernel (8 or 16)
+
+void sort_set_items(int items) { g_sort_items = items >= 16 ? 16 : 8; }
+int sort_items() { return g_sort_items; }
 
 uint64_t sort_scratch_words(uint64_t n, int key_bits) {
-    SortPlan p = make_plan(key_bits);
-    uint64_t tiles = (n + tile_keys<kSortItems>() - 1) / tile_keys<kSortItems>();
+    SortPlan p = sort_plan(key_bits);
+    uint64_t tiles = (n + tile_keys<kSortItemsMin>() - 1) / tile_keys<kSortItemsMin>();
     if (tiles == 0) tiles = 1;
     return kStatusOff + (uint64_t)p.passes * tiles * 512;
+}
+
+uint32_t* sort_hist_ptr(uint32_t* scratch) { return scratch + kHistOff; }
+
+static uint32_t num_tiles(uint32_t n) {
+    uint32_t t = kSortThreads * (uint32_t)g_sort_items;
+    return (n + t - 1) / t;
+}
+
+cudaError_t sort_clear_async(uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st) {
+    // counters, histograms and this sort's tile status; not the status word
+    size_t clear_words = kStatusOff - 4 + (size_t)plan.passes * num_tiles(n) * 512;
+    return cudaMemsetAsync(scratch + 4, 0, clear_words * sizeof(uint32_t), st);
+}
+
+cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPlan& plan, uint32_t* scratch,
+                                 cudaStream_t st) {
+    int hist_blocks = (int)((n + kSortThreads * 16 - 1) / (kSortThreads * 16));
+    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
+    if (hist_blocks < 1) hist_blocks = 1;
+    sort_histogram_kernel<<<hist_blocks, kSortThreads, 0, st>>>(keys, n, plan, scratch);
+    return cudaGetLastError();
 }
 
 template <int BINS, int ITEMS>
 static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t* ko, uint32_t* vo,
                                uint32_t n, int shift, int bits, int pass, uint32_t tiles,
                                uint32_t* scratch, cudaStream_t st) {
-    static bool configured = false;
     size_t sm = pass_smem_bytes<BINS, ITEMS>();
-    if (!configured) {
+    if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel<BINS, ITEMS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        configured = true;
     }
     sort_pass_kernel<BINS, ITEMS><<<tiles, kSortThreads, sm, st>>>(ki, vi, ko, vo, n, shift, bits,
                                                                    pass, tiles, scratch);
     return cudaGetLastError();
 }
 
-// Sorts (keys, vals) by bits [0, key_bits).  Returns via *in_tmp whether
-// the result ended in the tmp buffers (odd pass count).
-cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
-                             uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
-                             bool* in_tmp) {
-    SortPlan plan = make_plan(key_bits);
+// The digit passes alone: the histograms in scratch must be complete and the
+// tile status cleared (sort_clear_async + a histogram producer).
+cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                              uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
+                              bool* in_tmp) {
     *in_tmp = false;
     if (n == 0) return cudaSuccess;
-    uint32_t tiles = (n + tile_keys<kSortItems>() - 1) / tile_keys<kSortItems>();
-    // clear counters, histograms and this sort's tile status (not the status word)
-    size_t clear_words = kStatusOff - 4 + (size_t)plan.passes * tiles * 512;
-    cudaError_t e = cudaMemsetAsync(scratch + 4, 0, clear_words * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    int hist_blocks = (int)((n + kSortThreads * 16 - 1) / (kSortThreads * 16));
-    if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
-    if (hist_blocks < 1) hist_blocks = 1;
-    sort_histogram_kernel<<<hist_blocks, kSortThreads, 0, st>>>(keys, n, plan, scratch);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const uint32_t tiles = num_tiles(n);
     uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
     for (int p = 0; p < plan.passes; ++p) {
-        if (plan.bits[p] <= 8)
-            e = launch_pass<256, kSortItems>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+        cudaError_t e;
+        const bool wide = plan.bits[p] > 8;
+        if (g_sort_items >= 16)
+            e = wide ? launch_pass<512, 16>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st)
+                     : launch_pass<256, 16>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
         else
-            e = launch_pass<512, kSortItems>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+            e = wide ? launch_pass<512, 8>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st)
+                     : launch_pass<256, 8>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
         if (e != cudaSuccess) return e;
         uint32_t* t;
         t = ki; ki = ko; ko = t;
@@ -304,6 +317,20 @@ cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
     return cudaSuccess;
 }
 
-int sort_num_passes(int key_bits) { return make_plan(key_bits).passes; }
+// Sorts (keys, vals) by bits [0, key_bits).  Returns via *in_tmp whether
+// the result ended in the tmp buffers (odd pass count).
+cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                             uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
+                             bool* in_tmp) {
+    SortPlan plan = sort_plan(key_bits);
+    *in_tmp = false;
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = sort_clear_async(n, plan, scratch, st);
+    if (e != cudaSuccess) return e;
+    if ((e = sort_histogram_async(keys, n, plan, scratch, st)) != cudaSuccess) return e;
+    return sort_passes_async(keys, vals, keys_tmp, vals_tmp, n, plan, scratch, st, in_tmp);
+}
+
+int sort_num_passes(int key_bits) { return sort_plan(key_bits).passes; }
 
 }  // namespace sd

@@ -199,7 +199,7 @@ class DEMEngine:
         self._call("sd_engine_params", C.byref(p))
         return {"lo": tuple(p.lo), "hi": tuple(p.hi), "cell": p.cell, "dims": (p.nx, p.ny, p.nz),
                 "kn": p.kn, "damp": p.damp, "mu": p.mu, "gravity": tuple(p.gravity), "dt": p.dt,
-                "walls": p.walls}
+                "walls": p.walls, "rmax": p.rmax}
 
     def save_checkpoint(self, path: str) -> None:
         self._call("sd_engine_save_checkpoint", str(path).encode())

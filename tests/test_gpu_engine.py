@@ -47,6 +47,30 @@ def test_box_lattice_bit_exact(sdlib, orc, steps):
     eng.close()
 
 
+@pytest.mark.parametrize("contact_mode,sort_items", [(0, 8), (1, 16), (0, 16)])
+def test_every_knob_setting_is_bit_exact(sdlib, orc, contact_mode, sort_items):
+    """The autotuner's choices change speed only: each contact-scan variant
+    and sort tile size gives the same bits as the oracle."""
+    from stardust_gb300 import _abi, scenes
+    old = (_abi.tune_get("contact_mode"), _abi.tune_get("sort_items"))
+    try:
+        _abi.tune_set("contact_mode", contact_mode)
+        _abi.tune_set("sort_items", sort_items)
+        n = 30_000
+        pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=scenes.scaled_box(n), seed=11)
+        pos = pos.copy()
+        pos[:, 3] *= 1.2
+        cfg.cell = float(2 * pos[:, 3].max())
+        eng = run_engine(sdlib, pos, vel, cfg, dt, 25)
+        p, (op, ov, ow) = oracle_state(orc, eng, pos, vel, dt, 25)
+        assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
+        assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))
+        eng.close()
+    finally:
+        _abi.tune_set("contact_mode", old[0])
+        _abi.tune_set("sort_items", old[1])
+
+
 def test_dense_pack_forces_torques_pairs(sdlib, orc):
     """A compressed, spinning polydisperse pack with many contacts: the forces
     and torques of the step, and the contact pair set, are bit-exact."""
