@@ -95,6 +95,7 @@ typedef struct sd_stats {
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
 #define SD_DEVERR_PAIR_OVERFLOW 0x2u
 #define SD_DEVERR_BAD_INPUT 0x4u
+#define SD_DEVERR_WAIT_TIMEOUT 0x8u /* a bounded wait on a TMA copy gave up (results still exact) */
 
 typedef enum sd_field {
     SD_FIELD_POSITION = 0, /* float4 (x, y, z, r) */
@@ -216,7 +217,9 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  * (stardust_gb300.autotune) in place of the reference's hand block sweeps
  * (profiling/blocksweep*.txt).  Engines re-capture their step graph on the
  * next step after a change.  Knobs:
- *   "contact_mode"  0 = one-pass candidate scan, 1 = two-phase scan (default)
+ *   "contact_mode"  0 = one thread per sphere, candidates read from global memory;
+ *                   1 = one CTA per grid column, neighbour columns staged in shared
+ *                       memory by TMA bulk copies (default)
  *   "sort_items"    keys per thread of the sort's digit pass: 8 (default) or 16 */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);

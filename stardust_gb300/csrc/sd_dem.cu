@@ -2,18 +2,26 @@
 //
 // One step is three stages (plus the sort between them):
 //
-//   contact_integrate   thread per sorted slot i: gather every sphere in the
+//   contact_integrate   for each sorted slot i: gather every sphere in the
 //                       3x3 columns of cells z-1..z+1 around i (each column a
 //                       contiguous slot range because keys are z-fastest),
 //                       accumulate spring-dashpot + Coulomb contact forces and
 //                       box-wall forces, integrate (symplectic Euler), write
-//                       the next state at slot i and its new cell key.  No
-//                       atomics: every pair is evaluated from both sides, so
+//                       the next state at slot i and its new cell key, and
+//                       count the key digits for the sort.  No atomics on the
+//                       physics: every pair is evaluated from both sides, so
 //                       the result does not depend on thread timing.
 //   sort                (key, slot) onesweep radix sort, sd_sort.cu
 //   reorder             gather the next state into sorted order and fill
 //                       cell_start (lower-bound of every cell, empty cells
 //                       included) block-cooperatively -- no memset needed.
+//
+// The contact stage has two kernels with identical results (the autotuner
+// picks one, knob "contact_mode"):
+//   0  one thread per slot, candidates read through L1 from global memory;
+//   1  one CTA per (x, y) grid column: the 3x3 neighbour columns -- nine
+//      contiguous slot ranges -- are staged into shared memory with TMA bulk
+//      copies (cp.async.bulk + mbarrier), and candidates are read from there.
 //
 // Replaces the reference's step (simulation_kernel.cu:52-153:
 // updateSphereData -> cleanBuffers -> broad phase -> reactCollisions ->
@@ -23,7 +31,7 @@
 // spring-dashpot law with restitution damping and Coulomb friction, walls
 // and gravity.  The operation order here is the specification the CPU
 // oracle restates; the file is compiled with -fmad=false so nothing is
-// contracted.
+// contracted except the explicit __fmaf_rn.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,9 +60,9 @@ __device__ __forceinline__ uint32_t cell_key(const DemParams& p, float x, float 
 // (gamma_n = damp * sqrt(m_eff), damp = 2*beta*sqrt(kn),
 // beta = -ln e / sqrt(pi^2 + ln^2 e)) -- not clipped at zero, so a binary
 // collision restores exactly the configured restitution -- and
-// viscous-regularised Coulomb friction |Ft| = min(mu*max(Fn,0), gamma_n*|vt|).  n points from the
-// partner to this sphere; (dv, ws) give the relative contact velocity
-// v_rel = dv - ws x n with ws = ri*wi + rj*wj.
+// viscous-regularised Coulomb friction |Ft| = min(mu*max(Fn,0), gamma_n*|vt|).
+// n points from the partner to this sphere; (dv, ws) give the relative
+// contact velocity v_rel = dv - ws x n with ws = ri*wi + rj*wj.
 __device__ __forceinline__ void contact_response(const DemParams& p, float nx, float ny, float nz,
                                                  float delta, float dvx, float dvy, float dvz,
                                                  float wsx, float wsy, float wsz, float meff, float ri,
@@ -115,7 +123,134 @@ __device__ __forceinline__ void pair_contact(const DemParams& p, float dx, float
                      t);
 }
 
-// Passes whose digit histograms the contact kernel can build (keys up to 27
+// Where a kernel reads candidate positions from: slot s of column (X, Y)
+// is element s + delta(X, Y) of the source.
+struct GlobalSource {
+    const float4* __restrict__ pos;
+    __device__ __forceinline__ uint32_t delta(int32_t, int32_t) const { return 0u; }
+    __device__ __forceinline__ float4 load(uint32_t k) const { return __ldg(&pos[k]); }
+};
+
+struct TileSource {
+    const float4* tile;     // staged slots of the 3x3 neighbour columns
+    const uint32_t* shift;  // per neighbour column: tile offset - first slot (mod 2^32)
+    int32_t X, Y;           // the CTA's column
+    __device__ __forceinline__ uint32_t delta(int32_t x, int32_t y) const {
+        return shift[(x - X + 1) * 3 + (y - Y + 1)];
+    }
+    __device__ __forceinline__ float4 load(uint32_t k) const { return tile[k]; }
+};
+
+// Contacts of slot i over its candidate cells, then walls, integration and
+// the next-state write.  Returns the new cell key.
+template <bool RECORD, class SRC>
+__device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
+                                                  const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                  const float4* __restrict__ omg,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  float4* __restrict__ pos_n, float4* __restrict__ vel_n,
+                                                  float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ vals, float4* __restrict__ force,
+                                                  float4* __restrict__ torque, uint32_t& contacts) {
+    const float4 pi = pos[i], vi = vel[i], wi = omg[i];
+    const float ri = pi.w, mi = vi.w;
+    float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
+    // The candidate cells: the 3x3x3 block around i's cell, cut per axis to
+    // the cells a partner's centre can occupy, |x_j - x_i| < r_i + r_max
+    // (padded by 1e-5 against rounding).  Only non-contacts are dropped, and
+    // the surviving candidates keep the block's visiting order -- columns (x
+    // outer, y inner), slots ascending -- so the force sums are identical to
+    // a full 27-cell scan.
+    const float reach = (ri + p.rmax) * 1.00001f;
+    const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
+    const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
+    const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
+    const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, p.lo[0], p.cell, p.nx));
+    const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, p.lo[0], p.cell, p.nx));
+    const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, p.lo[1], p.cell, p.ny));
+    const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, p.lo[1], p.cell, p.ny));
+    const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, p.lo[2], p.cell, p.nz));
+    const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, p.lo[2], p.cell, p.nz));
+    for (int32_t X = x0; X <= x1; ++X) {
+        for (int32_t Y = y0; Y <= y1; ++Y) {
+            const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+            const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
+            const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+            const uint32_t d = src.delta(X, Y);
+            uint32_t s = s0;
+            // two candidates per iteration for load-level parallelism;
+            // contacts are applied in slot order.  The sphere itself has
+            // d2 == 0 and fails the contact test.
+            for (; s + 1 < s1; s += 2) {
+                const float4 pa = src.load(s + d);
+                const float4 pb = src.load(s + 1 + d);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float bx = pi.x - pb.x, by = pi.y - pb.y, bz = pi.z - pb.z;
+                const float da = dist2(ax, ay, az), db = dist2(bx, by, bz);
+                const float ra = ri + pa.w, rb = ri + pb.w;
+                if (da < ra * ra && da != 0.0f) {
+                    ++contacts;
+                    pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                }
+                if (db < rb * rb && db != 0.0f) {
+                    ++contacts;
+                    pair_contact(p, bx, by, bz, db, rb, pb.w, ri, mi, vi, wi, vel, omg, s + 1, f, t);
+                }
+            }
+            if (s < s1) {
+                const float4 pa = src.load(s + d);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float da = dist2(ax, ay, az);
+                const float ra = ri + pa.w;
+                if (da < ra * ra && da != 0.0f) {
+                    ++contacts;
+                    pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                }
+            }
+        }
+    }
+    if (p.walls) {
+        const float wsx = ri * wi.x, wsy = ri * wi.y, wsz = ri * wi.z;
+        const float xs[3] = {pi.x, pi.y, pi.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                if (!(p.walls & (1 << (2 * a + side)))) continue;
+                const float gap = side == 0 ? xs[a] - p.lo[a] : p.hi[a] - xs[a];
+                if (!(gap < ri)) continue;
+                float nn[3] = {0.f, 0.f, 0.f};
+                nn[a] = side == 0 ? 1.0f : -1.0f;
+                contact_response(p, nn[0], nn[1], nn[2], ri - gap, vi.x, vi.y, vi.z, wsx, wsy, wsz, mi, ri, f, t);
+            }
+        }
+    }
+    if (RECORD) {
+        // recorded by sphere id: the slot order changes in the reorder that
+        // ends the step
+        const uint32_t id = __float_as_uint(wi.w) & kIdMask;
+        if (id < n) {
+            force[id] = make_float4(f.x, f.y, f.z, 0.0f);
+            torque[id] = make_float4(t.x, t.y, t.z, 0.0f);
+        }
+    }
+    const float dt = p.dt;
+    const float nvx = vi.x + dt * (f.x / mi + p.g[0]);
+    const float nvy = vi.y + dt * (f.y / mi + p.g[1]);
+    const float nvz = vi.z + dt * (f.z / mi + p.g[2]);
+    const float nxp = pi.x + dt * nvx, nyp = pi.y + dt * nvy, nzp = pi.z + dt * nvz;
+    const float inertia = ((0.4f * mi) * ri) * ri;
+    pos_n[i] = make_float4(nxp, nyp, nzp, ri);
+    vel_n[i] = make_float4(nvx, nvy, nvz, mi);
+    omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia), wi.z + dt * (t.z / inertia),
+                           wi.w);
+    const uint32_t key = cell_key(p, nxp, nyp, nzp);
+    keys[i] = key;
+    vals[i] = i;
+    return key;
+}
+
+// Passes whose digit histograms the contact kernels can build (keys up to 27
 // bits, i.e. grids up to 2^27 cells); larger grids use the sort's own
 // histogram kernel.  The plan travels packed in one word: passes in bits
 // 0-1, then per pass q a 5-bit shift at 2+9q and a 4-bit width at 7+9q.
@@ -128,12 +263,39 @@ static uint32_t pack_hist_spec(const SortPlan& plan) {
     return v;
 }
 
-// Per-thread contact list of the two-phase scan (shared memory, thread-major
-// columns so consecutive lanes hit consecutive banks).
-constexpr int kContactList = 16;
-constexpr int kListStride = 256;
+// Adds the warp's keys to the block's shared digit histograms (all lanes
+// of the warp must call; `valid` marks lanes that hold a key).
+__device__ __forceinline__ void hist_add(uint32_t (*s_hist)[512], uint32_t spec, uint32_t key, bool valid) {
+    const int passes = (int)(spec & 3u);
+#pragma unroll
+    for (int q = 0; q < kFusedPasses; ++q) {
+        if (q >= passes) break;
+        const uint32_t shift = (spec >> (2 + 9 * q)) & 31u, bits = (spec >> (7 + 9 * q)) & 15u;
+        const uint32_t d = (key >> shift) & ((1u << bits) - 1u);
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
+        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[q][d], __popc(peers));
+    }
+}
 
-template <bool RECORD, int MODE>
+// Block's histograms to the global ones: one atomic per non-empty bin.
+__device__ __forceinline__ void hist_flush(uint32_t (*s_hist)[512], uint32_t spec, uint32_t* ghist) {
+    const int passes = (int)(spec & 3u);
+    for (int q = 0; q < passes; ++q) {
+        const uint32_t bits = (spec >> (7 + 9 * q)) & 15u;
+        for (uint32_t d = threadIdx.x; d < (1u << bits); d += blockDim.x)
+            if (s_hist[q][d]) atomicAdd(&ghist[q * 512 + d], s_hist[q][d]);
+    }
+}
+
+__device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contacts) {
+    uint32_t v = contacts;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane_id() == 0 && v) atomicAdd(reinterpret_cast<unsigned long long*>(status + 2), (unsigned long long)v);
+}
+
+// ---------------------------------------------- contact_mode 0: per slot
+template <bool RECORD>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -143,167 +305,156 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist) {
     __shared__ uint32_t s_hist[kFusedPasses][512];
-    __shared__ uint32_t s_list[MODE == 0 ? 1 : kContactList][kListStride];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t contacts = 0;
-    uint32_t key = 0;
-    if (i < n) {
-        const float4 pi = pos[i], vi = vel[i], wi = omg[i];
-        const float ri = pi.w, mi = vi.w;
-        float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
-        // The candidate cells: the 3x3x3 block around i's cell, cut per axis
-        // to the cells a partner's centre can occupy, |x_j - x_i| < r_i + r_max
-        // (padded by 1e-5 against rounding).  Only non-contacts are dropped,
-        // and the surviving candidates keep the block's visiting order --
-        // columns (x outer, y inner), slots ascending -- so the force sums are
-        // identical to a full 27-cell scan.
-        const float reach = (ri + p.rmax) * 1.00001f;
-        const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
-        const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
-        const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
-        const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, p.lo[0], p.cell, p.nx));
-        const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, p.lo[0], p.cell, p.nx));
-        const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, p.lo[1], p.cell, p.ny));
-        const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, p.lo[1], p.cell, p.ny));
-        const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, p.lo[2], p.cell, p.nz));
-        const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, p.lo[2], p.cell, p.nz));
-        if (MODE == 0) {
-            // one pass: test and apply each candidate in the scan loop
-            for (int32_t X = x0; X <= x1; ++X) {
-                for (int32_t Y = y0; Y <= y1; ++Y) {
-                    const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
-                    const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
-                    const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
-                    for (uint32_t s = s0; s < s1; ++s) {
-                        const float4 pa = __ldg(&pos[s]);
-                        const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
-                        const float da = dist2(ax, ay, az);
-                        const float ra = ri + pa.w;
-                        if (da < ra * ra && da != 0.0f) {
-                            ++contacts;
-                            pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
-                        }
-                    }
-                }
-            }
-        } else {
-            // two phases: a tight scan that only tests overlap and appends the
-            // contact's slot to a per-thread list in shared memory, then the
-            // force evaluation over the list.  A full list is evaluated before
-            // the scan resumes, so contacts are applied in scan order.  The
-            // sphere itself has d2 == 0 and fails the contact test.
-            uint32_t* my = &s_list[0][threadIdx.x];
-            int32_t X = x0, Y = y0;
-            uint32_t s, s1;
-            {
-                const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
-                s = __ldg(&cell_start[col + (uint32_t)z0]);
-                s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
-            }
-            bool done = false;
-            while (true) {
-                int cnt = 0;
-                while (true) {
-                    for (; s < s1 && cnt < kContactList; ++s) {
-                        const float4 pa = __ldg(&pos[s]);
-                        const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
-                        const float da = dist2(ax, ay, az);
-                        const float ra = ri + pa.w;
-                        if (da < ra * ra && da != 0.0f) my[kListStride * cnt++] = s;
-                    }
-                    if (cnt == kContactList) break;
-                    if (++Y > y1) {
-                        Y = y0;
-                        if (++X > x1) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
-                    s = __ldg(&cell_start[col + (uint32_t)z0]);
-                    s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
-                }
-                for (int c = 0; c < cnt; ++c) {
-                    const uint32_t sj = my[kListStride * c];
-                    const float4 pa = __ldg(&pos[sj]);
-                    const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
-                    pair_contact(p, ax, ay, az, dist2(ax, ay, az), ri + pa.w, pa.w, ri, mi, vi, wi, vel, omg, sj,
-                                 f, t);
-                }
-                contacts += cnt;
-                if (done) break;
-            }
-        }
-        if (p.walls) {
-            const float wsx = ri * wi.x, wsy = ri * wi.y, wsz = ri * wi.z;
-            const float xs[3] = {pi.x, pi.y, pi.z};
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-#pragma unroll
-                for (int side = 0; side < 2; ++side) {
-                    if (!(p.walls & (1 << (2 * a + side)))) continue;
-                    const float gap = side == 0 ? xs[a] - p.lo[a] : p.hi[a] - xs[a];
-                    if (!(gap < ri)) continue;
-                    float nn[3] = {0.f, 0.f, 0.f};
-                    nn[a] = side == 0 ? 1.0f : -1.0f;
-                    contact_response(p, nn[0], nn[1], nn[2], ri - gap, vi.x, vi.y, vi.z, wsx, wsy, wsz, mi,
-                                     ri, f, t);
-                }
-            }
-        }
-        if (RECORD) {
-            // recorded by sphere id: the slot order changes in the reorder
-            // that ends the step
-            const uint32_t id = __float_as_uint(wi.w) & kIdMask;
-            if (id < n) {
-                force[id] = make_float4(f.x, f.y, f.z, 0.0f);
-                torque[id] = make_float4(t.x, t.y, t.z, 0.0f);
-            }
-        }
-        const float dt = p.dt;
-        const float nvx = vi.x + dt * (f.x / mi + p.g[0]);
-        const float nvy = vi.y + dt * (f.y / mi + p.g[1]);
-        const float nvz = vi.z + dt * (f.z / mi + p.g[2]);
-        const float nxp = pi.x + dt * nvx, nyp = pi.y + dt * nvy, nzp = pi.z + dt * nvz;
-        const float inertia = ((0.4f * mi) * ri) * ri;
-        pos_n[i] = make_float4(nxp, nyp, nzp, ri);
-        vel_n[i] = make_float4(nvx, nvy, nvz, mi);
-        omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia),
-                               wi.z + dt * (t.z / inertia), wi.w);
-        key = cell_key(p, nxp, nyp, nzp);
-        keys[i] = key;
-        vals[i] = i;
-    }
+    uint32_t contacts = 0, key = 0;
+    if (i < n)
+        key = particle_step<RECORD>(p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
+                                    keys, vals, force, torque, contacts);
     if (ghist) {
-        // digit histograms of the keys just written, for the sort that
-        // follows: warp-aggregated into shared memory, then one global atomic
-        // per non-empty bin and block
         for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
         __syncthreads();
-        const bool valid = i < n;
-        const int passes = (int)(hist_spec & 3u);
-#pragma unroll
-        for (int q = 0; q < kFusedPasses; ++q) {
-            if (q >= passes) break;
-            const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
-            const uint32_t d = (key >> shift) & ((1u << bits) - 1u);
-            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
-            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[q][d], __popc(peers));
-        }
+        hist_add(s_hist, hist_spec, key, i < n);
         __syncthreads();
-        for (int q = 0; q < passes; ++q) {
-            const uint32_t bits = (hist_spec >> (7 + 9 * q)) & 15u;
-            for (uint32_t d = threadIdx.x; d < (1u << bits); d += blockDim.x)
-                if (s_hist[q][d]) atomicAdd(&ghist[q * 512 + d], s_hist[q][d]);
+        hist_flush(s_hist, hist_spec, ghist);
+    }
+    if (RECORD) count_contacts(status, contacts);
+}
+
+// ------------------------------------- contact_mode 1: TMA column tiles
+constexpr int kColThreads = 512;
+constexpr uint32_t kTileSlots = 4096;  // staged positions per CTA (64 KB)
+constexpr uint32_t kTmaSpinLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to this CTA's shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kTmaSpinLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (it > 64) __nanosleep(64);
+    }
+    return false;
+}
+
+// One CTA per (x, y) grid column.  Its spheres' candidates all lie in the
+// 3x3 neighbour columns, nine contiguous slot ranges of the sorted state,
+// which one thread stages into shared memory with TMA bulk copies.  A CTA
+// whose neighbourhood exceeds kTileSlots reads global memory instead; the
+// results are the same either way.
+template <bool RECORD>
+__global__ void __launch_bounds__(kColThreads, 2)
+dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                          const float4* __restrict__ vel, const float4* __restrict__ omg,
+                          const uint32_t* __restrict__ cell_start, float4* __restrict__ pos_n,
+                          float4* __restrict__ vel_n, float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
+                          uint32_t* __restrict__ vals, float4* __restrict__ force, float4* __restrict__ torque,
+                          uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+    extern __shared__ __align__(128) float4 s_tile[];
+    __shared__ uint32_t s_hist[kFusedPasses][512];
+    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ uint32_t s_beg[9], s_cnt[9], s_shift[9], s_total;
+
+    const int32_t X = (int32_t)blockIdx.x / p.ny, Y = (int32_t)blockIdx.x % p.ny;
+    if (threadIdx.x < 9) {
+        const int32_t Xn = X + (int32_t)threadIdx.x / 3 - 1, Yn = Y + (int32_t)threadIdx.x % 3 - 1;
+        uint32_t b = 0, c = 0;
+        if (Xn >= 0 && Xn < p.nx && Yn >= 0 && Yn < p.ny) {
+            const uint32_t cb = (uint32_t)(Xn * p.ny + Yn) * (uint32_t)p.nz;
+            b = min(cell_start[cb], n);
+            const uint32_t e = min(cell_start[cb + (uint32_t)p.nz], n);
+            c = e > b ? e - b : 0u;
         }
+        s_beg[threadIdx.x] = b;
+        s_cnt[threadIdx.x] = c;
     }
-    if (RECORD) {
-        uint32_t v = contacts;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane_id() == 0 && v)
-            atomicAdd(reinterpret_cast<unsigned long long*>(status + 2), (unsigned long long)v);
+    if (ghist)
+        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t off = 0;
+        for (int c = 0; c < 9; ++c) {
+            s_shift[c] = off - s_beg[c];
+            off += s_cnt[c];
+        }
+        s_total = off;
+        if (s_cnt[4] > 0 && off <= kTileSlots) mbar_init(&s_bar, 1);
     }
+    __syncthreads();
+    const uint32_t own_beg = s_beg[4], own_cnt = s_cnt[4];
+    if (own_cnt == 0) return;  // uniform across the CTA
+    const bool staged = s_total <= kTileSlots;
+    if (staged && threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&s_bar, s_total * 16u);
+        for (int c = 0; c < 9; ++c)
+            if (s_cnt[c]) bulk_copy_g2s(&s_tile[s_shift[c] + s_beg[c]], pos + s_beg[c], s_cnt[c] * 16u, &s_bar);
+    }
+    bool use_tile = staged;
+    if (staged && !mbar_wait_bounded(&s_bar, 0)) {
+        atomicOr(status, kErrWaitTimeout);
+        use_tile = false;  // read global memory instead; same results
+    }
+    const TileSource tile{s_tile, s_shift, X, Y};
+    const GlobalSource glob{pos};
+    uint32_t contacts = 0;
+    const uint32_t rounds = (own_cnt + blockDim.x - 1) / blockDim.x;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t k = r * blockDim.x + threadIdx.x;
+        const bool valid = k < own_cnt;
+        uint32_t key = 0;
+        if (valid) {
+            const uint32_t i = own_beg + k;
+            // The tile holds the neighbours of column (X, Y) only.  A sphere's
+            // cell is recomputed from its position exactly as its sort key
+            // was, so it always lies in this column; the check keeps every
+            // shared-memory index in bounds regardless.
+            const float4 q = pos[i];
+            const bool mine = axis_cell(q.x, p.lo[0], p.cell, p.nx) == X && axis_cell(q.y, p.lo[1], p.cell, p.ny) == Y;
+            if (!mine) atomicOr(status, kErrBadInput);
+            key = (use_tile && mine)
+                      ? particle_step<RECORD>(p, n, i, tile, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
+                                              vals, force, torque, contacts)
+                      : particle_step<RECORD>(p, n, i, glob, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
+                                              vals, force, torque, contacts);
+        }
+        if (ghist) hist_add(s_hist, hist_spec, key, valid);
+    }
+    if (ghist) {
+        __syncthreads();
+        hist_flush(s_hist, hist_spec, ghist);
+    }
+    if (RECORD) count_contacts(status, contacts);
+    // never leave with a bulk copy in flight into this CTA's shared memory
+    if (staged && !use_tile && threadIdx.x == 0) mbar_wait_bounded(&s_bar, 0);
 }
 
 __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
@@ -450,6 +601,15 @@ __global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, co
 
 static inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1) / threads; }
 
+cudaError_t dem_init_kernels() {
+    const int sm = (int)(kTileSlots * sizeof(float4));
+    cudaError_t e = cudaFuncSetAttribute(dem_contact_column_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(dem_contact_column_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
+}
+
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
     dem_keys_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos_n, b.keys, b.vals);
@@ -485,16 +645,25 @@ cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream
     return dem_reorder_async(b, st);
 }
 
-static int g_contact_mode = 1;  // 0: one-pass scan, 1: two-phase scan (default)
+static int g_contact_mode = 1;  // 0: per slot, 1: TMA column tiles (default)
 
 void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
 int dem_contact_mode() { return g_contact_mode; }
 
-template <bool RECORD, int MODE>
+template <bool RECORD>
 static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st) {
-    dem_contact_integrate_kernel<RECORD, MODE><<<grid_for(b.n, 256), 256, 0, st>>>(
-        p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals,
-        RECORD ? b.force : nullptr, RECORD ? b.torque : nullptr, b.dev_status, spec, ghist);
+    float4* f = RECORD ? b.force : nullptr;
+    float4* t = RECORD ? b.torque : nullptr;
+    if (g_contact_mode == 0) {
+        dem_contact_integrate_kernel<RECORD><<<grid_for(b.n, 256), 256, 0, st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            b.dev_status, spec, ghist);
+    } else {
+        const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
+        dem_contact_column_kernel<RECORD><<<cols, kColThreads, kTileSlots * sizeof(float4), st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            b.dev_status, spec, ghist);
+    }
 }
 
 static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
@@ -504,11 +673,9 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
     if (record) {
         cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        if (g_contact_mode == 0) launch_contact_t<true, 0>(p, b, spec, ghist, st);
-        else launch_contact_t<true, 1>(p, b, spec, ghist, st);
+        launch_contact_t<true>(p, b, spec, ghist, st);
     } else {
-        if (g_contact_mode == 0) launch_contact_t<false, 0>(p, b, spec, ghist, st);
-        else launch_contact_t<false, 1>(p, b, spec, ghist, st);
+        launch_contact_t<false>(p, b, spec, ghist, st);
     }
     return cudaGetLastError();
 }

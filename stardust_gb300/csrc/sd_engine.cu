@@ -223,6 +223,7 @@ sd_status prepare_with(sd_engine* h, const float4* pos, const float4* vel, const
     if (h->device >= ndev) return fail(h, SD_ERR_INVALID_ARG, "cuda_device out of range");
     SD_CUDA(h, cudaSetDevice(h->device));
     SD_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    SD_CUDA(h, sd::dem_init_kernels());
     if ((s = allocate(h, n))) {
         release_device(h);
         return s;
@@ -284,6 +285,9 @@ sd_status errors_to_status(sd_engine* h, uint32_t bits) {
     if (bits & sd::kErrLookbackTimeout)
         return fail(h, SD_ERR_ITER_LIMIT, "device: a decoupled look-back wait hit its spin limit");
     if (bits & sd::kErrPairOverflow) return fail(h, SD_ERR_CAPACITY, "device: contact-pair buffer overflow");
+    if (bits & sd::kErrWaitTimeout)
+        return fail(h, SD_ERR_ITER_LIMIT, "device: a TMA tile wait hit its limit (the step used global loads)");
+    if (bits & sd::kErrBadInput) return fail(h, SD_ERR_INVALID_ARG, "device: a sphere's cell disagreed with its key");
     return SD_OK;
 }
 

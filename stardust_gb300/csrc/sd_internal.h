@@ -12,6 +12,7 @@ enum : uint32_t {
     kErrLookbackTimeout = 1u << 0,  // a decoupled look-back spin hit its limit
     kErrPairOverflow = 1u << 1,     // a pair buffer was too small
     kErrBadInput = 1u << 2,         // non-finite or out-of-range input seen
+    kErrWaitTimeout = 1u << 3,      // a bounded wait on a TMA copy gave up
 };
 
 // ---- radix sort (sd_sort.cu)
@@ -79,6 +80,7 @@ struct DemBuffers {
 };
 
 int dem_key_bits(uint32_t ncells);
+cudaError_t dem_init_kernels();  // once per device, outside stream capture
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
 cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);

@@ -47,7 +47,7 @@ def test_box_lattice_bit_exact(sdlib, orc, steps):
     eng.close()
 
 
-@pytest.mark.parametrize("contact_mode,sort_items", [(0, 8), (1, 16), (0, 16)])
+@pytest.mark.parametrize("contact_mode,sort_items", [(0, 8), (1, 16), (0, 16), (1, 8)])
 def test_every_knob_setting_is_bit_exact(sdlib, orc, contact_mode, sort_items):
     """The autotuner's choices change speed only: each contact-scan variant
     and sort tile size gives the same bits as the oracle."""
