@@ -217,10 +217,10 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  * (stardust_gb300.autotune) in place of the reference's hand block sweeps
  * (profiling/blocksweep*.txt).  Engines re-capture their step graph on the
  * next step after a change.  Knobs:
- *   "contact_mode"  0 = one thread per sphere, candidates read from global memory;
+ *   "contact_mode"  0 = one thread per sphere, candidates read through L1 (default);
  *                   1 = one CTA per grid column, neighbour columns staged in shared
- *                       memory by TMA bulk copies (default)
- *   "sort_items"    keys per thread of the sort's digit pass: 8 (default) or 16 */
+ *                       memory by TMA bulk copies
+ *   "sort_items"    keys per thread of the sort's digit pass: 8 or 16 (default) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

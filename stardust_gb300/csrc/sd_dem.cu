@@ -123,21 +123,21 @@ __device__ __forceinline__ void pair_contact(const DemParams& p, float dx, float
                      t);
 }
 
-// Where a kernel reads candidate positions from: slot s of column (X, Y)
-// is element s + delta(X, Y) of the source.
+// Where a kernel reads candidate positions from: slot s of the neighbour
+// column coded c = (dx+1)*3 + (dy+1) relative to the sphere's own column is
+// element s + delta_of(c) of the source.
 struct GlobalSource {
     const float4* __restrict__ pos;
-    __device__ __forceinline__ uint32_t delta(int32_t, int32_t) const { return 0u; }
+    __device__ __forceinline__ uint32_t delta_of(uint32_t, int32_t, int32_t) const { return 0u; }
     __device__ __forceinline__ float4 load(uint32_t k) const { return __ldg(&pos[k]); }
 };
 
+// Used only for spheres of the CTA's own column, so the sphere's column and
+// the tile's centre column coincide.
 struct TileSource {
     const float4* tile;     // staged slots of the 3x3 neighbour columns
     const uint32_t* shift;  // per neighbour column: tile offset - first slot (mod 2^32)
-    int32_t X, Y;           // the CTA's column
-    __device__ __forceinline__ uint32_t delta(int32_t x, int32_t y) const {
-        return shift[(x - X + 1) * 3 + (y - Y + 1)];
-    }
+    __device__ __forceinline__ uint32_t delta_of(uint32_t c, int32_t, int32_t) const { return shift[c]; }
     __device__ __forceinline__ float4 load(uint32_t k) const { return tile[k]; }
 };
 
@@ -176,7 +176,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
             const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
             const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
-            const uint32_t d = src.delta(X, Y);
+            const uint32_t d = src.delta_of((uint32_t)((X - cx + 1) * 3 + (Y - cy + 1)), cx, cy);
             uint32_t s = s0;
             // two candidates per iteration for load-level parallelism;
             // contacts are applied in slot order.  The sphere itself has
@@ -423,7 +423,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
         atomicOr(status, kErrWaitTimeout);
         use_tile = false;  // read global memory instead; same results
     }
-    const TileSource tile{s_tile, s_shift, X, Y};
+    const TileSource tile{s_tile, s_shift};
     const GlobalSource glob{pos};
     uint32_t contacts = 0;
     const uint32_t rounds = (own_cnt + blockDim.x - 1) / blockDim.x;
@@ -645,7 +645,7 @@ cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream
     return dem_reorder_async(b, st);
 }
 
-static int g_contact_mode = 1;  // 0: per slot, 1: TMA column tiles (default)
+static int g_contact_mode = 0;  // 0: per slot (default), 1: TMA column tiles
 
 void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
 int dem_contact_mode() { return g_contact_mode; }

@@ -33,6 +33,7 @@ constexpr int kSortWarps = kSortThreads / kWarp;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1;
+constexpr int kLookback = 8;  // predecessor statuses read per look-back round trip
 
 // Scratch layout (u32 words):
 //   [0]                 status word (error bits; never cleared by the sort)
@@ -176,28 +177,43 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
         carry_g += tot;
     }
 
-    // decoupled look-back, one digit per thread per q
+    // decoupled look-back, one digit per thread per q.  The statuses of the
+    // kLookback nearest unresolved predecessors are loaded together, so a
+    // chain of aggregates costs one round trip per kLookback tiles.
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
-        uint32_t d = threadIdx.x + q * kSortThreads;
+        const uint32_t d = threadIdx.x + q * kSortThreads;
         uint32_t excl = 0;
         if (tile > 0) {
+            const uint32_t* pass_status = scratch + kStatusOff + (uint64_t)pass * num_tiles * 512 + d;
             int64_t p = (int64_t)tile - 1;
             uint32_t spins = 0;
-            while (p >= 0) {
-                const uint32_t* ps = scratch + kStatusOff + ((uint64_t)pass * num_tiles + (uint64_t)p) * 512;
-                uint32_t v = ld_relaxed(&ps[d]);
-                if ((v & ~kCountMask) == 0u) {
+            while (true) {
+                uint32_t v[kLookback];
+#pragma unroll
+                for (int w = 0; w < kLookback; ++w)
+                    v[w] = p - w >= 0 ? ld_relaxed(pass_status + (uint64_t)(p - w) * 512) : kFlagInc;
+                bool done = false;
+                int used = 0;
+#pragma unroll
+                for (int w = 0; w < kLookback; ++w) {
+                    if ((v[w] & ~kCountMask) == 0u) break;  // not published yet: retry from here
+                    excl += v[w] & kCountMask;
+                    used = w + 1;
+                    if (v[w] & kFlagInc) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (done) break;
+                p -= used;
+                if (used == 0) {
                     if (++spins > kSpinLimit) {
                         atomicOr(&scratch[0], kErrLookbackTimeout);
                         break;
                     }
                     if (spins > 64) __nanosleep(32);
-                    continue;
                 }
-                excl += v & kCountMask;
-                if (v & kFlagInc) break;
-                --p;
             }
             st_relaxed(&status[d], kFlagInc | ((excl + cnt[q]) & kCountMask));
         }
@@ -241,7 +257,7 @@ static size_t pass_smem_bytes() {
 
 // Smallest tile the pass kernel is instantiated with; sizes the status area.
 constexpr int kSortItemsMin = 8;
-static int g_sort_items = 8;  // keys per thread of the pass kernel (8 or 16)
+static int g_sort_items = 16;  // keys per thread of the pass kernel (8 or 16)
 
 void sort_set_items(int items) { g_sort_items = items >= 16 ? 16 : 8; }
 int sort_items() { return g_sort_items; }
