@@ -264,6 +264,24 @@ sd_status sd_hash_sort_collision_list(uint32_t* d_cells, uint32_t* d_spheres,
  * the device error bits accumulated since the caller last zeroed it. */
 sd_status sd_sort_status(const void* d_scratch, void* stream, uint32_t* errors);
 
+/* sd_sort_pairs without a caller scratch buffer, for callers that cannot
+ * allocate device memory (a stepping loop that must never block on the
+ * device allocator, or a host that only hands over the key/value buffers it
+ * owns).  No counterpart in the reference, whose sort takes its radix
+ * buffers from the engine's allocations.  Allocates nothing: the scratch is
+ * a fixed 8 MiB array in the library's device memory, held on every GPU
+ * that loads the library until exit.  Sorts whose scratch need
+ * (sd_sort_scratch_bytes) exceeds 8 MiB return SD_ERR_CAPACITY -- up to
+ * 2,093,056 keys of 32 bits, 4,188,160 keys of at most 18 bits.  The first
+ * call on a device looks up the array's device address (make that first
+ * call before any stream capture).  All calls share the array, so calls
+ * that overlap on the GPU race; each call re-clears what must start at zero.
+ * Same result layout as sd_sort_pairs (sorted pairs in d_keys/d_vals);
+ * d_status, when not NULL, receives the device error bits (one u32). */
+sd_status sd_sort_pairs_noalloc(uint32_t* d_keys, uint32_t* d_vals, uint32_t* d_keys_tmp,
+                                uint32_t* d_vals_tmp, uint64_t n, int32_t key_bits,
+                                uint32_t* d_status, void* stream);
+
 /* Candidate pairs of SpatialPartition::tranverseAndResolveCollisionList
  * (collision_resolution.cu:100-199): over the first *d_count sorted
  * entries, every home entry pairs with every later entry of its cell run;

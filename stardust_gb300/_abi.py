@@ -132,6 +132,7 @@ SIGNATURES = {
     "sd_sort_pairs": [P, P, P, P, U64, I32, P, U64, P],
     "sd_hash_sort_collision_list": [P, P, P, P, U64, P, U64, P],
     "sd_sort_status": [P, P, C.POINTER(U32)],
+    "sd_sort_pairs_noalloc": [P, P, P, P, U64, I32, P, P],
     "sd_hash_candidate_pairs": [P, P, P, U32, P, P, P, U64, P, P, U64, P],
     "sd_hash_pairs_scratch_bytes": [U64, C.POINTER(U64)],
     "sd_scene_lattice": [I32, I32, I32, F32, F32, P, F32, F32, F32, U64, P, P],

@@ -305,6 +305,12 @@ struct SplitMix {
 
 }  // namespace
 
+namespace sd {
+// Records the message sd_last_error(NULL, ...) returns, for entry points
+// defined in other translation units.
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace sd
+
 // =================================================================== C ABI
 extern "C" {
 

@@ -4,7 +4,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace sd {
+
+void set_last_error(const std::string& msg);  // message for sd_last_error(NULL, ...)
 
 // Device-side error word bits (read back by the host through sd_engine_stats
 // or the raw API's status word); equal to the public SD_DEVERR_* values.
