@@ -1,0 +1,146 @@
+// ref_harness.cpp -- runs the reference's own kernels (test infrastructure).
+//
+// oracle/ref_build.py compiles the reference's kernel sources
+// (src/engine/cuda/sh_collision_detection.cu, collision_resolution.cu,
+// physics_update.cu) unchanged, where they lie, into sm_103a cubins in
+// oracle/_ref/.  This harness loads those cubins with the CUDA driver API and
+// launches the reference kernels with the reference's launch shapes, so the
+// CPU restatement in sd_oracle.c can be pinned against the reference's own
+// code (tests/golden/make_ref_golden.py writes the golden vectors).
+//
+// Only kernels that are deterministic and stay in bounds on the inputs the
+// golden script builds are exposed: the key/phantom construction, the run
+// traversal on inputs where every sphere sits in exactly one run (so the
+// reference's non-atomic force writes do not race), and the three
+// rigid-body kernels (one thread per body or sphere).
+#include <cuda.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct Kern {
+    const char* part;  // substring of the mangled name
+    const char* module;
+    CUfunction fn = nullptr;
+};
+
+Kern g_k[] = {
+    {"constructCollisionListCUDA", "sh_collision_detection"},
+    {"tranverseCollisionListCUDA", "collision_resolution"},
+    {"updateSphereDataCUDA", "physics_update"},
+    {"computeForcesAndTorquesCUDA", "physics_update"},
+    {"advectParticlesCUDA", "physics_update"},
+};
+constexpr int kConstruct = 0, kTraverse = 1, kUpdate = 2, kForces = 3, kAdvect = 4;
+
+std::string g_err;
+
+int fail(const char* what, CUresult r) {
+    const char* s = nullptr;
+    cuGetErrorString(r, &s);
+    g_err = std::string(what) + ": " + (s ? s : "?");
+    return 1;
+}
+
+int launch(int k, unsigned grid, unsigned block, unsigned smem, CUstream st, void** args) {
+    if (!g_k[k].fn) {
+        g_err = std::string("kernel not loaded: ") + g_k[k].part;
+        return 1;
+    }
+    CUresult r = cuLaunchKernel(g_k[k].fn, grid, 1, 1, block, 1, 1, smem, st, args, nullptr);
+    if (r != CUDA_SUCCESS) return fail("cuLaunchKernel", r);
+    r = cuStreamSynchronize(st);
+    if (r != CUDA_SUCCESS) return fail("cuStreamSynchronize", r);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_err.c_str(); }
+
+// Loads the three cubins from `dir` into the current context and finds the
+// kernels by name.
+int ref_init(const char* dir) {
+    const char* mods[] = {"sh_collision_detection", "collision_resolution", "physics_update"};
+    for (const char* m : mods) {
+        std::string path = std::string(dir) + "/" + m + ".cubin";
+        CUmodule mod;
+        CUresult r = cuModuleLoad(&mod, path.c_str());
+        if (r != CUDA_SUCCESS) return fail(path.c_str(), r);
+        unsigned count = 0;
+        if ((r = cuModuleGetFunctionCount(&count, mod)) != CUDA_SUCCESS) return fail("cuModuleGetFunctionCount", r);
+        std::vector<CUfunction> fns(count);
+        if ((r = cuModuleEnumerateFunctions(fns.data(), count, mod)) != CUDA_SUCCESS)
+            return fail("cuModuleEnumerateFunctions", r);
+        for (CUfunction f : fns) {
+            const char* name = nullptr;
+            if (cuFuncGetName(&name, f) != CUDA_SUCCESS || !name) continue;
+            for (Kern& k : g_k)
+                if (std::strcmp(k.module, m) == 0 && std::strstr(name, k.part)) k.fn = f;
+        }
+    }
+    for (Kern& k : g_k)
+        if (!k.fn) {
+            g_err = std::string("kernel not found: ") + k.part;
+            return 1;
+        }
+    return 0;
+}
+
+// constructCollisionListCUDA<<<16, tpb, tpb*4>>> (sh_collision_detection.cu:298);
+// d_temp[0] must be zero on entry (the reference memsets it, :296).
+int ref_construct(unsigned n, float cell_dim, CUdeviceptr cells, CUdeviceptr spheres, CUdeviceptr sizes,
+                  CUdeviceptr pos, CUdeviceptr d_temp, unsigned tpb, CUstream st) {
+    void* args[] = {&n, &cell_dim, &cells, &spheres, &sizes, &pos, &d_temp};
+    return launch(kConstruct, 16, tpb, tpb * 4, st, args);
+}
+
+// tranverseCollisionListCUDA, run by ONE thread.  Every thread of that
+// kernel reads the entry count from collision_count[0] and then zeroes it
+// (collision_resolution.cu:117-120), so a multi-thread launch races.  With
+// one block of one thread and threads_per_block = 1, the thread's chunk is
+// (count - 1) / 16 + 1 entries (the kernel divides by its 16 blocks), so the
+// caller stores 16 * count in d_temp[0]: the single thread then walks every
+// run in order.  It reads up to entry 16 * count, so cells/spheres must hold
+// at least 16 * count + 1 entries, padded with the sentinel key 0xffffffff.
+int ref_traverse_serial(CUdeviceptr cells, CUdeviceptr spheres, CUdeviceptr pos, CUdeviceptr vel,
+                        CUdeviceptr force, CUdeviceptr mass, CUdeviceptr size, CUdeviceptr rigid, unsigned n,
+                        CUdeviceptr d_temp, CUstream st) {
+    CUdeviceptr test_count = d_temp + 4;
+    int tpb = 1;
+    void* args[] = {&cells, &spheres, &pos, &vel, &force, &mass, &size, &rigid, &n, &d_temp, &test_count, &tpb};
+    return launch(kTraverse, 1, 1, 4, st, args);
+}
+
+// updateSphereDataCUDA<<<ceil(n/64), 64>>> (physics_update.cu:124-139).
+int ref_update_spheres(int n_spheres, int n_bodies, CUdeviceptr pos, CUdeviceptr vel, CUdeviceptr init_rel,
+                       CUdeviceptr rel, CUdeviceptr body_of, CUdeviceptr bpos, CUdeviceptr bvel, CUdeviceptr bquat,
+                       CUdeviceptr bomega, CUstream st) {
+    void* args[] = {&n_spheres, &n_bodies, &pos, &vel, &init_rel, &rel, &body_of, &bpos, &bvel, &bquat, &bomega};
+    return launch(kUpdate, (unsigned)(n_spheres + 63) / 64, 64, 0, st, args);
+}
+
+// computeForcesAndTorquesCUDA<<<ceil(nb/64), 64>>> (physics_update.cu:210-227).
+int ref_body_forces(int n_spheres, int n_bodies, CUdeviceptr bforce, CUdeviceptr btorque, CUdeviceptr bmass,
+                    CUdeviceptr start, CUdeviceptr length, CUdeviceptr rel, CUdeviceptr sforce, CUdeviceptr body_of,
+                    CUstream st) {
+    void* args[] = {&n_spheres, &n_bodies, &bforce, &btorque, &bmass, &start, &length, &rel, &sforce, &body_of};
+    return launch(kForces, (unsigned)(n_bodies + 63) / 64, 64, 0, st, args);
+}
+
+// advectParticlesCUDA<<<ceil(nb/64), 64>>> (physics_update.cu:329-347).
+int ref_advect(int n_spheres, int n_bodies, float dt, CUdeviceptr bpos, CUdeviceptr bvel, CUdeviceptr bomega,
+               CUdeviceptr bforce, CUdeviceptr btorque, CUdeviceptr bquat, CUdeviceptr bmass, CUdeviceptr lin,
+               CUdeviceptr ang, CUdeviceptr inertia, CUstream st) {
+    void* args[] = {&n_spheres, &n_bodies, &dt, &bpos, &bvel, &bomega, &bforce, &btorque, &bquat, &bmass,
+                    &lin, &ang, &inertia};
+    return launch(kAdvect, (unsigned)(n_bodies + 63) / 64, 64, 0, st, args);
+}
+
+}  // extern "C"

@@ -19,8 +19,12 @@
  *         (collision_resolution.cu:30-98, cuda_helpers.cuh:43-63)
  *       - rigid-body update kernels
  *         (src/engine/cuda/physics_update.cu:26-310, cuda_helpers.cuh:65-171)
- *     These are pinned against the reference's own kernel source compiled for
- *     the host (oracle/ref_emu), see tests/test_oracle_pin.py.
+ *     These are pinned against the reference's own kernels: oracle/ref_build.py
+ *     compiles the reference sources unchanged into sm_103a cubins,
+ *     oracle/ref_harness.cpp runs them on a GPU, tests/golden/make_ref_golden.py
+ *     stores their outputs in tests/golden/, and tests/test_oracle_ref.py
+ *     checks this restatement against them (keys bit-exact; traversal forces
+ *     and rigid-body kernels to 1e-6 relative).
  *
  *  2. physics: the per-step pipeline of the GPU engine (linear spring-dashpot
  *     with restitution damping, Coulomb friction, box walls, symplectic Euler)
