@@ -34,8 +34,12 @@ Kern g_k[] = {
     {"updateSphereDataCUDA", "physics_update"},
     {"computeForcesAndTorquesCUDA", "physics_update"},
     {"advectParticlesCUDA", "physics_update"},
+    {"RadixTabulateCUDA", "sh_collision_detection"},
+    {"RadixSumCUDA", "sh_collision_detection"},
+    {"RadixReorderCUDA", "sh_collision_detection"},
 };
-constexpr int kConstruct = 0, kTraverse = 1, kUpdate = 2, kForces = 3, kAdvect = 4;
+constexpr int kConstruct = 0, kTraverse = 1, kUpdate = 2, kForces = 3, kAdvect = 4, kTab = 5, kSum = 6,
+              kReorder = 7;
 
 std::string g_err;
 
@@ -46,14 +50,19 @@ int fail(const char* what, CUresult r) {
     return 1;
 }
 
-int launch(int k, unsigned grid, unsigned block, unsigned smem, CUstream st, void** args) {
+int launch_async(int k, unsigned grid, unsigned block, unsigned smem, CUstream st, void** args) {
     if (!g_k[k].fn) {
         g_err = std::string("kernel not loaded: ") + g_k[k].part;
         return 1;
     }
     CUresult r = cuLaunchKernel(g_k[k].fn, grid, 1, 1, block, 1, 1, smem, st, args, nullptr);
     if (r != CUDA_SUCCESS) return fail("cuLaunchKernel", r);
-    r = cuStreamSynchronize(st);
+    return 0;
+}
+
+int launch(int k, unsigned grid, unsigned block, unsigned smem, CUstream st, void** args) {
+    if (launch_async(k, grid, block, smem, st, args)) return 1;
+    CUresult r = cuStreamSynchronize(st);
     if (r != CUDA_SUCCESS) return fail("cuStreamSynchronize", r);
     return 0;
 }
@@ -141,6 +150,83 @@ int ref_advect(int n_spheres, int n_bodies, float dt, CUdeviceptr bpos, CUdevice
     void* args[] = {&n_spheres, &n_bodies, &dt, &bpos, &bvel, &bomega, &bforce, &btorque, &bquat, &bmass,
                     &lin, &ang, &inertia};
     return launch(kAdvect, (unsigned)(n_bodies + 63) / 64, 64, 0, st, args);
+}
+
+// Buffers of one step of the reference's spatial-hash path.
+struct RefStep {
+    unsigned n;            // spheres (one-sphere bodies)
+    float cell_dim;
+    CUdeviceptr cells, spheres, cells_tmp, spheres_tmp;  // 9n u32 each
+    CUdeviceptr radices, radix_sums;                     // 16*256*12 and 256 u32
+    CUdeviceptr d_temp;                                  // 2 u32
+    CUdeviceptr pos, vel, force, size, mass, rigid;      // spheres
+    CUdeviceptr init_rel, rel;                           // spheres
+    CUdeviceptr bpos, bvel, bomega, bforce, btorque, bquat, bmass, lin, ang, inertia, start, length;  // bodies
+    float dt;
+};
+
+// Enqueues one step of the reference's spatial-hash path on `st`, with the
+// reference's launch shapes: constructCollisionList
+// (sh_collision_detection.cu:285-306), sortCollisionList over the 9n
+// entries -- 4 passes of Tabulate/Sum/Reorder, 16 blocks of 192 threads
+// (:310-360), run as written -- tranverseAndResolveCollisionList
+// (collision_resolution.cu:201-231), then computeForcesAndTorques, advect and
+// updateSphereData (physics_update.cu).  Nothing is synchronised; the caller
+// times it with events on `st`.
+// Stage masks for ref_step_async: construct, sort, traverse, rigid-body.
+enum { kStageConstruct = 1, kStageSort = 2, kStageTraverse = 4, kStageRigid = 8 };
+
+int ref_stages_async(const RefStep* b, int stages, CUstream st);
+
+int ref_step_async(const RefStep* b, CUstream st) { return ref_stages_async(b, 15, st); }
+
+int ref_stages_async(const RefStep* b, int stages, CUstream st) {
+    unsigned n = b->n, entries = 9 * b->n;
+    int tpb = 128;
+    if (stages & kStageConstruct) {
+        if (cuMemsetD32Async(b->d_temp, 0, 2, st) != CUDA_SUCCESS) return fail("memset", CUDA_ERROR_UNKNOWN);
+        float cd = b->cell_dim;
+        CUdeviceptr c = b->cells, s = b->spheres, sz = b->size, p = b->pos, t = b->d_temp;
+        void* a[] = {&n, &cd, &c, &s, &sz, &p, &t};
+        if (launch_async(kConstruct, 16, tpb, tpb * 4, st, a)) return 1;
+    }
+    if (stages & kStageSort) {
+        unsigned cells_per_group = (entries - 1) / 16 / 12 + 1;
+        CUdeviceptr k = b->cells, v = b->spheres, kt = b->cells_tmp, vt = b->spheres_tmp;
+        CUdeviceptr rad = b->radices, sums = b->radix_sums;
+        for (int shift = 0; shift < 32; shift += 8) {
+            void* a1[] = {&k, &rad, &entries, &cells_per_group, &shift};
+            if (launch_async(kTab, 16, 12 * 16, 12 * 256 * 4, st, a1)) return 1;
+            void* a2[] = {&rad, &sums};
+            if (launch_async(kSum, 16, 12 * 16, 256 * 4, st, a2)) return 1;
+            void* a3[] = {&k, &v, &kt, &vt, &rad, &sums, &entries, &cells_per_group, &shift};
+            if (launch_async(kReorder, 16, 12 * 16, (256 + 12 * 256) * 4, st, a3)) return 1;
+            CUdeviceptr x = k; k = kt; kt = x;
+            x = v; v = vt; vt = x;
+        }
+    }
+    if (stages & kStageTraverse) {
+        CUdeviceptr c = b->cells, s = b->spheres, p = b->pos, v = b->vel, f = b->force, m = b->mass, sz = b->size,
+                    rg = b->rigid, t = b->d_temp, tc = b->d_temp + 4;
+        void* a[] = {&c, &s, &p, &v, &f, &m, &sz, &rg, &n, &t, &tc, &tpb};
+        if (launch_async(kTraverse, 16, tpb, tpb * 4, st, a)) return 1;
+    }
+    if (stages & kStageRigid) {
+        int ns = (int)n, nb = (int)n;
+        CUdeviceptr bf = b->bforce, bt = b->btorque, bm = b->bmass, s0 = b->start, ln = b->length, rl = b->rel,
+                    f = b->force, rg = b->rigid;
+        void* a[] = {&ns, &nb, &bf, &bt, &bm, &s0, &ln, &rl, &f, &rg};
+        if (launch_async(kForces, (n + 63) / 64, 64, 0, st, a)) return 1;
+        float dt = b->dt;
+        CUdeviceptr bp = b->bpos, bv = b->bvel, bw = b->bomega, bq = b->bquat, li = b->lin, an = b->ang,
+                    in = b->inertia;
+        void* a2[] = {&ns, &nb, &dt, &bp, &bv, &bw, &bf, &bt, &bq, &bm, &li, &an, &in};
+        if (launch_async(kAdvect, (n + 63) / 64, 64, 0, st, a2)) return 1;
+        CUdeviceptr p = b->pos, v = b->vel, ir = b->init_rel;
+        void* a3[] = {&ns, &nb, &p, &v, &ir, &rl, &rg, &bp, &bv, &bq, &bw};
+        if (launch_async(kUpdate, (n + 63) / 64, 64, 0, st, a3)) return 1;
+    }
+    return 0;
 }
 
 }  // extern "C"
