@@ -90,6 +90,7 @@ typedef struct sd_stats {
     double momentum[3];
     uint32_t device_errors;   /* OR of device error bits (see SD_DEVERR_*) */
     uint32_t n_cells;
+    uint64_t n_bodies;        /* rigid clumps */
 } sd_stats;
 
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
@@ -145,13 +146,26 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4,
                                 const float* vel4, const float* omega4);
 
 /* DEMEngine::add(DEMParticle(id, grid_resolution, size, diameter, mass,
- * position, velocity)) (entity.cpp:9-59, entity.hpp:24-32) for one-sphere
- * entities (grid_resolution 1): a free sphere of radius diameter/2 and the
- * given mass at `position`.  Multi-sphere entities return
- * SD_ERR_UNSUPPORTED. */
+ * position, velocity)) (entity.cpp:9-59, entity.hpp:24-32).  grid_resolution
+ * 1 adds a free sphere of radius diameter/2; larger values add the
+ * reference's cube clump as one rigid body: grid_resolution^3 spheres of
+ * radius diameter/2 at (i, j, k) * size / floor(size/diameter)^2,
+ * i, j, k = 1..grid_resolution, placed about `position` as
+ * setParticlesInWorldSpace does (world = position - (local - COM)), total
+ * mass `mass`. */
 sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float size,
                                  float diameter, float mass, const float position[3],
                                  const float velocity[3]);
+
+/* Adds one rigid body made of n spheres (the reference's DEMParticle, a
+ * clump of spheres integrated as one body, physics_update.cu).  rel4[i] =
+ * (x, y, z, r): sphere offsets from the body's centre of mass in the body
+ * frame (equal to the world frame at t = 0); com, vel: the body's centre and
+ * velocity; omega (may be NULL): angular velocity.  The body's inertia is
+ * that of its spheres as solid balls of mass/n each.  Spheres of one body
+ * do not collide with each other (collision_resolution.cu:69). */
+sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float mass,
+                              const float com[3], const float vel[3], const float omega[3]);
 
 /* DEMEngine::loadJSONSetup (engine.cpp:65-108, schema of
  * setup/star_test.json): scene.domain, scene.gravity (magnitude, along -z),
@@ -186,6 +200,19 @@ sd_status sd_engine_sync(sd_engine* h);
 /* Copies a field in ORIGINAL sphere order (the order spheres were added)
  * into host memory; bytes must be n_spheres * 16. */
 sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+typedef enum sd_body_field {
+    SD_BODY_POSITION = 0,   /* float4 (x, y, z, mass) of the centre of mass */
+    SD_BODY_VELOCITY = 1,   /* float4 (vx, vy, vz, 0) */
+    SD_BODY_QUATERNION = 2, /* float4 (s, x, y, z), body to world */
+    SD_BODY_OMEGA = 3,      /* float4 (wx, wy, wz, 0) */
+    SD_BODY_ANGMOM = 4,     /* float4 (Lx, Ly, Lz, 0), world frame */
+    SD_BODY_INV_INERTIA = 5 /* 3 float4 rows of the body-frame inverse inertia (12 floats) */
+} sd_body_field;
+
+/* Copies a rigid-body field into host memory (bodies in the order they
+ * were added); bytes must be n_bodies * 16 (48 for SD_BODY_INV_INERTIA). */
+sd_status sd_engine_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+
 /* Overwrites a field (POSITION, VELOCITY, OMEGA) from host memory in
  * original sphere order.  The engine re-sorts before the next step. */
 sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src, size_t bytes);

@@ -49,6 +49,10 @@ def lib() -> C.CDLL:
             "sdo_contact_integrate_f64": (C.c_uint64, [P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]),
             "sdo_contact_pairs": (C.c_uint64, [P, C.c_uint32, P, P, P, P, C.c_uint64]),
             "sdo_run": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_int]),
+            "sdo_contact_integrate_bodies": (C.c_uint64, [P, C.c_uint32] + [P] * 13),
+            "sdo_slot_of": (None, [C.c_uint32, P, P]),
+            "sdo_body_step": (None, [P, C.c_uint32] + [P] * 18),
+            "sdo_run_bodies": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_uint32] + [P] * 10),
             "sdo_num_threads": (C.c_int, []),
             "sdo_set_num_threads": (None, [C.c_int]),
         }
@@ -223,6 +227,27 @@ def run(p: Params, pos, vel, omg, steps: int, prepare_first: bool = True):
     if rc != 0:
         raise RuntimeError("oracle run failed")
     return pos, vel, omg
+
+
+def run_bodies(p: Params, pos, vel, omg, steps: int, bodies: dict, r0, body_of):
+    """sdo_run_bodies: rigid clumps plus free spheres.  `bodies` holds float32
+    arrays pos/vel/quat/omega/angmom (nb x 4), inv (nb x 3 x 4), first/count
+    (uint32); they are copied and the stepped copies returned with the
+    cell-sorted sphere state."""
+    pos = np.array(pos, np.float32, copy=True)
+    vel = np.array(vel, np.float32, copy=True)
+    omg = np.array(omg, np.float32, copy=True)
+    b = {k: np.array(bodies[k], np.float32, copy=True) for k in ("pos", "vel", "quat", "omega", "angmom", "inv")}
+    first = np.ascontiguousarray(bodies["first"], np.uint32)
+    count = np.ascontiguousarray(bodies["count"], np.uint32)
+    r0 = np.ascontiguousarray(r0, np.float32)
+    body_of = np.ascontiguousarray(body_of, np.int32)
+    rc = lib().sdo_run_bodies(C.byref(p), len(pos), _p(pos), _p(vel), _p(omg), steps, len(first), _p(b["pos"]),
+                              _p(b["vel"]), _p(b["quat"]), _p(b["omega"]), _p(b["angmom"]), _p(b["inv"]),
+                              _p(first), _p(count), _p(r0), _p(body_of))
+    if rc != 0:
+        raise RuntimeError("oracle run failed")
+    return pos, vel, omg, b
 
 
 def unsort(arr: np.ndarray, omg: np.ndarray) -> np.ndarray:

@@ -485,11 +485,22 @@ void sdo_sort_reorder(const sdo_params* p, uint32_t n,
     free(k);
 }
 
+static inline uint32_t bits_f32(float v) {
+    uint32_t b;
+    memcpy(&b, &v, 4);
+    return b;
+}
+/* the FP64 twin carries no sphere ids (no clumps in the error statement) */
+static inline uint32_t bits_f64(double v) {
+    (void)v;
+    return 0u;
+}
+
 /* The engine's contact law and integrator.  The operation order below is
  * the specification the CUDA kernels follow; it is written once as a macro
  * template and instantiated for float (the parity oracle) and double (the
  * error statement). */
-#define SDO_DEFINE_STEP(REAL, SQRT, FMIN, FMA, SUFFIX)                                           \
+#define SDO_DEFINE_STEP(REAL, SQRT, FMIN, FMA, BITS, SUFFIX)                                           \
 static inline void contact_response##SUFFIX(                                                 \
     const sdo_params* p, REAL nx, REAL ny, REAL nz, REAL delta,                              \
     REAL dvx, REAL dvy, REAL dvz, REAL wsx, REAL wsy, REAL wsz, REAL meff, REAL ri,          \
@@ -520,7 +531,8 @@ static inline void contact_response##SUFFIX(                                    
                                                                                              \
 static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,                   \
     const REAL* pos, const REAL* vel, const REAL* omg, const uint32_t* cell_start,           \
-    REAL* pos_n, REAL* vel_n, REAL* omg_n, uint32_t* keys_n, REAL* force4, REAL* torque4) {  \
+    REAL* pos_n, REAL* vel_n, REAL* omg_n, uint32_t* keys_n, REAL* force4, REAL* torque4,    \
+    const int32_t* body_of, REAL* sf4, REAL* st4) {                                          \
     uint64_t contacts = 0;                                                                   \
     _Pragma("omp parallel for schedule(dynamic, 1024) reduction(+:contacts)")               \
     for (int64_t i = 0; i < (int64_t)n; ++i) {                                               \
@@ -529,6 +541,8 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
         const REAL* wi = omg + 4 * i;                                                        \
         REAL xi = pi[0], yi = pi[1], zi = pi[2], ri = pi[3], mi = vi[3];                     \
         REAL f[3] = {0, 0, 0}, t[3] = {0, 0, 0};                                             \
+        const uint32_t idb = BITS(wi[3]);                                                    \
+        const int clump_i = body_of && (idb & 0x80000000u);                                  \
         int32_t cx = axis_cell((float)xi, p->lo[0], p->cell, p->nx);                         \
         int32_t cy = axis_cell((float)yi, p->lo[1], p->cell, p->ny);                         \
         int32_t cz = axis_cell((float)zi, p->lo[2], p->cell, p->nz);                         \
@@ -549,9 +563,15 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
                     REAL d2 = FMA(dz, dz, FMA(dy, dy, dx * dx));                             \
                     REAL rs = ri + pj[3];                                                    \
                     if (!(d2 < rs * rs) || d2 == (REAL)0) continue;                          \
-                    ++contacts;                                                              \
                     const REAL* vj = vel + 4 * (size_t)s;                                    \
                     const REAL* wj = omg + 4 * (size_t)s;                                    \
+                    if (clump_i) {                                                           \
+                        const uint32_t jdb = BITS(wj[3]);                                    \
+                        if ((jdb & 0x80000000u) &&                                           \
+                            body_of[idb & 0x7fffffffu] == body_of[jdb & 0x7fffffffu])        \
+                            continue;                                                        \
+                    }                                                                        \
+                    ++contacts;                                                              \
                     REAL rj = pj[3], mj = vj[3];                                             \
                     REAL dist = SQRT(d2);                                                    \
                     REAL inv = (REAL)1 / dist;                                               \
@@ -585,6 +605,12 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
                       force4[4*i+3] = 0; }                                                   \
         if (torque4) { torque4[4*i] = t[0]; torque4[4*i+1] = t[1]; torque4[4*i+2] = t[2];    \
                        torque4[4*i+3] = 0; }                                                 \
+        if (clump_i) {                                                                       \
+            /* a clump sphere hands its contact force and torque to its body */              \
+            sf4[4*i] = f[0]; sf4[4*i+1] = f[1]; sf4[4*i+2] = f[2]; sf4[4*i+3] = 0;           \
+            st4[4*i] = t[0]; st4[4*i+1] = t[1]; st4[4*i+2] = t[2]; st4[4*i+3] = 0;           \
+            continue;                                                                        \
+        }                                                                                    \
         REAL dt = (REAL)p->dt;                                                               \
         REAL nvx = vi[0] + dt * (f[0] / mi + (REAL)p->g[0]);                                 \
         REAL nvy = vi[1] + dt * (f[1] / mi + (REAL)p->g[1]);                                 \
@@ -603,8 +629,8 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
     return contacts;                                                                         \
 }
 
-SDO_DEFINE_STEP(float, sqrtf, fminf, fmaf, _f32)
-SDO_DEFINE_STEP(double, sqrt, fmin, fma, _f64)
+SDO_DEFINE_STEP(float, sqrtf, fminf, fmaf, bits_f32, _f32)
+SDO_DEFINE_STEP(double, sqrt, fmin, fma, bits_f64, _f64)
 
 uint64_t sdo_contact_integrate(const sdo_params* p, uint32_t n,
                                const float* pos, const float* vel, const float* omg,
@@ -612,7 +638,7 @@ uint64_t sdo_contact_integrate(const sdo_params* p, uint32_t n,
                                float* pos_n, float* vel_n, float* omg_n, uint32_t* keys_n,
                                float* force4, float* torque4) {
     return contact_integrate_f32(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                 keys_n, force4, torque4);
+                                 keys_n, force4, torque4, NULL, NULL, NULL);
 }
 
 uint64_t sdo_contact_integrate_f64(const sdo_params* p, uint32_t n,
@@ -621,7 +647,7 @@ uint64_t sdo_contact_integrate_f64(const sdo_params* p, uint32_t n,
                                    double* pos_n, double* vel_n, double* omg_n, uint32_t* keys_n,
                                    double* force4, double* torque4) {
     return contact_integrate_f64(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                 keys_n, force4, torque4);
+                                 keys_n, force4, torque4, NULL, NULL, NULL);
 }
 
 static int cmp_u64(const void* a, const void* b) {
@@ -697,5 +723,158 @@ int sdo_run(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg,
         sdo_sort_reorder(p, n, pn, vn, wn, keys, NULL, pos, vel, omg, cs);
     }
     free(pn); free(keys); free(cs);
+    return 0;
+}
+
+/* ------------------------------------------------------ rigid clumps ----- */
+
+uint64_t sdo_contact_integrate_bodies(const sdo_params* p, uint32_t n, const float* pos, const float* vel,
+                                      const float* omg, const uint32_t* cell_start, const int32_t* body_of,
+                                      float* pos_n, float* vel_n, float* omg_n, uint32_t* keys_n,
+                                      float* force4, float* torque4, float* sf4, float* st4) {
+    return contact_integrate_f32(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys_n, force4, torque4,
+                                 body_of, sf4, st4);
+}
+
+void sdo_slot_of(uint32_t n, const float* omg, uint32_t* slot_of) {
+    for (uint32_t k = 0; k < n; ++k) slot_of[bits_f32(omg[4 * (size_t)k + 3]) & 0x7fffffffu] = k;
+}
+
+/* Rotation matrix (row-major) of a unit quaternion (s, x, y, z). */
+static void quat_rot(float qs, float qx, float qy, float qz, float* R) {
+    R[0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+    R[1] = 2.0f * (qx * qy - qs * qz);
+    R[2] = 2.0f * (qx * qz + qs * qy);
+    R[3] = 2.0f * (qx * qy + qs * qz);
+    R[4] = 1.0f - 2.0f * (qx * qx + qz * qz);
+    R[5] = 2.0f * (qy * qz - qs * qx);
+    R[6] = 2.0f * (qx * qz - qs * qy);
+    R[7] = 2.0f * (qy * qz + qs * qx);
+    R[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
+}
+
+/* One step of every rigid body: gather its spheres' contact forces and
+ * torques (sphere-id order), gravity, symplectic Euler on momentum and
+ * angular momentum, w = R I0^-1 R^T L (physics_update.cu:264-279 with a
+ * proper inverse), normalised first-order quaternion update
+ * q' = normalize(q + dt/2 (0, w) (x) q), then the spheres' next state and
+ * cell keys.  binv12 holds I0^-1 as three rows of four floats. */
+void sdo_body_step(const sdo_params* p, uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4,
+                   float* bang4, const float* binv12, const uint32_t* first, const uint32_t* count,
+                   const float* r0_4, const uint32_t* slot_of, const float* pos, const float* omg,
+                   const float* sf4, const float* st4, float* pos_n, float* vel_n, float* omg_n,
+                   uint32_t* keys_n) {
+    for (uint32_t b = 0; b < nb; ++b) {
+        float* bp = bpos4 + 4 * (size_t)b;
+        float* bv = bvel4 + 4 * (size_t)b;
+        float* bq = bquat4 + 4 * (size_t)b;
+        float* bw = bomg4 + 4 * (size_t)b;
+        float* bl = bang4 + 4 * (size_t)b;
+        const float* I = binv12 + 12 * (size_t)b;
+        const float x = bp[0], y = bp[1], z = bp[2], m = bp[3];
+        float Fx = 0, Fy = 0, Fz = 0, Tx = 0, Ty = 0, Tz = 0;
+        for (uint32_t k = 0; k < count[b]; ++k) {
+            const uint32_t s = slot_of[first[b] + k];
+            const float* ps = pos + 4 * (size_t)s;
+            const float* fs = sf4 + 4 * (size_t)s;
+            const float* ts = st4 + 4 * (size_t)s;
+            const float rx = ps[0] - x, ry = ps[1] - y, rz = ps[2] - z;
+            Fx = Fx + fs[0];
+            Fy = Fy + fs[1];
+            Fz = Fz + fs[2];
+            Tx = Tx + (ry * fs[2] - rz * fs[1]);
+            Ty = Ty + (rz * fs[0] - rx * fs[2]);
+            Tz = Tz + (rx * fs[1] - ry * fs[0]);
+            Tx = Tx + ts[0];
+            Ty = Ty + ts[1];
+            Tz = Tz + ts[2];
+        }
+        const float dt = p->dt;
+        const float vx = bv[0] + dt * (Fx / m + p->g[0]);
+        const float vy = bv[1] + dt * (Fy / m + p->g[1]);
+        const float vz = bv[2] + dt * (Fz / m + p->g[2]);
+        const float nxp = x + dt * vx, nyp = y + dt * vy, nzp = z + dt * vz;
+        const float Lx = bl[0] + dt * Tx, Ly = bl[1] + dt * Ty, Lz = bl[2] + dt * Tz;
+        float R[9], A[9], W[9];
+        quat_rot(bq[0], bq[1], bq[2], bq[3], R);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+                A[3 * r + c] = (R[3 * r] * I[c] + R[3 * r + 1] * I[4 + c]) + R[3 * r + 2] * I[8 + c];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+                W[3 * r + c] = (A[3 * r] * R[3 * c] + A[3 * r + 1] * R[3 * c + 1]) + A[3 * r + 2] * R[3 * c + 2];
+        const float wx = (W[0] * Lx + W[1] * Ly) + W[2] * Lz;
+        const float wy = (W[3] * Lx + W[4] * Ly) + W[5] * Lz;
+        const float wz = (W[6] * Lx + W[7] * Ly) + W[8] * Lz;
+        const float qs = bq[0], qx = bq[1], qy = bq[2], qz = bq[3];
+        const float h = 0.5f * dt;
+        const float ds = -((wx * qx + wy * qy) + wz * qz);
+        const float dx = qs * wx + (wy * qz - wz * qy);
+        const float dy = qs * wy + (wz * qx - wx * qz);
+        const float dz = qs * wz + (wx * qy - wy * qx);
+        const float ns = qs + h * ds, nx = qx + h * dx, ny = qy + h * dy, nz = qz + h * dz;
+        const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
+        const float q0 = ns / nrm, q1 = nx / nrm, q2 = ny / nrm, q3 = nz / nrm;
+        quat_rot(q0, q1, q2, q3, R);
+        for (uint32_t k = 0; k < count[b]; ++k) {
+            const uint32_t id = first[b] + k, s = slot_of[id];
+            const float* r0 = r0_4 + 4 * (size_t)id;
+            const float rx = (R[0] * r0[0] + R[1] * r0[1]) + R[2] * r0[2];
+            const float ry = (R[3] * r0[0] + R[4] * r0[1]) + R[5] * r0[2];
+            const float rz = (R[6] * r0[0] + R[7] * r0[1]) + R[8] * r0[2];
+            float* po = pos_n + 4 * (size_t)s;
+            float* vo = vel_n + 4 * (size_t)s;
+            float* wo = omg_n + 4 * (size_t)s;
+            po[0] = nxp + rx;
+            po[1] = nyp + ry;
+            po[2] = nzp + rz;
+            po[3] = pos[4 * (size_t)s + 3];
+            vo[0] = vx + (wy * rz - wz * ry);
+            vo[1] = vy + (wz * rx - wx * rz);
+            vo[2] = vz + (wx * ry - wy * rx);
+            vo[3] = m;
+            wo[0] = wx;
+            wo[1] = wy;
+            wo[2] = wz;
+            wo[3] = omg[4 * (size_t)s + 3];
+            keys_n[s] = sdo_cell_key(p, po[0], po[1], po[2]);
+        }
+        bp[0] = nxp; bp[1] = nyp; bp[2] = nzp;
+        bv[0] = vx; bv[1] = vy; bv[2] = vz;
+        bl[0] = Lx; bl[1] = Ly; bl[2] = Lz;
+        bq[0] = q0; bq[1] = q1; bq[2] = q2; bq[3] = q3;
+        bw[0] = wx; bw[1] = wy; bw[2] = wz;
+    }
+}
+
+int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
+                   uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
+                   const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
+                   const int32_t* body_of) {
+    size_t nc = (size_t)p->nx * p->ny * p->nz;
+    float* buf = (float*)malloc(sizeof(float) * 20 * (size_t)(n ? n : 1));
+    uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    uint32_t* slot = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    uint32_t* cs = (uint32_t*)malloc(sizeof(uint32_t) * (nc + 1));
+    if (!buf || !keys || !slot || !cs) {
+        free(buf); free(keys); free(slot); free(cs);
+        return -1;
+    }
+    float *pn = buf, *vn = pn + 4 * (size_t)n, *wn = vn + 4 * (size_t)n, *sf = wn + 4 * (size_t)n,
+          *st = sf + 4 * (size_t)n;
+    memcpy(pn, pos, 16 * (size_t)n);
+    memcpy(vn, vel, 16 * (size_t)n);
+    memcpy(wn, omg, 16 * (size_t)n);
+    sdo_cell_keys(p, n, pos, keys);
+    sdo_sort_reorder(p, n, pn, vn, wn, keys, NULL, pos, vel, omg, cs);
+    sdo_slot_of(n, omg, slot);
+    for (int s = 0; s < steps; ++s) {
+        contact_integrate_f32(p, n, pos, vel, omg, cs, pn, vn, wn, keys, NULL, NULL, body_of, sf, st);
+        sdo_body_step(p, nb, bpos4, bvel4, bquat4, bomg4, bang4, binv12, first, count, r0_4, slot, pos, omg, sf,
+                      st, pn, vn, wn, keys);
+        sdo_sort_reorder(p, n, pn, vn, wn, keys, NULL, pos, vel, omg, cs);
+        sdo_slot_of(n, omg, slot);
+    }
+    free(buf); free(keys); free(slot); free(cs);
     return 0;
 }

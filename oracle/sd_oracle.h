@@ -156,6 +156,29 @@ uint64_t sdo_contact_pairs(const sdo_params* p, uint32_t n, const float* pos,
 int sdo_run(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg,
             int steps, int prepare);
 
+/* ---- rigid clumps (spheres whose id has bit 31 set belong to body
+ * body_of[id]; pairs within one body are skipped, collision_resolution.cu:69) */
+
+/* sdo_contact_integrate with clumps: a clump sphere's contact force and
+ * torque go to sf4/st4 (slot order) instead of being integrated. */
+uint64_t sdo_contact_integrate_bodies(const sdo_params* p, uint32_t n, const float* pos, const float* vel,
+                                      const float* omg, const uint32_t* cell_start, const int32_t* body_of,
+                                      float* pos_n, float* vel_n, float* omg_n, uint32_t* keys_n,
+                                      float* force4, float* torque4, float* sf4, float* st4);
+/* slot_of[id] = slot of every sphere of a cell-sorted state. */
+void sdo_slot_of(uint32_t n, const float* omg, uint32_t* slot_of);
+/* One step of every body and the next state of its spheres. */
+void sdo_body_step(const sdo_params* p, uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4,
+                   float* bang4, const float* binv12, const uint32_t* first, const uint32_t* count,
+                   const float* r0_4, const uint32_t* slot_of, const float* pos, const float* omg,
+                   const float* sf4, const float* st4, float* pos_n, float* vel_n, float* omg_n,
+                   uint32_t* keys_n);
+/* sdo_run with rigid bodies (state arrays and body arrays updated in place). */
+int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
+                   uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
+                   const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
+                   const int32_t* body_of);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int sdo_num_threads(void);
 void sdo_set_num_threads(int n);

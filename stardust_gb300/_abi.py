@@ -50,6 +50,14 @@ SD_STAGE_REORDER = 2
 SD_DEVERR_LOOKBACK_TIMEOUT = 0x1
 SD_DEVERR_PAIR_OVERFLOW = 0x2
 SD_DEVERR_BAD_INPUT = 0x4
+SD_DEVERR_WAIT_TIMEOUT = 0x8
+
+SD_BODY_POSITION = 0
+SD_BODY_VELOCITY = 1
+SD_BODY_QUATERNION = 2
+SD_BODY_OMEGA = 3
+SD_BODY_ANGMOM = 4
+SD_BODY_INV_INERTIA = 5
 
 
 class SdConfig(C.Structure):
@@ -82,6 +90,7 @@ class SdStats(C.Structure):
         ("momentum", C.c_double * 3),
         ("device_errors", C.c_uint32),
         ("n_cells", C.c_uint32),
+        ("n_bodies", C.c_uint64),
     ]
 
 
@@ -110,6 +119,8 @@ SIGNATURES = {
     "sd_last_error": [P, C.c_char_p, C.c_size_t],
     "sd_engine_add_spheres": [P, U64, P, P, P],
     "sd_engine_add_particle": [P, I32, F32, F32, F32, P, P],
+    "sd_engine_add_clump": [P, U32, P, F32, P, P, P],
+    "sd_engine_get_bodies": [P, I32, P, C.c_size_t],
     "sd_engine_load_scene_json": [P, C.c_char_p],
     "sd_engine_prepare": [P],
     "sd_engine_step": [P, F32, I32],

@@ -141,9 +141,26 @@ struct TileSource {
     __device__ __forceinline__ float4 load(uint32_t k) const { return tile[k]; }
 };
 
+// Rigid-clump context of the contact stage (all null without clumps).
+struct ClumpCtx {
+    const int32_t* __restrict__ body_of;  // per sphere id
+    float4* __restrict__ sf;               // per slot: force handed to the body
+    float4* __restrict__ st;               // per slot: torque handed to the body
+};
+
+// True when slot s holds a sphere of the same rigid body as the clump sphere
+// with id bits `idb` (such pairs are skipped, collision_resolution.cu:69).
+__device__ __forceinline__ bool same_body(const ClumpCtx& cc, uint32_t idb, const float4* __restrict__ omg,
+                                          uint32_t s) {
+    const uint32_t jdb = __float_as_uint(__ldg(reinterpret_cast<const float*>(omg) + 4 * (size_t)s + 3));
+    return (jdb & kClumpFlag) && cc.body_of[idb & kIdMask] == cc.body_of[jdb & kIdMask];
+}
+
 // Contacts of slot i over its candidate cells, then walls, integration and
-// the next-state write.  Returns the new cell key.
-template <bool RECORD, class SRC>
+// the next-state write.  Returns the new cell key; a clump sphere hands its
+// force and torque to its body instead (the body kernel writes its next
+// state and key) and *has_key is false.
+template <bool RECORD, bool CLUMPS, class SRC>
 __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                   const float4* __restrict__ omg,
@@ -151,9 +168,12 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   float4* __restrict__ pos_n, float4* __restrict__ vel_n,
                                                   float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
                                                   uint32_t* __restrict__ vals, float4* __restrict__ force,
-                                                  float4* __restrict__ torque, uint32_t& contacts) {
+                                                  float4* __restrict__ torque, uint32_t& contacts,
+                                                  const ClumpCtx& cc, bool* has_key) {
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
+    const uint32_t idb = __float_as_uint(wi.w);
+    const bool clump_i = CLUMPS && (idb & kClumpFlag);
     float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
     // The candidate cells: the 3x3x3 block around i's cell, cut per axis to
     // the cells a partner's centre can occupy, |x_j - x_i| < r_i + r_max
@@ -188,11 +208,11 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                 const float bx = pi.x - pb.x, by = pi.y - pb.y, bz = pi.z - pb.z;
                 const float da = dist2(ax, ay, az), db = dist2(bx, by, bz);
                 const float ra = ri + pa.w, rb = ri + pb.w;
-                if (da < ra * ra && da != 0.0f) {
+                if (da < ra * ra && da != 0.0f && !(clump_i && same_body(cc, idb, omg, s))) {
                     ++contacts;
                     pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
                 }
-                if (db < rb * rb && db != 0.0f) {
+                if (db < rb * rb && db != 0.0f && !(clump_i && same_body(cc, idb, omg, s + 1))) {
                     ++contacts;
                     pair_contact(p, bx, by, bz, db, rb, pb.w, ri, mi, vi, wi, vel, omg, s + 1, f, t);
                 }
@@ -202,7 +222,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                 const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
                 const float da = dist2(ax, ay, az);
                 const float ra = ri + pa.w;
-                if (da < ra * ra && da != 0.0f) {
+                if (da < ra * ra && da != 0.0f && !(clump_i && same_body(cc, idb, omg, s))) {
                     ++contacts;
                     pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
                 }
@@ -234,6 +254,13 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             torque[id] = make_float4(t.x, t.y, t.z, 0.0f);
         }
     }
+    if (clump_i) {
+        cc.sf[i] = make_float4(f.x, f.y, f.z, 0.0f);
+        cc.st[i] = make_float4(t.x, t.y, t.z, 0.0f);
+        *has_key = false;
+        return 0u;
+    }
+    *has_key = true;
     const float dt = p.dt;
     const float nvx = vi.x + dt * (f.x / mi + p.g[0]);
     const float nvy = vi.y + dt * (f.y / mi + p.g[1]);
@@ -295,7 +322,7 @@ __device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contac
 }
 
 // ---------------------------------------------- contact_mode 0: per slot
-template <bool RECORD>
+template <bool RECORD, bool CLUMPS>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -303,17 +330,19 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ vel_n, float4* __restrict__ omg_n,
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
-                             uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+                             uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
+                             ClumpCtx cc) {
     __shared__ uint32_t s_hist[kFusedPasses][512];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
+    bool has_key = false;
     if (i < n)
-        key = particle_step<RECORD>(p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                    keys, vals, force, torque, contacts);
+        key = particle_step<RECORD, CLUMPS>(p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
+                                    keys, vals, force, torque, contacts, cc, &has_key);
     if (ghist) {
         for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
         __syncthreads();
-        hist_add(s_hist, hist_spec, key, i < n);
+        hist_add(s_hist, hist_spec, key, has_key);
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
     }
@@ -371,14 +400,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint3
 // which one thread stages into shared memory with TMA bulk copies.  A CTA
 // whose neighbourhood exceeds kTileSlots reads global memory instead; the
 // results are the same either way.
-template <bool RECORD>
+template <bool RECORD, bool CLUMPS>
 __global__ void __launch_bounds__(kColThreads, 2)
 dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                           const float4* __restrict__ vel, const float4* __restrict__ omg,
                           const uint32_t* __restrict__ cell_start, float4* __restrict__ pos_n,
                           float4* __restrict__ vel_n, float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
                           uint32_t* __restrict__ vals, float4* __restrict__ force, float4* __restrict__ torque,
-                          uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+                          uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
+                          ClumpCtx cc) {
     extern __shared__ __align__(128) float4 s_tile[];
     __shared__ uint32_t s_hist[kFusedPasses][512];
     __shared__ __align__(8) unsigned long long s_bar;
@@ -431,6 +461,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
         const uint32_t k = r * blockDim.x + threadIdx.x;
         const bool valid = k < own_cnt;
         uint32_t key = 0;
+        bool has_key = false;
         if (valid) {
             const uint32_t i = own_beg + k;
             // The tile holds the neighbours of column (X, Y) only.  A sphere's
@@ -441,12 +472,12 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
             const bool mine = axis_cell(q.x, p.lo[0], p.cell, p.nx) == X && axis_cell(q.y, p.lo[1], p.cell, p.ny) == Y;
             if (!mine) atomicOr(status, kErrBadInput);
             key = (use_tile && mine)
-                      ? particle_step<RECORD>(p, n, i, tile, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
-                                              vals, force, torque, contacts)
-                      : particle_step<RECORD>(p, n, i, glob, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
-                                              vals, force, torque, contacts);
+                      ? particle_step<RECORD, CLUMPS>(p, n, i, tile, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
+                                              vals, force, torque, contacts, cc, &has_key)
+                      : particle_step<RECORD, CLUMPS>(p, n, i, glob, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys,
+                                              vals, force, torque, contacts, cc, &has_key);
         }
-        if (ghist) hist_add(s_hist, hist_spec, key, valid);
+        if (ghist) hist_add(s_hist, hist_spec, key, has_key);
     }
     if (ghist) {
         __syncthreads();
@@ -455,6 +486,117 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
     if (RECORD) count_contacts(status, contacts);
     // never leave with a bulk copy in flight into this CTA's shared memory
     if (staged && !use_tile && threadIdx.x == 0) mbar_wait_bounded(&s_bar, 0);
+}
+
+// Rotation matrix (row-major) of a unit quaternion (s, x, y, z).
+__device__ __forceinline__ void quat_rot(float qs, float qx, float qy, float qz, float* R) {
+    R[0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+    R[1] = 2.0f * (qx * qy - qs * qz);
+    R[2] = 2.0f * (qx * qz + qs * qy);
+    R[3] = 2.0f * (qx * qy + qs * qz);
+    R[4] = 1.0f - 2.0f * (qx * qx + qz * qz);
+    R[5] = 2.0f * (qy * qz - qs * qx);
+    R[6] = 2.0f * (qx * qz - qs * qy);
+    R[7] = 2.0f * (qy * qz + qs * qx);
+    R[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
+}
+
+// One thread per rigid body (replaces computeForcesAndTorquesCUDA +
+// advectParticlesCUDA + updateSphereDataCUDA, physics_update.cu:26-310):
+// gather the body's sphere forces and torques in sphere-id order (the
+// segmented reduction, no atomics), add gravity, integrate momentum and
+// angular momentum, w = R I0^-1 R^T L, normalised first-order quaternion
+// update, then write every sphere's next state and cell key (and its
+// histogram digits for the sort).
+__global__ void __launch_bounds__(128)
+dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __restrict__ bvel,
+                float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
+                const float4* __restrict__ binv, const uint32_t* __restrict__ bfirst,
+                const uint32_t* __restrict__ bcount, const float4* __restrict__ r0, const uint32_t* __restrict__ slot_of,
+                const float4* __restrict__ pos, const float4* __restrict__ omg, const float4* __restrict__ sf,
+                const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
+                float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
+                uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
+    const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
+    const uint32_t first = bfirst[b], cnt = bcount[b];
+    float Fx = 0, Fy = 0, Fz = 0, Tx = 0, Ty = 0, Tz = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t s = slot_of[first + k];
+        if (s >= n) continue;  // a consistent slot table never trips this
+        const float4 ps = pos[s], fs = sf[s], ts = st[s];
+        const float rx = ps.x - x, ry = ps.y - y, rz = ps.z - z;
+        Fx = Fx + fs.x;
+        Fy = Fy + fs.y;
+        Fz = Fz + fs.z;
+        Tx = Tx + (ry * fs.z - rz * fs.y);
+        Ty = Ty + (rz * fs.x - rx * fs.z);
+        Tz = Tz + (rx * fs.y - ry * fs.x);
+        Tx = Tx + ts.x;
+        Ty = Ty + ts.y;
+        Tz = Tz + ts.z;
+    }
+    const float dt = p.dt;
+    const float vx = bv.x + dt * (Fx / m + p.g[0]);
+    const float vy = bv.y + dt * (Fy / m + p.g[1]);
+    const float vz = bv.z + dt * (Fz / m + p.g[2]);
+    const float nxp = x + dt * vx, nyp = y + dt * vy, nzp = z + dt * vz;
+    const float Lx = bl.x + dt * Tx, Ly = bl.y + dt * Ty, Lz = bl.z + dt * Tz;
+    const float4 i0 = binv[3 * b], i1 = binv[3 * b + 1], i2 = binv[3 * b + 2];
+    const float I[12] = {i0.x, i0.y, i0.z, i0.w, i1.x, i1.y, i1.z, i1.w, i2.x, i2.y, i2.z, i2.w};
+    float R[9], A[9], W[9];
+    quat_rot(bq.x, bq.y, bq.z, bq.w, R);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A[3 * r + c] = (R[3 * r] * I[c] + R[3 * r + 1] * I[4 + c]) + R[3 * r + 2] * I[8 + c];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            W[3 * r + c] = (A[3 * r] * R[3 * c] + A[3 * r + 1] * R[3 * c + 1]) + A[3 * r + 2] * R[3 * c + 2];
+    const float wx = (W[0] * Lx + W[1] * Ly) + W[2] * Lz;
+    const float wy = (W[3] * Lx + W[4] * Ly) + W[5] * Lz;
+    const float wz = (W[6] * Lx + W[7] * Ly) + W[8] * Lz;
+    const float qs = bq.x, qx = bq.y, qy = bq.z, qz = bq.w;
+    const float h = 0.5f * dt;
+    const float ds = -((wx * qx + wy * qy) + wz * qz);
+    const float dx = qs * wx + (wy * qz - wz * qy);
+    const float dy = qs * wy + (wz * qx - wx * qz);
+    const float dz = qs * wz + (wx * qy - wy * qx);
+    const float ns = qs + h * ds, nx = qx + h * dx, ny = qy + h * dy, nz = qz + h * dz;
+    const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
+    const float q0 = ns / nrm, q1 = nx / nrm, q2 = ny / nrm, q3 = nz / nrm;
+    quat_rot(q0, q1, q2, q3, R);
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t id = first + k, s = slot_of[id];
+        if (s >= n) continue;
+        const float4 o = r0[id];
+        const float rx = (R[0] * o.x + R[1] * o.y) + R[2] * o.z;
+        const float ry = (R[3] * o.x + R[4] * o.y) + R[5] * o.z;
+        const float rz = (R[6] * o.x + R[7] * o.y) + R[8] * o.z;
+        const float4 po = make_float4(nxp + rx, nyp + ry, nzp + rz, pos[s].w);
+        pos_n[s] = po;
+        vel_n[s] = make_float4(vx + (wy * rz - wz * ry), vy + (wz * rx - wx * rz), vz + (wx * ry - wy * rx), m);
+        omg_n[s] = make_float4(wx, wy, wz, omg[s].w);
+        const uint32_t key = cell_key(p, po.x, po.y, po.z);
+        keys[s] = key;
+        vals[s] = s;
+        if (ghist) {
+            const int passes = (int)(hist_spec & 3u);
+            for (int q = 0; q < passes; ++q) {
+                const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
+                atomicAdd(&ghist[q * 512 + ((key >> shift) & ((1u << bits) - 1u))], 1u);
+            }
+        }
+    }
+    bpos[b] = make_float4(nxp, nyp, nzp, m);
+    bvel[b] = make_float4(vx, vy, vz, bv.w);
+    bang[b] = make_float4(Lx, Ly, Lz, bl.w);
+    bquat[b] = make_float4(q0, q1, q2, q3);
+    bomg[b] = make_float4(wx, wy, wz, 0.0f);
 }
 
 __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
@@ -478,7 +620,7 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
                    const uint32_t* __restrict__ vals, const float4* __restrict__ pos_n,
                    const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
                    float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
-                   uint32_t* __restrict__ cell_start) {
+                   uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
@@ -488,7 +630,11 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
         if (src < n) {  // always true for a valid permutation
             pos[k] = pos_n[src];
             vel[k] = vel_n[src];
-            omg[k] = omg_n[src];
+            const float4 o = omg_n[src];
+            omg[k] = o;
+            // clump spheres: where their body finds them next step
+            const uint32_t idb = __float_as_uint(o.w);
+            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
         }
         s_keys[threadIdx.x + 1] = keys[k];
     }
@@ -511,11 +657,13 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
 __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                                  const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
                                  unsigned long long* __restrict__ pairs, unsigned long long* __restrict__ npairs,
-                                 uint64_t cap, uint32_t* __restrict__ status) {
+                                 uint64_t cap, uint32_t* __restrict__ status, const int32_t* __restrict__ body_of) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 pi = pos[i];
-    const uint32_t idi = __float_as_uint(omg[i].w) & kIdMask;
+    const uint32_t idbi = __float_as_uint(omg[i].w);
+    const uint32_t idi = idbi & kIdMask;
+    const int32_t bi = (body_of && (idbi & kClumpFlag)) ? body_of[idi] : -1;
     const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
     const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
     const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
@@ -536,7 +684,9 @@ __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restri
                 const float d2 = dist2(dx, dy, dz);
                 const float rs = pi.w + pj.w;
                 if (!(d2 < rs * rs) || d2 == 0.0f) continue;
-                const uint32_t idj = __float_as_uint(omg[s].w) & kIdMask;
+                const uint32_t idbj = __float_as_uint(omg[s].w);
+                const uint32_t idj = idbj & kIdMask;
+                if (bi >= 0 && (idbj & kClumpFlag) && body_of[idj] == bi) continue;  // same rigid body
                 if (idi < idj) {
                     unsigned long long slot = atomicAdd(npairs, 1ull);
                     if (slot < cap) pairs[slot] = ((unsigned long long)idi << 32) | idj;
@@ -576,6 +726,7 @@ __global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, co
     double e = 0, px = 0, py = 0, pz = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i], w = omg[i], q = pos[i];
+        if (__float_as_uint(w.w) & kClumpFlag) continue;  // counted with its body
         double m = v.w, r = q.w;
         double I = 0.4 * m * r * r;
         e += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z) +
@@ -603,11 +754,15 @@ static inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + thre
 
 cudaError_t dem_init_kernels() {
     const int sm = (int)(kTileSlots * sizeof(float4));
-    cudaError_t e = cudaFuncSetAttribute(dem_contact_column_kernel<false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(dem_contact_column_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    return e;
+    const void* kernels[] = {(const void*)dem_contact_column_kernel<false, false>,
+                             (const void*)dem_contact_column_kernel<true, false>,
+                             (const void*)dem_contact_column_kernel<false, true>,
+                             (const void*)dem_contact_column_kernel<true, true>};
+    for (const void* k : kernels) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
@@ -634,7 +789,8 @@ cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
     dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
-        b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start);
+        b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
+        b.nb ? b.slot_of : nullptr);
     return cudaGetLastError();
 }
 
@@ -654,18 +810,32 @@ template <bool RECORD>
 static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st) {
     float4* f = RECORD ? b.force : nullptr;
     float4* t = RECORD ? b.torque : nullptr;
+    const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
+    const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
+    const size_t tile = kTileSlots * sizeof(float4);
     if (g_contact_mode == 0) {
-        dem_contact_integrate_kernel<RECORD><<<grid_for(b.n, 256), 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist);
+        if (b.nb)
+            dem_contact_integrate_kernel<RECORD, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc);
+        else
+            dem_contact_integrate_kernel<RECORD, false><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc);
     } else {
-        const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
-        dem_contact_column_kernel<RECORD><<<cols, kColThreads, kTileSlots * sizeof(float4), st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist);
+        if (b.nb)
+            dem_contact_column_kernel<RECORD, true><<<cols, kColThreads, tile, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc);
+        else
+            dem_contact_column_kernel<RECORD, false><<<cols, kColThreads, tile, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc);
     }
 }
 
+// Contact + integration of free spheres, then (with clumps) the body
+// kernel, which completes the next state and keys of the clump spheres.
 static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
                                   uint32_t* ghist, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
@@ -676,6 +846,11 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
         launch_contact_t<true>(p, b, spec, ghist, st);
     } else {
         launch_contact_t<false>(p, b, spec, ghist, st);
+    }
+    if (b.nb) {
+        dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
+            p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
+            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n, spec, ghist);
     }
     return cudaGetLastError();
 }
@@ -707,7 +882,7 @@ cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) 
     cudaError_t e = cudaMemsetAsync(b.npairs, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess || b.n == 0) return e;
     dem_pairs_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.omg, b.cell_start, b.pairs, b.npairs,
-                                                         b.pair_cap, b.dev_status);
+                                                         b.pair_cap, b.dev_status, b.nb ? b.body_of : nullptr);
     return cudaGetLastError();
 }
 

@@ -49,6 +49,12 @@ struct sd_engine {
 
     // host sphere set in insertion order; omega.w carries the id bits
     std::vector<float4> h_pos, h_vel, h_omg;
+    // rigid clumps: per body (centre, mass), v, q, w, L, inverse inertia rows,
+    // first sphere id and sphere count; per sphere id its body and offset
+    std::vector<float4> hb_pos, hb_vel, hb_quat, hb_omg, hb_ang, hb_inv;
+    std::vector<uint32_t> hb_first, hb_count;
+    std::vector<int32_t> h_body_of;
+    std::vector<float4> h_r0;
 
     bool prepared = false;
     int device = 0;
@@ -210,6 +216,29 @@ sd_status allocate(sd_engine* h, uint32_t n) {
     if ((s = dev_alloc(h, &B.pairs, (size_t)B.pair_cap)) || (s = dev_alloc(h, &B.npairs, 1))) return s;
     SD_CUDA(h, cudaMemsetAsync(B.dev_status, 0, 8 * sizeof(uint32_t), h->stream));
     SD_CUDA(h, cudaMemsetAsync(B.sort_scratch, 0, 16 * sizeof(uint32_t), h->stream));
+    const uint32_t nb = (uint32_t)h->hb_pos.size();
+    B.nb = nb;
+    if (nb) {
+        if ((s = dev_alloc(h, &B.body_of, n)) || (s = dev_alloc(h, &B.r0, n)) || (s = dev_alloc(h, &B.slot_of, n)) ||
+            (s = dev_alloc(h, &B.sf, n)) || (s = dev_alloc(h, &B.st, n)) || (s = dev_alloc(h, &B.bpos, nb)) ||
+            (s = dev_alloc(h, &B.bvel, nb)) || (s = dev_alloc(h, &B.bquat, nb)) || (s = dev_alloc(h, &B.bomg, nb)) ||
+            (s = dev_alloc(h, &B.bang, nb)) || (s = dev_alloc(h, &B.binv, 3 * (size_t)nb)) ||
+            (s = dev_alloc(h, &B.bfirst, nb)) || (s = dev_alloc(h, &B.bcount, nb)))
+            return s;
+        SD_CUDA(h, cudaMemcpyAsync(B.body_of, h->h_body_of.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.r0, h->h_r0.data(), 16 * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemsetAsync(B.sf, 0, 16 * (size_t)n, h->stream));
+        SD_CUDA(h, cudaMemsetAsync(B.st, 0, 16 * (size_t)n, h->stream));
+        SD_CUDA(h, cudaMemsetAsync(B.slot_of, 0xff, 4 * (size_t)n, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bpos, h->hb_pos.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bvel, h->hb_vel.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bquat, h->hb_quat.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bomg, h->hb_omg.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bang, h->hb_ang.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.binv, h->hb_inv.data(), 48 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bfirst, h->hb_first.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(B.bcount, h->hb_count.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, h->stream));
+    }
     return SD_OK;
 }
 
@@ -388,6 +417,65 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, con
         float4 w = omega4 ? f4(omega4 + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
         w.w = id_as_float(id);
         h->h_omg.push_back(w);
+        h->h_body_of.push_back(-1);
+        h->h_r0.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+    return SD_OK;
+}
+
+sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float mass, const float com[3],
+                              const float vel[3], const float omega[3]) {
+    if (!h || !rel4 || !com || !vel) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "bodies cannot be added after prepare");
+    if (n == 0) return fail(h, SD_ERR_INVALID_ARG, "a clump needs at least one sphere");
+    if (!(mass > 0.0f) || !std::isfinite(mass)) return fail(h, SD_ERR_INVALID_ARG, "clump mass must be > 0");
+    if (h->h_pos.size() + n >= 0x7fffffffull) return fail(h, SD_ERR_CAPACITY, "more than 2^31-1 spheres");
+    for (uint32_t i = 0; i < n; ++i)
+        if (!(rel4[4 * i + 3] > 0.0f) || !std::isfinite(rel4[4 * i]) || !std::isfinite(rel4[4 * i + 1]) ||
+            !std::isfinite(rel4[4 * i + 2]))
+            return fail(h, SD_ERR_INVALID_ARG, "clump sphere " + std::to_string(i) + ": bad offset or radius");
+    // inertia of the spheres as solid balls of mass/n about the centre, in
+    // double, and its inverse by cofactors
+    const double ms = (double)mass / n;
+    double I[9] = {0};
+    for (uint32_t i = 0; i < n; ++i) {
+        const double x = rel4[4 * i], y = rel4[4 * i + 1], z = rel4[4 * i + 2], r = rel4[4 * i + 3];
+        const double self = 0.4 * ms * r * r, d2 = x * x + y * y + z * z;
+        const double v[3] = {x, y, z};
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) I[3 * a + b] += ms * ((a == b ? d2 : 0.0) - v[a] * v[b]) + (a == b ? self : 0.0);
+    }
+    const double c00 = I[4] * I[8] - I[5] * I[7], c01 = I[5] * I[6] - I[3] * I[8], c02 = I[3] * I[7] - I[4] * I[6];
+    const double det = I[0] * c00 + I[1] * c01 + I[2] * c02;
+    if (!(det > 0.0)) return fail(h, SD_ERR_INVALID_ARG, "clump inertia is singular");
+    double inv[9] = {c00 / det, (I[2] * I[7] - I[1] * I[8]) / det, (I[1] * I[5] - I[2] * I[4]) / det,
+                     c01 / det, (I[0] * I[8] - I[2] * I[6]) / det, (I[2] * I[3] - I[0] * I[5]) / det,
+                     c02 / det, (I[1] * I[6] - I[0] * I[7]) / det, (I[0] * I[4] - I[1] * I[3]) / det};
+    const double w[3] = {omega ? omega[0] : 0.0, omega ? omega[1] : 0.0, omega ? omega[2] : 0.0};
+    const uint32_t b = (uint32_t)h->hb_pos.size();
+    h->hb_pos.push_back(make_float4(com[0], com[1], com[2], mass));
+    h->hb_vel.push_back(make_float4(vel[0], vel[1], vel[2], 0.f));
+    h->hb_quat.push_back(make_float4(1.f, 0.f, 0.f, 0.f));
+    h->hb_omg.push_back(make_float4((float)w[0], (float)w[1], (float)w[2], 0.f));
+    h->hb_ang.push_back(make_float4((float)(I[0] * w[0] + I[1] * w[1] + I[2] * w[2]),
+                                    (float)(I[3] * w[0] + I[4] * w[1] + I[5] * w[2]),
+                                    (float)(I[6] * w[0] + I[7] * w[1] + I[8] * w[2]), 0.f));
+    for (int r = 0; r < 3; ++r)
+        h->hb_inv.push_back(make_float4((float)inv[3 * r], (float)inv[3 * r + 1], (float)inv[3 * r + 2], 0.f));
+    h->hb_first.push_back((uint32_t)h->h_pos.size());
+    h->hb_count.push_back(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* r = rel4 + 4 * i;
+        const uint32_t id = (uint32_t)h->h_pos.size();
+        h->h_pos.push_back(make_float4(com[0] + r[0], com[1] + r[1], com[2] + r[2], r[3]));
+        const double sv[3] = {w[1] * r[2] - w[2] * r[1], w[2] * r[0] - w[0] * r[2], w[0] * r[1] - w[1] * r[0]};
+        h->h_vel.push_back(make_float4((float)(vel[0] + sv[0]), (float)(vel[1] + sv[1]), (float)(vel[2] + sv[2]), mass));
+        float4 o = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+        const uint32_t bits = id_bits(id) | 0x80000000u;
+        std::memcpy(&o.w, &bits, 4);
+        h->h_omg.push_back(o);
+        h->h_body_of.push_back((int32_t)b);
+        h->h_r0.push_back(make_float4(r[0], r[1], r[2], 0.f));
     }
     return SD_OK;
 }
@@ -395,12 +483,40 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, con
 sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float size, float diameter, float mass,
                                  const float position[3], const float velocity[3]) {
     if (!h || !position || !velocity) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
-    (void)size;
-    if (grid_resolution != 1)
-        return fail(h, SD_ERR_UNSUPPORTED, "multi-sphere entities (grid_resolution > 1) are not supported by this engine");
-    float p[4] = {position[0], position[1], position[2], 0.5f * diameter};
-    float v[4] = {velocity[0], velocity[1], velocity[2], mass};
-    return sd_engine_add_spheres(h, 1, p, v, nullptr);
+    if (grid_resolution < 1 || grid_resolution > 64) return fail(h, SD_ERR_INVALID_ARG, "grid_resolution must be 1..64");
+    if (!(diameter > 0.0f) || !(size > 0.0f)) return fail(h, SD_ERR_INVALID_ARG, "size and diameter must be > 0");
+    if (grid_resolution == 1) {
+        float p[4] = {position[0], position[1], position[2], 0.5f * diameter};
+        float v[4] = {velocity[0], velocity[1], velocity[2], mass};
+        return sd_engine_add_spheres(h, 1, p, v, nullptr);
+    }
+    // DEMParticle::initParticles / getCenterOfMass / setParticlesInWorldSpace
+    // (entity.cpp:9-59): spacing size / floor(size/diameter)^2, local sphere
+    // positions (i, j, k) * dx, world = position - (local - COM), so the
+    // offsets from the body centre (= position) are COM - local
+    const float q = std::floor(size / diameter);
+    const float num = q * q;
+    if (!(num > 0.0f)) return fail(h, SD_ERR_INVALID_ARG, "size smaller than diameter");
+    const float dx = size / num;
+    const int R = grid_resolution;
+    std::vector<float> local;
+    for (int i = 1; i <= R; ++i)
+        for (int j = 1; j <= R; ++j)
+            for (int k = 1; k <= R; ++k) {
+                local.push_back((float)i * dx);
+                local.push_back((float)j * dx);
+                local.push_back((float)k * dx);
+            }
+    double c[3] = {0, 0, 0};
+    const size_t cnt = local.size() / 3;
+    for (size_t s = 0; s < cnt; ++s)
+        for (int a = 0; a < 3; ++a) c[a] += local[3 * s + a];
+    std::vector<float> rel(4 * cnt);
+    for (size_t s = 0; s < cnt; ++s) {
+        for (int a = 0; a < 3; ++a) rel[4 * s + a] = (float)(c[a] / (double)cnt) - local[3 * s + a];
+        rel[4 * s + 3] = 0.5f * diameter;
+    }
+    return sd_engine_add_clump(h, (uint32_t)cnt, rel.data(), mass, position, velocity, nullptr);
 }
 
 static bool json_vec3(const sd::JsonValue* v, float out[3]) {
@@ -483,13 +599,21 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
         if (m->get("mu") && !json_num(m->get("mu"), &c.mu)) return fail(h, SD_ERR_JSON, "material.mu");
     }
     std::vector<float> pos, vel;
+    // cube clumps (grid_resolution > 1) are added after the plain spheres
+    // parsed before them, so ids follow the file order
+    struct Cube {
+        size_t after;  // number of plain spheres (x4 floats) parsed before it
+        int32_t res;
+        float size, diameter, mass, p3[3], v3[3];
+    };
+    std::vector<Cube> cubes;
     if (const sd::JsonValue* ents = scene->get("entities")) {
         if (ents->kind != sd::JsonValue::Array) return fail(h, SD_ERR_JSON, "scene.entities must be an array");
         for (size_t i = 0; i < ents->arr.size(); ++i) {
             const sd::JsonValue& e = ents->arr[i];
             std::string where = "scene.entities[" + std::to_string(i) + "]";
             if (e.kind != sd::JsonValue::Object) return fail(h, SD_ERR_JSON, where + " must be an object");
-            if (!keys_subset(e, {"type", "position", "size", "mass", "velocity"}, &bad))
+            if (!keys_subset(e, {"type", "position", "size", "mass", "velocity", "grid_resolution", "diameter"}, &bad))
                 return fail(h, SD_ERR_JSON, "unknown key " + where + "." + bad);
             const sd::JsonValue* t = e.get("type");
             if (!t || t->kind != sd::JsonValue::String || t->str != "generic")
@@ -500,6 +624,17 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
                 return fail(h, SD_ERR_JSON, where + ".velocity must be [vx,vy,vz]");
             if (!json_num(e.get("size"), &size) || !(size > 0)) return fail(h, SD_ERR_JSON, where + ".size must be > 0");
             if (!json_num(e.get("mass"), &mass) || !(mass > 0)) return fail(h, SD_ERR_JSON, where + ".mass must be > 0");
+            float res = 1.0f, diam = size;
+            if (e.get("grid_resolution") &&
+                (!json_num(e.get("grid_resolution"), &res) || res != std::floor(res) || res < 1.0f || res > 64.0f))
+                return fail(h, SD_ERR_JSON, where + ".grid_resolution must be an integer in 1..64");
+            if (e.get("diameter") && (!json_num(e.get("diameter"), &diam) || !(diam > 0) || diam > size))
+                return fail(h, SD_ERR_JSON, where + ".diameter must be in (0, size]");
+            if (res > 1.0f) {
+                cubes.push_back(Cube{pos.size(), (int32_t)res, size, diam, mass, {p3[0], p3[1], p3[2]},
+                                     {v3[0], v3[1], v3[2]}});
+                continue;
+            }
             float p4[4] = {p3[0], p3[1], p3[2], 0.5f * size}, v4[4] = {v3[0], v3[1], v3[2], mass};
             pos.insert(pos.end(), p4, p4 + 4);
             vel.insert(vel.end(), v4, v4 + 4);
@@ -521,8 +656,23 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
             vel.insert(vel.end(), v4, v4 + 4);
         }
     }
+    for (const Cube& cb : cubes) {
+        const float q = std::floor(cb.size / cb.diameter);
+        if (!(q >= 1.0f)) return fail(h, SD_ERR_JSON, "a cube entity's size is smaller than its diameter");
+    }
     h->cfg = c;
-    return sd_engine_add_spheres(h, pos.size() / 4, pos.data(), vel.data(), nullptr);
+    size_t done = 0;  // floats of `pos` added so far
+    for (const Cube& cb : cubes) {
+        if (cb.after > done) {
+            if (sd_status s = sd_engine_add_spheres(h, (cb.after - done) / 4, pos.data() + done, vel.data() + done,
+                                                    nullptr))
+                return s;
+            done = cb.after;
+        }
+        if (sd_status s = sd_engine_add_particle(h, cb.res, cb.size, cb.diameter, cb.mass, cb.p3, cb.v3)) return s;
+    }
+    if (pos.size() == done) return SD_OK;
+    return sd_engine_add_spheres(h, (pos.size() - done) / 4, pos.data() + done, vel.data() + done, nullptr);
 }
 
 sd_status sd_engine_prepare(sd_engine* h) {
@@ -664,6 +814,33 @@ sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
     }
 }
 
+sd_status sd_engine_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes) {
+    if (!h || !host_dst) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    const size_t nb = h->B.nb;
+    const float4* src = nullptr;
+    size_t per = 16;
+    switch (field) {
+        case SD_BODY_POSITION: src = h->B.bpos; break;
+        case SD_BODY_VELOCITY: src = h->B.bvel; break;
+        case SD_BODY_QUATERNION: src = h->B.bquat; break;
+        case SD_BODY_OMEGA: src = h->B.bomg; break;
+        case SD_BODY_ANGMOM: src = h->B.bang; break;
+        case SD_BODY_INV_INERTIA: src = h->B.binv; per = 48; break;
+        default: return fail(h, SD_ERR_INVALID_ARG, "unknown body field");
+    }
+    if (bytes != nb * per) return fail(h, SD_ERR_INVALID_ARG, "bytes must be n_bodies * " + std::to_string(per));
+    if (nb == 0) return SD_OK;
+    SD_CUDA(h, cudaSetDevice(h->device));
+    SD_CUDA(h, cudaMemcpyAsync(host_dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (field == SD_BODY_VELOCITY || field == SD_BODY_OMEGA || field == SD_BODY_ANGMOM) {
+        float4* o = static_cast<float4*>(host_dst);
+        for (size_t i = 0; i < nb; ++i) o[i].w = 0.0f;
+    }
+    return SD_OK;
+}
+
 sd_status sd_engine_device_ptr(sd_engine* h, int32_t field, void** out) {
     if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
@@ -724,6 +901,7 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
     if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     std::memset(out, 0, sizeof(*out));
     out->n_spheres = h->prepared ? h->B.n : h->h_pos.size();
+    out->n_bodies = h->hb_pos.size();
     out->steps = h->steps;
     if (!h->prepared) return SD_OK;
     SD_CUDA(h, cudaSetDevice(h->device));
@@ -737,12 +915,30 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
     unsigned long long np = 0;
     SD_CUDA(h, cudaMemcpyAsync(&np, h->B.npairs, 8, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    // bodies: the kernel above counted free spheres only
+    const size_t nb = h->B.nb;
+    if (nb) {
+        std::vector<float4> bp(nb), bv(nb), bw(nb), bl(nb);
+        SD_CUDA(h, cudaMemcpy(bp.data(), h->B.bpos, 16 * nb, cudaMemcpyDeviceToHost));
+        SD_CUDA(h, cudaMemcpy(bv.data(), h->B.bvel, 16 * nb, cudaMemcpyDeviceToHost));
+        SD_CUDA(h, cudaMemcpy(bw.data(), h->B.bomg, 16 * nb, cudaMemcpyDeviceToHost));
+        SD_CUDA(h, cudaMemcpy(bl.data(), h->B.bang, 16 * nb, cudaMemcpyDeviceToHost));
+        for (size_t b = 0; b < nb; ++b) {
+            const double m = bp[b].w;
+            e[0] += 0.5 * m * ((double)bv[b].x * bv[b].x + (double)bv[b].y * bv[b].y + (double)bv[b].z * bv[b].z) +
+                    0.5 * ((double)bw[b].x * bl[b].x + (double)bw[b].y * bl[b].y + (double)bw[b].z * bl[b].z);
+            e[1] += m * bv[b].x;
+            e[2] += m * bv[b].y;
+            e[3] += m * bv[b].z;
+        }
+    }
     out->kinetic_energy = e[0];
     out->momentum[0] = e[1];
     out->momentum[1] = e[2];
     out->momentum[2] = e[3];
     out->contacts = np;
     out->n_cells = h->B.ncells;
+    out->n_bodies = nb;
     uint32_t bits = 0;
     if ((s = read_device_errors(h, &bits))) return s;
     // a pair overflow from this stats pass is not an error of the run
@@ -770,10 +966,18 @@ sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
         SD_CUDA(h, cudaMemcpyAsync(buf.data() + n, h->B.vel, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
         SD_CUDA(h, cudaMemcpyAsync(buf.data() + 2 * (size_t)n, h->B.omg, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
     }
+    // rigid bodies: the moving state from the device, the constant tables
+    // (inverse inertia, sphere ranges, body of each sphere, offsets) from the host
+    const uint32_t nb = h->B.nb;
+    std::vector<float4> bstate(5 * (size_t)nb);
+    float4* const bsrc[5] = {h->B.bpos, h->B.bvel, h->B.bquat, h->B.bomg, h->B.bang};
+    for (int k = 0; k < 5 && nb; ++k)
+        SD_CUDA(h, cudaMemcpyAsync(bstate.data() + k * (size_t)nb, bsrc[k], 16 * (size_t)nb, cudaMemcpyDeviceToHost,
+                                   h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     std::ofstream f(path, std::ios::binary);
     if (!f) return fail(h, SD_ERR_IO, std::string("cannot write ") + path);
-    uint32_t ver = 1;
+    uint32_t ver = 2;
     f.write(kCkptMagic, 8);
     f.write(reinterpret_cast<const char*>(&ver), 4);
     f.write(reinterpret_cast<const char*>(&n), 4);
@@ -781,6 +985,15 @@ sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
     f.write(reinterpret_cast<const char*>(&h->cfg), sizeof(sd_config));
     f.write(reinterpret_cast<const char*>(&h->P), sizeof(sd::DemParams));
     f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(float4)));
+    f.write(reinterpret_cast<const char*>(&nb), 4);
+    if (nb) {
+        f.write(reinterpret_cast<const char*>(bstate.data()), (std::streamsize)(bstate.size() * sizeof(float4)));
+        f.write(reinterpret_cast<const char*>(h->hb_inv.data()), (std::streamsize)(h->hb_inv.size() * sizeof(float4)));
+        f.write(reinterpret_cast<const char*>(h->hb_first.data()), 4 * (std::streamsize)nb);
+        f.write(reinterpret_cast<const char*>(h->hb_count.data()), 4 * (std::streamsize)nb);
+        f.write(reinterpret_cast<const char*>(h->h_body_of.data()), 4 * (std::streamsize)n);
+        f.write(reinterpret_cast<const char*>(h->h_r0.data()), 16 * (std::streamsize)n);
+    }
     if (!f) return fail(h, SD_ERR_IO, "write failed");
     return SD_OK;
 }
@@ -800,14 +1013,49 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
     f.read(reinterpret_cast<char*>(&steps), 8);
     f.read(reinterpret_cast<char*>(&cfg), sizeof cfg);
     f.read(reinterpret_cast<char*>(&P), sizeof P);
-    if (!f || std::memcmp(magic, kCkptMagic, 8) != 0 || ver != 1)
+    if (!f || std::memcmp(magic, kCkptMagic, 8) != 0 || (ver != 1 && ver != 2))
         return fail(h, SD_ERR_IO, "not a stardust-gb300 checkpoint");
     std::vector<float4> buf(3 * (size_t)n);
     f.read(reinterpret_cast<char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(float4)));
     if (!f) return fail(h, SD_ERR_IO, "truncated checkpoint");
+    uint32_t nb = 0;
+    if (ver >= 2) f.read(reinterpret_cast<char*>(&nb), 4);
+    if (!f || nb > n) return fail(h, SD_ERR_IO, "truncated or corrupt checkpoint (bodies)");
+    std::vector<float4> bstate(5 * (size_t)nb), binv(3 * (size_t)nb), r0(nb ? n : 0);
+    std::vector<uint32_t> bfirst(nb), bcount(nb);
+    std::vector<int32_t> body_of(nb ? n : 0);
+    if (nb) {
+        f.read(reinterpret_cast<char*>(bstate.data()), (std::streamsize)(bstate.size() * sizeof(float4)));
+        f.read(reinterpret_cast<char*>(binv.data()), (std::streamsize)(binv.size() * sizeof(float4)));
+        f.read(reinterpret_cast<char*>(bfirst.data()), 4 * (std::streamsize)nb);
+        f.read(reinterpret_cast<char*>(bcount.data()), 4 * (std::streamsize)nb);
+        f.read(reinterpret_cast<char*>(body_of.data()), 4 * (std::streamsize)n);
+        f.read(reinterpret_cast<char*>(r0.data()), 16 * (std::streamsize)n);
+        if (!f) return fail(h, SD_ERR_IO, "truncated checkpoint (bodies)");
+        for (uint32_t b = 0; b < nb; ++b)
+            if ((uint64_t)bfirst[b] + bcount[b] > n || bcount[b] == 0) return fail(h, SD_ERR_IO, "corrupt body table");
+        for (uint32_t i = 0; i < n; ++i)
+            if (body_of[i] < -1 || body_of[i] >= (int32_t)nb) return fail(h, SD_ERR_IO, "corrupt body table");
+    }
     if (std::memcmp(&cfg, &h->cfg, sizeof cfg) != 0)
         return fail(h, SD_ERR_STATE, "checkpoint was written by an engine with a different config");
     release_device(h);
+    const size_t nbz = nb;
+    h->hb_pos.assign(bstate.begin(), bstate.begin() + nbz);
+    h->hb_vel.assign(bstate.begin() + nbz, bstate.begin() + 2 * nbz);
+    h->hb_quat.assign(bstate.begin() + 2 * nbz, bstate.begin() + 3 * nbz);
+    h->hb_omg.assign(bstate.begin() + 3 * nbz, bstate.begin() + 4 * nbz);
+    h->hb_ang.assign(bstate.begin() + 4 * nbz, bstate.begin() + 5 * nbz);
+    h->hb_inv = std::move(binv);
+    h->hb_first = std::move(bfirst);
+    h->hb_count = std::move(bcount);
+    if (nb) {
+        h->h_body_of = std::move(body_of);
+        h->h_r0 = std::move(r0);
+    } else {
+        h->h_body_of.assign(n, -1);
+        h->h_r0.assign(n, make_float4(0.f, 0.f, 0.f, 0.f));
+    }
     // host copy in original id order
     h->h_pos.assign(n, float4{});
     h->h_vel.assign(n, float4{});

@@ -81,7 +81,19 @@ struct DemBuffers {
     unsigned long long* npairs;
     uint64_t pair_cap;
     bool sorted_in_tmp;             // set by dem_sort_async: result in the *_tmp buffers
+    // rigid clumps (all null / 0 when the scene has none).  A clump sphere's
+    // id (omg.w bits) has bit 31 set.
+    uint32_t nb;                    // bodies
+    int32_t* body_of;               // per sphere id: its body, -1 for free spheres
+    float4* r0;                     // per sphere id: body-frame offset from the body's centre
+    uint32_t* slot_of;              // per sphere id: current slot (kept by the reorder)
+    float4 *sf, *st;                // per slot: contact force / torque of clump spheres
+    float4 *bpos, *bvel, *bquat, *bomg, *bang;  // per body: (x,y,z,m), v, q=(s,x,y,z), w, L
+    float4* binv;                   // per body: 3 rows of the body-frame inverse inertia
+    uint32_t *bfirst, *bcount;      // per body: first sphere id, number of spheres
 };
+
+constexpr uint32_t kClumpFlag = 0x80000000u;
 
 int dem_key_bits(uint32_t ncells);
 cudaError_t dem_init_kernels();  // once per device, outside stream capture

@@ -108,11 +108,36 @@ class DEMEngine:
         self._n += len(p)
 
     def add(self, grid_resolution: int, size: float, diameter: float, mass: float, position, velocity) -> None:
-        """DEMEngine::add(DEMParticle(...)) for one-sphere entities."""
+        """DEMEngine::add(DEMParticle(...)): one sphere, or a rigid cube clump
+        of floor(size/diameter)^2 spheres when grid_resolution > 1."""
         p = (C.c_float * 3)(*position)
         v = (C.c_float * 3)(*velocity)
         self._call("sd_engine_add_particle", grid_resolution, size, diameter, mass, p, v)
-        self._n += 1
+        self._n = int(self.stats()["n_spheres"])
+
+    def add_clump(self, rel4, mass: float, com, velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0)) -> None:
+        """One rigid body made of spheres (rel4 rows: body-frame offset from
+        the centre of mass, radius); the body's inertia is that of its
+        spheres as solid balls of mass/n each."""
+        r = _f32(rel4)
+        c = (C.c_float * 3)(*com)
+        v = (C.c_float * 3)(*velocity)
+        w = (C.c_float * 3)(*omega)
+        self._call("sd_engine_add_clump", len(r), r.ctypes.data, mass, c, v, w)
+        self._n += len(r)
+
+    @property
+    def n_bodies(self) -> int:
+        return int(self.stats()["n_bodies"])
+
+    def bodies(self, field: int) -> np.ndarray:
+        """Rigid-body field (SD_BODY_*), one float4 row per body (3 rows per
+        body for SD_BODY_INV_INERTIA)."""
+        nb = self.n_bodies
+        rows = 3 * nb if field == _abi.SD_BODY_INV_INERTIA else nb
+        out = np.empty((rows, 4), dtype=np.float32)
+        self._call("sd_engine_get_bodies", field, out.ctypes.data, out.nbytes)
+        return out
 
     def load_scene_json(self, path: str) -> None:
         self._call("sd_engine_load_scene_json", str(path).encode())
@@ -191,7 +216,7 @@ class DEMEngine:
         return {
             "n_spheres": s.n_spheres, "steps": s.steps, "contacts": s.contacts,
             "kinetic_energy": s.kinetic_energy, "momentum": tuple(s.momentum),
-            "device_errors": s.device_errors, "n_cells": s.n_cells,
+            "device_errors": s.device_errors, "n_cells": s.n_cells, "n_bodies": s.n_bodies,
         }
 
     def params(self) -> dict:

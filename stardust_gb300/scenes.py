@@ -62,3 +62,69 @@ def with_ids(omg: np.ndarray) -> np.ndarray:
     o = np.array(omg, np.float32, copy=True)
     o.view(np.uint32)[:, 3] = np.arange(len(o), dtype=np.uint32)
     return o
+
+
+def _rotation(rng: np.random.Generator) -> np.ndarray:
+    """A uniformly random rotation matrix (normalised Gaussian quaternion)."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    s, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - s * z), 2 * (x * z + s * y)],
+                     [2 * (x * y + s * z), 1 - 2 * (x * x + z * z), 2 * (y * z - s * x)],
+                     [2 * (x * z - s * y), 2 * (y * z + s * x), 1 - 2 * (x * x + y * y)]])
+
+
+# body-frame sphere offsets of the clump shapes, in units of the sphere radius
+CLUMP_SHAPES = {
+    "dumbbell": np.array([[-0.8, 0, 0], [0.8, 0, 0]]),
+    "triangle": np.array([[1.0, 0, 0], [-0.5, 0.866, 0], [-0.5, -0.866, 0]]),
+    "tetra": np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]]) * 0.6,
+    "cube": np.array([[i, j, k] for i in (-0.9, 0.9) for j in (-0.9, 0.9) for k in (-0.9, 0.9)]),
+}
+
+
+def clump_box(n_side: int = 8, free_fraction: float = 0.25, seed: int = 0, spacing: float = 5.0):
+    """Rigid clumps and free spheres in a walled box.
+
+    Slots of a jittered n_side^3 lattice (spacing x r; below about 5.2 the
+    clumps of neighbouring slots can start in contact) each hold either a
+    randomly oriented clump (dumbbell, triangle, tetrahedron or 2x2x2 cube of
+    spheres of radius r = 0.01 m, overlapping, mass = density x summed sphere
+    volumes) or, with probability free_fraction, one free sphere; velocities
+    U[-0.2, 0.2] m/s, clump spins U[-20, 20] rad/s; box material as
+    box_lattice.  Returns (clumps, free_pos4, free_vel4, EngineConfig, dt),
+    clumps a list of (rel4, mass, com, vel, omega)."""
+    rng = np.random.default_rng(seed)
+    r = R_BOX
+    spacing = spacing * r
+    edge = n_side * spacing + 2 * r
+    names = list(CLUMP_SHAPES)
+    clumps, fp, fv = [], [], []
+    vol = 4.0 / 3.0 * math.pi * r ** 3
+    for i in range(n_side):
+        for j in range(n_side):
+            for k in range(n_side):
+                c = np.array([i, j, k], float) * spacing + r + 0.5 * spacing
+                c += rng.uniform(-0.1 * r, 0.1 * r, 3)
+                v = rng.uniform(-0.2, 0.2, 3)
+                if rng.random() < free_fraction:
+                    fp.append([*c, r])
+                    fv.append([*v, DENSITY * vol])
+                    continue
+                off = CLUMP_SHAPES[names[rng.integers(len(names))]] * r
+                off = off @ _rotation(rng).T
+                off -= off.mean(axis=0)
+                rel = np.concatenate([off, np.full((len(off), 1), r)], axis=1).astype(np.float32)
+                clumps.append((rel, float(DENSITY * vol * len(off)), tuple(c), tuple(v),
+                               tuple(rng.uniform(-20.0, 20.0, 3))))
+    cfg = EngineConfig(box_lo=(0.0, 0.0, 0.0), box_hi=(edge, edge, edge), walls=0x3F, cell=2 * r,
+                       kn=1e5, restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81))
+    return (clumps, np.array(fp, np.float32).reshape(-1, 4), np.array(fv, np.float32).reshape(-1, 4), cfg, 1e-5)
+
+
+def add_clump_scene(eng, clumps, free_pos4, free_vel4) -> None:
+    """Adds clump_box's bodies (ids first, in order) then its free spheres."""
+    for rel, mass, com, vel, omega in clumps:
+        eng.add_clump(rel, mass, com, vel, omega)
+    if len(free_pos4):
+        eng.add_spheres(free_pos4, free_vel4)

@@ -61,13 +61,33 @@ def test_add_spheres_validates(sdlib):
     eng.close()
 
 
-def test_multi_sphere_particle_unsupported(sdlib):
+def test_cube_particle_is_a_clump(sdlib):
+    """DEMParticle(grid_resolution > 1) (entity.cpp:9-59): grid_resolution^3
+    spheres spaced size / floor(size/diameter)^2, one rigid body."""
     eng = sdlib.DEMEngine()
+    eng.add(2, 0.2, 0.1, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
+    st = eng.stats()
+    assert st["n_spheres"] == 8 and st["n_bodies"] == 1
+    eng.add(1, 0.1, 0.1, 3.0, (0.2, 0.2, 0.2), (0, 0, 0))
+    st = eng.stats()
+    assert st["n_spheres"] == 9 and st["n_bodies"] == 1
     with pytest.raises(sdlib.SdError) as e:
-        eng.add(2, 0.15, 0.15, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
-    assert e.value.status == sdlib._abi.SD_ERR_UNSUPPORTED
-    eng.add(1, 0.1, 0.1, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
-    assert eng.stats()["n_spheres"] == 1
+        eng.add(2, 0.05, 0.1, 3.0, (0.5, 0.5, 0.5), (0, 0, 0))
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    eng.close()
+
+
+def test_add_clump_validates(sdlib):
+    eng = sdlib.DEMEngine()
+    rel = np.array([[0.05, 0, 0, 0.05], [-0.05, 0, 0, 0.05]], np.float32)
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add_clump(rel, 0.0, (0.5, 0.5, 0.5))
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add_clump(np.array([[0, 0, 0, -1.0]], np.float32), 1.0, (0.5, 0.5, 0.5))
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    eng.add_clump(rel, 1.0, (0.5, 0.5, 0.5), (0, 0, 1.0), (0, 2.0, 0))
+    assert eng.stats()["n_bodies"] == 1 and eng.n == 2
     eng.close()
 
 
@@ -112,6 +132,31 @@ def test_reference_scene_json_loads(sdlib, tmp_path):
     assert p["gravity"] == pytest.approx((0, 0, -9.81))
     assert p["cell"] == pytest.approx(0.15)  # 2 x radius (diameter = size)
     eng.close()
+
+
+def test_scene_json_cube_entities(sdlib, tmp_path):
+    # a generic entity with grid_resolution > 1 is a DEMParticle cube clump;
+    # sphere ids follow the file order
+    scene = {"scene": {"domain": 2, "entities": [
+        {"type": "generic", "position": [0.5, 0.5, 0.5], "size": 0.1, "mass": 1},
+        {"type": "generic", "position": [1, 1, 1], "size": 0.2, "diameter": 0.1, "grid_resolution": 2, "mass": 3},
+        {"type": "generic", "position": [1.5, 1.5, 1.5], "size": 0.1, "mass": 1}]}}
+    f = tmp_path / "cubes.json"
+    f.write_text(json.dumps(scene))
+    eng = sdlib.DEMEngine()
+    eng.load_scene_json(f)
+    st = eng.stats()
+    assert st["n_spheres"] == 10 and st["n_bodies"] == 1 and eng.n == 10
+    eng.close()
+    bad = {"scene": {"entities": [{"type": "generic", "position": [0, 0, 0], "size": 0.1, "mass": 1,
+                                   "grid_resolution": 2.5}]}}
+    g = tmp_path / "bad_cube.json"
+    g.write_text(json.dumps(bad))
+    e2 = sdlib.DEMEngine()
+    with pytest.raises(sdlib.SdError) as e:
+        e2.load_scene_json(g)
+    assert e.value.status == sdlib._abi.SD_ERR_JSON and "grid_resolution" in str(e.value)
+    e2.close()
 
 
 def test_scene_json_extensions_and_errors(sdlib, tmp_path):
