@@ -231,6 +231,7 @@ class DEMEngine:
 
     def load_checkpoint(self, path: str) -> None:
         self._call("sd_engine_load_checkpoint", str(path).encode())
+        self._n = int(self.stats()["n_spheres"])
 
 
 def scene_lattice(nx, ny, nz, spacing, jitter, origin, radius, mass, vmax, seed):
