@@ -1,6 +1,7 @@
 """Builds the CPU oracle (test infrastructure only).
 
-``oracle/liboracle.so`` is the plain-C restatement in sd_oracle.c, compiled
+``oracle/liboracle.so`` is the plain-C restatement in sd_oracle.c and
+sd_oracle_hull.c, compiled
 with -ffp-contract=off so each float operation rounds once (matching the
 -fmad=false CUDA kernels).  Only tests/, __graft_entry__.smoke() and
 bench.py's CPU legs load it.
@@ -14,18 +15,18 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
-SRC = HERE / "sd_oracle.c"
+SRCS = [HERE / "sd_oracle.c", HERE / "sd_oracle_hull.c"]
 
 
 def build(verbose: bool = False) -> Path:
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         raise RuntimeError("no C compiler for the oracle")
-    deps = [SRC, HERE / "sd_oracle.h", Path(__file__)]
+    deps = SRCS + [HERE / "sd_oracle.h", Path(__file__)]
     if LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
     cmd = [cc, "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
-           "-fPIC", "-shared", "-o", str(LIB), str(SRC), "-lm"]
+           "-fPIC", "-shared", "-o", str(LIB)] + [str(s) for s in SRCS] + ["-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if verbose or r.returncode != 0:
         sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

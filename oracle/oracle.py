@@ -53,6 +53,12 @@ def lib() -> C.CDLL:
             "sdo_slot_of": (None, [C.c_uint32, P, P]),
             "sdo_body_step": (None, [P, C.c_uint32] + [P] * 18),
             "sdo_run_bodies": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_uint32] + [P] * 10),
+            "sdo_morton_ref": (None, [C.c_uint32, P, P, P, P, P]),
+            "sdo_aabb_pairs": (C.c_uint64, [C.c_uint32, P, P, P, C.c_uint64]),
+            "sdo_hull_aabbs": (None, [C.c_uint32, P, P, P, P, P, P, P, P]),
+            "sdo_gjk_epa": (None, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, P, P, P]),
+            "sdo_hull_partners": (C.c_int64, [C.c_uint32, P, P, P, P, C.c_uint64]),
+            "sdo_hull_step": (None, [P, C.c_uint32] + [P] * 17),
             "sdo_num_threads": (C.c_int, []),
             "sdo_set_num_threads": (None, [C.c_int]),
         }
@@ -250,8 +256,170 @@ def run_bodies(p: Params, pos, vel, omg, steps: int, bodies: dict, r0, body_of):
     return pos, vel, omg, b
 
 
+# ------------------------------------------------------------------ hulls
+class HullParams(C.Structure):
+    """sdo_hull_params (oracle/sd_oracle.h)."""
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("kn", C.c_float), ("damp", C.c_float),
+                ("mu", C.c_float), ("g", C.c_float * 3), ("dt", C.c_float), ("walls", C.c_int32)]
+
+
+def hull_params(lo, hi, kn, damp, mu, g, dt, walls) -> HullParams:
+    p = HullParams()
+    for a in range(3):
+        p.lo[a], p.hi[a], p.g[a] = lo[a], hi[a], g[a]
+    p.kn, p.damp, p.mu, p.dt, p.walls = kn, damp, mu, dt, walls
+    return p
+
+
+def morton_ref(lo4, hi4, glo, ghi):
+    lo4 = np.ascontiguousarray(lo4, np.float32)
+    hi4 = np.ascontiguousarray(hi4, np.float32)
+    out = np.empty(len(lo4), np.uint32)
+    lib().sdo_morton_ref(len(lo4), _p(lo4), _p(hi4), _p(np.asarray(glo, np.float32)),
+                         _p(np.asarray(ghi, np.float32)), _p(out))
+    return out
+
+
+def aabb_pairs(lo4, hi4):
+    lo4 = np.ascontiguousarray(lo4, np.float32)
+    hi4 = np.ascontiguousarray(hi4, np.float32)
+    n = lib().sdo_aabb_pairs(len(lo4), _p(lo4), _p(hi4), None, 0)
+    out = np.empty(max(n, 1), np.uint64)
+    lib().sdo_aabb_pairs(len(lo4), _p(lo4), _p(hi4), _p(out), n)
+    return out[:n].copy()
+
+
+class Hulls:
+    """Host copy of a hull scene (arrays as the oracle and the engine use them)."""
+
+    def __init__(self, pos, vel, quat, omg, ang, iinv, vstart, vcount, verts):
+        f = lambda a: np.ascontiguousarray(a, np.float32).copy()
+        self.pos, self.vel, self.quat, self.omg, self.ang, self.iinv = map(f, (pos, vel, quat, omg, ang, iinv))
+        self.vstart = np.ascontiguousarray(vstart, np.uint32)
+        self.vcount = np.ascontiguousarray(vcount, np.uint32)
+        self.verts = f(verts)
+
+    @property
+    def n(self):
+        return len(self.pos)
+
+    def copy(self):
+        return Hulls(self.pos, self.vel, self.quat, self.omg, self.ang, self.iinv, self.vstart, self.vcount,
+                     self.verts)
+
+    def aabbs(self):
+        lo = np.empty((self.n, 4), np.float32)
+        hi = np.empty((self.n, 4), np.float32)
+        ext = np.empty((self.n, 6), np.uint32)
+        lib().sdo_hull_aabbs(self.n, _p(self.pos), _p(self.quat), _p(self.vstart), _p(self.vcount),
+                             _p(self.verts), _p(lo), _p(hi), _p(ext))
+        return lo, hi, ext
+
+    def gjk_epa(self, a, b, seed=None):
+        si = np.zeros(3, np.int32)
+        res = np.zeros(10, np.float32)
+        sd = None if seed is None else np.asarray(seed, np.float32)
+        lib().sdo_gjk_epa(_p(self.pos), _p(self.quat), _p(self.iinv), _p(self.vstart), _p(self.vcount),
+                          _p(self.verts), int(a), int(b), _p(sd), _p(si), _p(res))
+        return {"status": int(si[0]), "iters": int(si[1]), "epa_iters": int(si[2]), "depth": float(res[0]),
+                "normal": res[1:4].copy(), "point": res[4:7].copy(), "dir": res[7:10].copy()}
+
+    def partners(self):
+        lo, hi, _ = self.aabbs()
+        off = np.empty(self.n + 1, np.uint32)
+        cap = 2 * len(aabb_pairs(lo, hi)) + 1
+        part = np.empty(cap, np.uint32)
+        m = lib().sdo_hull_partners(self.n, _p(lo), _p(hi), _p(off), _p(part), cap)
+        if m < 0:
+            raise RuntimeError("partner capacity")
+        return off, part[:m].copy()
+
+    def step(self, p: HullParams, off=None, partners=None, seeds=None, record=False):
+        """One step in place; returns per-entry (status, iters, dir) and per-body (force, torque)."""
+        if off is None:
+            off, partners = self.partners()
+        m = len(partners)
+        st = np.empty(max(m, 1), np.int32)
+        it = np.empty(max(m, 1), np.int32)
+        d4 = np.empty((max(m, 1), 4), np.float32)
+        f = np.empty((self.n, 4), np.float32) if record else None
+        t = np.empty((self.n, 4), np.float32) if record else None
+        sd = None if seeds is None else np.ascontiguousarray(seeds, np.float32)
+        lib().sdo_hull_step(C.byref(p), self.n, _p(self.pos), _p(self.vel), _p(self.quat), _p(self.omg),
+                            _p(self.ang), _p(self.iinv), _p(self.vstart), _p(self.vcount), _p(self.verts),
+                            _p(off), _p(partners), _p(sd), _p(st), _p(it), _p(d4), _p(f), _p(t))
+        return {"off": off, "partners": partners, "status": st[:m], "iters": it[:m], "dir": d4[:m], "force": f,
+                "torque": t}
+
+
 def unsort(arr: np.ndarray, omg: np.ndarray) -> np.ndarray:
     """Back to insertion order by the ids in omg.w."""
     out = np.empty_like(arr)
     out[ids_of(omg)] = arr
     return out
+
+
+def quat_from_matrix(R: np.ndarray) -> np.ndarray:
+    """(s, x, y, z) of a proper rotation matrix (Shepperd's method), s >= 0."""
+    t = np.trace(R)
+    if t > 0:
+        s = np.sqrt(t + 1.0) * 2
+        q = [0.25 * s, (R[2, 1] - R[1, 2]) / s, (R[0, 2] - R[2, 0]) / s, (R[1, 0] - R[0, 1]) / s]
+    elif R[0, 0] > R[1, 1] and R[0, 0] > R[2, 2]:
+        s = np.sqrt(1.0 + R[0, 0] - R[1, 1] - R[2, 2]) * 2
+        q = [(R[2, 1] - R[1, 2]) / s, 0.25 * s, (R[0, 1] + R[1, 0]) / s, (R[0, 2] + R[2, 0]) / s]
+    elif R[1, 1] > R[2, 2]:
+        s = np.sqrt(1.0 + R[1, 1] - R[0, 0] - R[2, 2]) * 2
+        q = [(R[0, 2] - R[2, 0]) / s, (R[0, 1] + R[1, 0]) / s, 0.25 * s, (R[1, 2] + R[2, 1]) / s]
+    else:
+        s = np.sqrt(1.0 + R[2, 2] - R[0, 0] - R[1, 1]) * 2
+        q = [(R[1, 0] - R[0, 1]) / s, (R[0, 2] + R[2, 0]) / s, (R[1, 2] + R[2, 1]) / s, 0.25 * s]
+    q = np.array(q)
+    q /= np.linalg.norm(q)
+    return q if q[0] >= 0 else -q
+
+
+def matrix_from_quat(q) -> np.ndarray:
+    s, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - s * z), 2 * (x * z + s * y)],
+                     [2 * (x * y + s * z), 1 - 2 * (x * x + z * z), 2 * (y * z - s * x)],
+                     [2 * (x * z - s * y), 2 * (y * z + s * x), 1 - 2 * (x * x + y * y)]])
+
+
+def hulls_from_points(points, pos, quat, vel, mass, omega=None) -> Hulls:
+    """Principal-frame hull bodies (numpy, FP64): centre of the points as
+    equal point masses, their inertia diagonalised, vertices in the principal
+    frame; the body's centre and orientation follow."""
+    n = len(points)
+    P = np.zeros((n, 4)); Q = np.zeros((n, 4)); V = np.zeros((n, 4)); W = np.zeros((n, 4))
+    Lw = np.zeros((n, 4)); Ii = np.zeros((n, 4))
+    vc, verts = [], []
+    for i in range(n):
+        p = np.asarray(points[i], np.float64)
+        c = p.mean(axis=0)
+        r = p - c
+        m = float(mass[i])
+        ms = m / len(p)
+        I = ms * ((r * r).sum() * np.eye(3) - r.T @ r)
+        lam, E = np.linalg.eigh(I)
+        if np.linalg.det(E) < 0:
+            E[:, 2] *= -1
+        lam = np.maximum(lam, 1e-3 * lam.max())
+        Ru = matrix_from_quat(quat[i])
+        Rw = Ru @ E
+        body = r @ E
+        P[i, :3] = np.asarray(pos[i]) + Ru @ c
+        P[i, 3] = m
+        Q[i] = quat_from_matrix(Rw)
+        V[i, :3] = vel[i]
+        w = np.zeros(3) if omega is None else np.asarray(omega[i], np.float64)
+        W[i, :3] = w
+        Lw[i, :3] = Rw @ (lam * (Rw.T @ w))
+        Ii[i, :3] = 1.0 / lam
+        Ii[i, 3] = np.linalg.norm(body, axis=1).max()
+        vc.append(len(p))
+        verts.extend(body.tolist())
+    vs = np.concatenate([[0], np.cumsum(vc)[:-1]]).astype(np.uint32)
+    v4 = np.zeros((len(verts), 4))
+    v4[:, :3] = verts
+    return Hulls(P, V, Q, W, Lw, Ii, vs, np.array(vc, np.uint32), v4)

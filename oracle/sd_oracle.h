@@ -179,6 +179,42 @@ int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, floa
                    const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
                    const int32_t* body_of);
 
+/* ------------------------------------------------------ convex hulls
+ * (sd_oracle_hull.c).  Bodies: pos4 (x, y, z, mass), vel4, quat4 (s, x, y, z),
+ * omg4, ang4 (world angular momentum), iinv4 (body-frame principal inverse
+ * inertia xyz, bounding radius w); vertices verts4 (body frame) at
+ * [vstart[b], vstart[b] + vcount[b]). */
+
+typedef struct sdo_hull_params {
+    float lo[3], hi[3];
+    float kn, damp, mu;
+    float g[3];
+    float dt;
+    int32_t walls;
+} sdo_hull_params;
+
+/* Reference Morton code of each box centroid (testLBVH.cu:113-151). */
+void sdo_morton_ref(uint32_t n, const float* lo4, const float* hi4, const float* glo, const float* ghi,
+                    uint32_t* codes);
+/* Exact closed-box overlap pair set, ascending u64 (i << 32 | j), i < j. */
+uint64_t sdo_aabb_pairs(uint32_t n, const float* lo4, const float* hi4, uint64_t* out, uint64_t cap);
+/* World AABBs of rotated hulls; ext6 (may be NULL): per body the vertex
+ * index of the min x, y, z and max x, y, z. */
+void sdo_hull_aabbs(uint32_t nb, const float* pos4, const float* quat4, const uint32_t* vstart,
+                    const uint32_t* vcount, const float* verts4, float* lo4, float* hi4, uint32_t* ext6);
+/* GJK + EPA of one pair A < B (seed NULL: x_A - x_B). */
+void sdo_gjk_epa(const float* pos4, const float* quat4, const float* iinv4, const uint32_t* vstart,
+                 const uint32_t* vcount, const float* verts4, uint32_t A, uint32_t B, const float* seed,
+                 int32_t* status_iters3, float* res10);
+/* Per-body candidate partner lists (CSR, ascending) from the AABB pairs. */
+int64_t sdo_hull_partners(uint32_t nb, const float* lo4, const float* hi4, uint32_t* off, uint32_t* partners,
+                          uint64_t cap);
+/* One hull step over given partner lists (state updated in place). */
+void sdo_hull_step(const sdo_hull_params* p, uint32_t nb, float* pos4, float* vel4, float* quat4, float* omg4,
+                   float* ang4, const float* iinv4, const uint32_t* vstart, const uint32_t* vcount,
+                   const float* verts4, const uint32_t* off, const uint32_t* partners, const float* seeds4,
+                   int32_t* status, int32_t* iters, float* dir4, float* force4, float* torque4);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int sdo_num_threads(void);
 void sdo_set_num_threads(int n);

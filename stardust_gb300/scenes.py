@@ -128,3 +128,54 @@ def add_clump_scene(eng, clumps, free_pos4, free_vel4) -> None:
         eng.add_clump(rel, mass, com, vel, omega)
     if len(free_pos4):
         eng.add_spheres(free_pos4, free_vel4)
+
+
+def _random_quats(rng: np.random.Generator, n: int) -> np.ndarray:
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1.0
+    return q
+
+
+def hull_box(n: int = 65_536, seed: int = 0, radius: float = 0.01, box=(1.0, 1.0, 1.0), vmax: float = 0.1,
+             spacing: float | None = None):
+    """Convex hulls dropped into a walled box.
+
+    Each hull is the convex hull of 8-32 points sampled on the unit sphere
+    with radial noise U[0.8, 1.2], scaled to `radius` (0.01 m: 0.02 m
+    across), a random unit-quaternion orientation, mass = DENSITY x the
+    volume of a sphere of the mean point radius.  Centres on a jittered
+    lattice (spacing 2.5 x radius by default) filling the box from the
+    floor up; velocities U[-vmax, vmax]; kn 1e5, restitution 0.5, mu 0.3,
+    dt 1e-5.  Returns (points list, pos (n,3), quat (n,4), vel (n,3), mass
+    (n,), EngineConfig, dt)."""
+    rng = np.random.default_rng(seed)
+    sp = spacing if spacing is not None else 2.5 * radius
+    dims = [max(1, int((box[a] - 2 * radius) // sp)) for a in range(3)]
+    if dims[0] * dims[1] * dims[2] < n:
+        raise ValueError("box too small for n hulls at this spacing")
+    pts, centres = [], []
+    k = 0
+    for iz in range(dims[2]):
+        for iy in range(dims[1]):
+            for ix in range(dims[0]):
+                if k == n:
+                    break
+                centres.append([radius + (ix + 0.5) * sp, radius + (iy + 0.5) * sp, radius + (iz + 0.5) * sp])
+                k += 1
+    pos = np.array(centres) + rng.uniform(-0.05 * radius, 0.05 * radius, (n, 3))
+    mass = np.empty(n)
+    for i in range(n):
+        m = int(rng.integers(8, 33))
+        d = rng.normal(size=(m, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        p = d * rng.uniform(0.8, 1.2, (m, 1)) * radius
+        pts.append(p.astype(np.float32))
+        rm = float(np.linalg.norm(p, axis=1).mean())
+        mass[i] = DENSITY * 4.0 / 3.0 * math.pi * rm ** 3
+    quat = _random_quats(rng, n)
+    vel = rng.uniform(-vmax, vmax, (n, 3))
+    cfg = EngineConfig(box_lo=(0.0, 0.0, 0.0), box_hi=tuple(box), walls=0x3F, cell=4 * radius, kn=1e5,
+                       restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81))
+    return pts, pos.astype(np.float32), quat.astype(np.float32), vel.astype(np.float32), mass.astype(np.float32), \
+        cfg, 1e-5
