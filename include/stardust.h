@@ -90,7 +90,12 @@ typedef struct sd_stats {
     double momentum[3];
     uint32_t device_errors;   /* OR of device error bits (see SD_DEVERR_*) */
     uint32_t n_cells;
-    uint64_t n_bodies;        /* rigid clumps */
+    uint64_t n_bodies;        /* rigid clumps, or convex hulls */
+    /* convex-hull scenes, last step: candidate pairs (AABB overlaps), GJK
+     * support evaluations and EPA iterations summed over them */
+    uint64_t gjk_pairs;
+    uint64_t gjk_iters;
+    uint64_t epa_iters;
 } sd_stats;
 
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
@@ -206,12 +211,75 @@ typedef enum sd_body_field {
     SD_BODY_QUATERNION = 2, /* float4 (s, x, y, z), body to world */
     SD_BODY_OMEGA = 3,      /* float4 (wx, wy, wz, 0) */
     SD_BODY_ANGMOM = 4,     /* float4 (Lx, Ly, Lz, 0), world frame */
-    SD_BODY_INV_INERTIA = 5 /* 3 float4 rows of the body-frame inverse inertia (12 floats) */
+    SD_BODY_INV_INERTIA = 5, /* clumps: 3 float4 rows of the body-frame inverse inertia (12 floats) */
+    SD_BODY_HULL_INV_INERTIA = 6, /* hulls: (1/Ix, 1/Iy, 1/Iz, bounding radius), principal frame */
+    SD_BODY_FORCE = 7,      /* hulls, SD_FLAG_RECORD: total force of the last step */
+    SD_BODY_TORQUE = 8      /* hulls, SD_FLAG_RECORD: total torque of the last step */
 } sd_body_field;
 
 /* Copies a rigid-body field into host memory (bodies in the order they
  * were added); bytes must be n_bodies * 16 (48 for SD_BODY_INV_INERTIA). */
 sd_status sd_engine_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+
+/* ------------------------------------------------------ convex hulls
+ * A scene holds either spheres and clumps or convex hulls.  Hull scenes
+ * step through: world AABBs, an LBVH broad phase (sandbox/testLBVH.cu),
+ * GJK + EPA per candidate pair (sandbox/testGJK.cu:52-315 plus a
+ * penetration depth), the spring-dashpot law at the EPA contact point, and
+ * quaternion integration with a diagonal body-frame inertia. */
+
+/* One hull: the convex hull of n_points points (pts4 rows x, y, z, unused,
+ * in the body's local frame placed at pos with orientation quat (s, x, y, z),
+ * NULL = identity).  The centre of mass is the mean of the points and the
+ * inertia that of the points as equal masses; both are reduced to a
+ * principal frame.  No counterpart in the reference (its Hull struct,
+ * sandbox/primitives.hpp:37-57, is filled by hand in testGJK.cu:328-352). */
+sd_status sd_engine_add_hull(sd_engine* h, uint32_t n_points, const float* pts4, float mass,
+                             const float pos[3], const float quat[4], const float vel[3],
+                             const float omega[3]);
+
+/* The stored shapes: per hull its first vertex and vertex count, and the
+ * principal-frame vertices (float4 rows); *n_verts = total vertex count. */
+sd_status sd_engine_get_hull_shapes(sd_engine* h, uint32_t* vstart, uint32_t* vcount, float* verts4,
+                                    uint64_t verts_cap, uint64_t* n_verts);
+
+/* GJK seed of a candidate pair.  PLAIN: x_A - x_B, the reference seed
+ * (testGJK.cu:266).  PREVIOUS: the pair's final search direction of the
+ * previous step (in A's body frame) when it was separated then.  LEARNED:
+ * the warm-start network's direction for pairs seen in the previous step.
+ * GJK always runs to its own termination test, and a seeded run that does
+ * not converge is rerun from the plain seed, so the seed changes only the
+ * iteration count. */
+#define SD_GJK_SEED_PLAIN 0
+#define SD_GJK_SEED_LEARNED 1
+#define SD_GJK_SEED_PREVIOUS 2
+sd_status sd_engine_set_gjk_seed(sd_engine* h, int32_t mode);
+
+/* The candidate entries of the last step: off[n_bodies+1] (CSR), partner
+ * ids (ascending per body), info (status | GJK iterations << 8 | EPA
+ * iterations << 16; status 0 separated, 1 intersecting, 2 touching,
+ * 3 not converged), final GJK direction in A's frame (w = 1 when separated),
+ * the seeds used (w = 1 when seeded) and the 16 network inputs.  Any output
+ * may be NULL; *n_entries receives the count. */
+sd_status sd_engine_hull_entries(sd_engine* h, uint32_t* off, uint32_t* partners, uint32_t* info, float* dir4,
+                                 float* seed4, float* feat16, uint64_t cap, uint64_t* n_entries);
+
+/* ------------------------------------------------------ LBVH operators
+ * (sandbox/testLBVH.cu:42-907 as raw device operators).  Boxes are float4
+ * rows lo (x, y, z, -) and hi, 16-byte aligned, n < 2^30. */
+
+/* Device scratch for sd_lbvh_pairs / sd_lbvh_morton. */
+sd_status sd_lbvh_scratch_bytes(uint64_t n, uint64_t pair_cap, uint64_t* bytes);
+/* Every pair (i < j) of overlapping closed boxes, ascending u64
+ * (i << 32 | j).  d_count[0] = number of pairs (written up to cap),
+ * d_count[1] = device error bits (SD_DEVERR_PAIR_OVERFLOW when the partner
+ * lists exceeded 2 * cap entries). */
+sd_status sd_lbvh_pairs(uint64_t n, const float* d_lo4, const float* d_hi4, uint64_t* d_pairs, uint64_t cap,
+                        uint32_t* d_count, void* d_scratch, uint64_t scratch_bytes, void* stream);
+/* The reference's 30-bit Morton code of each box centroid relative to the
+ * boxes' global bounds (computeSpaceFillingCurveCUDA, testLBVH.cu:113-151). */
+sd_status sd_lbvh_morton(uint64_t n, const float* d_lo4, const float* d_hi4, uint32_t* d_codes, void* d_scratch,
+                         uint64_t scratch_bytes, void* stream);
 
 /* Overwrites a field (POSITION, VELOCITY, OMEGA) from host memory in
  * original sphere order.  The engine re-sorts before the next step. */

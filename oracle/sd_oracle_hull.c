@@ -90,7 +90,7 @@ void sdo_morton_ref(uint32_t n, const float* lo4, const float* hi4, const float*
         int32_t q[3];
         for (int a = 0; a < 3; ++a) {
             const float c = (lo4[4 * (size_t)i + a] + hi4[4 * (size_t)i + a]) * 0.5f;
-            const float p = (c - cen[a]) / cell[a];
+            const float p = cell[a] > 0.0f ? (c - cen[a]) / cell[a] : 0.0f;
             int32_t d = p >= 0.0f ? (int32_t)p : (int32_t)floorf(p);
             d = d < -512 ? -512 : (d > 511 ? 511 : d);
             q[a] = d + 512;
@@ -555,30 +555,37 @@ static void hull_contact_force(const sdo_hull_params* p, float delta, v3 m, v3 v
 
 /* Narrow phase + contact force of one directed entry (self, other).  The
  * pair is always evaluated as (A, B) = (min, max) so both directions give
- * the same numbers with opposite sign.  seed4: the seed of the pair
- * (w = 1 -> use xyz, else the reference seed).  Returns the GJK status and
- * adds the force and torque on self into f, t. */
+ * the same numbers with opposite sign.  seed4: the seed of the pair in A's
+ * body frame (w = 1 -> use xyz, else the reference seed x_A - x_B).
+ * Returns the GJK status; *f, *t receive the force and torque on self (zero
+ * without contact) and *dirA the final search direction in A's frame. */
 static int hull_entry(const sdo_hull_params* p, const float* pos4, const float* vel4, const float* quat4,
                       const float* omg4, const float* iinv4, const uint32_t* vstart, const uint32_t* vcount,
                       const float* verts4, uint32_t self, uint32_t other, const float* seed4, int* iters,
-                      v3* dir, v3* f, v3* t) {
+                      int* epa_iters, v3* dirA, v3* f, v3* t) {
     const uint32_t A = self < other ? self : other, B = self < other ? other : self;
     hpair P;
     make_pair(&P, pos4, quat4, vstart, vcount, verts4, A, B);
     v3 d0 = vneg(P.off);
-    int seeded = seed4 && seed4[3] == 1.0f;
-    if (seeded) d0 = ld3(seed4);
+    const int seeded = seed4 && seed4[3] == 1.0f;
+    if (seeded) d0 = rot(P.A.R, ld3(seed4));
     simplex_t S;
-    int st = gjk(&P, d0, &S, iters, dir);
+    v3 dir;
+    int st = gjk(&P, d0, &S, iters, &dir);
     if (st == GJK_NOCONV && seeded) {
         int it2 = 0;
-        st = gjk(&P, vneg(P.off), &S, &it2, dir);
+        st = gjk(&P, vneg(P.off), &S, &it2, &dir);
         *iters += it2;
     }
+    *f = mk(0.0f, 0.0f, 0.0f);
+    *t = mk(0.0f, 0.0f, 0.0f);
+    *epa_iters = 0;
+    *dirA = rotT(P.A.R, dir);
     if (st != GJK_HIT) return st;
     contact_t c;
     memset(&c, 0, sizeof c);
     epa(&P, &S, epa_tol(iinv4, A, B), &c);
+    *epa_iters = c.epa_iters;
     if (!c.ok) return GJK_TOUCH;
     const float mA = pos4[4 * (size_t)A + 3], mB = pos4[4 * (size_t)B + 3];
     const v3 rA = c.c, rB = vsub(c.c, P.off);
@@ -588,12 +595,11 @@ static int hull_entry(const sdo_hull_params* p, const float* pos4, const float* 
     v3 fb;
     hull_contact_force(p, c.depth, c.n, vsub(vB, vA), meff, &fb);
     if (self == B) {
-        *f = vadd(*f, fb);
-        *t = vadd(*t, vcross(rB, fb));
+        *f = fb;
+        *t = vcross(rB, fb);
     } else {
-        const v3 fa = vneg(fb);
-        *f = vadd(*f, fa);
-        *t = vadd(*t, vcross(rA, fa));
+        *f = vneg(fb);
+        *t = vcross(rA, *f);
     }
     return st;
 }
@@ -722,15 +728,17 @@ void sdo_hull_step(const sdo_hull_params* p, uint32_t nb, float* pos4, float* ve
         const uint32_t b = (uint32_t)bi;
         v3 f = mk(0.0f, 0.0f, 0.0f), t = mk(0.0f, 0.0f, 0.0f);
         for (uint32_t e = off[b]; e < off[b + 1]; ++e) {
-            int it = 0;
-            v3 dir = mk(0.0f, 0.0f, 0.0f);
+            int it = 0, eit = 0;
+            v3 dir, fe, te;
             const int st = hull_entry(p, pos4, vel4, quat4, omg4, iinv4, vstart, vcount, verts4, b, partners[e],
-                                      seeds4 ? seeds4 + 4 * (size_t)e : NULL, &it, &dir, &f, &t);
+                                      seeds4 ? seeds4 + 4 * (size_t)e : NULL, &it, &eit, &dir, &fe, &te);
+            f = vadd(f, fe);
+            t = vadd(t, te);
             if (status) status[e] = st;
             if (iters) iters[e] = it;
             if (dir4) {
                 dir4[4 * (size_t)e] = dir.x; dir4[4 * (size_t)e + 1] = dir.y; dir4[4 * (size_t)e + 2] = dir.z;
-                dir4[4 * (size_t)e + 3] = 0.0f;
+                dir4[4 * (size_t)e + 3] = st == GJK_SEP ? 1.0f : 0.0f;
             }
         }
         float R[9];

@@ -6,7 +6,8 @@ engine and operator classes over it (``stardust_gb300.engine``).
 """
 from . import _abi
 from ._abi import SdError, lib
-from .engine import DEMEngine, EngineConfig, SpatialPartition, scene_lattice, scene_rsa
+from .engine import (BoundingVolumes, DEMEngine, EngineConfig, SpatialPartition, add_hull_scene, scene_lattice,
+                     scene_rsa)
 
-__all__ = ["DEMEngine", "EngineConfig", "SpatialPartition", "SdError", "lib", "scene_lattice",
-           "scene_rsa", "_abi"]
+__all__ = ["BoundingVolumes", "DEMEngine", "EngineConfig", "SpatialPartition", "SdError", "add_hull_scene", "lib",
+           "scene_lattice", "scene_rsa", "_abi"]

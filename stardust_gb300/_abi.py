@@ -58,6 +58,13 @@ SD_BODY_QUATERNION = 2
 SD_BODY_OMEGA = 3
 SD_BODY_ANGMOM = 4
 SD_BODY_INV_INERTIA = 5
+SD_BODY_HULL_INV_INERTIA = 6
+SD_BODY_FORCE = 7
+SD_BODY_TORQUE = 8
+
+SD_GJK_SEED_PLAIN = 0
+SD_GJK_SEED_LEARNED = 1
+SD_GJK_SEED_PREVIOUS = 2
 
 
 class SdConfig(C.Structure):
@@ -91,6 +98,9 @@ class SdStats(C.Structure):
         ("device_errors", C.c_uint32),
         ("n_cells", C.c_uint32),
         ("n_bodies", C.c_uint64),
+        ("gjk_pairs", C.c_uint64),
+        ("gjk_iters", C.c_uint64),
+        ("epa_iters", C.c_uint64),
     ]
 
 
@@ -121,6 +131,13 @@ SIGNATURES = {
     "sd_engine_add_particle": [P, I32, F32, F32, F32, P, P],
     "sd_engine_add_clump": [P, U32, P, F32, P, P, P],
     "sd_engine_get_bodies": [P, I32, P, C.c_size_t],
+    "sd_engine_add_hull": [P, U32, P, F32, P, P, P, P],
+    "sd_engine_get_hull_shapes": [P, P, P, P, U64, C.POINTER(U64)],
+    "sd_engine_set_gjk_seed": [P, I32],
+    "sd_engine_hull_entries": [P, P, P, P, P, P, P, U64, C.POINTER(U64)],
+    "sd_lbvh_scratch_bytes": [U64, U64, C.POINTER(U64)],
+    "sd_lbvh_pairs": [U64, P, P, P, U64, P, P, U64, P],
+    "sd_lbvh_morton": [U64, P, P, P, P, U64, P],
     "sd_engine_load_scene_json": [P, C.c_char_p],
     "sd_engine_prepare": [P],
     "sd_engine_step": [P, F32, I32],

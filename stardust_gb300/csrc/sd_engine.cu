@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/stardust.h"
+#include "sd_engine_impl.h"
 #include "sd_internal.h"
 #include "sd_json.h"
 
@@ -42,35 +43,6 @@ struct CudaBuf {
 };
 
 }  // namespace
-
-struct sd_engine {
-    sd_config cfg{};
-    std::string err;
-
-    // host sphere set in insertion order; omega.w carries the id bits
-    std::vector<float4> h_pos, h_vel, h_omg;
-    // rigid clumps: per body (centre, mass), v, q, w, L, inverse inertia rows,
-    // first sphere id and sphere count; per sphere id its body and offset
-    std::vector<float4> hb_pos, hb_vel, hb_quat, hb_omg, hb_ang, hb_inv;
-    std::vector<uint32_t> hb_first, hb_count;
-    std::vector<int32_t> h_body_of;
-    std::vector<float4> h_r0;
-
-    bool prepared = false;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    sd::DemParams P{};
-    sd::DemBuffers B{};
-    std::vector<void*> allocations;
-    double* d_energy = nullptr;
-    float4* d_tmp = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = 0.0f;
-    bool graph_valid = false;
-    uint64_t steps = 0;
-    bool need_resort = false;
-    uint64_t graph_epoch = 0;
-};
 
 namespace {
 
@@ -121,6 +93,7 @@ sd_status dev_alloc(sd_engine* h, T** p, size_t count) {
 }
 
 void release_device(sd_engine* h) {
+    hull_release(h);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
     h->graph_valid = false;
@@ -339,6 +312,17 @@ namespace sd {
 // defined in other translation units.
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace sd
+
+sd_status sd_fail(sd_engine* h, sd_status code, const std::string& msg) { return fail(h, code, msg); }
+sd_status sd_cuda_fail(sd_engine* h, cudaError_t e, const char* where) { return cuda_fail(h, e, where); }
+sd_status sd_alloc_bytes(sd_engine* h, void** p, size_t bytes) {
+    char* q = nullptr;
+    sd_status s = dev_alloc(h, &q, bytes);
+    *p = q;
+    return s;
+}
+float sd_damp_from(float kn, float e) { return damp_from(kn, e); }
+uint64_t sd_tune_epoch() { return g_tune_epoch.load(); }
 
 // =================================================================== C ABI
 extern "C" {
@@ -678,6 +662,13 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
 sd_status sd_engine_prepare(sd_engine* h) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
     if (h->prepared) return fail(h, SD_ERR_STATE, "already prepared");
+    if (h->hull_mode()) {
+        if (!h->h_pos.empty())
+            return fail(h, SD_ERR_UNSUPPORTED, "a scene holds spheres/clumps or convex hulls, not both");
+        sd_status s = hull_prepare(h);
+        if (s) release_device(h);
+        return s;
+    }
     return prepare_with(h, h->h_pos.data(), h->h_vel.data(), h->h_omg.data(), (uint32_t)h->h_pos.size());
 }
 
@@ -686,6 +677,7 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(h, SD_ERR_INVALID_ARG, "dt must be positive and finite");
     if (n_steps < 0) return fail(h, SD_ERR_INVALID_ARG, "n_steps < 0");
+    if (h->hull_mode()) return hull_step(h, dt, n_steps);
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
@@ -749,6 +741,7 @@ static const float4* field_ptr(sd_engine* h, int32_t field) {
 sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes) {
     if (!h || !host_dst) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     uint32_t n = h->B.n;
     if (bytes != (size_t)n * sizeof(float4)) return fail(h, SD_ERR_INVALID_ARG, "bytes must be n_spheres * 16");
     if (field == SD_FIELD_IDS) return fail(h, SD_ERR_INVALID_ARG, "SD_FIELD_IDS is a device-pointer field");
@@ -777,6 +770,7 @@ sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_
 sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src, size_t bytes) {
     if (!h || !host_src) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     uint32_t n = h->B.n;
     if (bytes != (size_t)n * sizeof(float4)) return fail(h, SD_ERR_INVALID_ARG, "bytes must be n_spheres * 16");
     if (field != SD_FIELD_POSITION && field != SD_FIELD_VELOCITY && field != SD_FIELD_OMEGA)
@@ -797,6 +791,7 @@ sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src,
 sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
@@ -817,6 +812,7 @@ sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
 sd_status sd_engine_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes) {
     if (!h || !host_dst) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return hull_get_bodies(h, field, host_dst, bytes);
     const size_t nb = h->B.nb;
     const float4* src = nullptr;
     size_t per = 16;
@@ -844,6 +840,7 @@ sd_status sd_engine_get_bodies(sd_engine* h, int32_t field, void* host_dst, size
 sd_status sd_engine_device_ptr(sd_engine* h, int32_t field, void** out) {
     if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     if (field == SD_FIELD_IDS) {
         // ids live in the w lane of the omega array
         *out = reinterpret_cast<char*>(h->B.omg) + 12;
@@ -865,6 +862,7 @@ sd_status sd_engine_stream(sd_engine* h, void** out) {
 sd_status sd_engine_get_pairs(sd_engine* h, uint64_t* dst, uint64_t cap, uint64_t* n) {
     if (!h || !n) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
@@ -903,6 +901,7 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
     out->n_spheres = h->prepared ? h->B.n : h->h_pos.size();
     out->n_bodies = h->hb_pos.size();
     out->steps = h->steps;
+    if (h->hull_mode()) return hull_stats(h, out);
     if (!h->prepared) return SD_OK;
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
@@ -956,6 +955,7 @@ static const char kCkptMagic[8] = {'S', 'D', 'G', 'B', 'C', 'K', 'P', '1'};
 sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
     if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
@@ -1000,6 +1000,7 @@ sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
 
 sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
     if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes");
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(h, SD_ERR_IO, std::string("cannot open ") + path);
     char magic[8];

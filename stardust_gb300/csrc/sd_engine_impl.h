@@ -1,0 +1,82 @@
+// sd_engine_impl.h -- the engine handle, shared by the translation units that
+// implement the C ABI (sd_engine.cu: spheres and clumps; sd_hull_engine.cu:
+// convex hulls).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/stardust.h"
+#include "sd_internal.h"
+
+// Host copy and device state of a convex-hull scene (sd_hull_engine.cu).
+struct HullScene {
+    // host, in insertion order
+    std::vector<float4> pos, vel, quat, omg, ang, iinv, verts;
+    std::vector<uint32_t> vstart, vcount;
+    // device
+    sd::HullParams P{};
+    sd::HullBuffers H{};
+    sd::Lbvh tree{};
+    uint32_t* off[2] = {nullptr, nullptr};        // partner lists of even / odd steps
+    uint32_t* partners[2] = {nullptr, nullptr};
+    float4* dir[2] = {nullptr, nullptr};
+    unsigned long long* stats = nullptr;          // 4 counters of the last step
+    float* mlp = nullptr;                         // warm-start network (device)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int parity = 0;
+    int seed_mode = 0;                            // SD_GJK_SEED_*
+    float graph_dt = 0.0f;
+    bool graph_valid = false;
+    uint64_t graph_epoch = 0;
+};
+
+struct sd_engine {
+    sd_config cfg{};
+    std::string err;
+
+    // host sphere set in insertion order; omega.w carries the id bits
+    std::vector<float4> h_pos, h_vel, h_omg;
+    // rigid clumps: per body (centre, mass), v, q, w, L, inverse inertia rows,
+    // first sphere id and sphere count; per sphere id its body and offset
+    std::vector<float4> hb_pos, hb_vel, hb_quat, hb_omg, hb_ang, hb_inv;
+    std::vector<uint32_t> hb_first, hb_count;
+    std::vector<int32_t> h_body_of;
+    std::vector<float4> h_r0;
+    // convex hulls (a scene holds spheres/clumps or hulls, not both)
+    HullScene hull;
+
+    bool prepared = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    sd::DemParams P{};
+    sd::DemBuffers B{};
+    std::vector<void*> allocations;
+    double* d_energy = nullptr;
+    float4* d_tmp = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.0f;
+    bool graph_valid = false;
+    uint64_t steps = 0;
+    bool need_resort = false;
+    uint64_t graph_epoch = 0;
+
+    bool hull_mode() const { return !hull.pos.empty(); }
+};
+
+// shared helpers (sd_engine.cu)
+sd_status sd_fail(sd_engine* h, sd_status code, const std::string& msg);
+sd_status sd_cuda_fail(sd_engine* h, cudaError_t e, const char* where);
+sd_status sd_alloc_bytes(sd_engine* h, void** p, size_t bytes);
+float sd_damp_from(float kn, float e);
+uint64_t sd_tune_epoch();
+
+// hull mode (sd_hull_engine.cu)
+sd_status hull_prepare(sd_engine* h);
+sd_status hull_step(sd_engine* h, float dt, int32_t n_steps);
+sd_status hull_stats(sd_engine* h, sd_stats* out);
+sd_status hull_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+sd_status hull_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
+void hull_release(sd_engine* h);

@@ -1,0 +1,673 @@
+// sd_hull.cu -- convex-hull rigid bodies: world AABBs, GJK/EPA narrow
+// phase with atomic-free force reduction, quaternion integration.
+//
+// Narrow phase: sandbox/testGJK.cu:52-315 (support mapping of a vertex soup,
+// Minkowski difference B - A, simplex cases, termination dot(w, d) < 0,
+// at most 64 support evaluations) in the standard GJK formulation
+// (Gilbert, Johnson, Keerthi 1988) with the full line/triangle/tetrahedron
+// case analysis; EPA (van den Bergen 2001) for the penetration depth,
+// normal and witness points, which the reference lacks.
+//
+// Work split: one thread per candidate ENTRY (self, other) of the per-body
+// partner lists built by the LBVH; each entry evaluates its pair as
+// (A, B) = (min, max), so the two entries of a pair compute identical
+// numbers and take opposite signs -- exact action = reaction with no
+// atomics.  One thread per body then sums its entries in list order (the
+// segmented reduction), adds walls and gravity and integrates.
+//
+// Every float operation follows oracle/sd_oracle_hull.c in order
+// (-fmad=false), so results are bit-identical to the CPU restatement.
+#include "sd_common.cuh"
+
+namespace sd {
+
+namespace {
+
+constexpr int kHullThreads = 128;
+constexpr int kGjkMaxIt = 64;
+constexpr int kEpaMaxV = 48;
+constexpr int kEpaMaxF = 96;
+constexpr int kEpaMaxIt = 48;
+enum : int { kSep = 0, kHit = 1, kTouch = 2, kNoConv = 3 };
+
+struct v3 {
+    float x, y, z;
+};
+__device__ __forceinline__ v3 mk(float x, float y, float z) { return v3{x, y, z}; }
+__device__ __forceinline__ v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ v3 vsub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ v3 vneg(v3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ v3 vscale(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float vdot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ v3 vcross(v3 a, v3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ v3 vtriple(v3 a, v3 b, v3 c) { return vcross(vcross(a, b), c); }
+__device__ __forceinline__ bool vzero(v3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+__device__ __forceinline__ v3 f3(float4 a) { return mk(a.x, a.y, a.z); }
+
+struct Mat {
+    float r[9];
+};
+
+__device__ __forceinline__ Mat qrot(float4 q) {
+    const float qs = q.x, qx = q.y, qy = q.z, qz = q.w;
+    Mat R;
+    R.r[0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+    R.r[1] = 2.0f * (qx * qy - qs * qz);
+    R.r[2] = 2.0f * (qx * qz + qs * qy);
+    R.r[3] = 2.0f * (qx * qy + qs * qz);
+    R.r[4] = 1.0f - 2.0f * (qx * qx + qz * qz);
+    R.r[5] = 2.0f * (qy * qz - qs * qx);
+    R.r[6] = 2.0f * (qx * qz - qs * qy);
+    R.r[7] = 2.0f * (qy * qz + qs * qx);
+    R.r[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
+    return R;
+}
+__device__ __forceinline__ v3 rot(const Mat& R, v3 v) {
+    return mk((R.r[0] * v.x + R.r[1] * v.y) + R.r[2] * v.z, (R.r[3] * v.x + R.r[4] * v.y) + R.r[5] * v.z,
+              (R.r[6] * v.x + R.r[7] * v.y) + R.r[8] * v.z);
+}
+__device__ __forceinline__ v3 rotT(const Mat& R, v3 d) {
+    return mk((R.r[0] * d.x + R.r[3] * d.y) + R.r[6] * d.z, (R.r[1] * d.x + R.r[4] * d.y) + R.r[7] * d.z,
+              (R.r[2] * d.x + R.r[5] * d.y) + R.r[8] * d.z);
+}
+
+struct HBody {
+    Mat R;
+    const float4* V;
+    uint32_t nv;
+};
+
+struct Cso {
+    v3 w, a, b;
+    uint32_t key;
+};
+
+struct HPair {
+    HBody A, B;
+    v3 off;  // x_B - x_A
+};
+
+__device__ __forceinline__ uint32_t support(const HBody& h, v3 d, v3* out) {
+    const v3 db = rotT(h.R, d);
+    uint32_t best = 0;
+    float bd = vdot(db, f3(__ldg(h.V)));
+    for (uint32_t k = 1; k < h.nv; ++k) {
+        const float t = vdot(db, f3(__ldg(h.V + k)));
+        if (t > bd) {
+            bd = t;
+            best = k;
+        }
+    }
+    *out = rot(h.R, f3(__ldg(h.V + best)));
+    return best;
+}
+
+__device__ __forceinline__ Cso cso(const HPair& P, v3 d) {
+    Cso r;
+    const uint32_t ia = support(P.A, vneg(d), &r.a);
+    v3 bb;
+    const uint32_t ib = support(P.B, d, &bb);
+    r.b = vadd(bb, P.off);
+    r.w = vsub(r.b, r.a);
+    r.key = ia * 1024u + ib;
+    return r;
+}
+
+struct Simplex {
+    Cso s[4];
+    int n;
+    v3 d;
+};
+
+__device__ void simplex_line(Simplex& S) {
+    const v3 A = S.s[0].w, B = S.s[1].w;
+    const v3 AB = vsub(B, A), AO = vneg(A);
+    if (vdot(AB, AO) > 0.0f) {
+        S.d = vtriple(AB, AO, AB);
+    } else {
+        S.n = 1;
+        S.d = AO;
+    }
+}
+
+__device__ void simplex_tri(Simplex& S) {
+    const v3 A = S.s[0].w, B = S.s[1].w, C = S.s[2].w;
+    const v3 AB = vsub(B, A), AC = vsub(C, A), AO = vneg(A);
+    const v3 ABC = vcross(AB, AC);
+    bool star = false;
+    if (vdot(vcross(ABC, AC), AO) > 0.0f) {
+        if (vdot(AC, AO) > 0.0f) {
+            S.s[1] = S.s[2];
+            S.n = 2;
+            S.d = vtriple(AC, AO, AC);
+            return;
+        }
+        star = true;
+    } else if (vdot(vcross(AB, ABC), AO) > 0.0f) {
+        star = true;
+    }
+    if (star) {
+        S.n = 2;
+        if (vdot(AB, AO) > 0.0f) {
+            S.d = vtriple(AB, AO, AB);
+        } else {
+            S.n = 1;
+            S.d = AO;
+        }
+        return;
+    }
+    if (vdot(ABC, AO) > 0.0f) {
+        S.d = ABC;
+    } else {
+        const Cso t = S.s[1];
+        S.s[1] = S.s[2];
+        S.s[2] = t;
+        S.d = vneg(ABC);
+    }
+}
+
+__device__ bool simplex_tet(Simplex& S) {
+    const v3 A = S.s[0].w, B = S.s[1].w, C = S.s[2].w, D = S.s[3].w;
+    const v3 AO = vneg(A), AB = vsub(B, A), AC = vsub(C, A), AD = vsub(D, A);
+    const v3 ABC = vcross(AB, AC), ACD = vcross(AC, AD), ADB = vcross(AD, AB);
+    if (vdot(ABC, AO) > 0.0f) {
+        S.n = 3;
+        simplex_tri(S);
+        return false;
+    }
+    if (vdot(ACD, AO) > 0.0f) {
+        S.s[1] = S.s[2];
+        S.s[2] = S.s[3];
+        S.n = 3;
+        simplex_tri(S);
+        return false;
+    }
+    if (vdot(ADB, AO) > 0.0f) {
+        const Cso b = S.s[1];
+        S.s[1] = S.s[3];
+        S.s[2] = b;
+        S.n = 3;
+        simplex_tri(S);
+        return false;
+    }
+    return true;
+}
+
+__device__ int gjk(const HPair& P, v3 d0, Simplex& S, int* iters, v3* dir) {
+    v3 d = d0;
+    if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
+    Cso p = cso(P, d);
+    int it = 1;
+    if (vdot(p.w, d) < 0.0f) {
+        *iters = it;
+        *dir = d;
+        return kSep;
+    }
+    S.s[0] = p;
+    S.n = 1;
+    S.d = vneg(p.w);
+    for (;;) {
+        if (it >= kGjkMaxIt) {
+            *iters = it;
+            *dir = S.d;
+            return kNoConv;
+        }
+        if (vzero(S.d)) {
+            *iters = it;
+            *dir = S.d;
+            return kTouch;
+        }
+        p = cso(P, S.d);
+        ++it;
+        if (vdot(p.w, S.d) < 0.0f) {
+            *iters = it;
+            *dir = S.d;
+            return kSep;
+        }
+        S.s[3] = S.s[2];
+        S.s[2] = S.s[1];
+        S.s[1] = S.s[0];
+        S.s[0] = p;
+        S.n += 1;
+        if (S.n == 2) {
+            simplex_line(S);
+        } else if (S.n == 3) {
+            simplex_tri(S);
+        } else if (simplex_tet(S)) {
+            *iters = it;
+            *dir = S.d;
+            return kHit;
+        }
+    }
+}
+
+struct Face {
+    uint8_t i[3];
+    v3 n;
+    float dist;
+};
+
+__device__ __forceinline__ bool face_make(const Cso* V, uint8_t a, uint8_t b, uint8_t c, Face* f) {
+    const v3 nn = vcross(vsub(V[b].w, V[a].w), vsub(V[c].w, V[a].w));
+    const float len = sqrtf(vdot(nn, nn));
+    if (!(len > 0.0f)) return false;
+    f->i[0] = a;
+    f->i[1] = b;
+    f->i[2] = c;
+    f->n = mk(nn.x / len, nn.y / len, nn.z / len);
+    f->dist = vdot(f->n, V[a].w);
+    return true;
+}
+
+struct Contact {
+    float depth;
+    v3 n, c;
+    int epa_iters;
+    bool ok;
+};
+
+__device__ void epa(const HPair& P, const Simplex& S, float tol, Contact* out) {
+    Cso V[kEpaMaxV];
+    Face F[kEpaMaxF];
+    uint8_t E[3 * kEpaMaxF][2];
+    int nv = 4, nf = 0;
+    for (int k = 0; k < 4; ++k) V[k] = S.s[k];
+    const uint8_t init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+    for (int k = 0; k < 4; ++k) {
+        Face f;
+        if (!face_make(V, init[k][0], init[k][1], init[k][2], &f)) continue;
+        if (f.dist < 0.0f) {
+            const uint8_t t = f.i[1];
+            f.i[1] = f.i[2];
+            f.i[2] = t;
+            f.n = vneg(f.n);
+            f.dist = -f.dist;
+        }
+        F[nf++] = f;
+    }
+    out->ok = false;
+    out->epa_iters = 0;
+    if (nf == 0) return;
+    int best = 0;
+    for (int it = 0;; ++it) {
+        best = 0;
+        for (int k = 1; k < nf; ++k)
+            if (F[k].dist < F[best].dist) best = k;
+        out->epa_iters = it + 1;
+        if (it >= kEpaMaxIt || nv >= kEpaMaxV) break;
+        const Cso p = cso(P, F[best].n);
+        bool dup = false;
+        for (int k = 0; k < nv; ++k) dup |= V[k].key == p.key;
+        if (dup || vdot(p.w, F[best].n) - F[best].dist <= tol) break;
+        const uint8_t q = (uint8_t)nv;
+        V[nv++] = p;
+        int ne = 0, keep = 0;
+        for (int k = 0; k < nf; ++k) {
+            if (vdot(F[k].n, vsub(p.w, V[F[k].i[0]].w)) > 0.0f) {
+                for (int e = 0; e < 3; ++e) {
+                    const uint8_t a = F[k].i[e], b = F[k].i[(e + 1) % 3];
+                    int found = -1;
+                    for (int m = 0; m < ne; ++m)
+                        if (E[m][0] == b && E[m][1] == a) {
+                            found = m;
+                            break;
+                        }
+                    if (found >= 0) {
+                        E[found][0] = E[ne - 1][0];
+                        E[found][1] = E[ne - 1][1];
+                        --ne;
+                    } else {
+                        E[ne][0] = a;
+                        E[ne][1] = b;
+                        ++ne;
+                    }
+                }
+            } else {
+                F[keep++] = F[k];
+            }
+        }
+        nf = keep;
+        if (nf + ne > kEpaMaxF) break;
+        for (int m = 0; m < ne; ++m) {
+            Face f;
+            if (face_make(V, E[m][0], E[m][1], q, &f)) F[nf++] = f;
+        }
+        if (nf == 0) return;
+    }
+    Cso t[3] = {V[F[best].i[0]], V[F[best].i[1]], V[F[best].i[2]]};
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2 - a; ++b)
+            if (t[b].key > t[b + 1].key) {
+                const Cso s = t[b];
+                t[b] = t[b + 1];
+                t[b + 1] = s;
+            }
+    const v3 e0 = vsub(t[1].w, t[0].w), e1 = vsub(t[2].w, t[0].w);
+    const v3 nn = vcross(e0, e1);
+    const float len = sqrtf(vdot(nn, nn));
+    if (!(len > 0.0f)) return;
+    v3 n = mk(nn.x / len, nn.y / len, nn.z / len);
+    float depth = vdot(n, t[0].w);
+    if (depth < 0.0f) {
+        n = vneg(n);
+        depth = -depth;
+    }
+    const v3 pp = vscale(n, depth);
+    const v3 e2 = vsub(pp, t[0].w);
+    const float d00 = vdot(e0, e0), d01 = vdot(e0, e1), d11 = vdot(e1, e1);
+    const float d20 = vdot(e2, e0), d21 = vdot(e2, e1);
+    const float den = d00 * d11 - d01 * d01;
+    float l1 = 0.0f, l2 = 0.0f;
+    if (den != 0.0f) {
+        l1 = (d11 * d20 - d01 * d21) / den;
+        l2 = (d00 * d21 - d01 * d20) / den;
+    }
+    const float l0 = (1.0f - l1) - l2;
+    const v3 a = vadd(vadd(vscale(t[0].a, l0), vscale(t[1].a, l1)), vscale(t[2].a, l2));
+    const v3 b = vadd(vadd(vscale(t[0].b, l0), vscale(t[1].b, l1)), vscale(t[2].b, l2));
+    out->depth = depth;
+    out->n = vneg(n);
+    out->c = vscale(vadd(a, b), 0.5f);
+    out->ok = true;
+}
+
+__device__ __forceinline__ void make_pair(const HullBuffers& H, uint32_t A, uint32_t B, HPair* P) {
+    P->A.R = qrot(H.quat[A]);
+    P->B.R = qrot(H.quat[B]);
+    P->A.V = H.verts + H.vstart[A];
+    P->A.nv = H.vcount[A];
+    P->B.V = H.verts + H.vstart[B];
+    P->B.nv = H.vcount[B];
+    P->off = vsub(f3(H.pos[B]), f3(H.pos[A]));
+}
+
+__device__ __forceinline__ v3 contact_force(const HullParams& p, float delta, v3 m, v3 vr, float meff) {
+    const float vn = vdot(vr, m);
+    const float gn = p.damp * sqrtf(meff);
+    const float fn = p.kn * delta - gn * vn;
+    const float fc = fn > 0.0f ? fn : 0.0f;
+    const v3 vt = mk(vr.x - vn * m.x, vr.y - vn * m.y, vr.z - vn * m.z);
+    const float vt2 = vdot(vt, vt);
+    v3 f = mk(fn * m.x, fn * m.y, fn * m.z);
+    if (vt2 > 0.0f) {
+        const float vtm = sqrtf(vt2);
+        const float ftm = fminf(p.mu * fc, gn * vtm);
+        const float s = ftm / vtm;
+        f.x += -(s * vt.x);
+        f.y += -(s * vt.y);
+        f.z += -(s * vt.z);
+    }
+    return f;
+}
+
+// ------------------------------------------------------------- kernels
+
+__global__ void hull_aabb_kernel(HullBuffers H) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= H.nb) return;
+    const Mat R = qrot(H.quat[b]);
+    const float4* V = H.verts + H.vstart[b];
+    const uint32_t nv = H.vcount[b];
+    v3 w = rot(R, f3(V[0]));
+    float mn[3] = {w.x, w.y, w.z}, mx[3] = {w.x, w.y, w.z};
+    uint32_t imn[3] = {0, 0, 0}, imx[3] = {0, 0, 0};
+    for (uint32_t k = 1; k < nv; ++k) {
+        w = rot(R, f3(V[k]));
+        const float c[3] = {w.x, w.y, w.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (c[a] < mn[a]) {
+                mn[a] = c[a];
+                imn[a] = k;
+            }
+            if (c[a] > mx[a]) {
+                mx[a] = c[a];
+                imx[a] = k;
+            }
+        }
+    }
+    const float4 x = H.pos[b];
+    H.lo[b] = make_float4(x.x + mn[0], x.y + mn[1], x.z + mn[2], 0.f);
+    H.hi[b] = make_float4(x.x + mx[0], x.y + mx[1], x.z + mx[2], 0.f);
+    H.ext[2 * b] = imn[0] | (imn[1] << 8) | (imn[2] << 16);
+    H.ext[2 * b + 1] = imx[0] | (imx[1] << 8) | (imx[2] << 16);
+}
+
+// Seeds from the previous step's final directions (seed mode 2): the pair's
+// entry in the previous partner list of A (binary search) carries the
+// direction in A's body frame.  feat (may be null) receives the 12 MLP
+// inputs and w of seeds the previous-contact flag.
+__global__ void hull_prev_seed_kernel(HullBuffers H, uint32_t mode) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= H.cap) return;
+    const uint32_t total = H.off[H.nb];
+    if (e >= total || (uint64_t)total > H.cap) return;  // an overflowed step is reported, not evaluated
+    const uint32_t self = H.self[e], other = H.partners[e];
+    const uint32_t A = min(self, other), B = max(self, other);
+    // previous entry of (A, B); a previous list that overflowed is ignored
+    float4 prev = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t lo = H.prev_off[A];
+    const uint32_t end = (uint64_t)H.prev_off[H.nb] > H.cap ? lo : H.prev_off[A + 1];
+    uint32_t hi = end;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t v = H.prev_partners[mid];
+        if (v < B) lo = mid + 1;
+        else hi = mid;
+    }
+    const bool found = lo < end && H.prev_partners[lo] == B;
+    if (found) prev = H.prev_dir[lo];
+    const bool have = found && prev.w != 0.0f;
+    if (mode == 2u) {
+        H.seeds[e] = have ? make_float4(prev.x, prev.y, prev.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        H.seeds[e] = make_float4(0.f, 0.f, 0.f, have ? 1.0f : 0.0f);
+    }
+    if (H.feat) {
+        // 12 inputs in A's body frame: relative quaternion conj(qA) (x) qB,
+        // centre offset / (rhoA + rhoB), previous-contact flag, previous
+        // direction (unit), |offset| / (rhoA + rhoB)
+        const float4 qa = H.quat[A], qb = H.quat[B];
+        const float as = qa.x, ax = -qa.y, ay = -qa.z, az = -qa.w;
+        const float rs = as * qb.x - ((ax * qb.y + ay * qb.z) + az * qb.w);
+        const float rx = as * qb.y + qb.x * ax + (ay * qb.w - az * qb.z);
+        const float ry = as * qb.z + qb.x * ay + (az * qb.y - ax * qb.w);
+        const float rz = as * qb.w + qb.x * az + (ax * qb.z - ay * qb.y);
+        const Mat R = qrot(qa);
+        const float scale = 1.0f / (H.iinv[A].w + H.iinv[B].w);
+        const v3 o = vscale(rotT(R, vsub(f3(H.pos[B]), f3(H.pos[A]))), scale);
+        float* f = H.feat + 16 * (size_t)e;
+        f[0] = rs; f[1] = rx; f[2] = ry; f[3] = rz;
+        f[4] = o.x; f[5] = o.y; f[6] = o.z;
+        f[7] = have ? 1.0f : 0.0f;
+        f[8] = have ? prev.x : 0.0f; f[9] = have ? prev.y : 0.0f; f[10] = have ? prev.z : 0.0f;
+        f[11] = sqrtf(vdot(o, o));
+        f[12] = 0.0f; f[13] = 0.0f; f[14] = 0.0f; f[15] = 0.0f;
+    }
+}
+
+// Narrow phase of one entry: GJK (seeded or plain), EPA on a hit, contact
+// force and torque on the entry's own body.
+__global__ void __launch_bounds__(kHullThreads) hull_entry_kernel(HullParams p, HullBuffers H) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= H.cap) return;
+    const uint32_t total = H.off[H.nb];
+    if (e >= total || (uint64_t)total > H.cap) return;  // an overflowed step is reported, not evaluated
+    const uint32_t self = H.self[e], other = H.partners[e];
+    const uint32_t A = min(self, other), B = max(self, other);
+    HPair P;
+    make_pair(H, A, B, &P);
+    v3 d0 = vneg(P.off);
+    const float4 sd = H.seeds ? H.seeds[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool seeded = sd.w == 1.0f;
+    if (seeded) d0 = rot(P.A.R, f3(sd));
+    Simplex S;
+    int iters = 0;
+    v3 dir;
+    int st = gjk(P, d0, S, &iters, &dir);
+    if (st == kNoConv && seeded) {
+        int it2 = 0;
+        st = gjk(P, vneg(P.off), S, &it2, &dir);
+        iters += it2;
+    }
+    v3 f = mk(0.f, 0.f, 0.f), t = mk(0.f, 0.f, 0.f);
+    int epa_it = 0;
+    v3 dA = rotT(P.A.R, dir);  // final direction in A's frame (seed of the next step)
+    if (st == kHit) {
+        Contact c;
+        epa(P, S, (H.iinv[A].w + H.iinv[B].w) * 1e-7f, &c);
+        epa_it = c.epa_iters;
+        if (!c.ok) {
+            st = kTouch;
+        } else {
+            const float4 pa = H.pos[A], pb = H.pos[B];
+            const float mA = pa.w, mB = pb.w;
+            const v3 rA = c.c, rB = vsub(c.c, P.off);
+            const v3 vA = vadd(f3(H.vel[A]), vcross(f3(H.omg[A]), rA));
+            const v3 vB = vadd(f3(H.vel[B]), vcross(f3(H.omg[B]), rB));
+            const float meff = (mA * mB) / (mA + mB);
+            const v3 fb = contact_force(p, c.depth, c.n, vsub(vB, vA), meff);
+            if (self == B) {
+                f = fb;
+                t = vcross(rB, fb);
+            } else {
+                f = vneg(fb);
+                t = vcross(rA, f);
+            }
+        }
+    }
+    H.ef[e] = make_float4(f.x, f.y, f.z, 0.f);
+    H.et[e] = make_float4(t.x, t.y, t.z, 0.f);
+    H.info[e] = (uint32_t)st | ((uint32_t)iters << 8) | ((uint32_t)epa_it << 16);
+    H.dir[e] = make_float4(dA.x, dA.y, dA.z, st == kSep ? 1.0f : 0.0f);
+}
+
+// Per body: segmented sum of its entries (list order), walls, integration.
+__global__ void hull_integrate_kernel(HullParams p, HullBuffers H) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= H.nb) return;
+    v3 f = mk(0.f, 0.f, 0.f), t = mk(0.f, 0.f, 0.f);
+    const uint32_t e0 = H.off[b], e1 = H.off[b + 1];
+    if ((uint64_t)H.off[H.nb] <= H.cap) {
+        for (uint32_t e = e0; e < e1; ++e) {
+            f = vadd(f, f3(H.ef[e]));
+            t = vadd(t, f3(H.et[e]));
+        }
+    }
+    const float4 x4 = H.pos[b], v4 = H.vel[b], w4 = H.omg[b], q4 = H.quat[b];
+    const Mat R = qrot(q4);
+    if (p.walls) {
+        const float4* V = H.verts + H.vstart[b];
+        const uint32_t ex[2] = {H.ext[2 * b], H.ext[2 * b + 1]};
+        const float xs[3] = {x4.x, x4.y, x4.z};
+        for (int a = 0; a < 3; ++a) {
+            for (int side = 0; side < 2; ++side) {
+                if (!(p.walls & (1 << (2 * a + side)))) continue;
+                const uint32_t k = (ex[side] >> (8 * a)) & 0xffu;
+                const v3 r = rot(R, f3(V[k]));
+                const float rc[3] = {r.x, r.y, r.z};
+                const float xa = xs[a] + rc[a];
+                const float gap = side == 0 ? xa - p.lo[a] : p.hi[a] - xa;
+                if (!(gap < 0.0f)) continue;
+                float nn[3] = {0.0f, 0.0f, 0.0f};
+                nn[a] = side == 0 ? 1.0f : -1.0f;
+                const v3 vc = vadd(f3(v4), vcross(f3(w4), r));
+                const v3 fw = contact_force(p, -gap, mk(nn[0], nn[1], nn[2]), vc, x4.w);
+                f = vadd(f, fw);
+                t = vadd(t, vcross(r, fw));
+            }
+        }
+    }
+    if (H.force) H.force[b] = make_float4(f.x, f.y, f.z, 0.f);
+    if (H.torque) H.torque[b] = make_float4(t.x, t.y, t.z, 0.f);
+    const float dt = p.dt, m = x4.w;
+    const float vx = v4.x + dt * (f.x / m + p.g[0]);
+    const float vy = v4.y + dt * (f.y / m + p.g[1]);
+    const float vz = v4.z + dt * (f.z / m + p.g[2]);
+    const float px = x4.x + dt * vx, py = x4.y + dt * vy, pz = x4.z + dt * vz;
+    const float4 L4 = H.ang[b];
+    const float Lx = L4.x + dt * t.x, Ly = L4.y + dt * t.y, Lz = L4.z + dt * t.z;
+    const float4 ii = H.iinv[b];
+    v3 lb = rotT(R, mk(Lx, Ly, Lz));
+    lb = mk(lb.x * ii.x, lb.y * ii.y, lb.z * ii.z);
+    const v3 om = rot(R, lb);
+    const float wx = om.x, wy = om.y, wz = om.z;
+    const float qs = q4.x, qx = q4.y, qy = q4.z, qz = q4.w;
+    const float h = 0.5f * dt;
+    const float ds = -((wx * qx + wy * qy) + wz * qz);
+    const float dx = qs * wx + (wy * qz - wz * qy);
+    const float dy = qs * wy + (wz * qx - wx * qz);
+    const float dz = qs * wz + (wx * qy - wy * qx);
+    const float ns = qs + h * ds, nx = qx + h * dx, ny = qy + h * dy, nz = qz + h * dz;
+    const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
+    H.pos[b] = make_float4(px, py, pz, m);
+    H.vel[b] = make_float4(vx, vy, vz, 0.f);
+    H.ang[b] = make_float4(Lx, Ly, Lz, 0.f);
+    H.quat[b] = make_float4(ns / nrm, nx / nrm, ny / nrm, nz / nrm);
+    H.omg[b] = make_float4(wx, wy, wz, 0.f);
+}
+
+// Step statistics over the unique pairs (entries with self < other):
+// [0] pairs, [1] GJK support evaluations, [2] intersecting pairs,
+// [3] EPA iterations.
+__global__ void hull_stats_kernel(HullBuffers H, unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long s[4];
+    if (threadIdx.x < 4) s[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t total = min((uint64_t)H.off[H.nb], H.cap);
+    unsigned long long c[4] = {0, 0, 0, 0};
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        if (H.self[e] > H.partners[e]) continue;
+        const uint32_t inf = H.info[e];
+        c[0] += 1;
+        c[1] += (inf >> 8) & 0xffu;
+        c[2] += (inf & 0xffu) == (uint32_t)kHit;
+        c[3] += (inf >> 16) & 0xffu;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        for (int o = 16; o > 0; o >>= 1) c[k] += __shfl_down_sync(0xffffffffu, c[k], o);
+        if (lane_id() == 0) atomicAdd(&s[k], c[k]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) atomicAdd(out + threadIdx.x, s[threadIdx.x]);
+}
+
+inline uint32_t grid_for(uint64_t n, int threads) { return (uint32_t)((n + threads - 1) / threads); }
+
+}  // namespace
+
+cudaError_t hull_aabb_async(HullBuffers& H, cudaStream_t st) {
+    if (H.nb == 0) return cudaSuccess;
+    hull_aabb_kernel<<<grid_for(H.nb, 128), 128, 0, st>>>(H);
+    return cudaGetLastError();
+}
+
+cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st) {
+    if (H.nb == 0 || H.cap == 0) return cudaSuccess;
+    hull_prev_seed_kernel<<<grid_for(H.cap, 256), 256, 0, st>>>(H, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st) {
+    if (H.nb == 0 || H.cap == 0) return cudaSuccess;
+    hull_entry_kernel<<<grid_for(H.cap, kHullThreads), kHullThreads, 0, st>>>(p, H);
+    return cudaGetLastError();
+}
+
+cudaError_t hull_integrate_async(const HullParams& p, HullBuffers& H, cudaStream_t st) {
+    if (H.nb == 0) return cudaSuccess;
+    hull_integrate_kernel<<<grid_for(H.nb, 128), 128, 0, st>>>(p, H);
+    return cudaGetLastError();
+}
+
+cudaError_t hull_stats_async(HullBuffers& H, unsigned long long* out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 4 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess || H.nb == 0 || H.cap == 0) return e;
+    hull_stats_kernel<<<152, 256, 0, st>>>(H, out);
+    return cudaGetLastError();
+}
+
+}  // namespace sd

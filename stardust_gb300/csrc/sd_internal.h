@@ -54,6 +54,70 @@ cudaError_t ref_candidate_pairs_async(const uint32_t* cells, const uint32_t* sph
                                       uint64_t cap, unsigned long long* d_npairs, uint32_t* scratch,
                                       cudaStream_t st);
 
+// ---- scans and the LBVH broad phase (sd_lbvh.cu)
+uint64_t scan_scratch_words(uint32_t n);
+// out[0..n) = exclusive prefix sums of in, out[n] = total
+cudaError_t scan_exclusive_async(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch, cudaStream_t st);
+
+struct Lbvh {
+    uint32_t n;                          // leaves (boxes)
+    uint32_t *keys, *vals, *keys_tmp, *vals_tmp;
+    const uint32_t *skeys, *svals;       // sorted Morton codes / box ids (after the build)
+    uint32_t* sort_scratch;
+    float *bounds, *bound_part;          // global box (lo xyz, hi xyz) and per-block partials
+    int2* children;                      // n-1 internal nodes; bit 31 marks a leaf child
+    int32_t* parent;                     // internal nodes [0, n-1), leaves [n-1, 2n-1); root -1
+    uint32_t* visit;                     // refit arrival counters
+    float4 *node_lo, *node_hi, *leaf_lo, *leaf_hi;
+    uint32_t* counts;                    // per box id
+    uint32_t* scan_scratch;
+    uint32_t* status;                    // device error bits
+};
+uint64_t lbvh_scratch_bytes(uint32_t n);
+void lbvh_carve(void* scratch, uint32_t n, Lbvh* t);
+cudaError_t lbvh_morton_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
+cudaError_t lbvh_build_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
+// per box id: partners at [off[id], off[id+1]) ascending, self[] = id; off has n+1
+cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint32_t* self, uint64_t cap,
+                                cudaStream_t st);
+// ascending unique pairs (i < j) from the partner lists; pos has n+1 (pos[n] = count)
+cudaError_t lbvh_unique_pairs_async(Lbvh& t, const uint32_t* off, const uint32_t* partners, uint32_t* pos,
+                                    unsigned long long* out, uint64_t cap, cudaStream_t st);
+
+// ---- convex hulls (sd_hull.cu)
+struct HullParams {
+    float lo[3], hi[3];
+    float kn, damp, mu;
+    float g[3];
+    float dt;
+    int32_t walls;
+};
+
+struct HullBuffers {
+    uint32_t nb;
+    float4 *pos, *vel, *quat, *omg, *ang;  // (x,y,z,m), v, q=(s,x,y,z), w, world L
+    float4* iinv;                          // body-frame principal inverse inertia, w = bounding radius
+    uint32_t *vstart, *vcount;
+    float4* verts;                         // body-frame vertices
+    float4 *lo, *hi;                       // world AABBs
+    uint32_t* ext;                         // 2 per body: vertex index of min x|y<<8|z<<16, of max
+    uint32_t *off, *partners, *self;       // candidate entries (CSR, off has nb+1)
+    uint64_t cap;                          // entry capacity
+    float4 *ef, *et;                       // per entry: force / torque on self
+    uint32_t* info;                        // per entry: status | gjk iters << 8 | epa iters << 16
+    float4* dir;                           // per entry: final search direction in A's frame, w = 1 if separated
+    float4* seeds;                         // per entry: seed in A's frame, w = 1 to use (may be null)
+    float* feat;                           // per entry: 16 MLP inputs (may be null)
+    const uint32_t *prev_off, *prev_partners;  // the previous step's lists
+    const float4* prev_dir;
+    float4 *force, *torque;                // optional per body totals
+};
+cudaError_t hull_aabb_async(HullBuffers& H, cudaStream_t st);
+cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st);
+cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
+cudaError_t hull_integrate_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
+cudaError_t hull_stats_async(HullBuffers& H, unsigned long long* out, cudaStream_t st);
+
 // ---- physics pipeline (sd_dem.cu)
 struct DemParams {
     float lo[3], hi[3];

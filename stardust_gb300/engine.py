@@ -130,6 +130,53 @@ class DEMEngine:
     def n_bodies(self) -> int:
         return int(self.stats()["n_bodies"])
 
+    # -- convex hulls
+    def add_hull(self, points, mass: float, position, quat=None, velocity=(0.0, 0.0, 0.0),
+                 omega=(0.0, 0.0, 0.0)) -> None:
+        """One convex hull of `points` (n x 3, local frame) at `position`
+        with orientation `quat` (s, x, y, z)."""
+        pts = np.zeros((len(points), 4), np.float32)
+        pts[:, :3] = np.asarray(points, np.float32)
+        p = (C.c_float * 3)(*position)
+        q = None if quat is None else (C.c_float * 4)(*quat)
+        v = (C.c_float * 3)(*velocity)
+        w = (C.c_float * 3)(*omega)
+        self._call("sd_engine_add_hull", len(pts), pts.ctypes.data, mass, p, q, v, w)
+
+    def hull_shapes(self):
+        """(vstart, vcount, principal-frame vertices float4)."""
+        nb = self.n_bodies
+        nv = C.c_uint64()
+        self._call("sd_engine_get_hull_shapes", None, None, None, 0, C.byref(nv))
+        vs = np.empty(nb, np.uint32)
+        vc = np.empty(nb, np.uint32)
+        verts = np.empty((max(nv.value, 1), 4), np.float32)
+        self._call("sd_engine_get_hull_shapes", vs.ctypes.data, vc.ctypes.data, verts.ctypes.data, nv.value,
+                   C.byref(nv))
+        return vs, vc, verts[: nv.value]
+
+    def set_gjk_seed(self, mode: int) -> None:
+        self._call("sd_engine_set_gjk_seed", mode)
+
+    def hull_entries(self) -> dict:
+        """The last step's candidate entries (CSR) with status, iterations,
+        final directions, seeds and network inputs."""
+        nb = self.n_bodies
+        m = C.c_uint64()
+        off = np.empty(nb + 1, np.uint32)
+        self._call("sd_engine_hull_entries", off.ctypes.data, None, None, None, None, None, 0, C.byref(m))
+        n = m.value
+        part = np.empty(max(n, 1), np.uint32)
+        info = np.empty(max(n, 1), np.uint32)
+        d4 = np.empty((max(n, 1), 4), np.float32)
+        s4 = np.empty((max(n, 1), 4), np.float32)
+        f16 = np.empty((max(n, 1), 16), np.float32)
+        self._call("sd_engine_hull_entries", off.ctypes.data, part.ctypes.data, info.ctypes.data, d4.ctypes.data,
+                   s4.ctypes.data, f16.ctypes.data, n, C.byref(m))
+        return {"off": off, "partners": part[:n], "status": (info[:n] & 0xFF).astype(np.int32),
+                "iters": ((info[:n] >> 8) & 0xFF).astype(np.int32), "epa_iters": ((info[:n] >> 16) & 0xFF).astype(np.int32),
+                "dir": d4[:n], "seeds": s4[:n], "feat": f16[:n]}
+
     def bodies(self, field: int) -> np.ndarray:
         """Rigid-body field (SD_BODY_*), one float4 row per body (3 rows per
         body for SD_BODY_INV_INERTIA)."""
@@ -217,6 +264,7 @@ class DEMEngine:
             "n_spheres": s.n_spheres, "steps": s.steps, "contacts": s.contacts,
             "kinetic_energy": s.kinetic_energy, "momentum": tuple(s.momentum),
             "device_errors": s.device_errors, "n_cells": s.n_cells, "n_bodies": s.n_bodies,
+            "gjk_pairs": s.gjk_pairs, "gjk_iters": s.gjk_iters, "epa_iters": s.epa_iters,
         }
 
     def params(self) -> dict:
@@ -310,3 +358,45 @@ class SpatialPartition:
              None if body_of is None else body_of.data_ptr(), pair_a.data_ptr(), pair_b.data_ptr(), cap,
              npairs.data_ptr(), scratch.data_ptr(), scratch.numel() * scratch.element_size(),
              SpatialPartition._stream(stream))
+
+
+class BoundingVolumes:
+    """LBVH broad phase over boxes (sandbox/testLBVH.cu as raw device
+    operators) on CUDA tensors: lo/hi are (n, 4) float32 (x, y, z, -)."""
+
+    @staticmethod
+    def scratch_bytes(n: int, pair_cap: int) -> int:
+        b = C.c_uint64()
+        call("sd_lbvh_scratch_bytes", n, pair_cap, C.byref(b))
+        return b.value
+
+    @staticmethod
+    def pairs(lo, hi, cap: int, stream=None):
+        """Ascending unique pairs (i < j) of overlapping boxes as an int64
+        tensor of (i << 32 | j), and the device error bits."""
+        import torch
+        n = lo.shape[0]
+        scratch = torch.empty(BoundingVolumes.scratch_bytes(n, cap), dtype=torch.uint8, device=lo.device)
+        out = torch.empty(max(cap, 1), dtype=torch.int64, device=lo.device)
+        cnt = torch.zeros(2, dtype=torch.int32, device=lo.device)
+        call("sd_lbvh_pairs", n, lo.data_ptr(), hi.data_ptr(), out.data_ptr(), cap, cnt.data_ptr(),
+             scratch.data_ptr(), scratch.numel(), SpatialPartition._stream(stream))
+        c = cnt.cpu().numpy().view(np.uint32)
+        return out[: min(int(c[0]), cap)], int(c[0]), int(c[1])
+
+    @staticmethod
+    def morton(lo, hi, stream=None):
+        import torch
+        n = lo.shape[0]
+        scratch = torch.empty(BoundingVolumes.scratch_bytes(n, 0), dtype=torch.uint8, device=lo.device)
+        codes = torch.empty(max(n, 1), dtype=torch.int32, device=lo.device)
+        call("sd_lbvh_morton", n, lo.data_ptr(), hi.data_ptr(), codes.data_ptr(), scratch.data_ptr(),
+             scratch.numel(), SpatialPartition._stream(stream))
+        return codes[:n]
+
+
+def add_hull_scene(eng: DEMEngine, points, pos, quat, vel, mass, omega=None) -> None:
+    """Adds scenes.hull_box's hulls in order."""
+    for i in range(len(points)):
+        eng.add_hull(points[i], float(mass[i]), tuple(pos[i]), tuple(quat[i]), tuple(vel[i]),
+                     (0.0, 0.0, 0.0) if omega is None else tuple(omega[i]))

@@ -1,0 +1,144 @@
+"""Convex hulls on the GPU against the CPU oracle, through the C ABI.
+
+LBVH (sandbox/testLBVH.cu) pair sets and Morton codes are compared
+bit-exactly with oracle/sd_oracle_hull.c; the hull step (AABBs, LBVH,
+GJK/EPA per candidate entry, segmented force sum, quaternion integration)
+is compared bit-exactly, state and per-entry GJK results, over several
+steps."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def _boxes(n, seed, lo=0.0, hi=1.0, hmin=0.002, hmax=0.02):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    h = rng.uniform(hmin, hmax, (n, 3)).astype(np.float32)
+    L = np.zeros((n, 4), np.float32)
+    H = np.zeros((n, 4), np.float32)
+    L[:, :3] = c - h
+    H[:, :3] = c + h
+    return L, H
+
+
+@pytest.mark.parametrize("n,seed", [(0, 0), (1, 0), (2, 1), (777, 2), (50_000, 3)])
+def test_lbvh_pairs_bit_exact(sdlib, orc, n, seed):
+    import torch
+    L, H = _boxes(n, seed, -0.3, 1.7)
+    if n >= 2:
+        L[1], H[1] = L[0], H[0]  # duplicate box (equal Morton codes)
+    want = orc.aabb_pairs(L, H)
+    cap = len(want) + 16
+    got, cnt, err = sdlib.BoundingVolumes.pairs(torch.from_numpy(L).cuda(), torch.from_numpy(H).cuda(), cap)
+    torch.cuda.synchronize()
+    assert err == 0 and cnt == len(want)
+    assert np.array_equal(got.cpu().numpy().view(np.uint64), want)
+
+
+def test_lbvh_pairs_overflow_is_reported(sdlib, orc):
+    import torch
+    L, H = _boxes(3000, 4, hmin=0.02, hmax=0.05)
+    want = orc.aabb_pairs(L, H)
+    got, cnt, err = sdlib.BoundingVolumes.pairs(torch.from_numpy(L).cuda(), torch.from_numpy(H).cuda(), 10)
+    assert err & sdlib._abi.SD_DEVERR_PAIR_OVERFLOW
+    assert len(want) > 10
+
+
+def test_lbvh_morton_bit_exact(sdlib, orc):
+    import torch
+    L, H = _boxes(20_000, 5, -0.5, 2.0)
+    glo = L[:, :3].min(0)
+    ghi = H[:, :3].max(0)
+    want = orc.morton_ref(L, H, glo, ghi)
+    got = sdlib.BoundingVolumes.morton(torch.from_numpy(L).cuda(), torch.from_numpy(H).cuda())
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), want)
+
+
+def hull_engine(sd, n=3000, seed=1, spacing=0.0195, seed_mode=0, gravity=(0.0, 0.0, -9.81)):
+    from stardust_gb300 import _abi, scenes
+    pts, pos, quat, vel, mass, cfg, dt = scenes.hull_box(n, seed=seed, box=(0.4, 0.4, 0.4), spacing=spacing,
+                                                          vmax=0.3)
+    cfg.gravity = gravity
+    cfg.flags = _abi.SD_FLAG_RECORD
+    eng = sd.DEMEngine(cfg)
+    sd.add_hull_scene(eng, pts, pos, quat, vel, mass)
+    eng.prepare()
+    eng.set_gjk_seed(seed_mode)
+    return eng, cfg, dt
+
+
+def oracle_hulls(orc, eng):
+    from stardust_gb300 import _abi
+    vs, vc, verts = eng.hull_shapes()
+    b = {k: eng.bodies(f) for k, f in (("pos", _abi.SD_BODY_POSITION), ("vel", _abi.SD_BODY_VELOCITY),
+                                         ("quat", _abi.SD_BODY_QUATERNION), ("omg", _abi.SD_BODY_OMEGA),
+                                         ("ang", _abi.SD_BODY_ANGMOM), ("iinv", _abi.SD_BODY_HULL_INV_INERTIA))}
+    return orc.Hulls(b["pos"], b["vel"], b["quat"], b["omg"], b["ang"], b["iinv"], vs, vc, verts)
+
+
+def oracle_params(orc, cfg, dt):
+    return orc.hull_params(cfg.box_lo, cfg.box_hi, cfg.kn, orc.damp_from(cfg.kn, cfg.restitution), cfg.mu,
+                           cfg.gravity, dt, cfg.walls)
+
+
+@pytest.mark.parametrize("steps", [1, 5, 40])
+def test_hull_steps_bit_exact(sdlib, orc, steps):
+    from stardust_gb300 import _abi
+    eng, cfg, dt = hull_engine(sdlib)
+    H = oracle_hulls(orc, eng)
+    p = oracle_params(orc, cfg, dt)
+    for _ in range(steps):
+        out = H.step(p, record=True)
+    eng.step(dt, steps)
+    eng.sync()
+    st = eng.stats()
+    assert st["device_errors"] == 0
+    for k, f in (("pos", _abi.SD_BODY_POSITION), ("vel", _abi.SD_BODY_VELOCITY), ("quat", _abi.SD_BODY_QUATERNION),
+                 ("omg", _abi.SD_BODY_OMEGA), ("ang", _abi.SD_BODY_ANGMOM)):
+        assert np.array_equal(bits(eng.bodies(f)), bits(getattr(H, k))), k
+    assert np.array_equal(bits(eng.bodies(_abi.SD_BODY_FORCE)), bits(out["force"]))
+    assert np.array_equal(bits(eng.bodies(_abi.SD_BODY_TORQUE)), bits(out["torque"]))
+    e = eng.hull_entries()
+    assert np.array_equal(e["off"], out["off"]) and np.array_equal(e["partners"], out["partners"])
+    assert np.array_equal(e["status"], out["status"]) and np.array_equal(e["iters"], out["iters"])
+    hits = int((out["status"] == 1).sum())
+    assert hits > 20
+    uniq = e["partners"] > np.repeat(np.arange(len(e["off"]) - 1), np.diff(e["off"]))
+    assert st["gjk_pairs"] == int(uniq.sum())
+    assert st["gjk_iters"] == int(e["iters"][uniq].sum())
+    eng.close()
+
+
+def test_previous_direction_seed_cuts_iterations(sdlib, orc):
+    """Seeding GJK with the pair's previous separating direction: the same
+    contacts and bit-identical state (the seed only moves the iteration
+    count), fewer support evaluations, and the oracle fed the same seeds
+    agrees bit for bit."""
+    from stardust_gb300 import _abi
+    runs = {}
+    for mode in (_abi.SD_GJK_SEED_PLAIN, _abi.SD_GJK_SEED_PREVIOUS):
+        eng, cfg, dt = hull_engine(sdlib, seed_mode=mode)
+        eng.step(dt, 30)
+        H = oracle_hulls(orc, eng)
+        eng.step(dt, 1)
+        eng.sync()
+        e = eng.hull_entries()
+        st = eng.stats()
+        out = H.step(oracle_params(orc, cfg, dt), off=e["off"], partners=e["partners"],
+                     seeds=e["seeds"] if mode else None, record=True)
+        assert np.array_equal(e["iters"], out["iters"]) and np.array_equal(e["status"], out["status"])
+        assert np.array_equal(bits(eng.bodies(_abi.SD_BODY_POSITION)), bits(H.pos))
+        runs[mode] = (st, e, eng.bodies(_abi.SD_BODY_POSITION))
+        eng.close()
+    plain, prev = runs[0], runs[2]
+    assert np.array_equal(plain[1]["status"] == 1, prev[1]["status"] == 1)
+    mean_plain = plain[0]["gjk_iters"] / plain[0]["gjk_pairs"]
+    mean_prev = prev[0]["gjk_iters"] / prev[0]["gjk_pairs"]
+    assert mean_prev < 0.75 * mean_plain, (mean_plain, mean_prev)
+    d = np.abs(plain[2][:, :3].astype(np.float64) - prev[2][:, :3])
+    assert d.max() < 1e-6
