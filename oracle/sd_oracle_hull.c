@@ -233,128 +233,175 @@ typedef struct {
     v3 d;
 } simplex_t;
 
-static void simplex_line(simplex_t* S) {
-    const v3 A = S->s[0].w, B = S->s[1].w;
-    const v3 AB = vsub(B, A), AO = vneg(A);
-    if (vdot(AB, AO) > 0.0f) {
-        S->d = vtriple(AB, AO, AB);
-    } else {
-        S->n = 1;
-        S->d = AO;
-    }
-}
-
-static void simplex_tri(simplex_t* S) {
-    const v3 A = S->s[0].w, B = S->s[1].w, C = S->s[2].w;
-    const v3 AB = vsub(B, A), AC = vsub(C, A), AO = vneg(A);
-    const v3 ABC = vcross(AB, AC);
-    int star = 0;
-    if (vdot(vcross(ABC, AC), AO) > 0.0f) {
-        if (vdot(AC, AO) > 0.0f) {
-            S->s[1] = S->s[2];
-            S->n = 2;
-            S->d = vtriple(AC, AO, AC);
-            return;
-        }
-        star = 1;
-    } else if (vdot(vcross(AB, ABC), AO) > 0.0f) {
-        star = 1;
-    }
-    if (star) {
-        S->n = 2;
-        if (vdot(AB, AO) > 0.0f) {
-            S->d = vtriple(AB, AO, AB);
-        } else {
-            S->n = 1;
-            S->d = AO;
-        }
+/* Closest point to the origin of the simplex S->s[0..n) (Ericson, Real-Time
+ * Collision Detection, 5.1.2, 5.1.5, 5.1.6: Voronoi-region tests of the
+ * segment, triangle and tetrahedron).  Reduces the simplex to the vertices of
+ * the closest feature (kept in their order) and returns the point in *v; for
+ * a tetrahedron that contains the origin returns 1 and leaves S whole. */
+static void closest_tri(const csop* A, const csop* B, const csop* C, v3* v, int* mask) {
+    const v3 ab = vsub(B->w, A->w), ac = vsub(C->w, A->w), ap = vneg(A->w);
+    const float d1 = vdot(ab, ap), d2 = vdot(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) { *v = A->w; *mask = 1; return; }
+    const v3 bp = vneg(B->w);
+    const float d3 = vdot(ab, bp), d4 = vdot(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) { *v = B->w; *mask = 2; return; }
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+        const float t = d1 / (d1 - d3);
+        *v = vadd(A->w, vscale(ab, t));
+        *mask = 3;
         return;
     }
-    if (vdot(ABC, AO) > 0.0f) {
-        S->d = ABC;
-    } else {
-        const csop t = S->s[1];
-        S->s[1] = S->s[2];
-        S->s[2] = t;
-        S->d = vneg(ABC);
+    const v3 cp = vneg(C->w);
+    const float d5 = vdot(ab, cp), d6 = vdot(ac, cp);
+    if (d6 >= 0.0f && d5 <= d6) { *v = C->w; *mask = 4; return; }
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+        const float t = d2 / (d2 - d6);
+        *v = vadd(A->w, vscale(ac, t));
+        *mask = 5;
+        return;
     }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+        const float t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        *v = vadd(B->w, vscale(vsub(C->w, B->w), t));
+        *mask = 6;
+        return;
+    }
+    const float den = 1.0f / ((va + vb) + vc);
+    const float s = vb * den, t = vc * den;
+    *v = vadd(vadd(A->w, vscale(ab, s)), vscale(ac, t));
+    *mask = 7;
 }
 
-static int simplex_tet(simplex_t* S) {
-    const v3 A = S->s[0].w, B = S->s[1].w, C = S->s[2].w, D = S->s[3].w;
-    const v3 AO = vneg(A), AB = vsub(B, A), AC = vsub(C, A), AD = vsub(D, A);
-    const v3 ABC = vcross(AB, AC), ACD = vcross(AC, AD), ADB = vcross(AD, AB);
-    if (vdot(ABC, AO) > 0.0f) {
-        S->n = 3;
-        simplex_tri(S);
-        return 0;
-    }
-    if (vdot(ACD, AO) > 0.0f) {
-        S->s[1] = S->s[2];
-        S->s[2] = S->s[3];
-        S->n = 3;
-        simplex_tri(S);
-        return 0;
-    }
-    if (vdot(ADB, AO) > 0.0f) {
-        const csop b = S->s[1];
-        S->s[1] = S->s[3];
-        S->s[2] = b;
-        S->n = 3;
-        simplex_tri(S);
-        return 0;
-    }
-    return 1;
+static void keep(simplex_t* S, const int* idx, int m) {
+    csop t[4];
+    for (int k = 0; k < m; ++k) t[k] = S->s[idx[k]];
+    for (int k = 0; k < m; ++k) S->s[k] = t[k];
+    S->n = m;
 }
 
-/* GJK on B - A from seed direction d0.  Returns the status, the number of
- * support evaluations in *iters and, for a separated pair, the final search
- * direction (a separating direction) in *dir. */
+static void keep_mask(simplex_t* S, const int* tri, int mask) {
+    int idx[3], m = 0;
+    for (int k = 0; k < 3; ++k)
+        if (mask & (1 << k)) idx[m++] = tri[k];
+    keep(S, idx, m);
+}
+
+static int closest_simplex(simplex_t* S, v3* v) {
+    if (S->n == 1) {
+        *v = S->s[0].w;
+        return 0;
+    }
+    if (S->n == 2) {
+        const v3 A = S->s[0].w, ab = vsub(S->s[1].w, A);
+        const float t = vdot(vneg(A), ab);
+        if (t <= 0.0f) {
+            S->n = 1;
+            *v = A;
+            return 0;
+        }
+        const float den = vdot(ab, ab);
+        if (t >= den) {
+            S->s[0] = S->s[1];
+            S->n = 1;
+            *v = S->s[0].w;
+            return 0;
+        }
+        *v = vadd(A, vscale(ab, t / den));
+        return 0;
+    }
+    if (S->n == 3) {
+        static const int tri[3] = {0, 1, 2};
+        int mask;
+        closest_tri(&S->s[0], &S->s[1], &S->s[2], v, &mask);
+        keep_mask(S, tri, mask);
+        return 0;
+    }
+    /* tetrahedron: faces with the opposite vertex */
+    static const int face[4][4] = {{0, 1, 2, 3}, {0, 2, 3, 1}, {0, 3, 1, 2}, {1, 3, 2, 0}};
+    int best = -1, best_mask = 0;
+    float best_d = 0.0f;
+    v3 best_v = mk(0.0f, 0.0f, 0.0f);
+    for (int f = 0; f < 4; ++f) {
+        const v3 p = S->s[face[f][0]].w, q = S->s[face[f][1]].w, r = S->s[face[f][2]].w, o = S->s[face[f][3]].w;
+        const v3 nrm = vcross(vsub(q, p), vsub(r, p));
+        const float sp = vdot(vneg(p), nrm), so = vdot(vsub(o, p), nrm);
+        const int outside = (sp > 0.0f && so < 0.0f) || (sp < 0.0f && so > 0.0f) || so == 0.0f;
+        if (!outside) continue;
+        v3 cv;
+        int mask;
+        closest_tri(&S->s[face[f][0]], &S->s[face[f][1]], &S->s[face[f][2]], &cv, &mask);
+        const float dd = vdot(cv, cv);
+        if (best < 0 || dd < best_d) {
+            best = f;
+            best_d = dd;
+            best_v = cv;
+            best_mask = mask;
+        }
+    }
+    if (best < 0) return 1;
+    keep_mask(S, face[best], best_mask);
+    *v = best_v;
+    return 0;
+}
+
+/* GJK (distance form) on B - A from seed direction d0: v is the closest
+ * point of the current simplex to the origin, the next support is taken in
+ * -v, and the reference's test dot(w, d) < 0 ends it as separated.  Returns
+ * the status, the number of support evaluations in *iters and, for a
+ * separated pair, the separating search direction in *dir. */
 static int gjk(const hpair* P, v3 d0, simplex_t* S, int* iters, v3* dir) {
     v3 d = d0;
     if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
     csop p = cso(P, d);
     int it = 1;
+    *dir = d;
     if (vdot(p.w, d) < 0.0f) {
         *iters = it;
-        *dir = d;
         return GJK_SEP;
     }
     S->s[0] = p;
     S->n = 1;
-    S->d = vneg(p.w);
+    uint32_t seen[GJK_MAX_IT];
+    seen[0] = p.key;
+    v3 v = p.w;
+    float vv = vdot(v, v);
     for (;;) {
-        if (it >= GJK_MAX_IT) {
+        if (vv == 0.0f) {
             *iters = it;
-            *dir = S->d;
-            return GJK_NOCONV;
-        }
-        if (vzero(S->d)) {
-            *iters = it;
-            *dir = S->d;
             return GJK_TOUCH;
         }
-        p = cso(P, S->d);
-        ++it;
-        if (vdot(p.w, S->d) < 0.0f) {
+        if (it >= GJK_MAX_IT) {
             *iters = it;
-            *dir = S->d;
+            return GJK_NOCONV;
+        }
+        d = vneg(v);
+        *dir = d;
+        p = cso(P, d);
+        ++it;
+        if (vdot(p.w, d) < 0.0f) {
+            *iters = it;
             return GJK_SEP;
         }
-        S->s[3] = S->s[2];
-        S->s[2] = S->s[1];
-        S->s[1] = S->s[0];
+        /* a support point seen before in this run: no further progress is
+         * possible (the origin is on the boundary of B - A within rounding) */
+        for (int k = 0; k < it - 1; ++k) {
+            if (seen[k] == p.key) {
+                *iters = it;
+                return GJK_TOUCH;
+            }
+        }
+        seen[it - 1] = p.key;
+        for (int k = S->n; k > 0; --k) S->s[k] = S->s[k - 1];
         S->s[0] = p;
         S->n += 1;
-        if (S->n == 2) {
-            simplex_line(S);
-        } else if (S->n == 3) {
-            simplex_tri(S);
-        } else if (simplex_tet(S)) {
+        if (closest_simplex(S, &v)) {
             *iters = it;
-            *dir = S->d;
             return GJK_HIT;
         }
+        vv = vdot(v, v);
     }
 }
 
@@ -497,6 +544,11 @@ static void make_pair(hpair* P, const float* pos4, const float* quat4, const uin
     P->off = vsub(ld3(pos4 + 4 * (size_t)B), ld3(pos4 + 4 * (size_t)A));
 }
 
+/* The contact skin of a pair: 1e-4 of the summed bounding radii. */
+static inline float hull_skin(const float* iinv4, uint32_t A, uint32_t B) {
+    return (iinv4[4 * (size_t)A + 3] + iinv4[4 * (size_t)B + 3]) * 1e-4f;
+}
+
 /* The EPA stopping tolerance of a pair: 1e-7 of the summed bounding radii. */
 static inline float epa_tol(const float* iinv4, uint32_t A, uint32_t B) {
     return (iinv4[4 * (size_t)A + 3] + iinv4[4 * (size_t)B + 3]) * 1e-7f;
@@ -572,7 +624,7 @@ static int hull_entry(const sdo_hull_params* p, const float* pos4, const float* 
     simplex_t S;
     v3 dir;
     int st = gjk(&P, d0, &S, iters, &dir);
-    if (st == GJK_NOCONV && seeded) {
+    if (seeded && st != GJK_SEP) { /* only a separation certificate is taken from a seeded run */
         int it2 = 0;
         st = gjk(&P, vneg(P.off), &S, &it2, &dir);
         *iters += it2;
@@ -587,13 +639,17 @@ static int hull_entry(const sdo_hull_params* p, const float* pos4, const float* 
     epa(&P, &S, epa_tol(iinv4, A, B), &c);
     *epa_iters = c.epa_iters;
     if (!c.ok) return GJK_TOUCH;
+    /* contact skin: overlaps within it (float GJK cannot resolve them
+     * reliably) carry no force and the spring acts on depth - skin */
+    const float skin = hull_skin(iinv4, A, B);
+    if (!(c.depth > skin)) return GJK_TOUCH;
     const float mA = pos4[4 * (size_t)A + 3], mB = pos4[4 * (size_t)B + 3];
     const v3 rA = c.c, rB = vsub(c.c, P.off);
     const v3 vA = vadd(ld3(vel4 + 4 * (size_t)A), vcross(ld3(omg4 + 4 * (size_t)A), rA));
     const v3 vB = vadd(ld3(vel4 + 4 * (size_t)B), vcross(ld3(omg4 + 4 * (size_t)B), rB));
     const float meff = (mA * mB) / (mA + mB);
     v3 fb;
-    hull_contact_force(p, c.depth, c.n, vsub(vB, vA), meff, &fb);
+    hull_contact_force(p, c.depth - skin, c.n, vsub(vB, vA), meff, &fb);
     if (self == B) {
         *f = fb;
         *t = vcross(rB, fb);

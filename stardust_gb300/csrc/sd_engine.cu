@@ -276,6 +276,12 @@ sd_status resort_if_needed(sd_engine* h) {
 
 sd_status read_device_errors(sd_engine* h, uint32_t* bits) {
     uint32_t a = 0, b = 0;
+    if (h->hull_mode()) {
+        SD_CUDA(h, cudaMemcpyAsync(&a, h->hull.tree.status, 4, cudaMemcpyDeviceToHost, h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+        *bits = a;
+        return SD_OK;
+    }
     SD_CUDA(h, cudaMemcpyAsync(&a, h->B.dev_status, 4, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaMemcpyAsync(&b, h->B.sort_scratch, 4, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -289,7 +295,9 @@ sd_status errors_to_status(sd_engine* h, uint32_t bits) {
     if (bits & sd::kErrPairOverflow) return fail(h, SD_ERR_CAPACITY, "device: contact-pair buffer overflow");
     if (bits & sd::kErrWaitTimeout)
         return fail(h, SD_ERR_ITER_LIMIT, "device: a TMA tile wait hit its limit (the step used global loads)");
-    if (bits & sd::kErrBadInput) return fail(h, SD_ERR_INVALID_ARG, "device: a sphere's cell disagreed with its key");
+    if (bits & sd::kErrBadInput)
+        return fail(h, SD_ERR_INVALID_ARG, h->hull_mode() ? "device: a malformed bounding-volume tree was detected"
+                                                          : "device: a sphere's cell disagreed with its key");
     return SD_OK;
 }
 

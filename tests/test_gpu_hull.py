@@ -136,9 +136,10 @@ def test_previous_direction_seed_cuts_iterations(sdlib, orc):
         runs[mode] = (st, e, eng.bodies(_abi.SD_BODY_POSITION))
         eng.close()
     plain, prev = runs[0], runs[2]
+    # only separation certificates come from seeded runs, so the contact
+    # sets, forces and states are identical
     assert np.array_equal(plain[1]["status"] == 1, prev[1]["status"] == 1)
+    assert np.array_equal(bits(plain[2]), bits(prev[2]))
     mean_plain = plain[0]["gjk_iters"] / plain[0]["gjk_pairs"]
     mean_prev = prev[0]["gjk_iters"] / prev[0]["gjk_pairs"]
-    assert mean_prev < 0.75 * mean_plain, (mean_plain, mean_prev)
-    d = np.abs(plain[2][:, :3].astype(np.float64) - prev[2][:, :3])
-    assert d.max() < 1e-6
+    assert mean_prev < 0.6 * mean_plain, (mean_plain, mean_prev)
