@@ -426,6 +426,7 @@ sd_status sd_engine_hull_entries(sd_engine* h, uint32_t* off, uint32_t* partners
     const uint64_t m = o[nb];
     *n_entries = m;
     if (off) std::memcpy(off, o.data(), 4 * ((size_t)nb + 1));
+    if (!partners && !info && !dir4 && !seed4 && !feat16) return SD_OK;  // a count query
     if (m > cap) return sd_fail(h, SD_ERR_CAPACITY, "cap smaller than the entry count");
     if (m > S.H.cap) return sd_fail(h, SD_ERR_CAPACITY, "the step's entry buffer overflowed");
     cudaStream_t st = h->stream;
