@@ -264,6 +264,26 @@ sd_status sd_engine_set_gjk_seed(sd_engine* h, int32_t mode);
 sd_status sd_engine_hull_entries(sd_engine* h, uint32_t* off, uint32_t* partners, uint32_t* info, float* dir4,
                                  float* seed4, float* feat16, uint64_t cap, uint64_t* n_entries);
 
+/* ------------------------------------------------- GJK warm-start network
+ * 16 inputs (per candidate pair, in the body frame of its first hull A:
+ * relative quaternion conj(qA) qB (4), centre offset / (rhoA + rhoB) (3),
+ * previous-contact flag (1), the pair's previous separating direction (3),
+ * |offset| / (rhoA + rhoB) (1), zeros (4)) -> 64 -> ReLU -> 64 -> ReLU -> 3
+ * (a search direction in A's frame).  BF16 weights, FP32 accumulation on the
+ * tensor cores, trained on the GPU with Adam on the cosine loss
+ * 1 - y.t/|y| against separating directions plain GJK logged
+ * (sd_engine_hull_entries).  Parameters: 6288 floats, W1[64][16], b1[64],
+ * W2[64][64], b2[64], W3[16][64] (rows 3.. zero), b3[16].  No counterpart in
+ * the reference. */
+sd_status sd_engine_mlp_params(sd_engine* h, float* host, uint64_t n, int32_t set);
+/* Device rows of 16 inputs -> device rows (y0, y1, y2, 0). */
+sd_status sd_engine_mlp_forward(sd_engine* h, const float* d_feat16, float* d_out4, uint64_t n);
+/* Full-batch training on n device rows (inputs, target (tx, ty, tz, valid)):
+ * iters Adam steps of rate lr (iters = 0: the gradient only).  host_grad
+ * (may be NULL) receives the last gradient (6288 floats, mean over rows). */
+sd_status sd_engine_mlp_train(sd_engine* h, const float* d_feat16, const float* d_tgt4, uint64_t n, int32_t iters,
+                              float lr, float* host_grad);
+
 /* ------------------------------------------------------ LBVH operators
  * (sandbox/testLBVH.cu:42-907 as raw device operators).  Boxes are float4
  * rows lo (x, y, z, -) and hi, 16-byte aligned, n < 2^30. */

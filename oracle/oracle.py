@@ -423,3 +423,61 @@ def hulls_from_points(points, pos, quat, vel, mass, omega=None) -> Hulls:
     v4 = np.zeros((len(verts), 4))
     v4[:, :3] = verts
     return Hulls(P, V, Q, W, Lw, Ii, vs, np.array(vc, np.uint32), v4)
+
+
+# ------------------------------------------------------ warm-start network
+MLP_SIZES = {"W1": (64, 16), "b1": (64,), "W2": (64, 64), "b2": (64,), "W3": (16, 64), "b3": (16,)}
+MLP_PARAMS = 6288
+
+
+def mlp_unpack(p):
+    out, o = {}, 0
+    for k, shp in MLP_SIZES.items():
+        n = int(np.prod(shp))
+        out[k] = np.asarray(p[o:o + n], np.float64).reshape(shp)
+        o += n
+    return out
+
+
+def mlp_pack(d):
+    return np.concatenate([np.asarray(d[k], np.float32).ravel() for k in MLP_SIZES]).astype(np.float32)
+
+
+def bf16(x):
+    """Round-to-nearest-even to bfloat16, returned as float64."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def mlp_forward_backward(params, X, T, round_bf16=True):
+    """The network of sd_mlp.cu restated in float64: forward (rows of 16
+    inputs) and the gradient of mean over rows of valid * (1 - y.t/|y|),
+    with BF16 rounding where the tensor-core kernels round (inputs, hidden
+    activations, output gradient and activation gradients).  Returns
+    (y (n, 3), loss, grad (6288,))."""
+    r = bf16 if round_bf16 else (lambda a: np.asarray(a, np.float64))
+    P = mlp_unpack(params)
+    W1, W2, W3 = r(P["W1"]), r(P["W2"]), r(P["W3"])
+    n = len(X)
+    Xb = r(X)
+    Z1 = Xb @ W1.T + P["b1"]
+    H1 = r(np.maximum(Z1, 0))
+    Z2 = H1 @ W2.T + P["b2"]
+    H2 = r(np.maximum(Z2, 0))
+    Y = (H2 @ W3.T + P["b3"])[:, :3]
+    t = np.asarray(T, np.float64)
+    valid = t[:, 3] != 0
+    nn = np.sqrt((Y * Y).sum(1) + 1e-8)
+    c = (Y * t[:, :3]).sum(1) / nn
+    loss = float((valid * (1 - c)).sum() / n)
+    d = -(t[:, :3] - (c / nn)[:, None] * Y) / nn[:, None] / n
+    d[~valid] = 0
+    dY = np.zeros((n, 16))
+    dY[:, :3] = r(d)
+    dZ2 = r((dY @ W3) * (H2 > 0))
+    dZ1 = r((dZ2 @ W2) * (H1 > 0))
+    g = {"W3": dY.T @ H2, "b3": dY.sum(0), "W2": dZ2.T @ H1, "b2": dZ2.sum(0), "W1": dZ1.T @ Xb, "b1": dZ1.sum(0)}
+    g["W3"][3:] = 0
+    g["b3"][3:] = 0
+    return Y, loss, mlp_pack(g)

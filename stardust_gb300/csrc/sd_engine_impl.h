@@ -24,7 +24,8 @@ struct HullScene {
     uint32_t* partners[2] = {nullptr, nullptr};
     float4* dir[2] = {nullptr, nullptr};
     unsigned long long* stats = nullptr;          // 4 counters of the last step
-    float* mlp = nullptr;                         // warm-start network (device)
+    sd::MlpState mlp{};                           // warm-start network (device)
+    uint32_t mlp_step = 0;                        // Adam steps taken
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int parity = 0;
     int seed_mode = 0;                            // SD_GJK_SEED_*

@@ -510,11 +510,10 @@ __global__ void hull_prev_seed_kernel(HullBuffers H, uint32_t mode) {
     const bool found = lo < end && H.prev_partners[lo] == B;
     if (found) prev = H.prev_dir[lo];
     const bool have = found && prev.w != 0.0f;
-    if (mode == 2u) {
-        H.seeds[e] = have ? make_float4(prev.x, prev.y, prev.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    } else {
-        H.seeds[e] = make_float4(0.f, 0.f, 0.f, have ? 1.0f : 0.0f);
-    }
+    // mode 2 seeds from the previous direction; mode 1's seeds are written by
+    // the network afterwards; mode 0 runs plain GJK (the inputs are still
+    // recorded, for training)
+    H.seeds[e] = (mode == 2u && have) ? make_float4(prev.x, prev.y, prev.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
     if (H.feat) {
         // 12 inputs in A's body frame: relative quaternion conj(qA) (x) qB,
         // centre offset / (rhoA + rhoB), previous-contact flag, previous

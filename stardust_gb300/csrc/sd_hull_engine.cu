@@ -124,17 +124,14 @@ sd_status build_hull_graphs(sd_engine* h, float dt) {
         H.prev_off = S.off[par ^ 1];
         H.prev_partners = S.partners[par ^ 1];
         H.prev_dir = S.dir[par ^ 1];
-        if (S.seed_mode == SD_GJK_SEED_PLAIN) {
-            H.seeds = nullptr;
-            H.feat = nullptr;
-        }
         cudaGraph_t g = nullptr;
         HULL_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = sd::hull_aabb_async(H, h->stream);
         if (e == cudaSuccess) e = sd::lbvh_build_async(S.tree, H.lo, H.hi, h->stream);
         if (e == cudaSuccess) e = sd::lbvh_partners_async(S.tree, H.off, H.partners, H.self, H.cap, h->stream);
-        if (e == cudaSuccess && S.seed_mode != SD_GJK_SEED_PLAIN)
-            e = sd::hull_seed_async(H, (uint32_t)S.seed_mode, h->stream);
+        if (e == cudaSuccess) e = sd::hull_seed_async(H, (uint32_t)S.seed_mode, h->stream);
+        if (e == cudaSuccess && S.seed_mode == SD_GJK_SEED_LEARNED)
+            e = sd::mlp_forward_async(S.mlp, H.feat, H.seeds, H.off + H.nb, H.cap, true, h->stream);
         if (e == cudaSuccess) e = sd::hull_narrow_async(S.P, H, h->stream);
         if (e == cudaSuccess) e = sd::hull_integrate_async(S.P, H, h->stream);
         if (e == cudaSuccess) e = sd::hull_stats_async(H, S.stats, h->stream);
@@ -167,7 +164,7 @@ void hull_release(sd_engine* h) {
         S.dir[k] = nullptr;
     }
     S.stats = nullptr;
-    S.mlp = nullptr;
+    S.mlp = sd::MlpState{};
 }
 
 sd_status hull_prepare(sd_engine* h) {
@@ -215,6 +212,10 @@ sd_status hull_prepare(sd_engine* h) {
     void* tm = nullptr;
     if ((s = sd_alloc_bytes(h, &tm, sd::lbvh_scratch_bytes(nb)))) return s;
     sd::lbvh_carve(tm, nb, &S.tree);
+    void* mm = nullptr;
+    if ((s = sd_alloc_bytes(h, &mm, sd::mlp_state_bytes()))) return s;
+    S.mlp = sd::mlp_carve(mm);
+    HULL_CUDA(h, sd::mlp_init_kernels());
     cudaStream_t st = h->stream;
     HULL_CUDA(h, cudaMemcpyAsync(H.pos, S.pos.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, st));
     HULL_CUDA(h, cudaMemcpyAsync(H.vel, S.vel.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, st));
@@ -228,7 +229,29 @@ sd_status hull_prepare(sd_engine* h) {
     for (int k = 0; k < 2; ++k) HULL_CUDA(h, cudaMemsetAsync(S.off[k], 0, 4 * ((size_t)nb + 1), st));
     HULL_CUDA(h, cudaMemsetAsync(S.tree.status, 0, 16, st));
     HULL_CUDA(h, cudaMemsetAsync(S.stats, 0, 32, st));
-    HULL_CUDA(h, cudaStreamSynchronize(st));
+    HULL_CUDA(h, cudaMemsetAsync(S.mlp.status, 0, 16, st));
+    {
+        // network initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from
+        // a fixed SplitMix64 stream (only the 3 used outputs of layer 3)
+        std::vector<float> w(sd::mlp_param_count(), 0.0f);
+        uint64_t z = 0x5eed5eedull;
+        auto u01 = [&z]() {
+            uint64_t x = (z += 0x9e3779b97f4a7c15ull);
+            x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+            x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+            x ^= x >> 31;
+            return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+        };
+        const int in = 16, hid = 64;
+        for (int i = 0; i < hid * in; ++i) w[i] = (float)((2 * u01() - 1) / std::sqrt(12.0));
+        const int w2 = hid * in + hid;
+        for (int i = 0; i < hid * hid; ++i) w[w2 + i] = (float)((2 * u01() - 1) / std::sqrt((double)hid));
+        const int w3 = w2 + hid * hid + hid;
+        for (int i = 0; i < 3 * hid; ++i) w[w3 + i] = (float)((2 * u01() - 1) / std::sqrt((double)hid));
+        HULL_CUDA(h, sd::mlp_set_params_async(S.mlp, w.data(), st));
+        S.mlp_step = 0;
+        HULL_CUDA(h, cudaStreamSynchronize(st));
+    }
     S.parity = 0;
     S.graph_valid = false;
     h->prepared = true;
@@ -407,7 +430,6 @@ sd_status sd_engine_set_gjk_seed(sd_engine* h, int32_t mode) {
     if (!h) return sd_fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
     if (mode != SD_GJK_SEED_PLAIN && mode != SD_GJK_SEED_LEARNED && mode != SD_GJK_SEED_PREVIOUS)
         return sd_fail(h, SD_ERR_INVALID_ARG, "unknown GJK seed mode");
-    if (mode == SD_GJK_SEED_LEARNED) return sd_fail(h, SD_ERR_UNSUPPORTED, "the learned seed is not built yet");
     h->hull.seed_mode = mode;
     h->hull.graph_valid = false;
     return SD_OK;
@@ -436,6 +458,66 @@ sd_status sd_engine_hull_entries(sd_engine* h, uint32_t* off, uint32_t* partners
     if (seed4) HULL_CUDA(h, cudaMemcpyAsync(seed4, S.H.seeds, 16 * m, cudaMemcpyDeviceToHost, st));
     if (feat16) HULL_CUDA(h, cudaMemcpyAsync(feat16, S.H.feat, 64 * m, cudaMemcpyDeviceToHost, st));
     HULL_CUDA(h, cudaStreamSynchronize(st));
+    return SD_OK;
+}
+
+// ------------------------------------------------ warm-start network
+sd_status sd_engine_mlp_params(sd_engine* h, float* host, uint64_t n, int32_t set) {
+    if (!h || !host) return sd_fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared || !h->hull_mode()) return sd_fail(h, SD_ERR_STATE, "no prepared hull scene");
+    if (n != sd::mlp_param_count()) return sd_fail(h, SD_ERR_INVALID_ARG, "n must be the parameter count (6288)");
+    HullScene& S = h->hull;
+    HULL_CUDA(h, cudaSetDevice(h->device));
+    if (set) {
+        HULL_CUDA(h, sd::mlp_set_params_async(S.mlp, host, h->stream));
+        S.mlp_step = 0;
+    } else {
+        HULL_CUDA(h, cudaMemcpyAsync(host, S.mlp.params, 4 * n, cudaMemcpyDeviceToHost, h->stream));
+    }
+    HULL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SD_OK;
+}
+
+sd_status sd_engine_mlp_forward(sd_engine* h, const float* d_feat16, float* d_out4, uint64_t n) {
+    if (!h || (n && (!d_feat16 || !d_out4))) return sd_fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared || !h->hull_mode()) return sd_fail(h, SD_ERR_STATE, "no prepared hull scene");
+    if ((reinterpret_cast<uintptr_t>(d_feat16) | reinterpret_cast<uintptr_t>(d_out4)) & 15u)
+        return sd_fail(h, SD_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    HULL_CUDA(h, cudaSetDevice(h->device));
+    HULL_CUDA(h, sd::mlp_forward_async(h->hull.mlp, d_feat16, reinterpret_cast<float4*>(d_out4), nullptr, n, false,
+                                       h->stream));
+    HULL_CUDA(h, cudaStreamSynchronize(h->stream));
+    uint32_t st = 0;
+    HULL_CUDA(h, cudaMemcpy(&st, h->hull.mlp.status, 4, cudaMemcpyDeviceToHost));
+    if (st) return sd_fail(h, SD_ERR_ITER_LIMIT, "device: a tensor-core completion wait gave up");
+    return SD_OK;
+}
+
+sd_status sd_engine_mlp_train(sd_engine* h, const float* d_feat16, const float* d_tgt4, uint64_t n, int32_t iters,
+                              float lr, float* host_grad) {
+    if (!h || (n && (!d_feat16 || !d_tgt4))) return sd_fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared || !h->hull_mode()) return sd_fail(h, SD_ERR_STATE, "no prepared hull scene");
+    if (n >= (1ull << 31)) return sd_fail(h, SD_ERR_CAPACITY, "n must be < 2^31");
+    if (iters < 0 || !(lr >= 0.0f)) return sd_fail(h, SD_ERR_INVALID_ARG, "iters >= 0 and lr >= 0");
+    HullScene& S = h->hull;
+    HULL_CUDA(h, cudaSetDevice(h->device));
+    const float4* t4 = reinterpret_cast<const float4*>(d_tgt4);
+    if (iters == 0) {
+        HULL_CUDA(h, sd::mlp_train_async(S.mlp, d_feat16, t4, (uint32_t)n, (uint32_t)n, 0.0f, 1, false, h->stream));
+    }
+    for (int32_t k = 0; k < iters; ++k) {
+        S.mlp_step += 1;
+        HULL_CUDA(h, sd::mlp_train_async(S.mlp, d_feat16, t4, (uint32_t)n, (uint32_t)n, lr, S.mlp_step, true,
+                                         h->stream));
+    }
+    if (host_grad)
+        HULL_CUDA(h, cudaMemcpyAsync(host_grad, S.mlp.grad, 4ull * sd::mlp_param_count(), cudaMemcpyDeviceToHost,
+                                     h->stream));
+    HULL_CUDA(h, cudaStreamSynchronize(h->stream));
+    uint32_t st = 0;
+    HULL_CUDA(h, cudaMemcpy(&st, S.mlp.status, 4, cudaMemcpyDeviceToHost));
+    if (st) return sd_fail(h, SD_ERR_ITER_LIMIT, "device: a tensor-core completion wait gave up");
+    S.graph_valid = false;
     return SD_OK;
 }
 

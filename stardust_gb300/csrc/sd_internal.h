@@ -118,6 +118,27 @@ cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t 
 cudaError_t hull_integrate_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
 cudaError_t hull_stats_async(HullBuffers& H, unsigned long long* out, cudaStream_t st);
 
+// ---- GJK warm-start network (sd_mlp.cu)
+struct MlpState {
+    float *params, *m1, *m2, *grad;  // FP32 master parameters, Adam moments, last gradient
+    uint8_t* img;                    // packed BF16 operand images
+    float* part;                     // per-CTA gradient partials
+    uint32_t* status;                // device error bits
+};
+uint64_t mlp_state_bytes();
+uint32_t mlp_param_count();
+MlpState mlp_carve(void* base);
+cudaError_t mlp_init_kernels();
+cudaError_t mlp_set_params_async(MlpState& s, const float* host_params, cudaStream_t st);
+// seeds == true: out[e] = (y, 1) for rows with feat[7] == 1 (else 0), e < *d_count;
+// seeds == false: out[e] = (y, 0), e < n
+cudaError_t mlp_forward_async(const MlpState& s, const float* feat, float4* out, const uint32_t* d_count, uint64_t n,
+                              bool seeds, cudaStream_t st);
+// one full-batch gradient of the cosine loss (grad[] = its value) and, when
+// update, an Adam step (adam_step counts from 1)
+cudaError_t mlp_train_async(MlpState& s, const float* feat, const float4* tgt, uint32_t n, uint32_t n_valid, float lr,
+                            uint32_t adam_step, bool update, cudaStream_t st);
+
 // ---- physics pipeline (sd_dem.cu)
 struct DemParams {
     float lo[3], hi[3];

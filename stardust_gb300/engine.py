@@ -177,6 +177,30 @@ class DEMEngine:
                 "iters": ((info[:n] >> 8) & 0xFF).astype(np.int32), "epa_iters": ((info[:n] >> 16) & 0xFF).astype(np.int32),
                 "dir": d4[:n], "seeds": s4[:n], "feat": f16[:n]}
 
+    # -- GJK warm-start network (hull scenes)
+    def mlp_params(self) -> np.ndarray:
+        out = np.empty(6288, np.float32)
+        self._call("sd_engine_mlp_params", out.ctypes.data, 6288, 0)
+        return out
+
+    def set_mlp_params(self, params) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        self._call("sd_engine_mlp_params", p.ctypes.data, p.size, 1)
+
+    def mlp_forward(self, feat16):
+        """feat16: CUDA float32 tensor (n, 16) -> (n, 4) tensor (y0, y1, y2, 0)."""
+        import torch
+        out = torch.empty((feat16.shape[0], 4), dtype=torch.float32, device=feat16.device)
+        self._call("sd_engine_mlp_forward", feat16.data_ptr(), out.data_ptr(), feat16.shape[0])
+        return out
+
+    def mlp_train(self, feat16, tgt4, iters: int, lr: float = 1e-3) -> np.ndarray:
+        """Full-batch Adam steps on CUDA tensors; returns the last gradient."""
+        g = np.empty(6288, np.float32)
+        self._call("sd_engine_mlp_train", feat16.data_ptr(), tgt4.data_ptr(), feat16.shape[0], iters, lr,
+                   g.ctypes.data)
+        return g
+
     def bodies(self, field: int) -> np.ndarray:
         """Rigid-body field (SD_BODY_*), one float4 row per body (3 rows per
         body for SD_BODY_INV_INERTIA)."""

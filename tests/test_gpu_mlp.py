@@ -1,0 +1,139 @@
+"""The GJK warm-start network on the tensor cores (tcgen05) against its
+float64 restatement, and what it gains over plain GJK.
+
+Forward outputs and training gradients are compared with
+oracle.mlp_forward_backward, which rounds to BF16 where the kernels do;
+the remaining differences come from the FP32 accumulation order inside the
+tensor cores (and the odd BF16 rounding it flips), so the bounds are
+relative L2 errors of 1e-2."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def tiny_engine(sd):
+    from stardust_gb300 import scenes
+    pts, pos, quat, vel, mass, cfg, dt = scenes.hull_box(8, seed=0, box=(0.2, 0.2, 0.2))
+    eng = sd.DEMEngine(cfg)
+    sd.add_hull_scene(eng, pts, pos, quat, vel, mass)
+    eng.prepare()
+    return eng
+
+
+def random_batch(rng, n):
+    X = rng.normal(size=(n, 16)).astype(np.float32)
+    X[:, 12:] = 0
+    X[:, 7] = rng.random(n) < 0.7
+    t = rng.normal(size=(n, 3))
+    T = np.concatenate([t / np.linalg.norm(t, axis=1, keepdims=True), (rng.random((n, 1)) < 0.9)], 1).astype(np.float32)
+    return X, T
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("n", [1, 128, 1000, 20_000])
+def test_mlp_forward_matches_oracle(sdlib, orc, n):
+    import torch
+    eng = tiny_engine(sdlib)
+    rng = np.random.default_rng(n)
+    p = eng.mlp_params()
+    p[:-16] += rng.normal(size=p.size - 16).astype(np.float32) * 0.05
+    P = orc.mlp_unpack(p)
+    P["W3"][3:] = 0
+    p = orc.mlp_pack(P)
+    eng.set_mlp_params(p)
+    X, T = random_batch(rng, n)
+    y = eng.mlp_forward(torch.from_numpy(X).cuda()).cpu().numpy()
+    Y, _, _ = orc.mlp_forward_backward(p, X, T)
+    assert rel(y[:, :3], Y) < 1e-2
+    assert np.all(y[:, 3] == 0)
+    eng.close()
+
+
+def test_mlp_gradients_match_oracle(sdlib, orc):
+    import torch
+    eng = tiny_engine(sdlib)
+    rng = np.random.default_rng(7)
+    X, T = random_batch(rng, 3000)
+    p = eng.mlp_params()
+    g = eng.mlp_train(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), 0)
+    _, _, gr = orc.mlp_forward_backward(p, X, T)
+    G, R = orc.mlp_unpack(g), orc.mlp_unpack(gr)
+    for k in ("W1", "b1", "W2", "b2", "W3", "b3"):
+        assert rel(G[k], R[k]) < 2e-2, (k, rel(G[k], R[k]))
+    eng.close()
+
+
+def test_mlp_training_lowers_the_loss(sdlib, orc):
+    import torch
+    eng = tiny_engine(sdlib)
+    rng = np.random.default_rng(3)
+    X, T = random_batch(rng, 4096)
+    T[:, :3] = X[:, 8:11] / np.maximum(np.linalg.norm(X[:, 8:11], axis=1, keepdims=True), 1e-6)  # learnable
+    _, l0, _ = orc.mlp_forward_backward(eng.mlp_params(), X, T)
+    eng.mlp_train(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), 300, 3e-3)
+    _, l1, _ = orc.mlp_forward_backward(eng.mlp_params(), X, T)
+    assert l1 < 0.2 * l0, (l0, l1)
+    eng.close()
+
+
+def test_learned_seed_gains_over_plain_gjk(sdlib):
+    """Plain GJK logs its separating directions for 30 steps; the network is
+    trained on them (on the GPU); then a plain and a learned engine step the
+    same scene: identical contact sets and bit-identical states, and the
+    learned seed needs far fewer support evaluations per pair."""
+    import torch
+    from stardust_gb300 import _abi, scenes
+    pts, pos, quat, vel, mass, cfg, dt = scenes.hull_box(3000, seed=1, box=(0.4, 0.4, 0.4), spacing=0.0195,
+                                                          vmax=0.3)
+    mk = lambda: sdlib.DEMEngine(cfg)
+    plain = mk()
+    sdlib.add_hull_scene(plain, pts, pos, quat, vel, mass)
+    plain.prepare()
+    X, T = [], []
+    for _ in range(30):
+        plain.step(dt, 1)
+        e = plain.hull_entries()
+        selfs = np.repeat(np.arange(len(e["off"]) - 1), np.diff(e["off"]))
+        m = (e["partners"] > selfs) & (e["status"] == 0) & (e["feat"][:, 7] == 1)
+        d = e["dir"][m, :3]
+        X.append(e["feat"][m])
+        T.append(np.concatenate([d / np.linalg.norm(d, axis=1, keepdims=True), np.ones((m.sum(), 1))], 1))
+    X = torch.from_numpy(np.concatenate(X).astype(np.float32)).cuda()
+    T = torch.from_numpy(np.concatenate(T).astype(np.float32)).cuda()
+    plain.mlp_train(X, T, 400, 2e-3)
+    params = plain.mlp_params()
+    plain.close()
+
+    engines = {}
+    for mode in (_abi.SD_GJK_SEED_PLAIN, _abi.SD_GJK_SEED_LEARNED):
+        eng = mk()
+        sdlib.add_hull_scene(eng, pts, pos, quat, vel, mass)
+        eng.prepare()
+        eng.set_mlp_params(params)
+        eng.set_gjk_seed(mode)
+        engines[mode] = eng
+    it = {0: 0, 1: 0}
+    pairs = {0: 0, 1: 0}
+    for step in range(40):
+        for mode, eng in engines.items():
+            eng.step(dt, 1)
+            st = eng.stats()
+            if step >= 10:
+                it[mode] += st["gjk_iters"]
+                pairs[mode] += st["gjk_pairs"]
+        ep, el = engines[0].hull_entries(), engines[1].hull_entries()
+        assert np.array_equal(ep["status"] == 1, el["status"] == 1)
+    a = engines[0].bodies(_abi.SD_BODY_POSITION)
+    b = engines[1].bodies(_abi.SD_BODY_POSITION)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert pairs[0] == pairs[1]
+    ratio = it[0] / it[1]
+    print(f"mean GJK support evaluations per pair: plain {it[0] / pairs[0]:.3f}, learned {it[1] / pairs[1]:.3f}, "
+          f"ratio {ratio:.2f}")
+    assert ratio > 2.0
+    for eng in engines.values():
+        eng.close()
