@@ -268,8 +268,9 @@ sd_status sd_engine_hull_entries(sd_engine* h, uint32_t* off, uint32_t* partners
  * 16 inputs (per candidate pair, in the body frame of its first hull A:
  * relative quaternion conj(qA) qB (4), centre offset / (rhoA + rhoB) (3),
  * previous-contact flag (1), the pair's previous separating direction (3),
- * |offset| / (rhoA + rhoB) (1), zeros (4)) -> 64 -> ReLU -> 64 -> ReLU -> 3
- * (a search direction in A's frame).  BF16 weights, FP32 accumulation on the
+ * |offset| / (rhoA + rhoB) (1), zeros (4)) -> 64 -> ReLU -> 64 -> ReLU -> 3,
+ * added to inputs 8..10 (a residual network over the previous direction; its
+ * last layer starts at zero): a search direction in A's frame.  BF16 weights, FP32 accumulation on the
  * tensor cores, trained on the GPU with Adam on the cosine loss
  * 1 - y.t/|y| against separating directions plain GJK logged
  * (sd_engine_hull_entries).  Parameters: 6288 floats, W1[64][16], b1[64],

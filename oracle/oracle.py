@@ -452,7 +452,8 @@ def bf16(x):
 
 def mlp_forward_backward(params, X, T, round_bf16=True):
     """The network of sd_mlp.cu restated in float64: forward (rows of 16
-    inputs) and the gradient of mean over rows of valid * (1 - y.t/|y|),
+    inputs; the output adds inputs 8..10, a residual over the previous
+    direction) and the gradient of mean over rows of valid * (1 - y.t/|y|),
     with BF16 rounding where the tensor-core kernels round (inputs, hidden
     activations, output gradient and activation gradients).  Returns
     (y (n, 3), loss, grad (6288,))."""
@@ -465,7 +466,7 @@ def mlp_forward_backward(params, X, T, round_bf16=True):
     H1 = r(np.maximum(Z1, 0))
     Z2 = H1 @ W2.T + P["b2"]
     H2 = r(np.maximum(Z2, 0))
-    Y = (H2 @ W3.T + P["b3"])[:, :3]
+    Y = (H2 @ W3.T + P["b3"])[:, :3] + np.asarray(X, np.float64)[:, 8:11]  # residual over the previous direction
     t = np.asarray(T, np.float64)
     valid = t[:, 3] != 0
     nn = np.sqrt((Y * Y).sum(1) + 1e-8)

@@ -531,7 +531,9 @@ __global__ void hull_prev_seed_kernel(HullBuffers H, uint32_t mode) {
         f[0] = rs; f[1] = rx; f[2] = ry; f[3] = rz;
         f[4] = o.x; f[5] = o.y; f[6] = o.z;
         f[7] = have ? 1.0f : 0.0f;
-        f[8] = have ? prev.x : 0.0f; f[9] = have ? prev.y : 0.0f; f[10] = have ? prev.z : 0.0f;
+        const float pn = sqrtf((prev.x * prev.x + prev.y * prev.y) + prev.z * prev.z);
+        const float pi = (have && pn > 0.0f) ? 1.0f / pn : 0.0f;
+        f[8] = prev.x * pi; f[9] = prev.y * pi; f[10] = prev.z * pi;
         f[11] = sqrtf(vdot(o, o));
         f[12] = 0.0f; f[13] = 0.0f; f[14] = 0.0f; f[15] = 0.0f;
     }

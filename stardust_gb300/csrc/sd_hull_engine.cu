@@ -231,8 +231,10 @@ sd_status hull_prepare(sd_engine* h) {
     HULL_CUDA(h, cudaMemsetAsync(S.stats, 0, 32, st));
     HULL_CUDA(h, cudaMemsetAsync(S.mlp.status, 0, 16, st));
     {
-        // network initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from
-        // a fixed SplitMix64 stream (only the 3 used outputs of layer 3)
+        // network initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) for
+        // the hidden layers from a fixed SplitMix64 stream; the last layer
+        // starts at zero, so the untrained residual network returns the
+        // previous direction
         std::vector<float> w(sd::mlp_param_count(), 0.0f);
         uint64_t z = 0x5eed5eedull;
         auto u01 = [&z]() {
@@ -246,8 +248,6 @@ sd_status hull_prepare(sd_engine* h) {
         for (int i = 0; i < hid * in; ++i) w[i] = (float)((2 * u01() - 1) / std::sqrt(12.0));
         const int w2 = hid * in + hid;
         for (int i = 0; i < hid * hid; ++i) w[w2 + i] = (float)((2 * u01() - 1) / std::sqrt((double)hid));
-        const int w3 = w2 + hid * hid + hid;
-        for (int i = 0; i < 3 * hid; ++i) w[w3 + i] = (float)((2 * u01() - 1) / std::sqrt((double)hid));
         HULL_CUDA(h, sd::mlp_set_params_async(S.mlp, w.data(), st));
         S.mlp_step = 0;
         HULL_CUDA(h, cudaStreamSynchronize(st));

@@ -4,8 +4,11 @@
 // memory), plus the Adam update.
 //
 // Network: 16 inputs (12 used, see hull_prev_seed_kernel) -> 64 -> ReLU ->
-// 64 -> ReLU -> 16 outputs (3 used: a GJK search direction in the body frame
-// of the pair's first hull).  Weights are kept in FP32 (master copy, Adam
+// 64 -> ReLU -> 16 outputs (3 used), added to inputs 8..10 (the pair's
+// previous separating direction, zero for a new pair): a residual network
+// whose output is a GJK search direction in the body frame of the pair's
+// first hull.  With the last layer at zero it reproduces the previous
+// direction; training learns the correction.  Weights are kept in FP32 (master copy, Adam
 // moments) and re-packed after every update into BF16 operand images in the
 // UMMA canonical K-major layout without swizzle, so a CTA copies them to
 // shared memory as-is.
@@ -234,11 +237,12 @@ __global__ void __launch_bounds__(kRows) mlp_forward_kernel(const uint8_t* __res
     for (uint64_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         const uint64_t e = t * kRows + tid;
         const bool live = e < rows;
-        float f7 = 0.f;
+        float f7 = 0.f, skip[3] = {0.f, 0.f, 0.f};
         // layer 1 operand: this thread's row of inputs
         for (int k = 0; k < kIn; ++k) {
             const float v = live ? feat[16 * e + k] : 0.0f;
             if (k == 7) f7 = v;
+            if (k >= 8 && k < 11) skip[k - 8] = v;
             st_bf16(S.x, cm_off(tid, k, kIn), v);
         }
         if (!(ok = gemm_sync(tm + 0, S.x, S.w1, kHid, kIn, false, &S.bar, phase, status))) break;
@@ -260,7 +264,8 @@ __global__ void __launch_bounds__(kRows) mlp_forward_kernel(const uint8_t* __res
         float y[16];
         tmem_ld16(tm + lane_base + 128, y);
         if (live) {
-            const float y0 = y[0] + S.b[2 * kHid], y1 = y[1] + S.b[2 * kHid + 1], y2 = y[2] + S.b[2 * kHid + 2];
+            const float y0 = (y[0] + S.b[2 * kHid]) + skip[0], y1 = (y[1] + S.b[2 * kHid + 1]) + skip[1],
+                        y2 = (y[2] + S.b[2 * kHid + 2]) + skip[2];
             if (MODE == 0)
                 out[e] = f7 == 1.0f ? make_float4(y0, y1, y2, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
             else
@@ -339,7 +344,12 @@ __global__ void __launch_bounds__(kRows) mlp_train_kernel(const uint8_t* __restr
     for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         const uint32_t e = t * kRows + tid;
         const bool live = e < n;
-        for (int k = 0; k < kIn; ++k) st_bf16(S.x, cm_off(tid, k, kIn), live ? feat[16 * (size_t)e + k] : 0.0f);
+        float skip[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < kIn; ++k) {
+            const float v = live ? feat[16 * (size_t)e + k] : 0.0f;
+            if (k >= 8 && k < 11) skip[k - 8] = v;
+            st_bf16(S.x, cm_off(tid, k, kIn), v);
+        }
         ok = gemm_sync(tm + cL1, S.x, S.w1, kHid, kIn, false, &S.bar, phase, status);
         if (!ok) break;
         for (int c = 0; c < kHid; c += 16) {
@@ -365,7 +375,8 @@ __global__ void __launch_bounds__(kRows) mlp_train_kernel(const uint8_t* __restr
             const float4 g = live ? tgt[e] : make_float4(0.f, 0.f, 0.f, 0.f);
             float d[3] = {0.f, 0.f, 0.f};
             if (g.w != 0.0f) {
-                const float y0 = y[0] + S.b[2 * kHid], y1 = y[1] + S.b[2 * kHid + 1], y2 = y[2] + S.b[2 * kHid + 2];
+                const float y0 = (y[0] + S.b[2 * kHid]) + skip[0], y1 = (y[1] + S.b[2 * kHid + 1]) + skip[1],
+                            y2 = (y[2] + S.b[2 * kHid + 2]) + skip[2];
                 const float nn = sqrtf(((y0 * y0 + y1 * y1) + y2 * y2) + 1e-8f);
                 const float c = ((y0 * g.x + y1 * g.y) + y2 * g.z) / nn;
                 const float s = -inv_batch / nn;

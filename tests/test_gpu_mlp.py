@@ -40,7 +40,7 @@ def test_mlp_forward_matches_oracle(sdlib, orc, n):
     eng = tiny_engine(sdlib)
     rng = np.random.default_rng(n)
     p = eng.mlp_params()
-    p[:-16] += rng.normal(size=p.size - 16).astype(np.float32) * 0.05
+    p[:-16] += rng.normal(size=p.size - 16).astype(np.float32) * 0.05  # W3 starts at zero: perturb all
     P = orc.mlp_unpack(p)
     P["W3"][3:] = 0
     p = orc.mlp_pack(P)
@@ -72,7 +72,9 @@ def test_mlp_training_lowers_the_loss(sdlib, orc):
     eng = tiny_engine(sdlib)
     rng = np.random.default_rng(3)
     X, T = random_batch(rng, 4096)
-    T[:, :3] = X[:, 8:11] / np.maximum(np.linalg.norm(X[:, 8:11], axis=1, keepdims=True), 1e-6)  # learnable
+    # a learnable target: the previous-direction input turned 90 degrees about z
+    r = np.stack([X[:, 9], -X[:, 8], X[:, 10]], 1)
+    T[:, :3] = r / np.maximum(np.linalg.norm(r, axis=1, keepdims=True), 1e-6)
     _, l0, _ = orc.mlp_forward_backward(eng.mlp_params(), X, T)
     eng.mlp_train(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), 300, 3e-3)
     _, l1, _ = orc.mlp_forward_backward(eng.mlp_params(), X, T)
@@ -109,15 +111,15 @@ def test_learned_seed_gains_over_plain_gjk(sdlib):
     plain.close()
 
     engines = {}
-    for mode in (_abi.SD_GJK_SEED_PLAIN, _abi.SD_GJK_SEED_LEARNED):
+    for mode in (_abi.SD_GJK_SEED_PLAIN, _abi.SD_GJK_SEED_LEARNED, _abi.SD_GJK_SEED_PREVIOUS):
         eng = mk()
         sdlib.add_hull_scene(eng, pts, pos, quat, vel, mass)
         eng.prepare()
         eng.set_mlp_params(params)
         eng.set_gjk_seed(mode)
         engines[mode] = eng
-    it = {0: 0, 1: 0}
-    pairs = {0: 0, 1: 0}
+    it = {0: 0, 1: 0, 2: 0}
+    pairs = {0: 0, 1: 0, 2: 0}
     for step in range(40):
         for mode, eng in engines.items():
             eng.step(dt, 1)
@@ -132,8 +134,8 @@ def test_learned_seed_gains_over_plain_gjk(sdlib):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     assert pairs[0] == pairs[1]
     ratio = it[0] / it[1]
-    print(f"mean GJK support evaluations per pair: plain {it[0] / pairs[0]:.3f}, learned {it[1] / pairs[1]:.3f}, "
-          f"ratio {ratio:.2f}")
+    print(f"mean GJK support evaluations per pair: plain {it[0] / pairs[0]:.3f}, learned {it[1] / pairs[1]:.3f} "
+          f"(ratio {ratio:.2f}), previous direction without the network {it[2] / pairs[2]:.3f}")
     assert ratio > 2.0
     for eng in engines.values():
         eng.close()
