@@ -20,7 +20,11 @@ reorder + cell_start.  Timings:
              same stream, its algorithmic bytes / duration against the
              measured HBM peak;
   cpu_baseline  the CPU oracle (the restated step, OpenMP on the host cores)
-             on a bounded sample of the same scene.
+             on a bounded sample of the same scene;
+  gjk        the second half of the metric: mean GJK support evaluations per
+             candidate pair with the learned warm start vs plain GJK, on a
+             65,536-hull scene (bench_hulls), with the contact sets and states
+             of the two runs compared.
 
 ``--impl reference`` times the reference path on the host cores.  The
 reference has no CPU DEM path (its Device::CPU is never read), so this arm
@@ -217,6 +221,87 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
+    """GJK support evaluations per candidate pair, plain vs learned seed, on
+    the convex-hull step (65,536 hulls of 8-32 points, 0.02 m across, random
+    orientations, packed at 1.95 radii in a walled 1 m box): plain GJK logs
+    its separating directions for a few steps, the warm-start network is
+    trained on them on the GPU, then a plain and a learned engine step the
+    same scene, timed with CUDA events."""
+    import torch
+    import stardust_gb300 as sd
+    from stardust_gb300 import _abi, scenes
+    pts, pos, quat, vel, mass, cfg, dt = scenes.hull_box(n_hulls, seed=3, box=(1.0, 1.0, 1.0), spacing=0.0195,
+                                                          vmax=0.3)
+    cfg.cuda_device = local
+
+    def engine(mode, params=None):
+        e = sd.DEMEngine(cfg)
+        sd.add_hull_scene(e, pts, pos, quat, vel, mass)
+        e.prepare()
+        if params is not None:
+            e.set_mlp_params(params)
+        e.set_gjk_seed(mode)
+        return e
+
+    rng = np.random.default_rng(0)
+    plain = engine(_abi.SD_GJK_SEED_PLAIN)
+    X, T = [], []
+    for _ in range(10):
+        plain.step(dt, 1)
+        e = plain.hull_entries()
+        selfs = np.repeat(np.arange(len(e["off"]) - 1), np.diff(e["off"]))
+        m = np.flatnonzero((e["partners"] > selfs) & (e["status"] == 0) & (e["feat"][:, 7] == 1))
+        m = m[rng.permutation(len(m))[:20000]]
+        d = e["dir"][m, :3]
+        X.append(e["feat"][m])
+        T.append(np.concatenate([d / np.linalg.norm(d, axis=1, keepdims=True), np.ones((len(m), 1))], 1))
+    Xt = torch.from_numpy(np.concatenate(X).astype(np.float32)).cuda()
+    Tt = torch.from_numpy(np.concatenate(T).astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain.mlp_train(Xt, Tt, 400, 2e-3)
+    train_s = time.perf_counter() - t0
+    params = plain.mlp_params()
+    plain.close()
+    out = {"workload": f"{n_hulls} convex hulls (8-32 points, 0.02 m across), packed in a walled 1 m box, dt 1e-5 s",
+           "train_samples": int(Xt.shape[0]), "train_iters": 400, "train_s": train_s}
+    engines = {k: engine(m, params) for k, m in (("plain", _abi.SD_GJK_SEED_PLAIN),
+                                                   ("learned", _abi.SD_GJK_SEED_LEARNED),
+                                                   ("previous", _abi.SD_GJK_SEED_PREVIOUS))}
+    for k, e in engines.items():
+        e.step(dt, warmup)
+        e.sync()
+        st = torch.cuda.ExternalStream(e.stream(), device=torch.device("cuda", local))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        iters = pairs = 0
+        a.record(st)
+        for _ in range(steps):
+            e.step(dt, 1)
+        b.record(st)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / steps
+        for _ in range(3):  # counters of single steps
+            e.step(dt, 1)
+            s2 = e.stats()
+            iters += s2["gjk_iters"]
+            pairs += s2["gjk_pairs"]
+        out[f"ms_per_step_{k}"] = ms
+        out[f"iters_per_pair_{k}"] = iters / max(pairs, 1)
+        out[f"contacts_{k}"] = s2["contacts"]
+        out["pairs_per_step"] = s2["gjk_pairs"]
+    hp = engines["plain"].hull_entries()
+    hl = engines["learned"].hull_entries()
+    out["identical_contacts"] = bool(np.array_equal(hp["status"] == 1, hl["status"] == 1))
+    out["identical_state"] = bool(np.array_equal(engines["plain"].bodies(_abi.SD_BODY_POSITION).view(np.uint32),
+                                                 engines["learned"].bodies(_abi.SD_BODY_POSITION).view(np.uint32)))
+    out["ratio_plain_over_learned"] = out["iters_per_pair_plain"] / out["iters_per_pair_learned"]
+    out["hull_steps_per_s_learned"] = n_hulls / (out["ms_per_step_learned"] * 1e-3)
+    for e in engines.values():
+        e.close()
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -322,6 +407,12 @@ def run_ours(args, rank, world, local):
     st = eng.stats()
     eng.close()
 
+    # ---- learned GJK warm start on the convex-hull step (rank 0, N = 1)
+    gjk = None
+    if rank == 0 and world == 1 and not args.no_hulls:
+        gjk = bench_hulls(args.hulls, 20, 5, local)
+        log(f"gjk: {gjk}")
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -358,6 +449,7 @@ def run_ours(args, rank, world, local):
             "clocks": clocks,
             "gpu_launches": 5 * args.steps,
             "contacts": st["contacts"],
+            "gjk": gjk,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -377,6 +469,8 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-hulls", action="store_true")
+    ap.add_argument("--hulls", type=int, default=65_536)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
