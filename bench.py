@@ -470,12 +470,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-hulls", action="store_true")
+    ap.add_argument("--only-hulls", action="store_true", help="run only the convex-hull GJK section")
     ap.add_argument("--hulls", type=int, default=65_536)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.only_hulls:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"gjk": bench_hulls(args.hulls, args.steps, args.warmup, local)}), flush=True)
+        return 0
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
     return run_ours(args, rank, world, local)
