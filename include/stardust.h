@@ -172,6 +172,18 @@ sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float si
 sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float mass,
                               const float com[3], const float vel[3], const float omega[3]);
 
+/* A batch of independent sphere scenes stepped together (one launch per
+ * stage for all of them): each call adds one scene -- n spheres (pos4, vel4,
+ * omega4 as sd_engine_add_spheres) in its own walled box [lo, hi] with its
+ * own hash cell (0: 2 x the scene's largest radius).  Scenes share the
+ * material, gravity and time step of the config.  Once a scene is added,
+ * every sphere must come through this call; clumps are not batched.  Each
+ * scene's grid occupies its own range of cell keys, so one sort orders all
+ * scenes and no pair ever spans two scenes.  No counterpart in the
+ * reference (its engine holds one scene). */
+sd_status sd_engine_add_scene(sd_engine* h, uint64_t n, const float* pos4, const float* vel4, const float* omega4,
+                              const float lo[3], const float hi[3], float cell);
+
 /* DEMEngine::loadJSONSetup (engine.cpp:65-108, schema of
  * setup/star_test.json): scene.domain, scene.gravity (magnitude, along -z),
  * scene.entities[] of {type: "generic", position[3], size, mass,

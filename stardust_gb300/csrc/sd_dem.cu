@@ -49,6 +49,67 @@ __device__ __forceinline__ int32_t axis_cell(float x, float lo, float cell, int3
     return (int32_t)t;
 }
 
+// The grid a sphere lives in: the engine's one grid, or its scene's grid in a
+// batch (keys offset by the scene's base).
+struct Grid {
+    float lo[3], hi[3];
+    float cell;
+    int32_t nx, ny, nz;
+    uint32_t base;
+};
+
+__device__ __forceinline__ Grid grid_of(const DemParams& p) {
+    Grid g;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = p.lo[a];
+        g.hi[a] = p.hi[a];
+    }
+    g.cell = p.cell;
+    g.nx = p.nx;
+    g.ny = p.ny;
+    g.nz = p.nz;
+    g.base = 0;
+    return g;
+}
+
+// Scene of slot i: the last s with scene_first[s] <= i.
+__device__ __forceinline__ Grid grid_of_slot(const SceneGrid* __restrict__ scenes,
+                                             const uint32_t* __restrict__ first, uint32_t nscenes, uint32_t i) {
+    uint32_t a = 0, z = nscenes;  // invariant: first[a] <= i < first[z]
+    while (z - a > 1) {
+        const uint32_t m = (a + z) >> 1;
+        if (__ldg(first + m) <= i) a = m;
+        else z = m;
+    }
+    const SceneGrid* sg = scenes + a;
+    Grid g;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        g.lo[k] = __ldg(&sg->lo[k]);
+        g.hi[k] = __ldg(&sg->hi[k]);
+    }
+    g.cell = __ldg(&sg->cell);
+    g.nx = __ldg(&sg->nx);
+    g.ny = __ldg(&sg->ny);
+    g.nz = __ldg(&sg->nz);
+    g.base = __ldg(&sg->base);
+    return g;
+}
+
+__device__ __forceinline__ uint32_t cell_key_g(const Grid& g, float x, float y, float z) {
+    int32_t ix = axis_cell(x, g.lo[0], g.cell, g.nx);
+    int32_t iy = axis_cell(y, g.lo[1], g.cell, g.ny);
+    int32_t iz = axis_cell(z, g.lo[2], g.cell, g.nz);
+    return g.base + (uint32_t)((ix * g.ny + iy) * g.nz + iz);
+}
+
+struct Batch {
+    const SceneGrid* scenes;
+    const uint32_t* first;
+    uint32_t n;
+};
+
 __device__ __forceinline__ uint32_t cell_key(const DemParams& p, float x, float y, float z) {
     int32_t ix = axis_cell(x, p.lo[0], p.cell, p.nx);
     int32_t iy = axis_cell(y, p.lo[1], p.cell, p.ny);
@@ -160,7 +221,7 @@ __device__ __forceinline__ bool same_body(const ClumpCtx& cc, uint32_t idb, cons
 // the next-state write.  Returns the new cell key; a clump sphere hands its
 // force and torque to its body instead (the body kernel writes its next
 // state and key) and *has_key is false.
-template <bool RECORD, bool CLUMPS, class SRC>
+template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false>
 __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                   const float4* __restrict__ omg,
@@ -169,7 +230,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
                                                   uint32_t* __restrict__ vals, float4* __restrict__ force,
                                                   float4* __restrict__ torque, uint32_t& contacts,
-                                                  const ClumpCtx& cc, bool* has_key) {
+                                                  const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{}) {
+    const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
     const uint32_t idb = __float_as_uint(wi.w);
@@ -182,18 +244,18 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     // outer, y inner), slots ascending -- so the force sums are identical to
     // a full 27-cell scan.
     const float reach = (ri + p.rmax) * 1.00001f;
-    const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
-    const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
-    const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
-    const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, p.lo[0], p.cell, p.nx));
-    const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, p.lo[0], p.cell, p.nx));
-    const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, p.lo[1], p.cell, p.ny));
-    const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, p.lo[1], p.cell, p.ny));
-    const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, p.lo[2], p.cell, p.nz));
-    const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, p.lo[2], p.cell, p.nz));
+    const int32_t cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
+    const int32_t cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
+    const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
+    const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
+    const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
+    const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
+    const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
+    const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, g.lo[2], g.cell, g.nz));
+    const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, g.lo[2], g.cell, g.nz));
     for (int32_t X = x0; X <= x1; ++X) {
         for (int32_t Y = y0; Y <= y1; ++Y) {
-            const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+            const uint32_t col = g.base + (uint32_t)((X * g.ny + Y) * g.nz);
             const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)z0]);
             const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
             const uint32_t d = src.delta_of((uint32_t)((X - cx + 1) * 3 + (Y - cy + 1)), cx, cy);
@@ -237,7 +299,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 if (!(p.walls & (1 << (2 * a + side)))) continue;
-                const float gap = side == 0 ? xs[a] - p.lo[a] : p.hi[a] - xs[a];
+                const float gap = side == 0 ? xs[a] - g.lo[a] : g.hi[a] - xs[a];
                 if (!(gap < ri)) continue;
                 float nn[3] = {0.f, 0.f, 0.f};
                 nn[a] = side == 0 ? 1.0f : -1.0f;
@@ -271,7 +333,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     vel_n[i] = make_float4(nvx, nvy, nvz, mi);
     omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia), wi.z + dt * (t.z / inertia),
                            wi.w);
-    const uint32_t key = cell_key(p, nxp, nyp, nzp);
+    const uint32_t key = cell_key_g(g, nxp, nyp, nzp);
     keys[i] = key;
     vals[i] = i;
     return key;
@@ -322,7 +384,7 @@ __device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contac
 }
 
 // ---------------------------------------------- contact_mode 0: per slot
-template <bool RECORD, bool CLUMPS>
+template <bool RECORD, bool CLUMPS, bool BATCHED = false>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -331,14 +393,15 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
-                             ClumpCtx cc) {
+                             ClumpCtx cc, Batch bt = Batch{}) {
     __shared__ uint32_t s_hist[kFusedPasses][512];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     if (i < n)
-        key = particle_step<RECORD, CLUMPS>(p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                    keys, vals, force, torque, contacts, cc, &has_key);
+        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED>(p, n, i, GlobalSource{pos}, pos, vel, omg,
+                                                                    cell_start, pos_n, vel_n, omg_n, keys, vals,
+                                                                    force, torque, contacts, cc, &has_key, bt);
     if (ghist) {
         for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
         __syncthreads();
@@ -600,11 +663,12 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
 }
 
 __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
-                                uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+                                uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, Batch bt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 q = pos[i];
-    keys[i] = cell_key(p, q.x, q.y, q.z);
+    const Grid g = bt.n > 1 ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
+    keys[i] = cell_key_g(g, q.x, q.y, q.z);
     vals[i] = i;
 }
 
@@ -657,25 +721,27 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
 __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                                  const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
                                  unsigned long long* __restrict__ pairs, unsigned long long* __restrict__ npairs,
-                                 uint64_t cap, uint32_t* __restrict__ status, const int32_t* __restrict__ body_of) {
+                                 uint64_t cap, uint32_t* __restrict__ status, const int32_t* __restrict__ body_of,
+                                 Batch bt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const Grid g = bt.n > 1 ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i];
     const uint32_t idbi = __float_as_uint(omg[i].w);
     const uint32_t idi = idbi & kIdMask;
     const int32_t bi = (body_of && (idbi & kClumpFlag)) ? body_of[idi] : -1;
-    const int32_t cx = axis_cell(pi.x, p.lo[0], p.cell, p.nx);
-    const int32_t cy = axis_cell(pi.y, p.lo[1], p.cell, p.ny);
-    const int32_t cz = axis_cell(pi.z, p.lo[2], p.cell, p.nz);
+    const int32_t cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
+    const int32_t cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
+    const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
     const int32_t z0 = cz > 0 ? cz - 1 : 0;
-    const int32_t z1 = cz + 1 < p.nz ? cz + 1 : p.nz - 1;
+    const int32_t z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
     for (int32_t ddx = -1; ddx <= 1; ++ddx) {
         const int32_t X = cx + ddx;
-        if (X < 0 || X >= p.nx) continue;
+        if (X < 0 || X >= g.nx) continue;
         for (int32_t ddy = -1; ddy <= 1; ++ddy) {
             const int32_t Y = cy + ddy;
-            if (Y < 0 || Y >= p.ny) continue;
-            const uint32_t col = (uint32_t)((X * p.ny + Y) * p.nz);
+            if (Y < 0 || Y >= g.ny) continue;
+            const uint32_t col = g.base + (uint32_t)((X * g.ny + Y) * g.nz);
             const uint32_t s1 = min(cell_start[col + (uint32_t)z1 + 1], n);
             for (uint32_t s = cell_start[col + (uint32_t)z0]; s < s1; ++s) {
                 if (s == i) continue;
@@ -767,7 +833,8 @@ cudaError_t dem_init_kernels() {
 
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
-    dem_keys_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos_n, b.keys, b.vals);
+    dem_keys_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos_n, b.keys, b.vals,
+                                                        Batch{b.scenes, b.scene_first, b.nscenes});
     return cudaGetLastError();
 }
 
@@ -813,7 +880,11 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
     const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
     const size_t tile = kTileSlots * sizeof(float4);
-    if (g_contact_mode == 0) {
+    if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
+        dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            b.dev_status, spec, ghist, cc, Batch{b.scenes, b.scene_first, b.nscenes});
+    } else if (g_contact_mode == 0) {
         if (b.nb)
             dem_contact_integrate_kernel<RECORD, true><<<grid_for(b.n, 256), 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
@@ -882,7 +953,8 @@ cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) 
     cudaError_t e = cudaMemsetAsync(b.npairs, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess || b.n == 0) return e;
     dem_pairs_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.omg, b.cell_start, b.pairs, b.npairs,
-                                                         b.pair_cap, b.dev_status, b.nb ? b.body_of : nullptr);
+                                                         b.pair_cap, b.dev_status, b.nb ? b.body_of : nullptr,
+                                                         Batch{b.scenes, b.scene_first, b.nscenes});
     return cudaGetLastError();
 }
 

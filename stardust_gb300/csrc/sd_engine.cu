@@ -107,35 +107,106 @@ void release_device(sd_engine* h) {
     h->prepared = false;
 }
 
+// Grid dims of a box edge over a float cell: the edge over the cell is an
+// integer up to the cell's rounding (1 / 0.02f = 50.000001), which must not
+// add a cell layer.
+static sd_status grid_dims(sd_engine* h, const float* lo, const float* hi, float cell, int32_t* dims,
+                           uint64_t* ncells) {
+    *ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (!(hi[a] > lo[a])) return fail(h, SD_ERR_INVALID_ARG, "box: hi must exceed lo on every axis");
+        double nd = std::ceil(((double)hi[a] - (double)lo[a]) / (double)cell * (1.0 - 1e-6));
+        if (nd < 1) nd = 1;
+        if (nd > (1 << 20)) return fail(h, SD_ERR_INVALID_ARG, "grid too fine (> 2^20 cells per axis)");
+        dims[a] = (int32_t)nd;
+        *ncells *= (uint64_t)nd;
+    }
+    return SD_OK;
+}
+
+// A batch: per scene its grid (cell = given or 2 x its largest radius) at
+// consecutive key ranges, and its slot range.
+static sd_status derive_batch(sd_engine* h) {
+    h->scene_grids.clear();
+    h->scene_first.clear();
+    uint64_t base = 0;
+    uint32_t first = 0;
+    for (size_t k = 0; k < h->scenes.size(); ++k) {
+        const auto& sc = h->scenes[k];
+        if (sc.first != first) return fail(h, SD_ERR_STATE, "every sphere of a batch must belong to a scene");
+        float rmax = 0.0f;
+        for (uint32_t i = 0; i < sc.count; ++i) rmax = std::max(rmax, h->h_pos[sc.first + i].w);
+        const float cell = sc.cell > 0.0f ? sc.cell : (rmax > 0.0f ? 2.0f * rmax : sc.hi[0] - sc.lo[0]);
+        if (cell < 2.0f * rmax)
+            return fail(h, SD_ERR_INVALID_ARG, "scene " + std::to_string(k) + ": cell must be >= 2 * largest radius");
+        sd::SceneGrid g{};
+        int32_t dims[3];
+        uint64_t nc = 0;
+        sd_status s = grid_dims(h, sc.lo, sc.hi, cell, dims, &nc);
+        if (s) return s;
+        for (int a = 0; a < 3; ++a) {
+            g.lo[a] = sc.lo[a];
+            g.hi[a] = sc.hi[a];
+        }
+        g.cell = cell;
+        g.nx = dims[0];
+        g.ny = dims[1];
+        g.nz = dims[2];
+        g.base = (uint32_t)base;
+        base += nc;
+        if (base > (1ull << 30)) return fail(h, SD_ERR_INVALID_ARG, "the batch's grids exceed 2^30 cells");
+        h->scene_grids.push_back(g);
+        h->scene_first.push_back(first);
+        first += sc.count;
+    }
+    if (first != h->h_pos.size()) return fail(h, SD_ERR_STATE, "every sphere of a batch must belong to a scene");
+    h->scene_first.push_back(first);
+    return SD_OK;
+}
+
 sd_status derive_params(sd_engine* h) {
     const sd_config& c = h->cfg;
     sd::DemParams& P = h->P;
-    bool box_given = c.box_hi[0] != 0.f || c.box_hi[1] != 0.f || c.box_hi[2] != 0.f;
-    for (int a = 0; a < 3; ++a) {
-        P.lo[a] = box_given ? c.box_lo[a] : 0.0f;
-        P.hi[a] = box_given ? c.box_hi[a] : c.domain;
-        if (!(P.hi[a] > P.lo[a])) return fail(h, SD_ERR_INVALID_ARG, "box: hi must exceed lo on every axis");
-    }
     float rmax = 0.0f;
     for (auto& p : h->h_pos) rmax = std::max(rmax, p.w);
-    float cell = c.cell > 0.0f ? c.cell : 2.0f * rmax;
-    if (!(cell > 0.0f)) cell = (P.hi[0] - P.lo[0]);
-    // a sphere must fit within the 3x3x3 cell neighbourhood: every contact
-    // partner is then found in the adjacent cells
-    if (cell < 2.0f * rmax) return fail(h, SD_ERR_INVALID_ARG, "cell must be >= 2 * largest radius");
-    P.cell = cell;
-    uint64_t ncells = 1;
-    int32_t* dims[3] = {&P.nx, &P.ny, &P.nz};
-    for (int a = 0; a < 3; ++a) {
-        // the box edge over a float cell is an integer up to the cell's
-        // rounding (1 / 0.02f = 50.000001): do not let that add a cell layer
-        double nd = std::ceil(((double)P.hi[a] - (double)P.lo[a]) / (double)cell * (1.0 - 1e-6));
-        if (nd < 1) nd = 1;
-        if (nd > (1 << 20)) return fail(h, SD_ERR_INVALID_ARG, "grid too fine (> 2^20 cells per axis)");
-        *dims[a] = (int32_t)nd;
-        ncells *= (uint64_t)nd;
+    if (h->scenes.size() > 1) {
+        // a batch: the configured box and cell are not used
+        if (!h->hb_pos.empty()) return fail(h, SD_ERR_UNSUPPORTED, "rigid clumps are not supported in a batch");
+        sd_status s = derive_batch(h);
+        if (s) return s;
+        const sd::SceneGrid& g0 = h->scene_grids[0];
+        for (int a = 0; a < 3; ++a) {  // sd_engine_params reports the first scene
+            P.lo[a] = g0.lo[a];
+            P.hi[a] = g0.hi[a];
+        }
+        P.cell = g0.cell;
+        P.nx = g0.nx;
+        P.ny = g0.ny;
+        P.nz = g0.nz;
+    } else {
+        bool box_given = c.box_hi[0] != 0.f || c.box_hi[1] != 0.f || c.box_hi[2] != 0.f;
+        const bool one_scene = h->scenes.size() == 1;
+        for (int a = 0; a < 3; ++a) {
+            P.lo[a] = one_scene ? h->scenes[0].lo[a] : (box_given ? c.box_lo[a] : 0.0f);
+            P.hi[a] = one_scene ? h->scenes[0].hi[a] : (box_given ? c.box_hi[a] : c.domain);
+            if (!(P.hi[a] > P.lo[a])) return fail(h, SD_ERR_INVALID_ARG, "box: hi must exceed lo on every axis");
+        }
+        const float cfg_cell = one_scene ? h->scenes[0].cell : c.cell;
+        float cell = cfg_cell > 0.0f ? cfg_cell : 2.0f * rmax;
+        if (!(cell > 0.0f)) cell = (P.hi[0] - P.lo[0]);
+        // a sphere must fit within the 3x3x3 cell neighbourhood: every contact
+        // partner is then found in the adjacent cells
+        if (cell < 2.0f * rmax) return fail(h, SD_ERR_INVALID_ARG, "cell must be >= 2 * largest radius");
+        P.cell = cell;
+        int32_t dims[3];
+        uint64_t ncells = 0;
+        sd_status s = grid_dims(h, P.lo, P.hi, cell, dims, &ncells);
+        if (s) return s;
+        P.nx = dims[0];
+        P.ny = dims[1];
+        P.nz = dims[2];
+        if (ncells > (1ull << 30)) return fail(h, SD_ERR_INVALID_ARG, "grid has more than 2^30 cells");
     }
-    if (ncells > (1ull << 30)) return fail(h, SD_ERR_INVALID_ARG, "grid has more than 2^30 cells");
     if (!(c.restitution > 0.0f && c.restitution <= 1.0f))
         return fail(h, SD_ERR_INVALID_ARG, "restitution must be in (0, 1]");
     if (!(c.kn > 0.0f)) return fail(h, SD_ERR_INVALID_ARG, "kn must be > 0");
@@ -168,7 +239,12 @@ sd_status upload_and_sort(sd_engine* h, const float4* pos, const float4* vel, co
 sd_status allocate(sd_engine* h, uint32_t n) {
     sd::DemBuffers& B = h->B;
     B.n = n;
-    B.ncells = (uint32_t)((uint64_t)h->P.nx * h->P.ny * h->P.nz);
+    B.ncells = h->scenes.size() > 1 ? h->scene_first.empty() ? 0u
+                                                             : (uint32_t)((uint64_t)h->scene_grids.back().base +
+                                                                          (uint64_t)h->scene_grids.back().nx *
+                                                                              h->scene_grids.back().ny *
+                                                                              h->scene_grids.back().nz)
+                                    : (uint32_t)((uint64_t)h->P.nx * h->P.ny * h->P.nz);
     int bits = 1;
     while (bits < 32 && (1ull << bits) < (unsigned long long)B.ncells) ++bits;
     sd_status s;
@@ -189,6 +265,18 @@ sd_status allocate(sd_engine* h, uint32_t n) {
     if ((s = dev_alloc(h, &B.pairs, (size_t)B.pair_cap)) || (s = dev_alloc(h, &B.npairs, 1))) return s;
     SD_CUDA(h, cudaMemsetAsync(B.dev_status, 0, 8 * sizeof(uint32_t), h->stream));
     SD_CUDA(h, cudaMemsetAsync(B.sort_scratch, 0, 16 * sizeof(uint32_t), h->stream));
+    B.nscenes = h->scenes.size() > 1 ? (uint32_t)h->scenes.size() : 0u;
+    if (B.nscenes) {
+        sd::SceneGrid* g = nullptr;
+        uint32_t* f = nullptr;
+        if ((s = dev_alloc(h, &g, B.nscenes)) || (s = dev_alloc(h, &f, (size_t)B.nscenes + 1))) return s;
+        SD_CUDA(h, cudaMemcpyAsync(g, h->scene_grids.data(), sizeof(sd::SceneGrid) * B.nscenes, cudaMemcpyHostToDevice,
+                                   h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(f, h->scene_first.data(), 4 * ((size_t)B.nscenes + 1), cudaMemcpyHostToDevice,
+                                   h->stream));
+        B.scenes = g;
+        B.scene_first = f;
+    }
     const uint32_t nb = (uint32_t)h->hb_pos.size();
     B.nb = nb;
     if (nb) {
@@ -392,6 +480,8 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, con
                                 const float* omega4) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
     if (h->prepared) return fail(h, SD_ERR_STATE, "spheres cannot be added after prepare (reference: addEntityRuntime is a stub)");
+    if (!h->scenes.empty() && !h->adding_scene)
+        return fail(h, SD_ERR_STATE, "spheres added outside a scene of the batch (use sd_engine_add_scene)");
     if (n && (!pos4 || !vel4)) return fail(h, SD_ERR_INVALID_ARG, "pos4/vel4 NULL");
     if (h->h_pos.size() + n >= 0x7fffffffull) return fail(h, SD_ERR_CAPACITY, "more than 2^31-1 spheres");
     for (uint64_t i = 0; i < n; ++i) {
@@ -412,6 +502,34 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, con
         h->h_body_of.push_back(-1);
         h->h_r0.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
     }
+    return SD_OK;
+}
+
+sd_status sd_engine_add_scene(sd_engine* h, uint64_t n, const float* pos4, const float* vel4, const float* omega4,
+                              const float lo[3], const float hi[3], float cell) {
+    if (!h || !lo || !hi) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "scenes cannot be added after prepare");
+    if (!h->hb_pos.empty()) return fail(h, SD_ERR_UNSUPPORTED, "rigid clumps are not supported in a batch");
+    if (h->scenes.empty() && !h->h_pos.empty())
+        return fail(h, SD_ERR_STATE, "spheres added outside a scene: use sd_engine_add_scene for every sphere");
+    if (h->scenes.size() >= (1u << 20)) return fail(h, SD_ERR_CAPACITY, "too many scenes");
+    for (int a = 0; a < 3; ++a)
+        if (!(hi[a] > lo[a]) || !std::isfinite(lo[a]) || !std::isfinite(hi[a]))
+            return fail(h, SD_ERR_INVALID_ARG, "scene box: hi must exceed lo on every axis");
+    if (cell < 0.0f || !std::isfinite(cell)) return fail(h, SD_ERR_INVALID_ARG, "scene cell must be >= 0");
+    sd_engine::SceneHost sc{};
+    for (int a = 0; a < 3; ++a) {
+        sc.lo[a] = lo[a];
+        sc.hi[a] = hi[a];
+    }
+    sc.cell = cell;
+    sc.first = (uint32_t)h->h_pos.size();
+    sc.count = (uint32_t)n;
+    h->adding_scene = true;
+    sd_status s = sd_engine_add_spheres(h, n, pos4, vel4, omega4);
+    h->adding_scene = false;
+    if (s) return s;
+    h->scenes.push_back(sc);
     return SD_OK;
 }
 
@@ -962,6 +1080,7 @@ static const char kCkptMagic[8] = {'S', 'D', 'G', 'B', 'C', 'K', 'P', '1'};
 
 sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
     if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->scenes.size() > 1) return fail(h, SD_ERR_UNSUPPORTED, "checkpoints of a batch of scenes are not supported");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
     if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     SD_CUDA(h, cudaSetDevice(h->device));
@@ -1008,6 +1127,7 @@ sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
 
 sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
     if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->scenes.size() > 1) return fail(h, SD_ERR_UNSUPPORTED, "checkpoints of a batch of scenes are not supported");
     if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes");
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(h, SD_ERR_IO, std::string("cannot open ") + path);

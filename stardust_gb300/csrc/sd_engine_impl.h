@@ -48,6 +48,16 @@ struct sd_engine {
     std::vector<float4> h_r0;
     // convex hulls (a scene holds spheres/clumps or hulls, not both)
     HullScene hull;
+    // a batch of independent sphere scenes (sd_engine_add_scene): box, cell
+    // (0: 2 x the scene's largest radius), first sphere id, sphere count
+    struct SceneHost {
+        float lo[3], hi[3], cell;
+        uint32_t first, count;
+    };
+    std::vector<SceneHost> scenes;
+    std::vector<sd::SceneGrid> scene_grids;  // derived at prepare
+    std::vector<uint32_t> scene_first;
+    bool adding_scene = false;
 
     bool prepared = false;
     int device = 0;

@@ -151,9 +151,23 @@ struct DemParams {
     float rmax;  // largest sphere radius: bounds every contact partner's reach
 };
 
+// One scene of a batch: its box and grid, the first global cell key of its
+// grid (scenes occupy consecutive key ranges) and its first sphere slot
+// (scenes occupy consecutive slot ranges, in every step, because the sort
+// keeps each scene's keys together and no sphere leaves its scene).
+struct SceneGrid {
+    float lo[3], hi[3];
+    float cell;
+    int32_t nx, ny, nz;
+    uint32_t base;
+};
+
 struct DemBuffers {
     uint32_t n;
     uint32_t ncells;
+    uint32_t nscenes;               // 0 or 1: one scene (DemParams' grid); > 1: a batch
+    const SceneGrid* scenes;        // [nscenes]
+    const uint32_t* scene_first;    // [nscenes + 1] first slot of each scene, then n
     float4 *pos, *vel, *omg;        // current state, cell-sorted
     float4 *pos_n, *vel_n, *omg_n;  // next state, slot order of the current
     uint32_t *keys, *vals;          // sort keys / slot indices

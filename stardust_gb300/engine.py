@@ -115,6 +115,17 @@ class DEMEngine:
         self._call("sd_engine_add_particle", grid_resolution, size, diameter, mass, p, v)
         self._n = int(self.stats()["n_spheres"])
 
+    def add_scene(self, pos4, vel4, lo, hi, cell: float = 0.0, omega4=None) -> None:
+        """One scene of a batch: spheres in their own walled box [lo, hi]."""
+        p = _f32(pos4)
+        v = _f32(vel4)
+        w = None if omega4 is None else _f32(omega4)
+        lo3 = (C.c_float * 3)(*lo)
+        hi3 = (C.c_float * 3)(*hi)
+        self._call("sd_engine_add_scene", len(p), p.ctypes.data, v.ctypes.data, None if w is None else w.ctypes.data,
+                   lo3, hi3, cell)
+        self._n += len(p)
+
     def add_clump(self, rel4, mass: float, com, velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0)) -> None:
         """One rigid body made of spheres (rel4 rows: body-frame offset from
         the centre of mass, radius); the body's inertia is that of its

@@ -179,3 +179,27 @@ def hull_box(n: int = 65_536, seed: int = 0, radius: float = 0.01, box=(1.0, 1.0
                        restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81))
     return pts, pos.astype(np.float32), quat.astype(np.float32), vel.astype(np.float32), mass.astype(np.float32), \
         cfg, 1e-5
+
+
+def batch_boxes(n_scenes: int = 512, seed: int = 0, n_min: int = 256, n_max: int = 65_536, median: int = 4096,
+                sigma: float = 0.85, fraction: float = 0.35):
+    """Independent sphere boxes for a batch: per scene a sphere count drawn
+    lognormal (median 4,096, sigma 0.85, clipped to [256, 65,536]; ~3.1M
+    spheres for 512 scenes), box_lattice's material and spheres (r = 0.01 m,
+    m = 1e-3 kg) on a jittered cubic lattice whose spacing gives `fraction`
+    of the box volume, its own seed, velocities U[-0.1, 0.1] m/s.  Returns
+    (list of (pos4, vel4, lo, hi), EngineConfig, dt = 1e-5)."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(median * np.exp(sigma * rng.normal(size=n_scenes))), n_min, n_max).astype(int)
+    r = R_BOX
+    spacing = r * (4.0 / 3.0 * math.pi / fraction) ** (1.0 / 3.0)
+    out = []
+    for k, n in enumerate(counts):
+        side = int(math.ceil(n ** (1.0 / 3.0)))
+        pos, vel = scene_lattice(side, side, side, spacing, 0.05 * r, (0.5 * spacing,) * 3, r, M_BOX, 0.1,
+                                 seed * 100_003 + k)
+        edge = side * spacing
+        out.append((pos[:n].copy(), vel[:n].copy(), (0.0, 0.0, 0.0), (edge, edge, edge)))
+    cfg = EngineConfig(walls=0x3F, kn=1e5, restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81),
+                       pair_capacity=1 << 22)
+    return out, cfg, 1e-5

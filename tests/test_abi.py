@@ -227,3 +227,26 @@ def test_rsa_is_non_overlapping(sdlib):
     assert np.all(pos[:, :3] - pos[:, 3:4] >= lo - 1e-7) and np.all(pos[:, :3] + pos[:, 3:4] <= hi + 1e-7)
     assert np.all((pos[:, 3] >= 0.0025) & (pos[:, 3] <= 0.01))
     assert np.allclose(vel[:, 3], scenes.DENSITY * 4 / 3 * np.pi * pos[:, 3].astype(np.float64) ** 3, rtol=1e-6)
+
+
+def test_batch_api_rules(sdlib):
+    import numpy as np
+    pos = np.array([[0.5, 0.5, 0.5, 0.01]], np.float32)
+    vel = np.array([[0, 0, 0, 1e-3]], np.float32)
+    eng = sdlib.DEMEngine()
+    eng.add_scene(pos, vel, (0, 0, 0), (1, 1, 1))
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add_spheres(pos, vel)
+    assert e.value.status == sdlib._abi.SD_ERR_STATE
+    with pytest.raises(sdlib.SdError) as e:
+        eng.add_scene(pos, vel, (0, 0, 0), (1, 0, 1))
+    assert e.value.status == sdlib._abi.SD_ERR_INVALID_ARG
+    eng.add_scene(pos, vel, (0, 0, 0), (2, 2, 2))
+    assert eng.stats()["n_spheres"] == 2
+    eng.close()
+    e2 = sdlib.DEMEngine()
+    e2.add_spheres(pos, vel)
+    with pytest.raises(sdlib.SdError) as e:
+        e2.add_scene(pos, vel, (0, 0, 0), (1, 1, 1))
+    assert e.value.status == sdlib._abi.SD_ERR_STATE
+    e2.close()
