@@ -21,6 +21,8 @@ reorder + cell_start.  Timings:
              measured HBM peak;
   cpu_baseline  the CPU oracle (the restated step, OpenMP on the host cores)
              on a bounded sample of the same scene;
+  batch      512 independent scenes (~2.9M spheres) stepped together, one
+             launch per stage (bench_batch), against 16 of them stepped alone;
   gjk        the second half of the metric: mean GJK support evaluations per
              candidate pair with the learned warm start vs plain GJK, on a
              65,536-hull scene (bench_hulls), with the contact sets and states
@@ -302,6 +304,72 @@ def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
     return out
 
 
+def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
+    """Batched scenes: n_scenes independent walled boxes (sphere counts
+    lognormal in [256, 65,536], median 4,096; ~2.9M spheres for 512 scenes;
+    r = 0.01 m at 35 % volume fraction, dt 1e-5 s) stepped together, one
+    launch per stage, timed with CUDA events (the working set exceeds L2,
+    and a 256 MB write still precedes every timed step).  For comparison, 16
+    scenes spread over the size range are stepped alone, one engine each."""
+    import torch
+    import stardust_gb300 as sd
+    from stardust_gb300 import scenes
+    batch, cfg, dt = scenes.batch_boxes(n_scenes=n_scenes, seed=11)
+    cfg.cuda_device = local
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def timed(eng, k):
+        st = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+        a = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        b = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        for i in range(k):
+            with torch.cuda.stream(st):
+                flush.fill_(i & 0xFF)
+            a[i].record(st)
+            eng.step(dt, 1)
+            b[i].record(st)
+        torch.cuda.synchronize()
+        return sum(x.elapsed_time(y) for x, y in zip(a, b)) / k
+
+    eng = sd.DEMEngine(cfg)
+    for pos, vel, lo, hi in batch:
+        eng.add_scene(pos, vel, lo, hi)
+    eng.prepare()
+    eng.step(dt, warmup)
+    eng.sync()
+    tuned = None
+    if tune:
+        from stardust_gb300 import autotune
+        tuned = autotune.tune_engine(eng, dt, reps=3)
+    ms = timed(eng, steps)
+    st = eng.stats()
+    eng.close()
+    counts = np.array([len(b[0]) for b in batch])
+    total = int(counts.sum())
+    order = np.argsort(counts)
+    pick = order[np.linspace(0, len(order) - 1, 16).astype(int)]
+    alone_ms, alone_n = 0.0, 0
+    for k in pick:
+        pos, vel, lo, hi = batch[k]
+        e1 = sd.DEMEngine(cfg)
+        e1.add_scene(pos, vel, lo, hi)
+        e1.prepare()
+        e1.step(dt, warmup)
+        e1.sync()
+        alone_ms += timed(e1, max(steps // 2, 3))
+        alone_n += len(pos)
+        e1.close()
+    return {"workload": f"{n_scenes} independent walled boxes, {total} spheres (r 0.01 m, 35 % volume fraction), "
+                        f"counts lognormal in [256, 65536], median 4096, dt 1e-5 s",
+            "scenes": n_scenes, "spheres": total, "cells": st["n_cells"],
+            "count_quantiles": [int(np.quantile(counts, q)) for q in (0.0, 0.25, 0.5, 0.75, 1.0)],
+            "ms_per_step": ms, "particle_steps_per_s": total / (ms * 1e-3),
+            "per_scene_particle_steps_per_s_median": float(np.median(counts)) / (ms * 1e-3),
+            "alone_16_scenes": {"spheres": alone_n, "ms_per_step_sum": alone_ms,
+                                "particle_steps_per_s": alone_n / (alone_ms * 1e-3)},
+            "device_errors": st["device_errors"], "autotune": tuned}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -413,6 +481,12 @@ def run_ours(args, rank, world, local):
         gjk = bench_hulls(args.hulls, 20, 5, local)
         log(f"gjk: {gjk}")
 
+    # ---- batched scenes (rank 0, N = 1)
+    batch = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        batch = bench_batch(args.scenes, args.steps, args.warmup, local, not args.no_tune)
+        log(f"batch: {batch}")
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -450,6 +524,7 @@ def run_ours(args, rank, world, local):
             "gpu_launches": 5 * args.steps,
             "contacts": st["contacts"],
             "gjk": gjk,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -472,11 +547,20 @@ def main():
     ap.add_argument("--no-hulls", action="store_true")
     ap.add_argument("--only-hulls", action="store_true", help="run only the convex-hull GJK section")
     ap.add_argument("--hulls", type=int, default=65_536)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--only-batch", action="store_true", help="run only the batched-scenes section")
+    ap.add_argument("--scenes", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.only_batch:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"batch": bench_batch(args.scenes, args.steps, args.warmup, local, not args.no_tune)}),
+              flush=True)
+        return 0
     if args.only_hulls:
         import torch
         torch.cuda.set_device(local)
