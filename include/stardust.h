@@ -297,6 +297,32 @@ sd_status sd_engine_mlp_forward(sd_engine* h, const float* d_feat16, float* d_ou
 sd_status sd_engine_mlp_train(sd_engine* h, const float* d_feat16, const float* d_tgt4, uint64_t n, int32_t iters,
                               float lr, float* host_grad);
 
+/* ------------------------------------------------------ sweep and prune
+ * (SAPCollision, src/engine/cuda/collisions/SAP/sap_detection.cu:135-706). */
+
+/* Device scratch for sd_sap_pairs (pair_cap pairs) and
+ * sd_sap_process_collisions (pair_cap 0). */
+sd_status sd_sap_scratch_bytes(uint64_t n, uint64_t pair_cap, uint64_t* bytes);
+/* Exact broad phase: every pair (i < j) of overlapping closed boxes,
+ * ascending u64 (i << 32 | j), by sorting the lower x extents (order-
+ * preserving keys, negative coordinates allowed) and sweeping.  d_count[0] =
+ * pairs, d_count[1] = device error bits. */
+sd_status sd_sap_pairs(uint64_t n, const float* d_lo4, const float* d_hi4, uint64_t* d_pairs, uint64_t cap,
+                       uint32_t* d_count, void* d_scratch, uint64_t scratch_bytes, void* stream);
+/* sweepAndPruneCUDA (sap_detection.cu:385-440) on given sorted inputs: per
+ * sorted position tid a row of 16 int32 at d_rows[16 * tid] -- partner ids
+ * found in the next 64 sorted positions whose lower x <= the home upper x
+ * (which the kernel replaces by the home upper y once a y test has run) and
+ * lower y <= the home upper y; at most 9, unique, ids equal to tid skipped;
+ * unused entries -1 (every row is cleared first). */
+sd_status sd_sap_sweep(uint64_t n, const float* d_upperx, const float* d_lowerx_sorted, const float* d_uppery,
+                       const float* d_lowery, const uint32_t* d_idx_sorted, int32_t* d_rows, void* stream);
+/* SAPCollision::processCollisions (sap_detection.cu:668-706): AABBs of
+ * spheres (radius from d_radius, or pos.w when NULL), a stable radix sort of
+ * the lower x extents as uint32 float bits, then the sweep above. */
+sd_status sd_sap_process_collisions(uint64_t n, const float* d_pos4, const float* d_radius, int32_t* d_rows,
+                                    void* d_scratch, uint64_t scratch_bytes, void* stream);
+
 /* ------------------------------------------------------ LBVH operators
  * (sandbox/testLBVH.cu:42-907 as raw device operators).  Boxes are float4
  * rows lo (x, y, z, -) and hi, 16-byte aligned, n < 2^30. */

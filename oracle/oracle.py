@@ -59,6 +59,8 @@ def lib() -> C.CDLL:
             "sdo_gjk_epa": (None, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, P, P, P]),
             "sdo_hull_partners": (C.c_int64, [C.c_uint32, P, P, P, P, C.c_uint64]),
             "sdo_hull_step": (None, [P, C.c_uint32] + [P] * 17),
+            "sdo_sap_sweep_ref": (None, [C.c_uint32, P, P, P, P, P, P]),
+            "sdo_sap_process": (None, [C.c_uint32, P, P, P]),
             "sdo_num_threads": (C.c_int, []),
             "sdo_set_num_threads": (None, [C.c_int]),
         }
@@ -482,3 +484,21 @@ def mlp_forward_backward(params, X, T, round_bf16=True):
     g["W3"][3:] = 0
     g["b3"][3:] = 0
     return Y, loss, mlp_pack(g)
+
+
+def sap_sweep_ref(upperx, lowerx_sorted, uppery, lowery, idx_sorted):
+    n = len(upperx)
+    rows = np.empty((max(n, 1), 16), np.int32)
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    lib().sdo_sap_sweep_ref(n, _p(f(upperx)), _p(f(lowerx_sorted)), _p(f(uppery)), _p(f(lowery)),
+                            _p(np.ascontiguousarray(idx_sorted, np.uint32)), _p(rows))
+    return rows[:n]
+
+
+def sap_process(pos4, radius=None):
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    n = len(pos4)
+    rows = np.empty((max(n, 1), 16), np.int32)
+    r = None if radius is None else np.ascontiguousarray(radius, np.float32)
+    lib().sdo_sap_process(n, _p(pos4), _p(r), _p(rows))
+    return rows[:n]

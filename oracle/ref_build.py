@@ -24,7 +24,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-SOURCES = ("sh_collision_detection", "collision_resolution", "physics_update")
+SOURCES = {"sh_collision_detection": "src/engine/cuda/sh_collision_detection.cu",
+           "collision_resolution": "src/engine/cuda/collision_resolution.cu",
+           "physics_update": "src/engine/cuda/physics_update.cu",
+           "sap_detection": "src/engine/cuda/collisions/SAP/sap_detection.cu"}
 
 
 def reference_root() -> Path | None:
@@ -41,8 +44,8 @@ def build_cubins(verbose: bool = False) -> bool:
     if ref is None:
         return all((OUT / f"{s}.cubin").exists() for s in SOURCES)
     OUT.mkdir(exist_ok=True)
-    for s in SOURCES:
-        src = ref / "src" / "engine" / "cuda" / f"{s}.cu"
+    for s, rel in SOURCES.items():
+        src = ref / rel
         dst = OUT / f"{s}.cubin"
         if dst.exists() and dst.stat().st_mtime >= src.stat().st_mtime:
             continue

@@ -37,9 +37,10 @@ Kern g_k[] = {
     {"RadixTabulateCUDA", "sh_collision_detection"},
     {"RadixSumCUDA", "sh_collision_detection"},
     {"RadixReorderCUDA", "sh_collision_detection"},
+    {"sweepAndPruneCUDA", "sap_detection"},
 };
 constexpr int kConstruct = 0, kTraverse = 1, kUpdate = 2, kForces = 3, kAdvect = 4, kTab = 5, kSum = 6,
-              kReorder = 7;
+              kReorder = 7, kSweep = 8;
 
 std::string g_err;
 
@@ -76,7 +77,7 @@ const char* ref_last_error() { return g_err.c_str(); }
 // Loads the three cubins from `dir` into the current context and finds the
 // kernels by name.
 int ref_init(const char* dir) {
-    const char* mods[] = {"sh_collision_detection", "collision_resolution", "physics_update"};
+    const char* mods[] = {"sh_collision_detection", "collision_resolution", "physics_update", "sap_detection"};
     for (const char* m : mods) {
         std::string path = std::string(dir) + "/" + m + ".cubin";
         CUmodule mod;
@@ -100,6 +101,15 @@ int ref_init(const char* dir) {
             return 1;
         }
     return 0;
+}
+
+// sweepAndPruneCUDA<<<ceil(n/256), 256>>> (sap_detection.cu:613-629) on given
+// sorted inputs; rows (16 per sorted position) must be set to -1 first.
+int ref_sap_sweep(int n, CUdeviceptr upperx, CUdeviceptr lowerx_sorted, CUdeviceptr uppery, CUdeviceptr lowery,
+                  CUdeviceptr idx_sorted, CUdeviceptr idx, CUdeviceptr rows, CUstream st) {
+    int padding = 16;
+    void* args[] = {&n, &upperx, &lowerx_sorted, &uppery, &lowery, &idx_sorted, &idx, &rows, &padding};
+    return launch(kSweep, (unsigned)((n + 255) / 256), 256, 0, st, args);
 }
 
 // constructCollisionListCUDA<<<16, tpb, tpb*4>>> (sh_collision_detection.cu:298);

@@ -215,6 +215,12 @@ void sdo_hull_step(const sdo_hull_params* p, uint32_t nb, float* pos4, float* ve
                    const float* verts4, const uint32_t* off, const uint32_t* partners, const float* seeds4,
                    int32_t* status, int32_t* iters, float* dir4, float* force4, float* torque4);
 
+/* The reference's windowed sweep (sap_detection.cu:385-440) and its whole
+ * processCollisions pipeline; rows are 16 int32 per sorted position. */
+void sdo_sap_sweep_ref(uint32_t n, const float* upperx, const float* lowerx_sorted, const float* uppery,
+                       const float* lowery, const uint32_t* idx_sorted, int32_t* rows);
+void sdo_sap_process(uint32_t n, const float* pos4, const float* radius, int32_t* rows);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int sdo_num_threads(void);
 void sdo_set_num_threads(int n);

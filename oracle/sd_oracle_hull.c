@@ -813,3 +813,71 @@ void sdo_hull_step(const sdo_hull_params* p, uint32_t nb, float* pos4, float* ve
     }
     free(lo); free(ext); free(F);
 }
+
+/* ------------------------------------------------ sweep and prune (ref) */
+
+/* sweepAndPruneCUDA (src/engine/cuda/collisions/SAP/sap_detection.cu:
+ * 385-440) with populateCollisions (:293-323): per sorted position tid,
+ * partners among the next 64 sorted positions; the x test compares the
+ * phantom's lower x with the home upper x, which the kernel overwrites with
+ * the home upper y (:413) once an x test passes, and the y test compares
+ * the phantom's lower y with it; a partner is kept when it is not in the
+ * row yet, fewer than 10 are kept and its id differs from tid.  Rows are
+ * 16 int32, cleared to -1 first. */
+void sdo_sap_sweep_ref(uint32_t n, const float* upperx, const float* lowerx_sorted, const float* uppery,
+                       const float* lowery, const uint32_t* idx_sorted, int32_t* rows) {
+    for (uint32_t tid = 0; tid < n; ++tid) {
+        int32_t* row = rows + 16 * (size_t)tid;
+        for (int k = 0; k < 16; ++k) row[k] = -1;
+        int len = 0;
+        const uint32_t home = idx_sorted[tid];
+        float home_upper = upperx[home];
+        const uint32_t end = tid + 64 < n ? tid + 64 : n;
+        for (uint32_t i = tid + 1; i < end; ++i) {
+            const float pl = lowerx_sorted[i];
+            const uint32_t ph = idx_sorted[i];
+            if (!(pl <= home_upper)) continue;
+            home_upper = uppery[home];
+            if (!(lowery[ph] <= home_upper)) continue;
+            int unique = 1;
+            for (int k = 0; k < 16; ++k) unique &= row[k] != (int32_t)ph;
+            if (unique && len <= 8 && ph != tid) row[len++] = (int32_t)ph;
+        }
+    }
+}
+
+static inline uint32_t f32_bits(float v) {
+    uint32_t b;
+    memcpy(&b, &v, 4);
+    return b;
+}
+
+/* SAPCollision::processCollisions (sap_detection.cu:668-706): AABB = centre
+ * -/+ radius (radius4 NULL: pos.w), stable radix sort of the lower x
+ * extents' float bits (sortLowestExtents :278-290, the sort's intended
+ * semantics), projections, the sweep above. */
+void sdo_sap_process(uint32_t n, const float* pos4, const float* radius, int32_t* rows) {
+    const size_t m = n ? n : 1;
+    uint32_t* keys = (uint32_t*)malloc(4 * m * 4);
+    float* proj = (float*)malloc(4 * m * 4);
+    if (!keys || !proj) {
+        free(keys); free(proj);
+        return;
+    }
+    uint32_t *vals = keys + m, *tk = vals + m, *tv = tk + m;
+    float *upperx = proj, *uppery = proj + m, *lowery = proj + 2 * m, *lowerx_sorted = proj + 3 * m;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* p = pos4 + 4 * (size_t)i;
+        const float r = radius ? radius[i] : p[3];
+        upperx[i] = p[0] + r;
+        uppery[i] = p[1] + r;
+        lowery[i] = p[1] - r;
+        keys[i] = f32_bits(p[0] - r);
+        vals[i] = i;
+    }
+    sdo_radix_sort_pairs(keys, vals, n, 32, tk, tv);
+    for (uint32_t i = 0; i < n; ++i) memcpy(&lowerx_sorted[i], &keys[i], 4);
+    sdo_sap_sweep_ref(n, upperx, lowerx_sorted, uppery, lowery, vals, rows);
+    free(keys);
+    free(proj);
+}

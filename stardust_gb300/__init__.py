@@ -6,8 +6,9 @@ engine and operator classes over it (``stardust_gb300.engine``).
 """
 from . import _abi
 from ._abi import SdError, lib
-from .engine import (BoundingVolumes, DEMEngine, EngineConfig, SpatialPartition, add_hull_scene, scene_lattice,
-                     scene_rsa)
+from .engine import (BoundingVolumes, DEMEngine, EngineConfig, SpatialPartition, SweepAndPrune, add_hull_scene,
+                     scene_lattice, scene_rsa)
 
-__all__ = ["BoundingVolumes", "DEMEngine", "EngineConfig", "SpatialPartition", "SdError", "add_hull_scene", "lib",
+__all__ = ["BoundingVolumes", "DEMEngine", "EngineConfig", "SpatialPartition", "SweepAndPrune", "SdError",
+           "add_hull_scene", "lib",
            "scene_lattice", "scene_rsa", "_abi"]

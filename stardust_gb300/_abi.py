@@ -139,6 +139,10 @@ SIGNATURES = {
     "sd_engine_mlp_params": [P, P, U64, I32],
     "sd_engine_mlp_forward": [P, P, P, U64],
     "sd_engine_mlp_train": [P, P, P, U64, I32, F32, P],
+    "sd_sap_scratch_bytes": [U64, U64, C.POINTER(U64)],
+    "sd_sap_pairs": [U64, P, P, P, U64, P, P, U64, P],
+    "sd_sap_sweep": [U64, P, P, P, P, P, P, P],
+    "sd_sap_process_collisions": [U64, P, P, P, P, U64, P],
     "sd_lbvh_scratch_bytes": [U64, U64, C.POINTER(U64)],
     "sd_lbvh_pairs": [U64, P, P, P, U64, P, P, U64, P],
     "sd_lbvh_morton": [U64, P, P, P, P, U64, P],

@@ -559,8 +559,8 @@ sd_status sd_lbvh_pairs(uint64_t n, const float* d_lo4, const float* d_hi4, uint
     if (e == cudaSuccess) e = sd::lbvh_build_async(t, lo, hi, st);
     if (e == cudaSuccess) e = sd::lbvh_partners_async(t, off, partners, self, 2 * cap, st);
     if (e == cudaSuccess)
-        e = sd::lbvh_unique_pairs_async(t, off, partners, pos, reinterpret_cast<unsigned long long*>(d_pairs), cap,
-                                        st);
+        e = sd::lbvh_unique_pairs_async(t, off, partners, 2 * cap, pos, reinterpret_cast<unsigned long long*>(d_pairs),
+                                        cap, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_count, pos + n, 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_count + 1, t.status, 4, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return sd_cuda_fail(nullptr, e, "sd_lbvh_pairs");

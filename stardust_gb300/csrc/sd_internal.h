@@ -80,9 +80,27 @@ cudaError_t lbvh_build_async(Lbvh& t, const float4* lo, const float4* hi, cudaSt
 // per box id: partners at [off[id], off[id+1]) ascending, self[] = id; off has n+1
 cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint32_t* self, uint64_t cap,
                                 cudaStream_t st);
+// ascending unique pairs (i < j) of any per-box partner lists (CSR, partners
+// ascending per box); counts n, pos n+1 (pos[n] = count), scan scratch
+cudaError_t csr_unique_pairs_async(uint32_t n, const uint32_t* off, const uint32_t* partners, uint64_t partners_cap,
+                                   uint32_t* counts, uint32_t* scan_scratch, uint32_t* pos, unsigned long long* out,
+                                   uint64_t cap, cudaStream_t st);
 // ascending unique pairs (i < j) from the partner lists; pos has n+1 (pos[n] = count)
-cudaError_t lbvh_unique_pairs_async(Lbvh& t, const uint32_t* off, const uint32_t* partners, uint32_t* pos,
-                                    unsigned long long* out, uint64_t cap, cudaStream_t st);
+cudaError_t lbvh_unique_pairs_async(Lbvh& t, const uint32_t* off, const uint32_t* partners, uint64_t partners_cap,
+                                    uint32_t* pos, unsigned long long* out, uint64_t cap, cudaStream_t st);
+
+// ---- sweep and prune (sd_sap.cu)
+uint64_t sap_scratch_bytes(uint64_t n, uint64_t pair_cap);
+cudaError_t sap_aabb_async(uint32_t n, const float4* pos, const float* radius, float4* lo, float4* hi,
+                           cudaStream_t st);
+cudaError_t sap_sort_lower_x_async(uint32_t n, const float4* lo, bool ordered, uint32_t* keys, uint32_t* vals,
+                                   uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* sort_scratch, bool* in_tmp,
+                                   cudaStream_t st);
+cudaError_t sap_sweep_ref_async(uint32_t n, const float* upperx, const float* lowerx_sorted, const float* uppery,
+                                const float* lowery, const uint32_t* idx_sorted, int32_t* rows, cudaStream_t st);
+// exact pair set; d_count2[0] = pairs, d_count2[1] = device error bits
+cudaError_t sap_pairs_async(uint32_t n, const float4* lo, const float4* hi, void* scratch, uint64_t pair_cap,
+                            unsigned long long* out, uint32_t* d_count2, cudaStream_t st);
 
 // ---- convex hulls (sd_hull.cu)
 struct HullParams {

@@ -308,19 +308,23 @@ __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const flo
 
 // Unique pairs (i < j) of the partner lists, ascending u64.
 __global__ void upper_count_kernel(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ partners,
-                                   uint32_t* __restrict__ cnt) {
+                                   uint32_t* __restrict__ cnt, uint64_t partners_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t c = 0;
+    if ((uint64_t)off[n] > partners_cap) {  // overflowed lists are reported, not read
+        cnt[i] = 0;
+        return;
+    }
     for (uint32_t e = off[i]; e < off[i + 1]; ++e) c += partners[e] > i;
     cnt[i] = c;
 }
 
 __global__ void upper_write_kernel(uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ partners,
                                    const uint32_t* __restrict__ pos, unsigned long long* __restrict__ out,
-                                   uint64_t cap) {
+                                   uint64_t cap, uint64_t partners_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (uint64_t)off[n] > partners_cap) return;
     uint32_t w = pos[i];
     for (uint32_t e = off[i]; e < off[i + 1]; ++e) {
         const uint32_t j = partners[e];
@@ -445,15 +449,21 @@ cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint
     return cudaGetLastError();
 }
 
-cudaError_t lbvh_unique_pairs_async(Lbvh& t, const uint32_t* off, const uint32_t* partners, uint32_t* pos,
-                                    unsigned long long* out, uint64_t cap, cudaStream_t st) {
-    const uint32_t n = t.n;
+cudaError_t csr_unique_pairs_async(uint32_t n, const uint32_t* off, const uint32_t* partners, uint64_t partners_cap,
+                                   uint32_t* counts, uint32_t* scan_scratch, uint32_t* pos, unsigned long long* out,
+                                   uint64_t cap, cudaStream_t st) {
     if (n == 0) return cudaMemsetAsync(pos, 0, 4, st);
-    upper_count_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(n, off, partners, t.counts);
-    cudaError_t e = scan_exclusive_async(t.counts, pos, n, t.scan_scratch, st);
+    upper_count_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(n, off, partners, counts, partners_cap);
+    cudaError_t e = scan_exclusive_async(counts, pos, n, scan_scratch, st);
     if (e != cudaSuccess) return e;
-    upper_write_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(n, off, partners, pos, out, cap);
+    upper_write_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(n, off, partners, pos, out, cap,
+                                                                           partners_cap);
     return cudaGetLastError();
+}
+
+cudaError_t lbvh_unique_pairs_async(Lbvh& t, const uint32_t* off, const uint32_t* partners, uint64_t partners_cap,
+                                    uint32_t* pos, unsigned long long* out, uint64_t cap, cudaStream_t st) {
+    return csr_unique_pairs_async(t.n, off, partners, partners_cap, t.counts, t.scan_scratch, pos, out, cap, st);
 }
 
 }  // namespace sd

@@ -435,3 +435,48 @@ def add_hull_scene(eng: DEMEngine, points, pos, quat, vel, mass, omega=None) -> 
     for i in range(len(points)):
         eng.add_hull(points[i], float(mass[i]), tuple(pos[i]), tuple(quat[i]), tuple(vel[i]),
                      (0.0, 0.0, 0.0) if omega is None else tuple(omega[i]))
+
+
+class SweepAndPrune:
+    """SAPCollision (src/engine/cuda/collisions/SAP/sap_detection.cu) as raw
+    device operators on CUDA tensors."""
+
+    @staticmethod
+    def scratch_bytes(n: int, pair_cap: int = 0) -> int:
+        b = C.c_uint64()
+        call("sd_sap_scratch_bytes", n, pair_cap, C.byref(b))
+        return b.value
+
+    @staticmethod
+    def pairs(lo, hi, cap: int, stream=None):
+        """Exact pair set: (int64 tensor of (i << 32 | j) ascending, count, device error bits)."""
+        import torch
+        n = lo.shape[0]
+        scratch = torch.empty(SweepAndPrune.scratch_bytes(n, cap), dtype=torch.uint8, device=lo.device)
+        out = torch.empty(max(cap, 1), dtype=torch.int64, device=lo.device)
+        cnt = torch.zeros(2, dtype=torch.int32, device=lo.device)
+        call("sd_sap_pairs", n, lo.data_ptr(), hi.data_ptr(), out.data_ptr(), cap, cnt.data_ptr(), scratch.data_ptr(),
+             scratch.numel(), SpatialPartition._stream(stream))
+        c = cnt.cpu().numpy().view(np.uint32)
+        return out[: min(int(c[0]), cap)], int(c[0]), int(c[1])
+
+    @staticmethod
+    def sweep(upperx, lowerx_sorted, uppery, lowery, idx_sorted, stream=None):
+        """sweepAndPruneCUDA rows (n, 16) int32 on given sorted inputs."""
+        import torch
+        n = upperx.shape[0]
+        rows = torch.empty((max(n, 1), 16), dtype=torch.int32, device=upperx.device)
+        call("sd_sap_sweep", n, upperx.data_ptr(), lowerx_sorted.data_ptr(), uppery.data_ptr(), lowery.data_ptr(),
+             idx_sorted.data_ptr(), rows.data_ptr(), SpatialPartition._stream(stream))
+        return rows[:n]
+
+    @staticmethod
+    def process_collisions(pos4, radius=None, stream=None):
+        """SAPCollision::processCollisions: rows (n, 16) int32 per sorted position."""
+        import torch
+        n = pos4.shape[0]
+        scratch = torch.empty(SweepAndPrune.scratch_bytes(n, 0), dtype=torch.uint8, device=pos4.device)
+        rows = torch.empty((max(n, 1), 16), dtype=torch.int32, device=pos4.device)
+        call("sd_sap_process_collisions", n, pos4.data_ptr(), None if radius is None else radius.data_ptr(),
+             rows.data_ptr(), scratch.data_ptr(), scratch.numel(), SpatialPartition._stream(stream))
+        return rows[:n]

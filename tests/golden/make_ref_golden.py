@@ -12,7 +12,11 @@ them on seeded inputs:
   resolveCollisionsCUDA (collision_resolution.cu:30-199) over the stably
   sorted entries, run by one thread (see ref_harness.cpp) -> per-sphere force;
 * ``ref_rigid.npz`` -- updateSphereDataCUDA, computeForcesAndTorquesCUDA,
-  advectParticlesCUDA (physics_update.cu:26-310).
+  advectParticlesCUDA (physics_update.cu:26-310);
+* ``ref_sap_<case>.npz`` -- sweepAndPruneCUDA
+  (src/engine/cuda/collisions/SAP/sap_detection.cu:385-440) over sphere AABBs
+  whose lower x extents are stably sorted as uint32 float bits -> 16-entry
+  rows per sorted position (cleared to -1 before the launch).
 
 Usage:  python tests/golden/make_ref_golden.py OUT_DIR
 """
@@ -187,6 +191,33 @@ def run_rigid(lib, out: Path):
     print(f"rigid: {nb} bodies, {ns} spheres")
 
 
+def run_sap(lib, out: Path):
+    import torch
+    from oracle import oracle as orc
+    for name, n, rlo, rhi, seed in (("a", 3000, 0.002, 0.01, 21), ("b", 2000, 0.01, 0.04, 22)):
+        rng = np.random.default_rng(seed)
+        pos = np.zeros((n, 4), np.float32)
+        pos[:, :3] = rng.uniform(0.05, 0.95, (n, 3))
+        pos[:, 3] = rng.uniform(rlo, rhi, n)
+        r = pos[:, 3]
+        upperx = (pos[:, 0] + r).astype(np.float32)
+        uppery = (pos[:, 1] + r).astype(np.float32)
+        lowery = (pos[:, 1] - r).astype(np.float32)
+        keys = (pos[:, 0] - r).astype(np.float32).view(np.uint32).copy()
+        ids = np.arange(n, dtype=np.uint32)
+        ks, vs = orc.radix_sort_pairs(keys, ids, 32)
+        lowerx_sorted = ks.view(np.float32)
+        rows = dev(np.full((n, 16), -1, np.int32))
+        d = [dev(a) for a in (upperx, lowerx_sorted, uppery, lowery, vs, ids)]
+        torch.cuda.synchronize()
+        check(lib, lib.ref_sap_sweep(n, *[ptr(t) for t in d], ptr(rows), C.c_void_p(0)), "sap sweep")
+        torch.cuda.synchronize()
+        res = host(rows, np.int32, (n, 16))
+        np.savez_compressed(out / f"ref_sap_{name}.npz", pos=pos, upperx=upperx, lowerx_sorted=lowerx_sorted,
+                            uppery=uppery, lowery=lowery, idx_sorted=vs, rows=res)
+        print(f"sap {name}: {n} boxes, {(res >= 0).sum()} row entries")
+
+
 def main():
     out = Path(sys.argv[1] if len(sys.argv) > 1 else ".")
     out.mkdir(parents=True, exist_ok=True)
@@ -198,6 +229,7 @@ def main():
     hashed = run_hash(lib, out)
     run_traverse(lib, out, hashed)
     run_rigid(lib, out)
+    run_sap(lib, out)
 
 
 if __name__ == "__main__":

@@ -272,3 +272,17 @@ def test_candidate_pairs_miss_mixed_sign_diagonals(orc):
     k, v = orc.radix_sort_pairs(cells, spheres, 32)
     a, b = orc.ref_candidate_pairs(k, v, count)
     assert list(zip(a.tolist(), b.tolist())) == [(1, 0)]
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_golden_reference_sap_sweep(orc, case):
+    """sweepAndPruneCUDA (sap_detection.cu:385-440) run by the reference's own
+    kernel (tests/golden/make_ref_golden.py): the oracle's rows are equal,
+    including the kernel's use of the home upper y in later x tests; and the
+    whole processCollisions pipeline restated from the positions gives the
+    same rows."""
+    g = np.load(GOLDEN / f"ref_sap_{case}.npz")
+    rows = orc.sap_sweep_ref(g["upperx"], g["lowerx_sorted"], g["uppery"], g["lowery"], g["idx_sorted"])
+    assert np.array_equal(rows, g["rows"])
+    assert np.array_equal(orc.sap_process(g["pos"]), g["rows"])
+    assert (g["rows"] >= 0).sum() > 1000
