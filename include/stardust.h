@@ -172,6 +172,24 @@ sd_status sd_engine_add_particle(sd_engine* h, int32_t grid_resolution, float si
 sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float mass,
                               const float com[3], const float vel[3], const float omega[3]);
 
+/* A rigid triangle mesh -- the walls of a rotating drum -- that rotates at
+ * omega rad/s about the line through centre along axis (omega = 0: a static
+ * mesh).  tri9: n_tris triangles, 9 floats each (three vertices, world frame
+ * at time 0); patch (may be NULL: each triangle its own): the face a
+ * triangle belongs to -- per sphere, only the deepest contact of each face
+ * acts, so a sphere touching several triangles of one flat or gently curved
+ * face feels one contact.  Sphere-triangle contacts use the sphere contact
+ * law against the moving wall.  Candidate triangles come from a static grid
+ * in the mesh's own frame (the mesh moves rigidly, so the grid is built
+ * once).  One mesh per engine; not in a batch.  Replaces DEMEngine::addMesh
+ * (engine.cpp:117-121) with DEMMesh (entity.hpp:64-120), whose triangles the
+ * reference never used in a step. */
+sd_status sd_engine_add_mesh(sd_engine* h, uint32_t n_tris, const float* tri9, const int32_t* patch,
+                             const float centre[3], const float axis[3], float omega);
+/* The mesh pose on the device: R[9] (mesh to world, row-major), centre[3],
+ * axis[3], omega, q[4] (s, x, y, z), dq[4] (the rotation of one step). */
+sd_status sd_engine_get_mesh_state(sd_engine* h, float* state24);
+
 /* A batch of independent sphere scenes stepped together (one launch per
  * stage for all of them): each call adds one scene -- n spheres (pos4, vel4,
  * omega4 as sd_engine_add_spheres) in its own walled box [lo, hi] with its

@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
             "sdo_hull_step": (None, [P, C.c_uint32] + [P] * 17),
             "sdo_sap_sweep_ref": (None, [C.c_uint32, P, P, P, P, P, P]),
             "sdo_sap_process": (None, [C.c_uint32, P, P, P]),
+            "sdo_run_full": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_uint32] + [P] * 11),
+            "sdo_mesh_advance": (None, [P, C.c_int]),
             "sdo_num_threads": (C.c_int, []),
             "sdo_set_num_threads": (None, [C.c_int]),
         }
@@ -502,3 +504,48 @@ def sap_process(pos4, radius=None):
     r = None if radius is None else np.ascontiguousarray(radius, np.float32)
     lib().sdo_sap_process(n, _p(pos4), _p(r), _p(rows))
     return rows[:n]
+
+
+class Mesh(C.Structure):
+    """sdo_mesh (oracle/sd_oracle.h)."""
+    _fields_ = [("ntri", C.c_uint32), ("tri", C.c_void_p), ("patch", C.c_void_p), ("state", C.c_float * 24)]
+
+
+def make_mesh(tris, patch, centre, state24):
+    """Oracle mesh from world triangles at time 0 (mesh frame = world - centre)
+    and the engine's pose state; keeps the arrays alive on the object."""
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3) - np.asarray(centre, np.float32)
+    t4 = np.zeros((len(t), 3, 4), np.float32)
+    t4[:, :, :3] = t
+    t4 = np.ascontiguousarray(t4)
+    pa = np.ascontiguousarray(np.arange(len(t)) if patch is None else patch, np.int32)
+    m = Mesh()
+    m.ntri = len(t)
+    m.tri = t4.ctypes.data
+    m.patch = pa.ctypes.data
+    for k in range(24):
+        m.state[k] = float(state24[k])
+    m._keep = (t4, pa)
+    return m
+
+
+def run_full(p: Params, pos, vel, omg, steps: int, bodies=None, r0=None, body_of=None, mesh=None):
+    """sdo_run_full: optional clumps (as run_bodies) and an optional mesh."""
+    pos = np.array(pos, np.float32, copy=True)
+    vel = np.array(vel, np.float32, copy=True)
+    omg = np.array(omg, np.float32, copy=True)
+    if bodies is not None:
+        b = {k: np.array(bodies[k], np.float32, copy=True) for k in ("pos", "vel", "quat", "omega", "angmom", "inv")}
+        first = np.ascontiguousarray(bodies["first"], np.uint32)
+        count = np.ascontiguousarray(bodies["count"], np.uint32)
+        nb = len(first)
+        args = [_p(b["pos"]), _p(b["vel"]), _p(b["quat"]), _p(b["omega"]), _p(b["angmom"]), _p(b["inv"]), _p(first),
+                _p(count), _p(np.ascontiguousarray(r0, np.float32)), _p(np.ascontiguousarray(body_of, np.int32))]
+    else:
+        b, nb = None, 0
+        args = [None] * 10
+    rc = lib().sdo_run_full(C.byref(p), len(pos), _p(pos), _p(vel), _p(omg), steps, nb, *args,
+                            None if mesh is None else C.byref(mesh))
+    if rc != 0:
+        raise RuntimeError("oracle run failed")
+    return pos, vel, omg, b

@@ -529,10 +529,101 @@ static inline void contact_response##SUFFIX(                                    
     }                                                                                        \
 }                                                                                            \
                                                                                              \
+/* mesh walls: closest point of each triangle (Ericson 5.1.5), all        \
+ * triangles in ascending order, deepest contact per patch kept */         \
+static inline void closest_tri##SUFFIX(const REAL* p, const REAL* a, const REAL* b,         \
+    const REAL* c, REAL* q) {                                                                \
+    REAL ab[3], ac[3], ap[3], bp[3], cp[3];                                                  \
+    for (int k = 0; k < 3; ++k) { ab[k] = b[k] - a[k]; ac[k] = c[k] - a[k]; ap[k] = p[k] - a[k]; } \
+    REAL d1 = (ab[0] * ap[0] + ab[1] * ap[1]) + ab[2] * ap[2];                               \
+    REAL d2 = (ac[0] * ap[0] + ac[1] * ap[1]) + ac[2] * ap[2];                               \
+    if (d1 <= 0 && d2 <= 0) { for (int k = 0; k < 3; ++k) q[k] = a[k]; return; }            \
+    for (int k = 0; k < 3; ++k) bp[k] = p[k] - b[k];                                         \
+    REAL d3 = (ab[0] * bp[0] + ab[1] * bp[1]) + ab[2] * bp[2];                               \
+    REAL d4 = (ac[0] * bp[0] + ac[1] * bp[1]) + ac[2] * bp[2];                               \
+    if (d3 >= 0 && d4 <= d3) { for (int k = 0; k < 3; ++k) q[k] = b[k]; return; }           \
+    REAL vc = d1 * d4 - d3 * d2;                                                             \
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) {                                                     \
+        REAL v = d1 / (d1 - d3);                                                             \
+        for (int k = 0; k < 3; ++k) q[k] = a[k] + ab[k] * v;                                 \
+        return;                                                                              \
+    }                                                                                        \
+    for (int k = 0; k < 3; ++k) cp[k] = p[k] - c[k];                                         \
+    REAL d5 = (ab[0] * cp[0] + ab[1] * cp[1]) + ab[2] * cp[2];                               \
+    REAL d6 = (ac[0] * cp[0] + ac[1] * cp[1]) + ac[2] * cp[2];                               \
+    if (d6 >= 0 && d5 <= d6) { for (int k = 0; k < 3; ++k) q[k] = c[k]; return; }           \
+    REAL vb = d5 * d2 - d1 * d6;                                                             \
+    if (vb <= 0 && d2 >= 0 && d6 <= 0) {                                                     \
+        REAL w = d2 / (d2 - d6);                                                             \
+        for (int k = 0; k < 3; ++k) q[k] = a[k] + ac[k] * w;                                 \
+        return;                                                                              \
+    }                                                                                        \
+    REAL va = d3 * d6 - d5 * d4;                                                             \
+    if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {                                      \
+        REAL w = (d4 - d3) / ((d4 - d3) + (d5 - d6));                                        \
+        for (int k = 0; k < 3; ++k) q[k] = b[k] + (c[k] - b[k]) * w;                         \
+        return;                                                                              \
+    }                                                                                        \
+    REAL den = (REAL)1 / ((va + vb) + vc);                                                   \
+    REAL v = vb * den, w = vc * den;                                                         \
+    for (int k = 0; k < 3; ++k) q[k] = (a[k] + ab[k] * v) + ac[k] * w;                       \
+}                                                                                            \
+                                                                                             \
+static void mesh_contacts##SUFFIX(const sdo_params* p, const sdo_mesh* m, const REAL* pi,   \
+    const REAL* vi, const REAL* wi, REAL* f, REAL* t) {                                      \
+    const float* S = m->state;                                                               \
+    REAL R[9];                                                                               \
+    for (int k = 0; k < 9; ++k) R[k] = (REAL)S[k];                                           \
+    REAL d[3] = {pi[0] - (REAL)S[9], pi[1] - (REAL)S[10], pi[2] - (REAL)S[11]};              \
+    REAL q[3] = {(R[0] * d[0] + R[3] * d[1]) + R[6] * d[2],                                  \
+                 (R[1] * d[0] + R[4] * d[1]) + R[7] * d[2],                                  \
+                 (R[2] * d[0] + R[5] * d[1]) + R[8] * d[2]};                                 \
+    REAL r2 = pi[3] * pi[3];                                                                 \
+    int32_t pid[4]; REAL pd2[4], pv[4][3], pq[4][3]; int np = 0;                             \
+    for (uint32_t tr = 0; tr < m->ntri; ++tr) {                                              \
+        REAL a[3], b[3], c[3], cl[3], v[3];                                                  \
+        for (int k = 0; k < 3; ++k) {                                                        \
+            a[k] = (REAL)m->tri[12 * (size_t)tr + k];                                        \
+            b[k] = (REAL)m->tri[12 * (size_t)tr + 4 + k];                                    \
+            c[k] = (REAL)m->tri[12 * (size_t)tr + 8 + k];                                    \
+        }                                                                                    \
+        closest_tri##SUFFIX(q, a, b, c, cl);                                                 \
+        for (int k = 0; k < 3; ++k) v[k] = q[k] - cl[k];                                     \
+        REAL d2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];                                 \
+        if (!(d2 < r2) || d2 == (REAL)0) continue;                                           \
+        int32_t pa = m->patch[tr];                                                           \
+        int k = 0;                                                                           \
+        while (k < np && pid[k] != pa) ++k;                                                  \
+        if (k < np) {                                                                        \
+            if (d2 < pd2[k]) { pd2[k] = d2; for (int j = 0; j < 3; ++j) { pv[k][j] = v[j]; pq[k][j] = cl[j]; } } \
+        } else if (np < 4) {                                                                 \
+            pid[np] = pa; pd2[np] = d2;                                                      \
+            for (int j = 0; j < 3; ++j) { pv[np][j] = v[j]; pq[np][j] = cl[j]; }             \
+            ++np;                                                                            \
+        }                                                                                    \
+    }                                                                                        \
+    REAL ax[3] = {(REAL)S[12], (REAL)S[13], (REAL)S[14]}, om = (REAL)S[15];                  \
+    for (int k = 0; k < np; ++k) {                                                           \
+        REAL dist = SQRT(pd2[k]);                                                            \
+        REAL inv = (REAL)1 / dist;                                                           \
+        REAL nl[3] = {pv[k][0] * inv, pv[k][1] * inv, pv[k][2] * inv};                       \
+        REAL nn[3], qw[3];                                                                   \
+        for (int r = 0; r < 3; ++r) {                                                        \
+            nn[r] = (R[3 * r] * nl[0] + R[3 * r + 1] * nl[1]) + R[3 * r + 2] * nl[2];        \
+            qw[r] = (R[3 * r] * pq[k][0] + R[3 * r + 1] * pq[k][1]) + R[3 * r + 2] * pq[k][2]; \
+        }                                                                                    \
+        REAL vw[3] = {(ax[1] * qw[2] - ax[2] * qw[1]) * om, (ax[2] * qw[0] - ax[0] * qw[2]) * om, \
+                      (ax[0] * qw[1] - ax[1] * qw[0]) * om};                                 \
+        REAL ri = pi[3];                                                                     \
+        contact_response##SUFFIX(p, nn[0], nn[1], nn[2], ri - dist, vi[0] - vw[0],           \
+            vi[1] - vw[1], vi[2] - vw[2], ri * wi[0], ri * wi[1], ri * wi[2], vi[3], ri, f, t); \
+    }                                                                                        \
+}                                                                                            \
+                                                                                             \
 static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,                   \
     const REAL* pos, const REAL* vel, const REAL* omg, const uint32_t* cell_start,           \
     REAL* pos_n, REAL* vel_n, REAL* omg_n, uint32_t* keys_n, REAL* force4, REAL* torque4,    \
-    const int32_t* body_of, REAL* sf4, REAL* st4) {                                          \
+    const int32_t* body_of, REAL* sf4, REAL* st4, const sdo_mesh* mesh) {                    \
     uint64_t contacts = 0;                                                                   \
     _Pragma("omp parallel for schedule(dynamic, 1024) reduction(+:contacts)")               \
     for (int64_t i = 0; i < (int64_t)n; ++i) {                                               \
@@ -586,6 +677,7 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
                 }                                                                            \
             }                                                                                \
         }                                                                                    \
+        if (mesh && mesh->ntri) mesh_contacts##SUFFIX(p, mesh, pi, vi, wi, f, t);            \
         if (p->walls) {                                                                      \
             REAL wsx = ri * wi[0], wsy = ri * wi[1], wsz = ri * wi[2];                       \
             REAL xs[3] = {xi, yi, zi};                                                       \
@@ -638,7 +730,7 @@ uint64_t sdo_contact_integrate(const sdo_params* p, uint32_t n,
                                float* pos_n, float* vel_n, float* omg_n, uint32_t* keys_n,
                                float* force4, float* torque4) {
     return contact_integrate_f32(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                 keys_n, force4, torque4, NULL, NULL, NULL);
+                                 keys_n, force4, torque4, NULL, NULL, NULL, NULL);
 }
 
 uint64_t sdo_contact_integrate_f64(const sdo_params* p, uint32_t n,
@@ -647,7 +739,7 @@ uint64_t sdo_contact_integrate_f64(const sdo_params* p, uint32_t n,
                                    double* pos_n, double* vel_n, double* omg_n, uint32_t* keys_n,
                                    double* force4, double* torque4) {
     return contact_integrate_f64(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n,
-                                 keys_n, force4, torque4, NULL, NULL, NULL);
+                                 keys_n, force4, torque4, NULL, NULL, NULL, NULL);
 }
 
 static int cmp_u64(const void* a, const void* b) {
@@ -733,7 +825,7 @@ uint64_t sdo_contact_integrate_bodies(const sdo_params* p, uint32_t n, const flo
                                       float* pos_n, float* vel_n, float* omg_n, uint32_t* keys_n,
                                       float* force4, float* torque4, float* sf4, float* st4) {
     return contact_integrate_f32(p, n, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys_n, force4, torque4,
-                                 body_of, sf4, st4);
+                                 body_of, sf4, st4, NULL);
 }
 
 void sdo_slot_of(uint32_t n, const float* omg, uint32_t* slot_of) {
@@ -847,10 +939,10 @@ void sdo_body_step(const sdo_params* p, uint32_t nb, float* bpos4, float* bvel4,
     }
 }
 
-int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
-                   uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
-                   const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
-                   const int32_t* body_of) {
+int sdo_run_full(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
+                 uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
+                 const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
+                 const int32_t* body_of, sdo_mesh* mesh) {
     size_t nc = (size_t)p->nx * p->ny * p->nz;
     float* buf = (float*)malloc(sizeof(float) * 20 * (size_t)(n ? n : 1));
     uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
@@ -869,12 +961,40 @@ int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, floa
     sdo_sort_reorder(p, n, pn, vn, wn, keys, NULL, pos, vel, omg, cs);
     sdo_slot_of(n, omg, slot);
     for (int s = 0; s < steps; ++s) {
-        contact_integrate_f32(p, n, pos, vel, omg, cs, pn, vn, wn, keys, NULL, NULL, body_of, sf, st);
-        sdo_body_step(p, nb, bpos4, bvel4, bquat4, bomg4, bang4, binv12, first, count, r0_4, slot, pos, omg, sf,
-                      st, pn, vn, wn, keys);
+        contact_integrate_f32(p, n, pos, vel, omg, cs, pn, vn, wn, keys, NULL, NULL, body_of, sf, st, mesh);
+        if (nb)
+            sdo_body_step(p, nb, bpos4, bvel4, bquat4, bomg4, bang4, binv12, first, count, r0_4, slot, pos, omg, sf,
+                          st, pn, vn, wn, keys);
         sdo_sort_reorder(p, n, pn, vn, wn, keys, NULL, pos, vel, omg, cs);
         sdo_slot_of(n, omg, slot);
+        if (mesh && mesh->ntri) sdo_mesh_advance(mesh->state, 1);
     }
     free(buf); free(keys); free(slot); free(cs);
     return 0;
+}
+
+
+int sdo_run_bodies(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
+                   uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
+                   const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
+                   const int32_t* body_of) {
+    return sdo_run_full(p, n, pos, vel, omg, steps, nb, bpos4, bvel4, bquat4, bomg4, bang4, binv12, first, count,
+                        r0_4, body_of, NULL);
+}
+
+/* The mesh pose of the next step (advance != 0): q <- normalize(dq (x) q),
+ * then R <- R(q); the kernel mesh_advance_kernel's expressions. */
+void sdo_mesh_advance(float* S, int advance) {
+    float qs = S[16], qx = S[17], qy = S[18], qz = S[19];
+    if (advance) {
+        const float ds = S[20], dx = S[21], dy = S[22], dz = S[23];
+        const float ns = ds * qs - ((dx * qx + dy * qy) + dz * qz);
+        const float nx = (ds * qx + qs * dx) + (dy * qz - dz * qy);
+        const float ny = (ds * qy + qs * dy) + (dz * qx - dx * qz);
+        const float nz = (ds * qz + qs * dz) + (dx * qy - dy * qx);
+        const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
+        qs = ns / nrm; qx = nx / nrm; qy = ny / nrm; qz = nz / nrm;
+        S[16] = qs; S[17] = qx; S[18] = qy; S[19] = qz;
+    }
+    quat_rot(qs, qx, qy, qz, S);
 }

@@ -156,6 +156,19 @@ uint64_t sdo_contact_pairs(const sdo_params* p, uint32_t n, const float* pos,
 int sdo_run(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg,
             int steps, int prepare);
 
+/* A rigid triangle mesh: tri holds 12 floats per triangle (3 rows x, y, z,
+ * unused) in the mesh frame, patch a face id per triangle, state 24 floats
+ * R[9] (mesh to world), c[3], axis[3], omega, q[4], dq[4] (as the engine's
+ * device state).  Every triangle is tested, in ascending order; the deepest
+ * contact per patch is kept. */
+typedef struct sdo_mesh {
+    uint32_t ntri;
+    const float* tri;
+    const int32_t* patch;
+    float state[24];
+} sdo_mesh;
+void sdo_mesh_advance(float* state24, int advance);
+
 /* ---- rigid clumps (spheres whose id has bit 31 set belong to body
  * body_of[id]; pairs within one body are skipped, collision_resolution.cu:69) */
 
@@ -220,6 +233,13 @@ void sdo_hull_step(const sdo_hull_params* p, uint32_t nb, float* pos4, float* ve
 void sdo_sap_sweep_ref(uint32_t n, const float* upperx, const float* lowerx_sorted, const float* uppery,
                        const float* lowery, const uint32_t* idx_sorted, int32_t* rows);
 void sdo_sap_process(uint32_t n, const float* pos4, const float* radius, int32_t* rows);
+
+/* sdo_run_bodies with an optional mesh (mesh may be NULL, nb may be 0); the
+ * mesh state advances after every step. */
+int sdo_run_full(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg, int steps,
+                 uint32_t nb, float* bpos4, float* bvel4, float* bquat4, float* bomg4, float* bang4,
+                 const float* binv12, const uint32_t* first, const uint32_t* count, const float* r0_4,
+                 const int32_t* body_of, sdo_mesh* mesh);
 
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int sdo_num_threads(void);

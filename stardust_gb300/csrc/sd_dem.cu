@@ -217,11 +217,112 @@ __device__ __forceinline__ bool same_body(const ClumpCtx& cc, uint32_t idb, cons
     return (jdb & kClumpFlag) && cc.body_of[idb & kIdMask] == cc.body_of[jdb & kIdMask];
 }
 
+// ------------------------------------------------------------- mesh walls
+
+__device__ __forceinline__ float3 f3v(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 mul3(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+
+// Closest point of triangle (a, b, c) to p (Ericson, Real-Time Collision
+// Detection, 5.1.5: Voronoi regions of vertices, edges, face).
+__device__ __forceinline__ float3 closest_on_triangle(float3 p, float3 a, float3 b, float3 c) {
+    const float3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+    const float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) return a;
+    const float3 bp = sub3(p, b);
+    const float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) return b;
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) return add3(a, mul3(ab, d1 / (d1 - d3)));
+    const float3 cp = sub3(p, c);
+    const float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+    if (d6 >= 0.0f && d5 <= d6) return c;
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) return add3(a, mul3(ac, d2 / (d2 - d6)));
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f)
+        return add3(b, mul3(sub3(c, b), (d4 - d3) / ((d4 - d3) + (d5 - d6))));
+    const float den = 1.0f / ((va + vb) + vc);
+    return add3(add3(a, mul3(ab, vb * den)), mul3(ac, vc * den));
+}
+
+// Contacts of a sphere (centre x, radius ri) with the mesh: the triangles
+// listed in its cell of the mesh grid, ascending; per patch the deepest
+// contact (the first of equal depth) is kept; each kept contact applies the
+// sphere law against the moving wall (velocity omega axis x (q - c)).
+__device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView& m, float4 pi, float4 vi, float4 wi,
+                                              float3& f, float3& t) {
+    const float* S = m.state;
+    float R[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = __ldg(S + k);
+    const float3 c = make_float3(__ldg(S + 9), __ldg(S + 10), __ldg(S + 11));
+    const float3 ax = make_float3(__ldg(S + 12), __ldg(S + 13), __ldg(S + 14));
+    const float om = __ldg(S + 15);
+    const float3 d = sub3(make_float3(pi.x, pi.y, pi.z), c);
+    const float3 q = make_float3((R[0] * d.x + R[3] * d.y) + R[6] * d.z, (R[1] * d.x + R[4] * d.y) + R[7] * d.z,
+                                 (R[2] * d.x + R[5] * d.y) + R[8] * d.z);  // R^T d: mesh frame
+    const int32_t ix = axis_cell(q.x, m.lo[0], m.h, m.nx);
+    const int32_t iy = axis_cell(q.y, m.lo[1], m.h, m.ny);
+    const int32_t iz = axis_cell(q.z, m.lo[2], m.h, m.nz);
+    const uint32_t cell = (uint32_t)((ix * m.ny + iy) * m.nz + iz);
+    const uint32_t e0 = __ldg(m.cell_off + cell), e1 = __ldg(m.cell_off + cell + 1);
+    if (e0 == e1) return;
+    const float r2 = pi.w * pi.w;
+    int32_t pid[kMeshPatches];
+    float pd2[kMeshPatches];
+    float3 pv[kMeshPatches], pq[kMeshPatches];
+    int np = 0;
+    for (uint32_t e = e0; e < e1; ++e) {
+        const uint32_t tr = __ldg(m.cell_tri + e);
+        const float3 a = f3v(__ldg(m.tri + 3 * tr)), b = f3v(__ldg(m.tri + 3 * tr + 1)),
+                     cc = f3v(__ldg(m.tri + 3 * tr + 2));
+        const float3 cl = closest_on_triangle(q, a, b, cc);
+        const float3 v = sub3(q, cl);
+        const float d2 = dot3(v, v);
+        if (!(d2 < r2) || d2 == 0.0f) continue;
+        const int32_t pa = __ldg(m.patch + tr);
+        int k = 0;
+        while (k < np && pid[k] != pa) ++k;
+        if (k < np) {
+            if (d2 < pd2[k]) {
+                pd2[k] = d2;
+                pv[k] = v;
+                pq[k] = cl;
+            }
+        } else if (np < kMeshPatches) {
+            pid[np] = pa;
+            pd2[np] = d2;
+            pv[np] = v;
+            pq[np] = cl;
+            ++np;
+        }
+    }
+    for (int k = 0; k < np; ++k) {
+        const float dist = sqrtf(pd2[k]);
+        const float inv = 1.0f / dist;
+        const float3 nl = mul3(pv[k], inv);
+        const float3 n = make_float3((R[0] * nl.x + R[1] * nl.y) + R[2] * nl.z,
+                                     (R[3] * nl.x + R[4] * nl.y) + R[5] * nl.z,
+                                     (R[6] * nl.x + R[7] * nl.y) + R[8] * nl.z);
+        const float3 qw = make_float3((R[0] * pq[k].x + R[1] * pq[k].y) + R[2] * pq[k].z,
+                                      (R[3] * pq[k].x + R[4] * pq[k].y) + R[5] * pq[k].z,
+                                      (R[6] * pq[k].x + R[7] * pq[k].y) + R[8] * pq[k].z);  // q - c, world
+        const float3 vw = mul3(make_float3(ax.y * qw.z - ax.z * qw.y, ax.z * qw.x - ax.x * qw.z,
+                                           ax.x * qw.y - ax.y * qw.x), om);
+        const float ri = pi.w;
+        contact_response(p, n.x, n.y, n.z, ri - dist, vi.x - vw.x, vi.y - vw.y, vi.z - vw.z, ri * wi.x, ri * wi.y,
+                         ri * wi.z, vi.w, ri, f, t);
+    }
+}
+
 // Contacts of slot i over its candidate cells, then walls, integration and
 // the next-state write.  Returns the new cell key; a clump sphere hands its
 // force and torque to its body instead (the body kernel writes its next
 // state and key) and *has_key is false.
-template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false>
+template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false, bool MESH = false>
 __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                   const float4* __restrict__ omg,
@@ -230,7 +331,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
                                                   uint32_t* __restrict__ vals, float4* __restrict__ force,
                                                   float4* __restrict__ torque, uint32_t& contacts,
-                                                  const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{}) {
+                                                  const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{},
+                                                  const MeshView* mesh = nullptr) {
     const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
@@ -291,6 +393,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             }
         }
     }
+    if (MESH) mesh_contacts(p, *mesh, pi, vi, wi, f, t);
     if (p.walls) {
         const float wsx = ri * wi.x, wsy = ri * wi.y, wsz = ri * wi.z;
         const float xs[3] = {pi.x, pi.y, pi.z};
@@ -384,7 +487,7 @@ __device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contac
 }
 
 // ---------------------------------------------- contact_mode 0: per slot
-template <bool RECORD, bool CLUMPS, bool BATCHED = false>
+template <bool RECORD, bool CLUMPS, bool BATCHED = false, bool MESH = false>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -393,15 +496,16 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
-                             ClumpCtx cc, Batch bt = Batch{}) {
+                             ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{}) {
     __shared__ uint32_t s_hist[kFusedPasses][512];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     if (i < n)
-        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED>(p, n, i, GlobalSource{pos}, pos, vel, omg,
-                                                                    cell_start, pos_n, vel_n, omg_n, keys, vals,
-                                                                    force, torque, contacts, cc, &has_key, bt);
+        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH>(p, n, i, GlobalSource{pos}, pos, vel, omg,
+                                                                          cell_start, pos_n, vel_n, omg_n, keys, vals,
+                                                                          force, torque, contacts, cc, &has_key, bt,
+                                                                          &mesh);
     if (ghist) {
         for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
         __syncthreads();
@@ -816,7 +920,46 @@ __global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, co
     }
 }
 
+// The mesh pose of the next step: q <- normalize(dq (x) q) (Hamilton
+// product), then the rotation matrix of q (the expression of the rigid
+// bodies).
+__global__ void mesh_advance_kernel(float* __restrict__ S, int advance) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    float qs = S[16], qx = S[17], qy = S[18], qz = S[19];
+    if (advance) {
+        const float ds = S[20], dx = S[21], dy = S[22], dz = S[23];
+        const float ns = ds * qs - ((dx * qx + dy * qy) + dz * qz);
+        const float nx = (ds * qx + qs * dx) + (dy * qz - dz * qy);
+        const float ny = (ds * qy + qs * dy) + (dz * qx - dx * qz);
+        const float nz = (ds * qz + qs * dz) + (dx * qy - dy * qx);
+        const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
+        qs = ns / nrm;
+        qx = nx / nrm;
+        qy = ny / nrm;
+        qz = nz / nrm;
+        S[16] = qs;
+        S[17] = qx;
+        S[18] = qy;
+        S[19] = qz;
+    }
+    S[0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+    S[1] = 2.0f * (qx * qy - qs * qz);
+    S[2] = 2.0f * (qx * qz + qs * qy);
+    S[3] = 2.0f * (qx * qy + qs * qz);
+    S[4] = 1.0f - 2.0f * (qx * qx + qz * qz);
+    S[5] = 2.0f * (qy * qz - qs * qx);
+    S[6] = 2.0f * (qx * qz - qs * qy);
+    S[7] = 2.0f * (qy * qz + qs * qx);
+    S[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
+}
+
 static inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1) / threads; }
+
+cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st) {
+    if (m.ntri == 0) return cudaSuccess;
+    mesh_advance_kernel<<<1, 32, 0, st>>>(m.state, advance);
+    return cudaGetLastError();
+}
 
 cudaError_t dem_init_kernels() {
     const int sm = (int)(kTileSlots * sizeof(float4));
@@ -880,7 +1023,16 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
     const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
     const size_t tile = kTileSlots * sizeof(float4);
-    if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
+    if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
+        if (b.nb)
+            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
+        else
+            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
+    } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
             b.dev_status, spec, ghist, cc, Batch{b.scenes, b.scene_first, b.nscenes});
@@ -938,7 +1090,8 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     if (plan.passes > kFusedPasses) {
         cudaError_t e = dem_contact_integrate_async(p, b, record, st);
         if (e != cudaSuccess) return e;
-        return dem_sort_reorder_async(p, b, st);
+        if ((e = dem_sort_reorder_async(p, b, st)) != cudaSuccess) return e;
+        return mesh_advance_async(b.mesh, 1, st);
     }
     cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
     if (e != cudaSuccess) return e;
@@ -946,7 +1099,8 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
                                &b.sorted_in_tmp)) != cudaSuccess)
         return e;
-    return dem_reorder_async(b, st);
+    if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
+    return mesh_advance_async(b.mesh, 1, st);
 }
 
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {

@@ -172,6 +172,7 @@ sd_status derive_params(sd_engine* h) {
     if (h->scenes.size() > 1) {
         // a batch: the configured box and cell are not used
         if (!h->hb_pos.empty()) return fail(h, SD_ERR_UNSUPPORTED, "rigid clumps are not supported in a batch");
+        if (!h->mesh.tri.empty()) return fail(h, SD_ERR_UNSUPPORTED, "meshes are not supported in a batch");
         sd_status s = derive_batch(h);
         if (s) return s;
         const sd::SceneGrid& g0 = h->scene_grids[0];
@@ -236,6 +237,124 @@ sd_status upload_and_sort(sd_engine* h, const float4* pos, const float4* vel, co
     return SD_OK;
 }
 
+// The mesh's static grid (mesh frame): cell edge 2 x the largest sphere
+// radius (grown until the grid has at most 2^25 cells), every triangle
+// listed in every cell its box, grown by that radius, touches -- so a
+// sphere's own cell lists every triangle it can reach -- in ascending order.
+sd_status build_mesh(sd_engine* h) {
+    auto& M = h->mesh;
+    sd::MeshView& V = h->B.mesh;
+    const uint32_t nt = (uint32_t)(M.tri.size() / 3);
+    float rmax = 0.0f;
+    for (auto& p : h->h_pos) rmax = std::max(rmax, p.w);
+    if (!(rmax > 0.0f)) rmax = 1e-3f;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (const float4& v : M.tri) {
+        const float c[3] = {v.x, v.y, v.z};
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], c[a]);
+            hi[a] = std::max(hi[a], c[a]);
+        }
+    }
+    float hcell = 2.0f * rmax;
+    int32_t dims[3];
+    uint64_t nc = 0;
+    for (;;) {
+        nc = 1;
+        for (int a = 0; a < 3; ++a) {
+            const double ext = (double)hi[a] - lo[a] + 2.0 * rmax;
+            dims[a] = (int32_t)std::max(1.0, std::ceil(ext / hcell));
+            nc *= (uint64_t)dims[a];
+        }
+        if (nc <= (1ull << 25)) break;
+        hcell *= 1.5f;
+    }
+    for (int a = 0; a < 3; ++a) V.lo[a] = lo[a] - rmax;
+    V.h = hcell;
+    V.nx = dims[0];
+    V.ny = dims[1];
+    V.nz = dims[2];
+    auto cell_of = [&](float x, int a) {
+        float t = (x - V.lo[a]) / V.h;
+        if (!(t >= 0.0f)) return 0;
+        if (t >= (float)dims[a]) return dims[a] - 1;
+        return (int)t;
+    };
+    std::vector<uint32_t> off(nc + 1, 0);
+    std::vector<uint32_t> list;
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<uint32_t> fill;
+        if (pass == 1) {
+            for (uint64_t c = 0; c < nc; ++c) off[c + 1] += off[c];
+            list.assign(off[nc], 0u);
+            fill.assign(off.begin(), off.end() - 1);
+        }
+        for (uint32_t t = 0; t < nt; ++t) {
+            float tl[3] = {INFINITY, INFINITY, INFINITY}, th[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int k = 0; k < 3; ++k) {
+                const float4 v = M.tri[3 * (size_t)t + k];
+                const float c[3] = {v.x, v.y, v.z};
+                for (int a = 0; a < 3; ++a) {
+                    tl[a] = std::min(tl[a], c[a]);
+                    th[a] = std::max(th[a], c[a]);
+                }
+            }
+            int c0[3], c1[3];
+            for (int a = 0; a < 3; ++a) {
+                c0[a] = cell_of(tl[a] - rmax, a);
+                c1[a] = cell_of(th[a] + rmax, a);
+            }
+            for (int x = c0[0]; x <= c1[0]; ++x)
+                for (int y = c0[1]; y <= c1[1]; ++y)
+                    for (int z = c0[2]; z <= c1[2]; ++z) {
+                        const uint64_t c = ((uint64_t)x * dims[1] + y) * dims[2] + z;
+                        if (pass == 0) off[c + 1]++;
+                        else list[fill[c]++] = t;
+                    }
+        }
+        if (pass == 0 && off.size() > 1) {
+            uint64_t tot = 0;
+            for (uint64_t c = 1; c <= nc; ++c) tot += off[c];
+            if (tot >= 0xffffffffull) return fail(h, SD_ERR_CAPACITY, "mesh grid lists exceed 2^32 entries");
+        }
+    }
+    sd_status s;
+    float4* tri = nullptr;
+    int32_t* patch = nullptr;
+    uint32_t *coff = nullptr, *ctri = nullptr;
+    float* state = nullptr;
+    if ((s = dev_alloc(h, &tri, M.tri.size())) || (s = dev_alloc(h, &patch, nt)) ||
+        (s = dev_alloc(h, &coff, nc + 1)) || (s = dev_alloc(h, &ctri, std::max<size_t>(list.size(), 1))) ||
+        (s = dev_alloc(h, &state, 24)))
+        return s;
+    SD_CUDA(h, cudaMemcpyAsync(tri, M.tri.data(), 16 * M.tri.size(), cudaMemcpyHostToDevice, h->stream));
+    SD_CUDA(h, cudaMemcpyAsync(patch, M.patch.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+    SD_CUDA(h, cudaMemcpyAsync(coff, off.data(), 4 * (nc + 1), cudaMemcpyHostToDevice, h->stream));
+    if (!list.empty())
+        SD_CUDA(h, cudaMemcpyAsync(ctri, list.data(), 4 * list.size(), cudaMemcpyHostToDevice, h->stream));
+    // pose: R (set by the first mesh_advance with advance = 0), centre, axis,
+    // omega, q = identity, dq set when the step's time step is known
+    float* S = M.state;
+    std::memset(S, 0, sizeof M.state);
+    for (int a = 0; a < 3; ++a) {
+        S[9 + a] = M.centre[a];
+        S[12 + a] = M.axis[a];
+    }
+    S[15] = M.omega;
+    S[16] = 1.0f;
+    S[20] = 1.0f;
+    SD_CUDA(h, cudaMemcpyAsync(state, S, sizeof M.state, cudaMemcpyHostToDevice, h->stream));
+    V.ntri = nt;
+    V.tri = tri;
+    V.patch = patch;
+    V.cell_off = coff;
+    V.cell_tri = ctri;
+    V.state = state;
+    M.dt = 0.0f;
+    SD_CUDA(h, sd::mesh_advance_async(V, 0, h->stream));
+    return SD_OK;
+}
+
 sd_status allocate(sd_engine* h, uint32_t n) {
     sd::DemBuffers& B = h->B;
     B.n = n;
@@ -265,6 +384,9 @@ sd_status allocate(sd_engine* h, uint32_t n) {
     if ((s = dev_alloc(h, &B.pairs, (size_t)B.pair_cap)) || (s = dev_alloc(h, &B.npairs, 1))) return s;
     SD_CUDA(h, cudaMemsetAsync(B.dev_status, 0, 8 * sizeof(uint32_t), h->stream));
     SD_CUDA(h, cudaMemsetAsync(B.sort_scratch, 0, 16 * sizeof(uint32_t), h->stream));
+    if (!h->mesh.tri.empty()) {
+        if ((s = build_mesh(h))) return s;
+    }
     B.nscenes = h->scenes.size() > 1 ? (uint32_t)h->scenes.size() : 0u;
     if (B.nscenes) {
         sd::SceneGrid* g = nullptr;
@@ -334,6 +456,15 @@ sd_status build_graph(sd_engine* h, float dt) {
     }
     h->P.dt = dt;
     bool record = (h->cfg.flags & SD_FLAG_RECORD) != 0;
+    if (h->B.mesh.ntri && h->mesh.dt != dt) {
+        // the rotation of one step, in double: angle omega dt about the axis
+        const double half = 0.5 * (double)h->mesh.omega * (double)dt;
+        float dq[4] = {(float)std::cos(half), (float)(std::sin(half) * h->mesh.axis[0]),
+                       (float)(std::sin(half) * h->mesh.axis[1]), (float)(std::sin(half) * h->mesh.axis[2])};
+        SD_CUDA(h, cudaMemcpyAsync(h->B.mesh.state + 20, dq, sizeof dq, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+        h->mesh.dt = dt;
+    }
     cudaGraph_t g = nullptr;
     SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
@@ -502,6 +633,47 @@ sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, con
         h->h_body_of.push_back(-1);
         h->h_r0.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
     }
+    return SD_OK;
+}
+
+sd_status sd_engine_add_mesh(sd_engine* h, uint32_t n_tris, const float* tri9, const int32_t* patch,
+                             const float centre[3], const float axis[3], float omega) {
+    if (!h || (n_tris && !tri9) || !centre) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->prepared) return fail(h, SD_ERR_STATE, "meshes cannot be added after prepare");
+    if (!h->mesh.tri.empty()) return fail(h, SD_ERR_UNSUPPORTED, "one mesh per engine");
+    if (n_tris == 0 || n_tris >= (1u << 26)) return fail(h, SD_ERR_INVALID_ARG, "n_tris must be in 1..2^26");
+    double a[3] = {axis ? axis[0] : 0.0, axis ? axis[1] : 0.0, axis ? axis[2] : 1.0};
+    const double an = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (!(an > 0.0)) return fail(h, SD_ERR_INVALID_ARG, "mesh axis is zero");
+    if (!std::isfinite(omega)) return fail(h, SD_ERR_INVALID_ARG, "omega must be finite");
+    auto& M = h->mesh;
+    M.tri.resize(3 * (size_t)n_tris);
+    M.patch.resize(n_tris);
+    for (uint32_t t = 0; t < n_tris; ++t) {
+        for (int k = 0; k < 3; ++k) {
+            const float* v = tri9 + 9 * (size_t)t + 3 * k;
+            if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2])) {
+                M.tri.clear();
+                M.patch.clear();
+                return fail(h, SD_ERR_INVALID_ARG, "mesh vertex not finite");
+            }
+            M.tri[3 * (size_t)t + k] = make_float4(v[0] - centre[0], v[1] - centre[1], v[2] - centre[2], 0.0f);
+        }
+        M.patch[t] = patch ? patch[t] : (int32_t)t;
+    }
+    for (int k = 0; k < 3; ++k) {
+        M.centre[k] = centre[k];
+        M.axis[k] = (float)(a[k] / an);
+    }
+    M.omega = omega;
+    return SD_OK;
+}
+
+sd_status sd_engine_get_mesh_state(sd_engine* h, float* state24) {
+    if (!h || !state24) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (!h->prepared || !h->B.mesh.ntri) return fail(h, SD_ERR_STATE, "no prepared mesh");
+    SD_CUDA(h, cudaMemcpyAsync(state24, h->B.mesh.state, 24 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
     return SD_OK;
 }
 
@@ -1081,6 +1253,7 @@ static const char kCkptMagic[8] = {'S', 'D', 'G', 'B', 'C', 'K', 'P', '1'};
 sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
     if (!h || !path) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (h->scenes.size() > 1) return fail(h, SD_ERR_UNSUPPORTED, "checkpoints of a batch of scenes are not supported");
+    if (!h->mesh.tri.empty()) return fail(h, SD_ERR_UNSUPPORTED, "checkpoints of a scene with a mesh are not supported");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
     if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
     SD_CUDA(h, cudaSetDevice(h->device));

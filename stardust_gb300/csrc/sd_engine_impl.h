@@ -58,6 +58,14 @@ struct sd_engine {
     std::vector<sd::SceneGrid> scene_grids;  // derived at prepare
     std::vector<uint32_t> scene_first;
     bool adding_scene = false;
+    // a rigid triangle mesh rotating about an axis (sd_engine_add_mesh)
+    struct MeshHost {
+        std::vector<float4> tri;       // 3 rows per triangle, mesh frame (world at t = 0 minus centre)
+        std::vector<int32_t> patch;
+        float centre[3] = {0, 0, 0}, axis[3] = {0, 0, 1}, omega = 0.0f;
+        float state[24] = {0};
+        float dt = 0.0f;               // dq of the graph's time step
+    } mesh;
 
     bool prepared = false;
     int device = 0;

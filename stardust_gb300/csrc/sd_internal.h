@@ -180,9 +180,29 @@ struct SceneGrid {
     uint32_t base;
 };
 
+// A rigid triangle mesh (walls of a rotating drum): triangles in the mesh's
+// own frame, a static uniform grid over that frame listing, per cell, every
+// triangle within the largest sphere radius (ascending triangle ids), and
+// the pose.  state (device, 24 floats): R[9] (mesh to world), c[3] (centre
+// of rotation), axis[3] (unit), omega, q[4] (s,x,y,z), dq[4] (the rotation of
+// one step); mesh_advance_async applies q <- normalize(dq q), R <- R(q).
+struct MeshView {
+    uint32_t ntri;
+    const float4* tri;        // 3 rows per triangle (x, y, z, 0), mesh frame
+    const int32_t* patch;     // per triangle: the face it belongs to
+    const uint32_t* cell_off; // ncells + 1
+    const uint32_t* cell_tri;
+    float lo[3];
+    float h;
+    int32_t nx, ny, nz;
+    float* state;
+};
+constexpr int kMeshPatches = 4;  // deepest contact kept per patch, up to this many patches per sphere
+
 struct DemBuffers {
     uint32_t n;
     uint32_t ncells;
+    MeshView mesh;                  // mesh.ntri == 0: no mesh
     uint32_t nscenes;               // 0 or 1: one scene (DemParams' grid); > 1: a batch
     const SceneGrid* scenes;        // [nscenes]
     const uint32_t* scene_first;    // [nscenes + 1] first slot of each scene, then n
@@ -229,5 +249,7 @@ cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, 
 cudaError_t dem_scatter_in_async(const float4* src_by_id, const float4* omg, float4* dst, uint32_t n, bool keep_w,
                                  cudaStream_t st);
 cudaError_t dem_energy_async(const DemBuffers& b, double* d_out, cudaStream_t st);
+// advance != 0: q <- normalize(dq q); then R <- R(q)
+cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st);
 
 }  // namespace sd

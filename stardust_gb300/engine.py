@@ -126,6 +126,20 @@ class DEMEngine:
                    lo3, hi3, cell)
         self._n += len(p)
 
+    def add_mesh(self, tris, centre, axis=(0.0, 0.0, 1.0), omega: float = 0.0, patch=None) -> None:
+        """A rigid triangle mesh (tris: (n, 3, 3) world vertices at time 0)
+        rotating at omega about the line through centre along axis."""
+        t = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        pa = None if patch is None else np.ascontiguousarray(patch, np.int32)
+        c = (C.c_float * 3)(*centre)
+        a = (C.c_float * 3)(*axis)
+        self._call("sd_engine_add_mesh", len(t), t.ctypes.data, None if pa is None else pa.ctypes.data, c, a, omega)
+
+    def mesh_state(self) -> np.ndarray:
+        out = np.empty(24, np.float32)
+        self._call("sd_engine_get_mesh_state", out.ctypes.data)
+        return out
+
     def add_clump(self, rel4, mass: float, com, velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0)) -> None:
         """One rigid body made of spheres (rel4 rows: body-frame offset from
         the centre of mass, radius); the body's inertia is that of its

@@ -203,3 +203,98 @@ def batch_boxes(n_scenes: int = 512, seed: int = 0, n_min: int = 256, n_max: int
     cfg = EngineConfig(walls=0x3F, kn=1e5, restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81),
                        pair_capacity=1 << 22)
     return out, cfg, 1e-5
+
+
+def drum_mesh(radius: float, length: float, n_around: int, n_along: int, n_rings: int, centre):
+    """A closed cylinder along x: the side wall (n_around x n_along quads, two
+    triangles each, patch 0) and two end caps (a fan plus n_rings - 1 rings of
+    n_around sectors, patches 1 and 2).  Returns (tris (n, 3, 3), patch)."""
+    cx, cy, cz = centre
+    th = np.linspace(0.0, 2.0 * math.pi, n_around + 1)[:-1]
+    xs = np.linspace(-0.5 * length, 0.5 * length, n_along + 1)
+    ring = lambda x, r, k: (cx + x, cy + r * math.cos(th[k % n_around]), cz + r * math.sin(th[k % n_around]))
+    tris, patch = [], []
+    for i in range(n_along):
+        for k in range(n_around):
+            a, b = ring(xs[i], radius, k), ring(xs[i], radius, k + 1)
+            c, d = ring(xs[i + 1], radius, k), ring(xs[i + 1], radius, k + 1)
+            tris += [(a, b, d), (a, d, c)]
+            patch += [0, 0]
+    radii = np.linspace(0.0, radius, n_rings + 1)
+    for side, x in ((1, -0.5 * length), (2, 0.5 * length)):
+        centre_pt = (cx + x, cy, cz)
+        for k in range(n_around):
+            tris.append((centre_pt, ring(x, radii[1], k), ring(x, radii[1], k + 1)))
+            patch.append(side)
+        for j in range(1, n_rings):
+            for k in range(n_around):
+                a, b = ring(x, radii[j], k), ring(x, radii[j], k + 1)
+                c, d = ring(x, radii[j + 1], k), ring(x, radii[j + 1], k + 1)
+                tris += [(a, b, d), (a, d, c)]
+                patch += [side, side]
+    return np.array(tris, np.float32), np.array(patch, np.int32)
+
+
+def drum_scene(n_spheres: int = 2_097_152, radius: float = 0.5, length: float = 0.5, n_around: int = 128,
+               n_along: int = 65, n_rings: int = 8, r_range=(0.0012, 0.0024), clump_fraction: float = 0.1,
+               omega: float = 2.0, density: float = 2500.0, seed: int = 0):
+    """The rotating drum: a closed cylinder along x (20,480 triangles with the
+    defaults) turning at omega rad/s, filled from the bottom with bodies on a
+    jittered lattice (spacing 2.1 x the largest radius): single spheres with
+    radii U[r_range], and clump_fraction of the bodies 4-sphere tetrahedral
+    clumps (sphere radius U[r_min, 0.75 r_max], centres 0.6 r from the body
+    centre, random orientation), until n_spheres spheres; density 2500
+    kg/m^3, kn 1e5, restitution 0.5, mu 0.3, gravity -z, dt 2e-6 s.  Returns
+    dict(tris, patch, centre, axis, omega, pos, vel, clumps, cfg, dt)."""
+    rng = np.random.default_rng(seed)
+    rmin, rmax = r_range
+    centre = (0.5 * length, radius, radius)
+    tris, patch = drum_mesh(radius, length, n_around, n_along, n_rings, centre)
+    sp = 2.1 * rmax
+    margin = 1.2 * rmax
+    xs = np.arange(margin, length - margin + 1e-12, sp)
+    ys = np.arange(margin, 2 * radius - margin + 1e-12, sp)
+    zs = np.arange(margin, 2 * radius - margin + 1e-12, sp)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    sites = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    ok = (sites[:, 1] - centre[1]) ** 2 + (sites[:, 2] - centre[2]) ** 2 < (radius - margin) ** 2
+    sites = sites[ok]
+    sites = sites[np.argsort(sites[:, 2], kind="stable")]
+    need = int(math.ceil(n_spheres / (1.0 + 3.0 * clump_fraction)))
+    if need > len(sites):
+        raise ValueError(f"the drum holds {len(sites)} bodies at this spacing, {need} requested")
+    n_bodies = min(len(sites), int(need * 1.02) + 8)  # slack for the random clump share
+    sites = sites[:n_bodies] + rng.uniform(-0.02 * rmax, 0.02 * rmax, (n_bodies, 3))
+    is_clump = rng.random(n_bodies) < clump_fraction
+    tet = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], float) / math.sqrt(3.0)
+    pos, vel, clumps = [], [], []
+    count = 0
+    for b in range(n_bodies):
+        if count >= n_spheres:
+            break
+        if is_clump[b] and count + 4 <= n_spheres:
+            r = rng.uniform(rmin, 0.75 * rmax)
+            off = (tet * 0.6 * r) @ _rotation(rng).T
+            rel = np.concatenate([off, np.full((4, 1), r)], 1).astype(np.float32)
+            mass = density * 4.0 / 3.0 * math.pi * r ** 3 * 4
+            clumps.append((rel, float(mass), tuple(sites[b]), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)))
+            count += 4
+        else:
+            r = rng.uniform(rmin, rmax)
+            pos.append([*sites[b], r])
+            vel.append([0.0, 0.0, 0.0, density * 4.0 / 3.0 * math.pi * r ** 3])
+            count += 1
+    cfg = EngineConfig(box_lo=(0.0, 0.0, 0.0), box_hi=(length, 2 * radius, 2 * radius), walls=0, cell=2 * rmax,
+                       kn=1e5, restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81), pair_capacity=1 << 22)
+    return {"tris": tris, "patch": patch, "centre": centre, "axis": (1.0, 0.0, 0.0), "omega": omega,
+            "pos": np.array(pos, np.float32).reshape(-1, 4), "vel": np.array(vel, np.float32).reshape(-1, 4),
+            "clumps": clumps, "cfg": cfg, "dt": 2e-6}
+
+
+def add_drum_scene(eng, d) -> None:
+    """Adds drum_scene's clumps (ids first), spheres and mesh."""
+    for rel, mass, com, v, w in d["clumps"]:
+        eng.add_clump(rel, mass, com, v, w)
+    if len(d["pos"]):
+        eng.add_spheres(d["pos"], d["vel"])
+    eng.add_mesh(d["tris"], d["centre"], d["axis"], d["omega"], d["patch"])
