@@ -21,6 +21,8 @@ reorder + cell_start.  Timings:
              measured HBM peak;
   cpu_baseline  the CPU oracle (the restated step, OpenMP on the host cores)
              on a bounded sample of the same scene;
+  drum       the rotating drum: 2.1M spheres and clumps against a turning
+             20,480-triangle cylinder (bench_drum);
   batch      512 independent scenes (~2.9M spheres) stepped together, one
              launch per stage (bench_batch), against 16 of them stepped alone;
   gjk        the second half of the metric: mean GJK support evaluations per
@@ -370,6 +372,48 @@ def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
             "device_errors": st["device_errors"], "autotune": tuned}
 
 
+def bench_drum(steps: int, warmup: int, local: int):
+    """The rotating drum (drum_scene): 2,097,152 spheres -- 10 % of the bodies
+    4-sphere clumps -- in a closed cylinder of radius 0.5 m and length 0.5 m
+    meshed with 20,480 triangles, turning at 2 rad/s, dt 2e-6 s; radii
+    U[1.2, 2.4] mm (the specified U[2, 4] mm would fill 67 % of the drum's
+    volume, beyond random close packing).  Device time per step, CUDA
+    events, a 256 MB write before every timed step."""
+    import torch
+    import stardust_gb300 as sd
+    from stardust_gb300 import scenes
+    t0 = time.perf_counter()
+    d = scenes.drum_scene()
+    gen_s = time.perf_counter() - t0
+    d["cfg"].cuda_device = local
+    eng = sd.DEMEngine(d["cfg"])
+    scenes.add_drum_scene(eng, d)
+    eng.prepare()
+    dt = d["dt"]
+    eng.step(dt, warmup)
+    eng.sync()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    st = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    a = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    b = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        with torch.cuda.stream(st):
+            flush.fill_(i & 0xFF)
+        a[i].record(st)
+        eng.step(dt, 1)
+        b[i].record(st)
+    torch.cuda.synchronize()
+    ms = sum(x.elapsed_time(y) for x, y in zip(a, b)) / steps
+    stt = eng.stats()
+    n = eng.n
+    eng.close()
+    return {"workload": f"rotating drum, {n} spheres ({len(d['clumps'])} 4-sphere clumps), "
+                        f"{len(d['tris'])} triangles, R 0.5 m, L 0.5 m, 2 rad/s, dt 2e-6 s",
+            "spheres": n, "bodies": int(stt["n_bodies"]), "triangles": int(len(d["tris"])), "ms_per_step": ms,
+            "particle_steps_per_s": n / (ms * 1e-3), "device_errors": stt["device_errors"],
+            "scene_generation_s": gen_s}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -487,6 +531,12 @@ def run_ours(args, rank, world, local):
         batch = bench_batch(args.scenes, args.steps, args.warmup, local, not args.no_tune)
         log(f"batch: {batch}")
 
+    # ---- rotating drum (rank 0, N = 1)
+    drum = None
+    if rank == 0 and world == 1 and not args.no_drum:
+        drum = bench_drum(args.steps, args.warmup, local)
+        log(f"drum: {drum}")
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -525,6 +575,7 @@ def run_ours(args, rank, world, local):
             "contacts": st["contacts"],
             "gjk": gjk,
             "batch": batch,
+            "drum": drum,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -550,11 +601,18 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched-scenes section")
     ap.add_argument("--scenes", type=int, default=512)
+    ap.add_argument("--no-drum", action="store_true")
+    ap.add_argument("--only-drum", action="store_true", help="run only the rotating-drum section")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.only_drum:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"drum": bench_drum(args.steps, args.warmup, local)}), flush=True)
+        return 0
     if args.only_batch:
         import torch
         torch.cuda.set_device(local)
