@@ -464,12 +464,9 @@ def run_ours(args, rank, world, local):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     clocks = clk.summary()
     eng.sync()
-    total_ms = sum(step_ms)
-    t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = world * n * args.steps / (total_ms * 1e-3)
+    from stardust_gb300 import replicas
+    total_ms = replicas.max_over_ranks(sum(step_ms), device=f"cuda:{local}")
+    value = replicas.job_rate(n * args.steps, total_ms * 1e-3, device=f"cuda:{local}")
 
     # ---- dominant kernel alone: contact + integrate (idempotent stage)
     kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -512,10 +509,7 @@ def run_ours(args, rank, world, local):
                    "get_state", eng._h)
     barrier()
     e2e_s = time.perf_counter() - t0
-    t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e = world * n * args.steps / float(t.item())
+    e2e = replicas.job_rate(n * args.steps, e2e_s, device=f"cuda:{local}")
     st = eng.stats()
     eng.close()
 
