@@ -539,15 +539,42 @@ __global__ void hull_prev_seed_kernel(HullBuffers H, uint32_t mode) {
     }
 }
 
-// Narrow phase of one entry: GJK (seeded or plain), EPA on a hit, contact
-// force and torque on the entry's own body.
-__global__ void __launch_bounds__(kHullThreads) hull_entry_kernel(HullParams p, HullBuffers H) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= H.cap) return;
+// Unique pairs: per body the number of its entries with a larger partner,
+// then the list of those entries (body order, partner order).
+__global__ void hull_unique_count_kernel(HullBuffers H) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= H.nb) return;
+    uint32_t c = 0;
+    if ((uint64_t)H.off[H.nb] <= H.cap)
+        for (uint32_t e = H.off[b]; e < H.off[b + 1]; ++e) c += H.partners[e] > b;
+    H.ucount[b] = c;
+}
+
+__global__ void hull_unique_fill_kernel(HullBuffers H) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= H.nb || (uint64_t)H.off[H.nb] > H.cap) return;
+    uint32_t w = H.upos[b];
+    for (uint32_t e = H.off[b]; e < H.off[b + 1]; ++e)
+        if (H.partners[e] > b) H.ulist[w++] = e;
+}
+
+// Narrow phase of one pair (A, B), A < B, from its entry in A's list: GJK
+// (seeded or plain), EPA on a hit, contact force; the entry of A and its
+// mirror in B's list (binary search: lists are ascending) receive the
+// force and torque on their own body, the same status and direction.
+__global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, HullBuffers H) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t total = H.off[H.nb];
-    if (e >= total || (uint64_t)total > H.cap) return;  // an overflowed step is reported, not evaluated
-    const uint32_t self = H.self[e], other = H.partners[e];
-    const uint32_t A = min(self, other), B = max(self, other);
+    if ((uint64_t)total > H.cap || u >= H.upos[H.nb]) return;  // an overflowed step is reported, not evaluated
+    const uint32_t e = H.ulist[u];
+    const uint32_t A = H.self[e], B = H.partners[e];
+    uint32_t lo = H.off[B], hi = H.off[B + 1];
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (H.partners[mid] < A) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint32_t em = lo;  // the mirror entry (B, A)
     HPair P;
     make_pair(H, A, B, &P);
     v3 d0 = vneg(P.off);
@@ -563,9 +590,9 @@ __global__ void __launch_bounds__(kHullThreads) hull_entry_kernel(HullParams p, 
         st = gjk(P, vneg(P.off), &S, &it2, &dir);
         iters += it2;
     }
-    v3 f = mk(0.f, 0.f, 0.f), t = mk(0.f, 0.f, 0.f);
+    v3 fa = mk(0.f, 0.f, 0.f), ta = mk(0.f, 0.f, 0.f), fbv = mk(0.f, 0.f, 0.f), tb = mk(0.f, 0.f, 0.f);
     int epa_it = 0;
-    v3 dA = rotT(P.A.R, dir);  // final direction in A's frame (seed of the next step)
+    const v3 dA = rotT(P.A.R, dir);  // final direction in A's frame (seed of the next step)
     if (st == kHit) {
         Contact c;
         epa(P, S, (H.iinv[A].w + H.iinv[B].w) * 1e-7f, &c);
@@ -582,20 +609,24 @@ __global__ void __launch_bounds__(kHullThreads) hull_entry_kernel(HullParams p, 
             const v3 vA = vadd(f3(H.vel[A]), vcross(f3(H.omg[A]), rA));
             const v3 vB = vadd(f3(H.vel[B]), vcross(f3(H.omg[B]), rB));
             const float meff = (mA * mB) / (mA + mB);
-            const v3 fb = contact_force(p, c.depth - skin, c.n, vsub(vB, vA), meff);
-            if (self == B) {
-                f = fb;
-                t = vcross(rB, fb);
-            } else {
-                f = vneg(fb);
-                t = vcross(rA, f);
-            }
+            fbv = contact_force(p, c.depth - skin, c.n, vsub(vB, vA), meff);
+            tb = vcross(rB, fbv);
+            fa = vneg(fbv);
+            ta = vcross(rA, fa);
         }
     }
-    H.ef[e] = make_float4(f.x, f.y, f.z, 0.f);
-    H.et[e] = make_float4(t.x, t.y, t.z, 0.f);
-    H.info[e] = (uint32_t)st | ((uint32_t)iters << 8) | ((uint32_t)epa_it << 16);
-    H.dir[e] = make_float4(dA.x, dA.y, dA.z, st == kSep ? 1.0f : 0.0f);
+    const uint32_t info = (uint32_t)st | ((uint32_t)iters << 8) | ((uint32_t)epa_it << 16);
+    const float4 d4 = make_float4(dA.x, dA.y, dA.z, st == kSep ? 1.0f : 0.0f);
+    H.ef[e] = make_float4(fa.x, fa.y, fa.z, 0.f);
+    H.et[e] = make_float4(ta.x, ta.y, ta.z, 0.f);
+    H.info[e] = info;
+    H.dir[e] = d4;
+    if (em < H.off[B + 1]) {  // always true for consistent lists
+        H.ef[em] = make_float4(fbv.x, fbv.y, fbv.z, 0.f);
+        H.et[em] = make_float4(tb.x, tb.y, tb.z, 0.f);
+        H.info[em] = info;
+        H.dir[em] = d4;
+    }
 }
 
 // Per body: segmented sum of its entries (list order), walls, integration.
@@ -705,9 +736,16 @@ cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Each pair is evaluated once, by one thread, into both of its entries.
+// The grid covers the largest possible pair count (cap / 2); threads past
+// the step's count return at once.
 cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st) {
     if (H.nb == 0 || H.cap == 0) return cudaSuccess;
-    hull_entry_kernel<<<grid_for(H.cap, kHullThreads), kHullThreads, 0, st>>>(p, H);
+    hull_unique_count_kernel<<<grid_for(H.nb, 256), 256, 0, st>>>(H);
+    cudaError_t e = scan_exclusive_async(H.ucount, H.upos, H.nb, H.uscan, st);
+    if (e != cudaSuccess) return e;
+    hull_unique_fill_kernel<<<grid_for(H.nb, 256), 256, 0, st>>>(H);
+    hull_pair_kernel<<<grid_for(H.cap / 2 + 1, kHullThreads), kHullThreads, 0, st>>>(p, H);
     return cudaGetLastError();
 }
 

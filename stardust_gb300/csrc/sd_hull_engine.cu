@@ -201,7 +201,8 @@ sd_status hull_prepare(sd_engine* h) {
         (s = halloc(h, &H.lo, nb)) || (s = halloc(h, &H.hi, nb)) || (s = halloc(h, &H.ext, 2 * (size_t)nb)) ||
         (s = halloc(h, &H.self, cap)) || (s = halloc(h, &H.ef, cap)) || (s = halloc(h, &H.et, cap)) ||
         (s = halloc(h, &H.info, cap)) || (s = halloc(h, &H.seeds, cap)) || (s = halloc(h, &H.feat, 16 * cap)) ||
-        (s = halloc(h, &S.stats, 4)))
+        (s = halloc(h, &S.stats, 4)) || (s = halloc(h, &H.ucount, nb)) || (s = halloc(h, &H.upos, (size_t)nb + 1)) ||
+        (s = halloc(h, &H.ulist, cap / 2 + 1)) || (s = halloc(h, &H.uscan, sd::scan_scratch_words(nb) + 1)))
         return s;
     for (int k = 0; k < 2; ++k)
         if ((s = halloc(h, &S.off[k], (size_t)nb + 1)) || (s = halloc(h, &S.partners[k], cap)) ||

@@ -129,6 +129,7 @@ struct HullBuffers {
     const uint32_t *prev_off, *prev_partners;  // the previous step's lists
     const float4* prev_dir;
     float4 *force, *torque;                // optional per body totals
+    uint32_t *ucount, *upos, *ulist, *uscan;  // unique pairs: per body count, offsets (nb+1), entry list, scan scratch
 };
 cudaError_t hull_aabb_async(HullBuffers& H, cudaStream_t st);
 cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st);
