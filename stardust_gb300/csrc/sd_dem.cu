@@ -674,18 +674,16 @@ __device__ __forceinline__ void quat_rot(float qs, float qx, float qy, float qz,
 // segmented reduction, no atomics), add gravity, integrate momentum and
 // angular momentum, w = R I0^-1 R^T L, normalised first-order quaternion
 // update, then write every sphere's next state and cell key (and its
-// histogram digits for the sort).
-__global__ void __launch_bounds__(128)
-dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __restrict__ bvel,
-                float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
-                const float4* __restrict__ binv, const uint32_t* __restrict__ bfirst,
-                const uint32_t* __restrict__ bcount, const float4* __restrict__ r0, const uint32_t* __restrict__ slot_of,
-                const float4* __restrict__ pos, const float4* __restrict__ omg, const float4* __restrict__ sf,
-                const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
-                float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
-                uint32_t hist_spec, uint32_t* __restrict__ ghist) {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
+// digits to the block's shared sort histograms when s_hist is given).
+__device__ __forceinline__ void body_step(
+    const DemParams& p, uint32_t b, float4* __restrict__ bpos, float4* __restrict__ bvel,
+    float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
+    const float4* __restrict__ binv, const uint32_t* __restrict__ bfirst, const uint32_t* __restrict__ bcount,
+    const float4* __restrict__ r0, const uint32_t* __restrict__ slot_of, const float4* __restrict__ pos,
+    const float4* __restrict__ omg, const float4* __restrict__ sf, const float4* __restrict__ st,
+    float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n, uint32_t hist_spec,
+    uint32_t (*s_hist)[512]) {
     const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
     const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
     const uint32_t first = bfirst[b], cnt = bcount[b];
@@ -751,11 +749,11 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
         const uint32_t key = cell_key(p, po.x, po.y, po.z);
         keys[s] = key;
         vals[s] = s;
-        if (ghist) {
+        if (s_hist) {
             const int passes = (int)(hist_spec & 3u);
             for (int q = 0; q < passes; ++q) {
                 const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
-                atomicAdd(&ghist[q * 512 + ((key >> shift) & ((1u << bits) - 1u))], 1u);
+                atomicAdd(&s_hist[q][(key >> shift) & ((1u << bits) - 1u)], 1u);
             }
         }
     }
@@ -764,6 +762,34 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
     bang[b] = make_float4(Lx, Ly, Lz, bl.w);
     bquat[b] = make_float4(q0, q1, q2, q3);
     bomg[b] = make_float4(wx, wy, wz, 0.0f);
+}
+
+// One thread per body.  The clump spheres' key digits are counted in shared
+// memory and added to the global histograms once per block: a global atomic
+// per sphere piles onto the few bins of the high digits (one L2 slice) and
+// stalls the whole kernel behind it.
+__global__ void __launch_bounds__(128)
+dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __restrict__ bvel,
+                float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
+                const float4* __restrict__ binv, const uint32_t* __restrict__ bfirst,
+                const uint32_t* __restrict__ bcount, const float4* __restrict__ r0, const uint32_t* __restrict__ slot_of,
+                const float4* __restrict__ pos, const float4* __restrict__ omg, const float4* __restrict__ sf,
+                const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
+                float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
+                uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t s_hist[kFusedPasses][512];
+    if (ghist) {
+        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+        __syncthreads();
+    }
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb)
+        body_step(p, b, bpos, bvel, bquat, bomg, bang, binv, bfirst, bcount, r0, slot_of, pos, omg, sf, st, pos_n,
+                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr);
+    if (ghist) {
+        __syncthreads();
+        hist_flush(s_hist, hist_spec, ghist);
+    }
 }
 
 __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
@@ -811,7 +837,16 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
     const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
     const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
     const uint32_t cnt = b1 - b0;
+    // cells at or before the block's first key take b0 and cells after its
+    // last key (only the last block has them: the tail up to ncells) take
+    // b1, without a search -- an empty region past the last sphere can be
+    // tens of thousands of cells, all in that one block
+    const int64_t kfirst = cnt ? (int64_t)s_keys[1] : hi, klast = cnt ? (int64_t)s_keys[cnt] : lo;
     for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += kReorderThreads) {
+        if (c <= kfirst || c > klast) {
+            cell_start[c] = c <= kfirst ? b0 : b1;
+            continue;
+        }
         uint32_t a = 0, z = cnt;  // first index in [0, cnt) with key >= c, else cnt
         while (a < z) {
             uint32_t m = (a + z) >> 1;
