@@ -49,6 +49,21 @@ __device__ __forceinline__ int32_t axis_cell(float x, float lo, float cell, int3
     return (int32_t)t;
 }
 
+// Cells [c0, c1] on one axis that can hold a centre within `reach` of x,
+// from one reciprocal instead of two divisions.  The range is widened by a
+// margin far above the rounding error of either form, so it contains every
+// cell the exact division would give; a wider range only adds candidates
+// that fail the distance test, and the contacts keep their visiting order,
+// so forces are unchanged bit for bit.
+__device__ __forceinline__ void axis_window(float x, float reach, float lo, float ic, int32_t n, int32_t& c0,
+                                            int32_t& c1) {
+    const float t = (x - lo) * ic, r = reach * ic;
+    const float m = 1e-3f + 4e-7f * (float)n;
+    const float a = t - r - m, b = t + r + m;
+    c0 = a >= 0.0f ? (a < (float)n ? (int32_t)a : n - 1) : 0;
+    c1 = b >= 0.0f ? (b < (float)n ? (int32_t)b : n - 1) : 0;
+}
+
 // The grid a sphere lives in: the engine's one grid, or its scene's grid in a
 // batch (keys offset by the scene's base).
 struct Grid {
@@ -188,6 +203,7 @@ __device__ __forceinline__ void pair_contact(const DemParams& p, float dx, float
 // column coded c = (dx+1)*3 + (dy+1) relative to the sphere's own column is
 // element s + delta_of(c) of the source.
 struct GlobalSource {
+    static constexpr bool kExactWindow = false;  // any superset of the partner cells will do
     const float4* __restrict__ pos;
     __device__ __forceinline__ uint32_t delta_of(uint32_t, int32_t, int32_t) const { return 0u; }
     __device__ __forceinline__ float4 load(uint32_t k) const { return __ldg(&pos[k]); }
@@ -196,6 +212,7 @@ struct GlobalSource {
 // Used only for spheres of the CTA's own column, so the sphere's column and
 // the tile's centre column coincide.
 struct TileSource {
+    static constexpr bool kExactWindow = true;  // columns must lie in the staged 3x3 block
     const float4* tile;     // staged slots of the 3x3 neighbour columns
     const uint32_t* shift;  // per neighbour column: tile offset - first slot (mod 2^32)
     __device__ __forceinline__ uint32_t delta_of(uint32_t c, int32_t, int32_t) const { return shift[c]; }
@@ -346,15 +363,23 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     // outer, y inner), slots ascending -- so the force sums are identical to
     // a full 27-cell scan.
     const float reach = (ri + p.rmax) * 1.00001f;
-    const int32_t cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
-    const int32_t cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
-    const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
-    const int32_t x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
-    const int32_t x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
-    const int32_t y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
-    const int32_t y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
-    const int32_t z0 = max(cz - 1, axis_cell(pi.z - reach, g.lo[2], g.cell, g.nz));
-    const int32_t z1 = min(cz + 1, axis_cell(pi.z + reach, g.lo[2], g.cell, g.nz));
+    int32_t cx = 0, cy = 0, x0, x1, y0, y1, z0, z1;
+    if constexpr (SRC::kExactWindow) {
+        cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
+        cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
+        const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
+        x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
+        x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
+        y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
+        y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
+        z0 = max(cz - 1, axis_cell(pi.z - reach, g.lo[2], g.cell, g.nz));
+        z1 = min(cz + 1, axis_cell(pi.z + reach, g.lo[2], g.cell, g.nz));
+    } else {
+        const float ic = 1.0f / g.cell;
+        axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
+        axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
+        axis_window(pi.z, reach, g.lo[2], ic, g.nz, z0, z1);
+    }
     for (int32_t X = x0; X <= x1; ++X) {
         for (int32_t Y = y0; Y <= y1; ++Y) {
             const uint32_t col = g.base + (uint32_t)((X * g.ny + Y) * g.nz);
