@@ -597,7 +597,12 @@ def main():
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--no-drum", action="store_true")
     ap.add_argument("--only-drum", action="store_true", help="run only the rotating-drum section")
+    ap.add_argument("--z-div", type=int, default=None,
+                    help="z cells per cell edge for every engine (default: the library's automatic choice)")
     args = ap.parse_args()
+    if args.z_div is not None:
+        from stardust_gb300 import _abi
+        _abi.tune_set("z_div", args.z_div)
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3

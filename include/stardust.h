@@ -114,8 +114,11 @@ typedef enum sd_field {
 } sd_field;
 
 /* Derived step parameters (box, grid, contact-law constants).  Cell key of
- * a position: ix = clamp(trunc((x - lo[0]) / cell), 0, nx-1) (same for y, z),
- * key = (ix*ny + iy)*nz + iz.  Normal damping gamma_n = damp * sqrt(m_eff). */
+ * a position: ix = clamp(trunc((x - lo[0]) / cell), 0, nx-1) (same for y),
+ * iz = clamp(trunc((z - lo[2]) / cell_z), 0, nz-1), key = (ix*ny + iy)*nz + iz.
+ * cell_z = cell / z_div: the z axis is split z_div times finer than x and y
+ * (knob "z_div"), which shortens the candidate range of each neighbour
+ * column.  Normal damping gamma_n = damp * sqrt(m_eff). */
 typedef struct sd_params {
     float lo[3], hi[3];
     float cell;
@@ -125,6 +128,8 @@ typedef struct sd_params {
     float dt;        /* dt of the captured step graph (0 before the first step) */
     int32_t walls;
     float rmax;      /* largest sphere radius */
+    float cell_z;    /* z edge of a cell: cell / z_div */
+    int32_t z_div;   /* z cells per cell edge (1 for a batch of scenes) */
 } sd_params;
 
 typedef struct sd_engine sd_engine;
@@ -392,7 +397,10 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *   "contact_mode"  0 = one thread per sphere, candidates read through L1 (default);
  *                   1 = one CTA per grid column, neighbour columns staged in shared
  *                       memory by TMA bulk copies
- *   "sort_items"    keys per thread of the sort's digit pass: 8 or 16 (default) */
+ *   "sort_items"    keys per thread of the sort's digit pass: 8 or 16 (default)
+ *   "z_div"         z cells per cell edge for engines prepared afterwards: 1, 2, 4 or 8,
+ *                   or 0 (default) = the largest of 4, 2, 1 that keeps keys within
+ *                   20 bits and the sort's pass count; a batch of scenes always uses 1 */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

@@ -22,6 +22,7 @@ class Params(C.Structure):
         ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
         ("kn", C.c_float), ("damp", C.c_float), ("mu", C.c_float),
         ("g", C.c_float * 3), ("dt", C.c_float), ("walls", C.c_int32),
+        ("cell_z", C.c_float),
     ]
 
 
@@ -129,6 +130,7 @@ def params_from_engine(ep: dict, dt: float) -> Params:
         p.hi[a] = ep["hi"][a]
         p.g[a] = ep["gravity"][a]
     p.cell = ep["cell"]
+    p.cell_z = ep.get("cell_z", 0.0)
     p.nx, p.ny, p.nz = ep["dims"]
     p.kn = ep["kn"]
     p.damp = ep["damp"]

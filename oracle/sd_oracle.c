@@ -439,10 +439,13 @@ static inline int32_t axis_cell(float x, float lo, float cell, int32_t n) {
     return (int32_t)t;
 }
 
+/* z cell edge: the engine splits z z_div times finer than x and y */
+static inline float cell_z_of(const sdo_params* p) { return p->cell_z > 0.0f ? p->cell_z : p->cell; }
+
 uint32_t sdo_cell_key(const sdo_params* p, float x, float y, float z) {
     int32_t ix = axis_cell(x, p->lo[0], p->cell, p->nx);
     int32_t iy = axis_cell(y, p->lo[1], p->cell, p->ny);
-    int32_t iz = axis_cell(z, p->lo[2], p->cell, p->nz);
+    int32_t iz = axis_cell(z, p->lo[2], cell_z_of(p), p->nz);
     return (uint32_t)((ix * p->ny + iy) * p->nz + iz);
 }
 
@@ -636,8 +639,9 @@ static uint64_t contact_integrate##SUFFIX(const sdo_params* p, uint32_t n,      
         const int clump_i = body_of && (idb & 0x80000000u);                                  \
         int32_t cx = axis_cell((float)xi, p->lo[0], p->cell, p->nx);                         \
         int32_t cy = axis_cell((float)yi, p->lo[1], p->cell, p->ny);                         \
-        int32_t cz = axis_cell((float)zi, p->lo[2], p->cell, p->nz);                         \
-        int32_t z0 = cz > 0 ? cz - 1 : 0, z1 = cz + 1 < p->nz ? cz + 1 : p->nz - 1;          \
+        /* z cells of every centre within one cell edge (r_i + r_j <= cell), padded */     \
+        int32_t z0 = axis_cell((float)zi - p->cell * 1.00001f, p->lo[2], cell_z_of(p), p->nz); \
+        int32_t z1 = axis_cell((float)zi + p->cell * 1.00001f, p->lo[2], cell_z_of(p), p->nz); \
         for (int32_t ddx = -1; ddx <= 1; ++ddx) {                                            \
             int32_t X = cx + ddx;                                                            \
             if (X < 0 || X >= p->nx) continue;                                               \
@@ -757,8 +761,8 @@ uint64_t sdo_contact_pairs(const sdo_params* p, uint32_t n, const float* pos,
         memcpy(&idi, omg + 4 * (size_t)i + 3, 4);
         int32_t cx = axis_cell(pi[0], p->lo[0], p->cell, p->nx);
         int32_t cy = axis_cell(pi[1], p->lo[1], p->cell, p->ny);
-        int32_t cz = axis_cell(pi[2], p->lo[2], p->cell, p->nz);
-        int32_t z0 = cz > 0 ? cz - 1 : 0, z1 = cz + 1 < p->nz ? cz + 1 : p->nz - 1;
+        int32_t z0 = axis_cell(pi[2] - p->cell * 1.00001f, p->lo[2], cell_z_of(p), p->nz);
+        int32_t z1 = axis_cell(pi[2] + p->cell * 1.00001f, p->lo[2], cell_z_of(p), p->nz);
         for (int32_t ddx = -1; ddx <= 1; ++ddx) {
             int32_t X = cx + ddx;
             if (X < 0 || X >= p->nx) continue;

@@ -102,13 +102,15 @@ void sdo_ref_advect(int n_bodies, float dt, const float* body_mass, const float*
 typedef struct sdo_params {
     float lo[3], hi[3];     /* box; walls on the six faces when walls != 0 */
     float cell;             /* grid cell edge */
-    int32_t nx, ny, nz;     /* grid dims; cell key = (ix*ny + iy)*nz + iz */
+    int32_t nx, ny, nz;     /* grid dims (nz counts z cells of cell_z); key = (ix*ny + iy)*nz + iz */
     float kn;               /* normal stiffness, N/m */
     float damp;             /* 2*beta*sqrt(kn); gamma_n = damp*sqrt(m_eff) */
     float mu;               /* Coulomb coefficient */
     float g[3];             /* gravity */
     float dt;
     int32_t walls;          /* bit a*2+s: wall on axis a, side s (0 low, 1 high) */
+    float cell_z;           /* z cell edge (cell / z_div of the engine); 0 = cell.
+                               iz = clamp(trunc((z - lo[2]) / cell_z), 0, nz-1) */
 } sdo_params;
 
 /* Cell key of a position (clamped into the grid). */

@@ -110,7 +110,7 @@ class SdParams(C.Structure):
         ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
         ("kn", C.c_float), ("damp", C.c_float), ("mu", C.c_float),
         ("gravity", C.c_float * 3), ("dt", C.c_float), ("walls", C.c_int32),
-        ("rmax", C.c_float),
+        ("rmax", C.c_float), ("cell_z", C.c_float), ("z_div", C.c_int32),
     ]
 
 

@@ -68,7 +68,8 @@ __device__ __forceinline__ void axis_window(float x, float reach, float lo, floa
 // batch (keys offset by the scene's base).
 struct Grid {
     float lo[3], hi[3];
-    float cell;
+    float cell;   // x and y cell edge
+    float cellz;  // z cell edge (cell / z_div)
     int32_t nx, ny, nz;
     uint32_t base;
 };
@@ -81,6 +82,7 @@ __device__ __forceinline__ Grid grid_of(const DemParams& p) {
         g.hi[a] = p.hi[a];
     }
     g.cell = p.cell;
+    g.cellz = p.cell_z;
     g.nx = p.nx;
     g.ny = p.ny;
     g.nz = p.nz;
@@ -105,6 +107,7 @@ __device__ __forceinline__ Grid grid_of_slot(const SceneGrid* __restrict__ scene
         g.hi[k] = __ldg(&sg->hi[k]);
     }
     g.cell = __ldg(&sg->cell);
+    g.cellz = g.cell;  // scenes of a batch keep z_div 1
     g.nx = __ldg(&sg->nx);
     g.ny = __ldg(&sg->ny);
     g.nz = __ldg(&sg->nz);
@@ -115,7 +118,7 @@ __device__ __forceinline__ Grid grid_of_slot(const SceneGrid* __restrict__ scene
 __device__ __forceinline__ uint32_t cell_key_g(const Grid& g, float x, float y, float z) {
     int32_t ix = axis_cell(x, g.lo[0], g.cell, g.nx);
     int32_t iy = axis_cell(y, g.lo[1], g.cell, g.ny);
-    int32_t iz = axis_cell(z, g.lo[2], g.cell, g.nz);
+    int32_t iz = axis_cell(z, g.lo[2], g.cellz, g.nz);
     return g.base + (uint32_t)((ix * g.ny + iy) * g.nz + iz);
 }
 
@@ -128,7 +131,7 @@ struct Batch {
 __device__ __forceinline__ uint32_t cell_key(const DemParams& p, float x, float y, float z) {
     int32_t ix = axis_cell(x, p.lo[0], p.cell, p.nx);
     int32_t iy = axis_cell(y, p.lo[1], p.cell, p.ny);
-    int32_t iz = axis_cell(z, p.lo[2], p.cell, p.nz);
+    int32_t iz = axis_cell(z, p.lo[2], p.cell_z, p.nz);
     return (uint32_t)((ix * p.ny + iy) * p.nz + iz);
 }
 
@@ -367,18 +370,17 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     if constexpr (SRC::kExactWindow) {
         cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
         cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
-        const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
         x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
         x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
         y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
         y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
-        z0 = max(cz - 1, axis_cell(pi.z - reach, g.lo[2], g.cell, g.nz));
-        z1 = min(cz + 1, axis_cell(pi.z + reach, g.lo[2], g.cell, g.nz));
+        z0 = axis_cell(pi.z - reach, g.lo[2], g.cellz, g.nz);
+        z1 = axis_cell(pi.z + reach, g.lo[2], g.cellz, g.nz);
     } else {
         const float ic = 1.0f / g.cell;
         axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
         axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
-        axis_window(pi.z, reach, g.lo[2], ic, g.nz, z0, z1);
+        axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
     }
     for (int32_t X = x0; X <= x1; ++X) {
         for (int32_t Y = y0; Y <= y1; ++Y) {
@@ -474,33 +476,40 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
 constexpr int kFusedPasses = 3;
 
 static uint32_t pack_hist_spec(const SortPlan& plan) {
-    uint32_t v = (uint32_t)plan.passes & 3u;
+    uint32_t v = ((uint32_t)plan.passes & 3u) | (plan.stride == 1024 ? 1u << 29 : 0u);
     for (int q = 0; q < plan.passes && q < kFusedPasses; ++q)
         v |= ((uint32_t)plan.shift[q] & 31u) << (2 + 9 * q) | ((uint32_t)plan.bits[q] & 15u) << (7 + 9 * q);
     return v;
 }
 
+// Words of a block's shared digit histograms: pass q at q * stride (3 x 512
+// or 2 x 1024), the layout of the sort's global histograms.
+constexpr int kHistWords = 2048;
+__device__ __forceinline__ uint32_t spec_stride(uint32_t spec) { return (spec >> 29) & 1u ? 1024u : 512u; }
+
 // Adds the warp's keys to the block's shared digit histograms (all lanes
 // of the warp must call; `valid` marks lanes that hold a key).
-__device__ __forceinline__ void hist_add(uint32_t (*s_hist)[512], uint32_t spec, uint32_t key, bool valid) {
+__device__ __forceinline__ void hist_add(uint32_t* s_hist, uint32_t spec, uint32_t key, bool valid) {
     const int passes = (int)(spec & 3u);
+    const uint32_t stride = spec_stride(spec);
 #pragma unroll
     for (int q = 0; q < kFusedPasses; ++q) {
         if (q >= passes) break;
         const uint32_t shift = (spec >> (2 + 9 * q)) & 31u, bits = (spec >> (7 + 9 * q)) & 15u;
         const uint32_t d = (key >> shift) & ((1u << bits) - 1u);
         const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
-        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[q][d], __popc(peers));
+        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[q * stride + d], __popc(peers));
     }
 }
 
 // Block's histograms to the global ones: one atomic per non-empty bin.
-__device__ __forceinline__ void hist_flush(uint32_t (*s_hist)[512], uint32_t spec, uint32_t* ghist) {
+__device__ __forceinline__ void hist_flush(const uint32_t* s_hist, uint32_t spec, uint32_t* ghist) {
     const int passes = (int)(spec & 3u);
+    const uint32_t stride = spec_stride(spec);
     for (int q = 0; q < passes; ++q) {
         const uint32_t bits = (spec >> (7 + 9 * q)) & 15u;
         for (uint32_t d = threadIdx.x; d < (1u << bits); d += blockDim.x)
-            if (s_hist[q][d]) atomicAdd(&ghist[q * 512 + d], s_hist[q][d]);
+            if (s_hist[q * stride + d]) atomicAdd(&ghist[q * stride + d], s_hist[q * stride + d]);
     }
 }
 
@@ -522,7 +531,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
                              ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{}) {
-    __shared__ uint32_t s_hist[kFusedPasses][512];
+    __shared__ uint32_t s_hist[kHistWords];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
@@ -532,7 +541,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                                                                           force, torque, contacts, cc, &has_key, bt,
                                                                           &mesh);
     if (ghist) {
-        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+        for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
         hist_add(s_hist, hist_spec, key, has_key);
         __syncthreads();
@@ -602,7 +611,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
                           uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
                           ClumpCtx cc) {
     extern __shared__ __align__(128) float4 s_tile[];
-    __shared__ uint32_t s_hist[kFusedPasses][512];
+    __shared__ uint32_t s_hist[kHistWords];
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ uint32_t s_beg[9], s_cnt[9], s_shift[9], s_total;
 
@@ -620,7 +629,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
         s_cnt[threadIdx.x] = c;
     }
     if (ghist)
-        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+        for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t off = 0;
@@ -708,7 +717,7 @@ __device__ __forceinline__ void body_step(
     const float4* __restrict__ omg, const float4* __restrict__ sf, const float4* __restrict__ st,
     float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n, uint32_t hist_spec,
-    uint32_t (*s_hist)[512]) {
+    uint32_t* s_hist) {
     const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
     const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
     const uint32_t first = bfirst[b], cnt = bcount[b];
@@ -776,9 +785,10 @@ __device__ __forceinline__ void body_step(
         vals[s] = s;
         if (s_hist) {
             const int passes = (int)(hist_spec & 3u);
+            const uint32_t stride = spec_stride(hist_spec);
             for (int q = 0; q < passes; ++q) {
                 const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
-                atomicAdd(&s_hist[q][(key >> shift) & ((1u << bits) - 1u)], 1u);
+                atomicAdd(&s_hist[q * stride + ((key >> shift) & ((1u << bits) - 1u))], 1u);
             }
         }
     }
@@ -802,9 +812,9 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
                 const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
                 float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
                 uint32_t hist_spec, uint32_t* __restrict__ ghist) {
-    __shared__ uint32_t s_hist[kFusedPasses][512];
+    __shared__ uint32_t s_hist[kHistWords];
     if (ghist) {
-        for (int q = threadIdx.x; q < kFusedPasses * 512; q += blockDim.x) (&s_hist[0][0])[q] = 0;
+        for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
     }
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -896,9 +906,11 @@ __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restri
     const int32_t bi = (body_of && (idbi & kClumpFlag)) ? body_of[idi] : -1;
     const int32_t cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
     const int32_t cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
-    const int32_t cz = axis_cell(pi.z, g.lo[2], g.cell, g.nz);
-    const int32_t z0 = cz > 0 ? cz - 1 : 0;
-    const int32_t z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
+    // every partner centre is within one cell edge (a contact needs
+    // |dz| < r_i + r_j <= cell); truncation of the rounded quotient is
+    // monotone, so these z cells contain all of them
+    const int32_t z0 = axis_cell(pi.z - g.cell * 1.00001f, g.lo[2], g.cellz, g.nz);
+    const int32_t z1 = axis_cell(pi.z + g.cell * 1.00001f, g.lo[2], g.cellz, g.nz);
     for (int32_t ddx = -1; ddx <= 1; ++ddx) {
         const int32_t X = cx + ddx;
         if (X < 0 || X >= g.nx) continue;

@@ -17,6 +17,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <fstream>
 #include <mutex>
@@ -124,6 +125,27 @@ static sd_status grid_dims(sd_engine* h, const float* lo, const float* hi, float
     return SD_OK;
 }
 
+// z cells per cell edge (knob "z_div"; 0 = automatic): automatically the
+// largest of 4, 2, 1 whose finer grid keeps keys within 20 bits and sorts in
+// as many passes as the plain one (a 50 x 50 x 100 grid: 18-bit keys ->
+// 20-bit keys, 2 passes either way).  Larger grids keep z_div 1: a wider
+// digit pass and a 4x larger cell table cost more there than the shorter
+// candidate ranges save (measured on the 2.1M-sphere drum).
+static int32_t g_z_div = 0;
+static int key_bits_of(uint64_t ncells) {
+    int b = 1;
+    while (b < 32 && (1ull << b) < ncells) ++b;
+    return b;
+}
+static int32_t z_div_for(uint64_t ncells) {
+    if (g_z_div > 0) return ncells * (uint64_t)g_z_div <= (1ull << 30) ? g_z_div : 1;
+    const int p0 = sd::sort_num_passes(key_bits_of(ncells));
+    for (int32_t d : {4, 2})
+        if (key_bits_of(ncells * (uint64_t)d) <= 20 && sd::sort_num_passes(key_bits_of(ncells * (uint64_t)d)) == p0)
+            return d;
+    return 1;
+}
+
 // A batch: per scene its grid (cell = given or 2 x its largest radius) at
 // consecutive key ranges, and its slot range.
 static sd_status derive_batch(sd_engine* h) {
@@ -184,6 +206,8 @@ sd_status derive_params(sd_engine* h) {
         P.nx = g0.nx;
         P.ny = g0.ny;
         P.nz = g0.nz;
+        P.cell_z = g0.cell;
+        P.z_div = 1;
     } else {
         bool box_given = c.box_hi[0] != 0.f || c.box_hi[1] != 0.f || c.box_hi[2] != 0.f;
         const bool one_scene = h->scenes.size() == 1;
@@ -205,8 +229,11 @@ sd_status derive_params(sd_engine* h) {
         if (s) return s;
         P.nx = dims[0];
         P.ny = dims[1];
-        P.nz = dims[2];
         if (ncells > (1ull << 30)) return fail(h, SD_ERR_INVALID_ARG, "grid has more than 2^30 cells");
+        const int32_t zd = h->z_div_fixed > 0 ? h->z_div_fixed : z_div_for(ncells);
+        P.nz = dims[2] * zd;
+        P.z_div = zd;
+        P.cell_z = cell / (float)zd;
     }
     if (!(c.restitution > 0.0f && c.restitution <= 1.0f))
         return fail(h, SD_ERR_INVALID_ARG, "restitution must be in (0, 1]");
@@ -999,6 +1026,10 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
     } else if (k == "sort_items") {
         if (value != 8 && value != 16) return fail(nullptr, SD_ERR_INVALID_ARG, "sort_items must be 8 or 16");
         sd::sort_set_items(value);
+    } else if (k == "z_div") {
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+            return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
+        g_z_div = value;
     } else {
         return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     }
@@ -1011,6 +1042,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     std::string k(knob);
     if (k == "contact_mode") *value = sd::dem_contact_mode();
     else if (k == "sort_items") *value = sd::sort_items();
+    else if (k == "z_div") *value = g_z_div;
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }
@@ -1185,8 +1217,12 @@ sd_status sd_engine_get_pairs(sd_engine* h, uint64_t* dst, uint64_t cap, uint64_
 
 sd_status sd_engine_params(sd_engine* h, sd_params* out) {
     if (!h || !out) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
-    sd_status s = derive_params(h);
-    if (s) return s;
+    // a prepared engine reports the parameters its buffers were sized for
+    // (a later "z_div" knob change applies to engines prepared after it)
+    if (!h->prepared) {
+        sd_status s = derive_params(h);
+        if (s) return s;
+    }
     static_assert(sizeof(sd_params) == sizeof(sd::DemParams), "sd_params mirrors DemParams");
     std::memcpy(out, &h->P, sizeof(sd_params));
     out->dt = h->graph_valid ? h->graph_dt : 0.0f;
@@ -1277,7 +1313,7 @@ sd_status sd_engine_save_checkpoint(sd_engine* h, const char* path) {
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     std::ofstream f(path, std::ios::binary);
     if (!f) return fail(h, SD_ERR_IO, std::string("cannot write ") + path);
-    uint32_t ver = 2;
+    uint32_t ver = 3;  // 3: DemParams carries cell_z and z_div
     f.write(kCkptMagic, 8);
     f.write(reinterpret_cast<const char*>(&ver), 4);
     f.write(reinterpret_cast<const char*>(&n), 4);
@@ -1314,9 +1350,15 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
     f.read(reinterpret_cast<char*>(&n), 4);
     f.read(reinterpret_cast<char*>(&steps), 8);
     f.read(reinterpret_cast<char*>(&cfg), sizeof cfg);
-    f.read(reinterpret_cast<char*>(&P), sizeof P);
-    if (!f || std::memcmp(magic, kCkptMagic, 8) != 0 || (ver != 1 && ver != 2))
+    if (!f || std::memcmp(magic, kCkptMagic, 8) != 0 || ver < 1 || ver > 3)
         return fail(h, SD_ERR_IO, "not a stardust-gb300 checkpoint");
+    // versions 1 and 2 end the parameters at rmax and were written with z_div 1
+    f.read(reinterpret_cast<char*>(&P), ver >= 3 ? sizeof P : offsetof(sd::DemParams, cell_z));
+    if (ver < 3) {
+        P.cell_z = P.cell;
+        P.z_div = 1;
+    }
+    if (!f || P.z_div < 1 || P.z_div > 8) return fail(h, SD_ERR_IO, "truncated or corrupt checkpoint (grid)");
     std::vector<float4> buf(3 * (size_t)n);
     f.read(reinterpret_cast<char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(float4)));
     if (!f) return fail(h, SD_ERR_IO, "truncated checkpoint");
@@ -1371,12 +1413,14 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path) {
         h->h_vel[id] = buf[n + s];
         h->h_omg[id] = buf[2 * (size_t)n + s];
     }
-    // upload in the saved (sorted) slot order: a stable re-sort of a sorted
-    // state is the identity, so slot order -- and with it every summation
-    // order -- is exactly that of the run that wrote the checkpoint
+    // upload in the saved (sorted) slot order, on the saved grid: a stable
+    // re-sort of a sorted state is the identity, so slot order -- and with
+    // it every summation order -- is exactly that of the run that wrote the
+    // checkpoint
+    h->z_div_fixed = P.z_div;
     sd_status s = prepare_with(h, buf.data(), buf.data() + n, buf.data() + 2 * (size_t)n, n);
     if (s) return s;
-    if (std::memcmp(&P.cell, &h->P.cell, sizeof(float)) != 0)
+    if (std::memcmp(&P.cell, &h->P.cell, sizeof(float)) != 0 || P.nz != h->P.nz)
         return fail(h, SD_ERR_STATE, "checkpoint grid differs from the derived grid");
     h->steps = steps;
     return SD_OK;

@@ -68,6 +68,7 @@ struct sd_engine {
     } mesh;
 
     bool prepared = false;
+    int32_t z_div_fixed = 0;  // z cells per cell edge taken from a checkpoint (0: the "z_div" knob)
     int device = 0;
     cudaStream_t stream = nullptr;
     sd::DemParams P{};

@@ -26,13 +26,15 @@ struct SortPlan {
     int passes;
     int shift[4];
     int bits[4];
+    int stride;  // words per pass of the digit histograms and per tile of the look-back status: 512, or 1024
+                 // when a digit is 10 bits wide (19- and 20-bit keys, sorted in two passes)
 };
 SortPlan sort_plan(int key_bits);
 uint64_t sort_scratch_words(uint64_t n, int key_bits);
 int sort_num_passes(int key_bits);
 void sort_set_items(int items);
 int sort_items();
-uint32_t* sort_hist_ptr(uint32_t* scratch);  // [4][512] global digit histograms
+uint32_t* sort_hist_ptr(uint32_t* scratch);  // global digit histograms, pass q at q * plan.stride (2048 words)
 cudaError_t sort_clear_async(uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st);
 cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPlan& plan, uint32_t* scratch,
                                  cudaStream_t st);
@@ -168,6 +170,11 @@ struct DemParams {
     float dt;
     int32_t walls;
     float rmax;  // largest sphere radius: bounds every contact partner's reach
+    // z cells are `cell / z_div` high (nz counts them): a finer z split
+    // shortens each neighbour column's candidate range without adding
+    // columns; cell keys stay (ix*ny + iy)*nz + iz
+    float cell_z;
+    int32_t z_div;
 };
 
 // One scene of a batch: its box and grid, the first global cell key of its

@@ -16,8 +16,10 @@
 //      over the predecessors' published counts, stages the tile in shared
 //      memory in digit order and writes it out in coalesced runs.
 //
-// Digits are up to 9 bits wide: a key range of `key_bits` bits takes
-// ceil(key_bits / 9) passes (18-bit cell keys: 2 passes; 32-bit: 4 of 8).
+// Digits are up to 9 bits wide -- a key range of `key_bits` bits takes
+// ceil(key_bits / 9) passes (18-bit cell keys: 2 passes; 32-bit: 4 of 8) --
+// except 19- and 20-bit keys, which take 2 passes of 10-bit digits (1024
+// bins) rather than 3.
 // Look-back waits are bounded (kSpinLimit) and report through the status
 // word instead of hanging.
 #include <cuda_runtime.h>
@@ -38,9 +40,10 @@ constexpr int kLookback = 8;  // predecessor statuses read per look-back round t
 // Scratch layout (u32 words):
 //   [0]                 status word (error bits; never cleared by the sort)
 //   [4 .. 8)            per-pass tile counters
-//   [16 .. 16+4*512)    per-pass global digit histograms
-//   [kStatusOff ..)     per-pass tile status [pass][tile][512] (only the
-//                       pass's digit bins are used)
+//   [16 .. 16+2048)     per-pass global digit histograms, pass q at
+//                       q * stride (4 x 512, or 2 x 1024)
+//   [kStatusOff ..)     per-pass tile status [pass][tile][stride] (only
+//                       the pass's digit bins are used)
 constexpr uint64_t kHistOff = 16;
 constexpr uint64_t kStatusOff = kHistOff + 4 * 512;
 
@@ -48,13 +51,14 @@ SortPlan sort_plan(int key_bits) {
     SortPlan p{};
     if (key_bits < 1) key_bits = 1;
     if (key_bits > 32) key_bits = 32;
-    p.passes = (key_bits + 8) / 9;
+    p.passes = (key_bits == 19 || key_bits == 20) ? 2 : (key_bits + 8) / 9;
     int base = key_bits / p.passes, extra = key_bits % p.passes, sh = 0;
     for (int i = 0; i < p.passes; ++i) {
         p.bits[i] = base + (i < extra ? 1 : 0);
         p.shift[i] = sh;
         sh += p.bits[i];
     }
+    p.stride = p.bits[0] > 9 ? 1024 : 512;
     return p;
 }
 
@@ -65,8 +69,8 @@ constexpr uint32_t tile_keys() { return kSortThreads * ITEMS; }
 __global__ void __launch_bounds__(kSortThreads)
 sort_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan plan,
                       uint32_t* __restrict__ scratch) {
-    __shared__ uint32_t hist[4][512];
-    for (int i = threadIdx.x; i < 4 * 512; i += blockDim.x) (&hist[0][0])[i] = 0;
+    __shared__ uint32_t hist[2048];  // pass p at p * plan.stride
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -79,27 +83,29 @@ sort_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan pl
             if (p >= plan.passes) break;
             uint32_t d = (k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1u);
             uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
-            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&hist[p][d], __popc(peers & active));
+            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&hist[p * plan.stride + d], __popc(peers & active));
         }
     }
     __syncthreads();
     for (int p = 0; p < plan.passes; ++p) {
         uint32_t nb = 1u << plan.bits[p];
         for (uint32_t d = threadIdx.x; d < nb; d += blockDim.x)
-            if (hist[p][d]) atomicAdd(&scratch[kHistOff + p * 512 + d], hist[p][d]);
+            if (hist[p * plan.stride + d]) atomicAdd(&scratch[kHistOff + p * plan.stride + d], hist[p * plan.stride + d]);
     }
 }
 
 // ------------------------------------------------------------ onesweep pass
-// BINS: 256 or 512 digit bins (template so the 8-bit passes do half the
+// BINS: 256, 512 or 1024 digit bins (template so narrow passes do less
 // per-digit work).  ITEMS: keys per thread (tile = 256 * ITEMS keys).
+// stride: the plan's histogram and status stride.
 template <int BINS, int ITEMS>
 __global__ void __launch_bounds__(kSortThreads)
 sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                  uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
-                 int shift, int bits, int pass, uint32_t num_tiles, uint32_t* __restrict__ scratch) {
+                 int shift, int bits, int pass, uint32_t num_tiles, uint32_t stride,
+                 uint32_t* __restrict__ scratch) {
     constexpr int TILE = kSortThreads * ITEMS;
-    constexpr int DPT = BINS / kSortThreads;  // digits per thread (1 or 2)
+    constexpr int DPT = BINS / kSortThreads;  // digits per thread (1, 2 or 4)
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* s_keys = smem;                            // TILE
     uint32_t* s_vals = s_keys + TILE;                   // TILE
@@ -153,7 +159,7 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
     }
     // publish this tile's aggregate before anything else so successors can
     // make progress
-    uint32_t* status = scratch + kStatusOff + ((uint64_t)pass * num_tiles + tile) * 512;
+    uint32_t* status = scratch + kStatusOff + ((uint64_t)pass * num_tiles + tile) * stride;
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
         uint32_t d = threadIdx.x + q * kSortThreads;
@@ -162,7 +168,7 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
 
     // tile-local digit starts and global digit starts (exclusive scans over
     // digits; digit d = threadIdx.x + q*256)
-    const uint32_t* ghist = scratch + kHistOff + pass * 512;
+    const uint32_t* ghist = scratch + kHistOff + pass * stride;
     uint32_t carry_t = 0, carry_g = 0;
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
@@ -185,14 +191,14 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
         const uint32_t d = threadIdx.x + q * kSortThreads;
         uint32_t excl = 0;
         if (tile > 0) {
-            const uint32_t* pass_status = scratch + kStatusOff + (uint64_t)pass * num_tiles * 512 + d;
+            const uint32_t* pass_status = scratch + kStatusOff + (uint64_t)pass * num_tiles * stride + d;
             int64_t p = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (true) {
                 uint32_t v[kLookback];
 #pragma unroll
                 for (int w = 0; w < kLookback; ++w)
-                    v[w] = p - w >= 0 ? ld_relaxed(pass_status + (uint64_t)(p - w) * 512) : kFlagInc;
+                    v[w] = p - w >= 0 ? ld_relaxed(pass_status + (uint64_t)(p - w) * stride) : kFlagInc;
                 bool done = false;
                 int used = 0;
 #pragma unroll
@@ -266,7 +272,7 @@ uint64_t sort_scratch_words(uint64_t n, int key_bits) {
     SortPlan p = sort_plan(key_bits);
     uint64_t tiles = (n + tile_keys<kSortItemsMin>() - 1) / tile_keys<kSortItemsMin>();
     if (tiles == 0) tiles = 1;
-    return kStatusOff + (uint64_t)p.passes * tiles * 512;
+    return kStatusOff + (uint64_t)p.passes * tiles * (uint64_t)p.stride;
 }
 
 uint32_t* sort_hist_ptr(uint32_t* scratch) { return scratch + kHistOff; }
@@ -278,7 +284,7 @@ static uint32_t num_tiles(uint32_t n) {
 
 cudaError_t sort_clear_async(uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st) {
     // counters, histograms and this sort's tile status; not the status word
-    size_t clear_words = kStatusOff - 4 + (size_t)plan.passes * num_tiles(n) * 512;
+    size_t clear_words = kStatusOff - 4 + (size_t)plan.passes * num_tiles(n) * (size_t)plan.stride;
     return cudaMemsetAsync(scratch + 4, 0, clear_words * sizeof(uint32_t), st);
 }
 
@@ -293,7 +299,7 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
 
 template <int BINS, int ITEMS>
 static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t* ko, uint32_t* vo,
-                               uint32_t n, int shift, int bits, int pass, uint32_t tiles,
+                               uint32_t n, int shift, int bits, int pass, uint32_t tiles, uint32_t stride,
                                uint32_t* scratch, cudaStream_t st) {
     size_t sm = pass_smem_bytes<BINS, ITEMS>();
     if (sm > 48 * 1024) {
@@ -302,7 +308,7 @@ static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t*
         if (e != cudaSuccess) return e;
     }
     sort_pass_kernel<BINS, ITEMS><<<tiles, kSortThreads, sm, st>>>(ki, vi, ko, vo, n, shift, bits,
-                                                                   pass, tiles, scratch);
+                                                                   pass, tiles, stride, scratch);
     return cudaGetLastError();
 }
 
@@ -317,13 +323,16 @@ cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp
     uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
     for (int p = 0; p < plan.passes; ++p) {
         cudaError_t e;
-        const bool wide = plan.bits[p] > 8;
+        const int b = plan.bits[p], sh = plan.shift[p];
+        const uint32_t sd = (uint32_t)plan.stride;
         if (g_sort_items >= 16)
-            e = wide ? launch_pass<512, 16>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st)
-                     : launch_pass<256, 16>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+            e = b > 9   ? launch_pass<1024, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
+                : b > 8 ? launch_pass<512, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
+                        : launch_pass<256, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st);
         else
-            e = wide ? launch_pass<512, 8>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st)
-                     : launch_pass<256, 8>(ki, vi, ko, vo, n, plan.shift[p], plan.bits[p], p, tiles, scratch, st);
+            e = b > 9   ? launch_pass<1024, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
+                : b > 8 ? launch_pass<512, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
+                        : launch_pass<256, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st);
         if (e != cudaSuccess) return e;
         uint32_t* t;
         t = ki; ki = ko; ko = t;

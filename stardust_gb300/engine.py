@@ -321,7 +321,7 @@ class DEMEngine:
         self._call("sd_engine_params", C.byref(p))
         return {"lo": tuple(p.lo), "hi": tuple(p.hi), "cell": p.cell, "dims": (p.nx, p.ny, p.nz),
                 "kn": p.kn, "damp": p.damp, "mu": p.mu, "gravity": tuple(p.gravity), "dt": p.dt,
-                "walls": p.walls, "rmax": p.rmax}
+                "walls": p.walls, "rmax": p.rmax, "cell_z": p.cell_z, "z_div": p.z_div}
 
     def save_checkpoint(self, path: str) -> None:
         self._call("sd_engine_save_checkpoint", str(path).encode())

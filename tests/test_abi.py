@@ -97,8 +97,9 @@ def test_params_derivation(sdlib):
     eng = sdlib.DEMEngine(cfg)
     eng.add_spheres(pos, vel)
     p = eng.params()
-    assert p["dims"] == (32, 32, 32)
-    assert p["cell"] == pytest.approx(0.02)
+    # 32^3 cells, z split 4x finer: 17-bit keys still sort in 2 passes
+    assert p["z_div"] == 4 and p["dims"] == (32, 32, 128)
+    assert p["cell"] == pytest.approx(0.02) and p["cell_z"] == pytest.approx(0.005)
     # gamma_n = damp sqrt(m_eff); damp = 2 beta sqrt(kn), beta = -ln e / sqrt(pi^2 + ln^2 e)
     le = np.log(0.5)
     beta = -le / np.sqrt(np.pi ** 2 + le ** 2)
@@ -159,6 +160,33 @@ def test_scene_json_cube_entities(sdlib, tmp_path):
     e2.close()
 
 
+@pytest.mark.parametrize("knob, box, want", [
+    (0, (1.0, 1.0, 2.0), 4),    # 50 x 50 x 100: 18-bit keys -> 20-bit, 2 passes of 10-bit digits
+    (0, (1.4, 1.4, 1.4), 2),    # 70^3: 19 bits; x4 would need 21 bits and a third pass
+    (0, (5.0, 5.0, 5.0), 1),    # 250^3: 24-bit keys, no split (the wider passes cost more than they save)
+    (1, (1.0, 1.0, 2.0), 1),
+    (8, (1.0, 1.0, 2.0), 8),
+])
+def test_z_div_rule_and_knob(sdlib, knob, box, want):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("z_div")
+    try:
+        _abi.tune_set("z_div", knob)
+        cfg = sdlib.EngineConfig(box_lo=(0, 0, 0), box_hi=box, walls=0x3F, cell=0.02, kn=1e5, restitution=0.5,
+                                 mu=0.3, gravity=(0.0, 0.0, -9.81))
+        eng = sdlib.DEMEngine(cfg)
+        eng.add_spheres(np.array([[0.5, 0.5, 0.5, 0.01]], np.float32), np.array([[0, 0, 0, 1e-3]], np.float32))
+        p = eng.params()
+        nz = int(np.ceil(box[2] / np.float32(0.02) * (1 - 1e-6)))
+        assert p["z_div"] == want and p["dims"][2] == nz * want
+        assert p["cell_z"] == np.float32(np.float32(0.02) / np.float32(want))
+        eng.close()
+    finally:
+        _abi.tune_set("z_div", old)
+    with pytest.raises(Exception):
+        _abi.tune_set("z_div", 3)
+
+
 def test_scene_json_extensions_and_errors(sdlib, tmp_path):
     ok = {"scene": {"box": {"lo": [0, 0, 0], "hi": [1, 1, 2]}, "walls": 63, "cell": 0.05,
                     "material": {"kn": 2e5, "restitution": 0.8, "mu": 0.1},
@@ -168,7 +196,7 @@ def test_scene_json_extensions_and_errors(sdlib, tmp_path):
     eng = sdlib.DEMEngine()
     eng.load_scene_json(f)
     p = eng.params()
-    assert p["dims"] == (20, 20, 40) and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
+    assert p["dims"] == (20, 20, 160) and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
     eng.close()
     for bad, what in (({"scene": {"domain": 1, "colour": 3}}, "colour"),
                       ({"scene": {"entities": [{"type": "mesh", "position": [0, 0, 0], "size": 1, "mass": 1}]}}, "generic"),

@@ -71,6 +71,64 @@ def test_every_knob_setting_is_bit_exact(sdlib, orc, contact_mode, sort_items):
         _abi.tune_set("sort_items", old[1])
 
 
+@pytest.mark.parametrize("z_div", [1, 2, 8])
+def test_z_division_is_bit_exact(sdlib, orc, z_div):
+    """Splitting the z axis finer than x and y changes the slot order (and
+    with it the summation order the oracle follows) and the candidate
+    ranges, never the contact set: every split matches the oracle bit for
+    bit, pairs included."""
+    from stardust_gb300 import _abi, scenes
+    old = _abi.tune_get("z_div")
+    try:
+        _abi.tune_set("z_div", z_div)
+        n = 20_000
+        pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=scenes.scaled_box(n), seed=5)
+        pos = pos.copy()
+        pos[:, 3] *= 1.25
+        cfg.cell = float(2 * pos[:, 3].max())
+        eng = run_engine(sdlib, pos, vel, cfg, dt, 20)
+        assert eng.params()["z_div"] == z_div
+        p, (op, ov, ow) = oracle_state(orc, eng, pos, vel, dt, 20)
+        assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
+        assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))
+        assert np.array_equal(bits(eng.omegas())[:, :3], bits(orc.unsort(ow, ow))[:, :3])
+        sp, sv, sw, _, cs = orc.prepare(p, eng.positions(), eng.velocities(), orc.with_ids(eng.omegas(), np.arange(n)))
+        pairs = eng.pairs()
+        assert len(pairs) > n and np.array_equal(pairs, orc.contact_pairs(p, sp, sw, cs))
+        eng.close()
+    finally:
+        _abi.tune_set("z_div", old)
+
+
+def test_checkpoint_keeps_its_z_division(sdlib, tmp_path):
+    """A checkpoint written under one z split resumes bit-exactly under
+    another knob setting: the engine takes the saved split."""
+    from stardust_gb300 import _abi, scenes
+    old = _abi.tune_get("z_div")
+    try:
+        pos, vel, cfg, dt = scenes.box_lattice(n_side=12, seed=6)
+        _abi.tune_set("z_div", 4)
+        a = run_engine(sdlib, pos, vel, cfg, dt, 30, record=False)
+        ck = tmp_path / "ck.bin"
+        a.save_checkpoint(ck)
+        a.step(dt, 30)
+        a.sync()
+        ref = a.positions(), a.velocities()
+        _abi.tune_set("z_div", 1)
+        c = sdlib.DEMEngine(a.config)
+        c.add_spheres(pos, vel)
+        c.load_checkpoint(ck)
+        assert c.params()["z_div"] == 4
+        c.step(dt, 30)
+        c.sync()
+        assert np.array_equal(bits(ref[0]), bits(c.positions()))
+        assert np.array_equal(bits(ref[1]), bits(c.velocities()))
+        a.close()
+        c.close()
+    finally:
+        _abi.tune_set("z_div", old)
+
+
 def test_dense_pack_forces_torques_pairs(sdlib, orc):
     """A compressed, spinning polydisperse pack with many contacts: the forces
     and torques of the step, and the contact pair set, are bit-exact."""

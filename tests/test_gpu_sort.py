@@ -23,7 +23,7 @@ def run_sort(sd, keys, vals, key_bits):
 
 
 @pytest.mark.parametrize("n", [1, 2, 31, 2047, 2048, 2049, 100_000, 1_000_003])
-@pytest.mark.parametrize("key_bits", [18, 32])
+@pytest.mark.parametrize("key_bits", [18, 20, 32])
 def test_sort_random(sdlib, n, key_bits):
     rng = np.random.default_rng(n + key_bits)
     keys = rng.integers(0, 1 << key_bits, n, dtype=np.uint64).astype(np.uint32)
@@ -34,7 +34,7 @@ def test_sort_random(sdlib, n, key_bits):
     assert np.array_equal(v, vals[order])
 
 
-@pytest.mark.parametrize("key_bits", [1, 5, 8, 9, 10, 17, 25, 27])
+@pytest.mark.parametrize("key_bits", [1, 5, 8, 9, 10, 17, 19, 20, 21, 25, 27])
 def test_sort_key_widths(sdlib, key_bits):
     rng = np.random.default_rng(key_bits)
     n = 300_000
