@@ -399,8 +399,8 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                       memory by TMA bulk copies
  *   "sort_items"    keys per thread of the sort's digit pass: 8 or 16 (default)
  *   "z_div"         z cells per cell edge for engines prepared afterwards: 1, 2, 4 or 8,
- *                   or 0 (default) = the largest of 4, 2, 1 that keeps keys within
- *                   20 bits and the sort's pass count; a batch of scenes always uses 1 */
+ *                   or 0 (default) = 2 when that keeps keys within 20 bits and the
+ *                   sort's pass count, else 1; a batch of scenes always uses 1 */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

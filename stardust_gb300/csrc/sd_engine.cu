@@ -125,12 +125,13 @@ static sd_status grid_dims(sd_engine* h, const float* lo, const float* hi, float
     return SD_OK;
 }
 
-// z cells per cell edge (knob "z_div"; 0 = automatic): automatically the
-// largest of 4, 2, 1 whose finer grid keeps keys within 20 bits and sorts in
-// as many passes as the plain one (a 50 x 50 x 100 grid: 18-bit keys ->
-// 20-bit keys, 2 passes either way).  Larger grids keep z_div 1: a wider
-// digit pass and a 4x larger cell table cost more there than the shorter
-// candidate ranges save (measured on the 2.1M-sphere drum).
+// z cells per cell edge (knob "z_div"; 0 = automatic): automatically 2 when
+// the finer grid keeps keys within 20 bits and sorts in as many passes as
+// the plain one (a 50 x 50 x 100 grid: 18-bit keys -> 19 bits, 2 passes
+// either way), else 1.  Measured on 1,048,576 spheres, per step: z_div 1
+// 0.216 ms, 2 0.205 ms, 4 0.208 ms (the 10-bit digits of a 20-bit key cost
+// more than the shorter candidate ranges save); on the 2.1M-sphere drum
+// (23-bit keys) any split was slower.
 static int32_t g_z_div = 0;
 static int key_bits_of(uint64_t ncells) {
     int b = 1;
@@ -140,10 +141,8 @@ static int key_bits_of(uint64_t ncells) {
 static int32_t z_div_for(uint64_t ncells) {
     if (g_z_div > 0) return ncells * (uint64_t)g_z_div <= (1ull << 30) ? g_z_div : 1;
     const int p0 = sd::sort_num_passes(key_bits_of(ncells));
-    for (int32_t d : {4, 2})
-        if (key_bits_of(ncells * (uint64_t)d) <= 20 && sd::sort_num_passes(key_bits_of(ncells * (uint64_t)d)) == p0)
-            return d;
-    return 1;
+    const uint64_t n2 = ncells * 2;
+    return key_bits_of(n2) <= 20 && sd::sort_num_passes(key_bits_of(n2)) == p0 ? 2 : 1;
 }
 
 // A batch: per scene its grid (cell = given or 2 x its largest radius) at
