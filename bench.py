@@ -12,10 +12,10 @@ reorder + cell_start.  Timings:
   value      device time per step (CUDA events on the engine's stream, one
              event pair per step, the L2 flushed by a 256 MB write before
              every timed step), whole job over ranks;
-  e2e        the same steps through the public C ABI with host buffers:
-             per step, upload positions + velocities from pinned host memory
-             (sd_engine_set_state), step, read positions back
-             (sd_engine_get_state);
+  e2e        the same steps through the public C ABI with the state in
+             pinned host memory: per step, upload positions + velocities
+             (sd_engine_set_state), step, read positions + velocities back
+             into the same buffers (sd_engine_get_state);
   roofline   the dominant kernel (contact + integrate) timed alone on the
              same stream, its algorithmic bytes / duration against the
              measured HBM peak;
@@ -490,23 +490,32 @@ def run_ours(args, rank, world, local):
     achieved = n * CONTACT_BYTES_PER_SPHERE / (contact_ms * 1e-3) / 1e9
     traffic_ps = recorded_traffic()
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: the host owns the
+    # state; every step uploads positions and velocities from pinned memory,
+    # steps, and reads the new positions and velocities back into the same
+    # buffers (the next step's inputs)
     hpos = torch.from_numpy(eng.positions()).pin_memory()
     hvel = torch.from_numpy(eng.velocities()).pin_memory()
-    hout = torch.empty_like(hpos).pin_memory()
     import ctypes as C
     lib = _abi.lib()
     nbytes = hpos.numel() * 4
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+
+    def host_step():
         _abi.check(lib.sd_engine_set_state(eng._h, _abi.SD_FIELD_POSITION, C.c_void_p(hpos.data_ptr()), nbytes),
                    "set_state", eng._h)
         _abi.check(lib.sd_engine_set_state(eng._h, _abi.SD_FIELD_VELOCITY, C.c_void_p(hvel.data_ptr()), nbytes),
                    "set_state", eng._h)
         _abi.check(lib.sd_engine_step(eng._h, dt, 1), "step", eng._h)
-        _abi.check(lib.sd_engine_get_state(eng._h, _abi.SD_FIELD_POSITION, C.c_void_p(hout.data_ptr()), nbytes),
+        _abi.check(lib.sd_engine_get_state(eng._h, _abi.SD_FIELD_POSITION, C.c_void_p(hpos.data_ptr()), nbytes),
                    "get_state", eng._h)
+        _abi.check(lib.sd_engine_get_state(eng._h, _abi.SD_FIELD_VELOCITY, C.c_void_p(hvel.data_ptr()), nbytes),
+                   "get_state", eng._h)
+
+    host_step()  # untimed: the stage timing above left the engine to re-sort once
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e = replicas.job_rate(n * args.steps, e2e_s, device=f"cuda:{local}")
@@ -554,7 +563,7 @@ def run_ours(args, rank, world, local):
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}",
                        "knobs": {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items")}},
             "autotune": tuned,
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes},
             "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": None if traffic_ps is None else traffic_ps * n,

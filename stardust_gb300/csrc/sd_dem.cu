@@ -961,6 +961,36 @@ __global__ void dem_scatter_in_kernel(const float4* __restrict__ src, const floa
     dst[i] = v;
 }
 
+// slot_of_id[id] = slot for every sphere (ids in the omega w lane).
+__global__ void dem_slot_of_id_kernel(const float4* __restrict__ omg, uint32_t* __restrict__ slot_of_id, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = __float_as_uint(omg[i].w) & kIdMask;
+    if (id < n) slot_of_id[id] = i;
+}
+
+// Id-ordered host buffer <-> slot-ordered state, one thread per id: the
+// host side is read or written in order (one pass over the host link); the
+// slot side is the random one, in device memory.
+__global__ void dem_by_id_in_kernel(const float4* __restrict__ host_src, const uint32_t* __restrict__ slot_of_id,
+                                    float4* __restrict__ dst, uint32_t n, bool keep_w) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const uint32_t s = slot_of_id[id];
+    if (s >= n) return;
+    float4 v = host_src[id];
+    if (keep_w) v.w = dst[s].w;
+    dst[s] = v;
+}
+
+__global__ void dem_by_id_out_kernel(const float4* __restrict__ src, const uint32_t* __restrict__ slot_of_id,
+                                     float4* __restrict__ host_dst, uint32_t n) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const uint32_t s = slot_of_id[id];
+    if (s < n) host_dst[id] = src[s];
+}
+
 // Kinetic energy (translational + rotational, solid spheres) and linear
 // momentum, accumulated in double.
 __global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ vel,
@@ -1044,6 +1074,30 @@ cudaError_t dem_init_kernels() {
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+// Counts the slots whose sphere's cell key, from its current position,
+// differs from the sorted key it is placed under.
+__global__ void dem_keys_changed_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                                        const uint32_t* __restrict__ sorted_keys, Batch bt,
+                                        uint32_t* __restrict__ count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool changed = false;
+    if (i < n) {
+        const float4 q = pos[i];
+        const Grid g = bt.n > 1 ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
+        changed = cell_key_g(g, q.x, q.y, q.z) != sorted_keys[i];
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, changed);
+    if (lane_id() == 0 && m) atomicAdd(count, __popc(m));
+}
+
+cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess || b.n == 0) return e;
+    dem_keys_changed_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.sorted_in_tmp ? b.keys_tmp : b.keys,
+                                                                Batch{b.scenes, b.scene_first, b.nscenes}, count);
+    return cudaGetLastError();
 }
 
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
@@ -1187,6 +1241,22 @@ cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) 
 cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     dem_unsort_kernel<<<grid_for(n, 256), 256, 0, st>>>(src, omg, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_host_in_async(const float4* host_src, const float4* omg, float4* dst, uint32_t* slot_of_id,
+                              uint32_t n, bool keep_w, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dem_slot_of_id_kernel<<<grid_for(n, 256), 256, 0, st>>>(omg, slot_of_id, n);
+    dem_by_id_in_kernel<<<grid_for(n, 256), 256, 0, st>>>(host_src, slot_of_id, dst, n, keep_w);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_host_out_async(const float4* src, const float4* omg, float4* host_dst, uint32_t* slot_of_id,
+                               uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dem_slot_of_id_kernel<<<grid_for(n, 256), 256, 0, st>>>(omg, slot_of_id, n);
+    dem_by_id_out_kernel<<<grid_for(n, 256), 256, 0, st>>>(src, slot_of_id, host_dst, n);
     return cudaGetLastError();
 }
 

@@ -471,6 +471,7 @@ sd_status prepare_with(sd_engine* h, const float4* pos, const float4* vel, const
         return s;
     }
     h->prepared = true;
+    h->keys_current = true;
     h->steps = 0;
     return SD_OK;
 }
@@ -516,6 +517,7 @@ sd_status resort_if_needed(sd_engine* h) {
     SD_CUDA(h, sd::dem_keys_from_state_async(h->P, B, h->stream));
     SD_CUDA(h, sd::dem_sort_reorder_async(h->P, B, h->stream));
     h->need_resort = false;
+    h->keys_current = true;
     return SD_OK;
 }
 
@@ -1010,6 +1012,7 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
         if ((s = build_graph(h, dt))) return s;
     }
     for (int32_t i = 0; i < n_steps; ++i) SD_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+    if (n_steps > 0 && !h->hull_mode()) h->keys_current = true;  // every step ends with a sort + reorder
     h->steps += (uint64_t)n_steps;
     return SD_OK;
 }
@@ -1067,6 +1070,20 @@ static const float4* field_ptr(sd_engine* h, int32_t field) {
     }
 }
 
+// Device address of a host buffer that kernels can read and write in place:
+// page-locked memory mapped into the device's address space (cudaHostAlloc,
+// cudaHostRegister, torch's pinned tensors).  Kernels then move the data
+// over the host link themselves, with no staging copy; for other memory
+// this returns nullptr and the caller stages through device memory.
+static void* mapped_host(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // unregistered pointers may report an error: clear it
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes) {
     if (!h || !host_dst) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
@@ -1084,6 +1101,9 @@ sd_status sd_engine_get_state(sd_engine* h, int32_t field, void* host_dst, size_
     if (field == SD_FIELD_FORCE || field == SD_FIELD_TORQUE) {
         // recorded by sphere id already
         SD_CUDA(h, cudaMemcpyAsync(host_dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    } else if (float4* dev_view = static_cast<float4*>(mapped_host(host_dst))) {
+        SD_CUDA(h, sd::dem_host_out_async(src, h->B.omg, dev_view, reinterpret_cast<uint32_t*>(h->d_tmp), n,
+                                          h->stream));
     } else {
         SD_CUDA(h, sd::dem_unsort_async(src, h->B.omg, h->d_tmp, n, h->stream));
         SD_CUDA(h, cudaMemcpyAsync(host_dst, h->d_tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -1107,13 +1127,29 @@ sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src,
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
-    SD_CUDA(h, cudaMemcpyAsync(h->d_tmp, host_src, bytes, cudaMemcpyHostToDevice, h->stream));
     float4* dst = const_cast<float4*>(field_ptr(h, field));
     // the omega array's w lane holds the slot's sphere id: keep it
-    SD_CUDA(h, sd::dem_scatter_in_async(h->d_tmp, h->B.omg, dst, n, field == SD_FIELD_OMEGA, h->stream));
+    const bool keep_w = field == SD_FIELD_OMEGA;
+    if (const float4* in = static_cast<const float4*>(mapped_host(host_src))) {
+        SD_CUDA(h, sd::dem_host_in_async(in, h->B.omg, dst, reinterpret_cast<uint32_t*>(h->d_tmp), n, keep_w,
+                                         h->stream));
+    } else {
+        SD_CUDA(h, cudaMemcpyAsync(h->d_tmp, host_src, bytes, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, sd::dem_scatter_in_async(h->d_tmp, h->B.omg, dst, n, keep_w, h->stream));
+    }
+    // Only a position change can change cell keys.  When every sphere stays
+    // in the cell it is sorted under, a stable re-sort is the identity and
+    // the cell table still holds: count the slots whose key changed, and
+    // re-sort before the next step only if there are any.
+    const bool check = field == SD_FIELD_POSITION && h->keys_current && !h->need_resort;
+    uint32_t changed = 1;
+    if (check) {
+        uint32_t* d_changed = h->B.dev_status + 4;
+        SD_CUDA(h, sd::dem_keys_changed_async(h->P, h->B, d_changed, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(&changed, d_changed, 4, cudaMemcpyDeviceToHost, h->stream));
+    }
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
-    // only a position change can change cell keys
-    if (field == SD_FIELD_POSITION) h->need_resort = true;
+    if (field == SD_FIELD_POSITION && changed != 0) h->need_resort = true;
     return SD_OK;
 }
 
@@ -1124,6 +1160,7 @@ sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;
+    h->keys_current = false;  // a lone stage can leave keys and slots apart
     switch (stage) {
         case SD_STAGE_CONTACT: {
             if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(h, SD_ERR_INVALID_ARG, "dt must be positive");

@@ -81,6 +81,9 @@ struct sd_engine {
     bool graph_valid = false;
     uint64_t steps = 0;
     bool need_resort = false;
+    // the sorted key arrays hold the cell key of every slot's sphere (true
+    // after a full sort + reorder; a partial sd_engine_launch_stage clears it)
+    bool keys_current = false;
     uint64_t graph_epoch = 0;
 
     bool hull_mode() const { return !hull.pos.empty(); }

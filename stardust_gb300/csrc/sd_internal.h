@@ -220,7 +220,7 @@ struct DemBuffers {
     uint32_t *keys_tmp, *vals_tmp;  // sort ping-pong
     uint32_t* cell_start;           // ncells + 1
     uint32_t* sort_scratch;
-    uint32_t* dev_status;           // [0] error bits, [1] contacts lo, [2] contacts hi
+    uint32_t* dev_status;           // [0] error bits, [2..3] contact count (u64), [4] changed keys
     float4 *force, *torque;         // optional per-slot outputs (may be null)
     unsigned long long* pairs;      // optional contact pairs (may be null)
     unsigned long long* npairs;
@@ -242,6 +242,9 @@ constexpr uint32_t kClumpFlag = 0x80000000u;
 
 int dem_key_bits(uint32_t ncells);
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
+// Counts, into *count (device), the slots whose key from the current position
+// differs from the sorted key they sit under.
+cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st);
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
 cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
@@ -254,6 +257,13 @@ int dem_contact_mode();
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n,
                              cudaStream_t st);
+// State fields between a host buffer in sphere-id order that the device can
+// address (mapped page-locked memory) and the slot-ordered device arrays;
+// slot_of_id (n words) receives the id -> slot table.
+cudaError_t dem_host_in_async(const float4* host_src, const float4* omg, float4* dst, uint32_t* slot_of_id,
+                              uint32_t n, bool keep_w, cudaStream_t st);
+cudaError_t dem_host_out_async(const float4* src, const float4* omg, float4* host_dst, uint32_t* slot_of_id,
+                               uint32_t n, cudaStream_t st);
 cudaError_t dem_scatter_in_async(const float4* src_by_id, const float4* omg, float4* dst, uint32_t n, bool keep_w,
                                  cudaStream_t st);
 cudaError_t dem_energy_async(const DemBuffers& b, double* d_out, cudaStream_t st);

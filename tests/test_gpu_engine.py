@@ -5,6 +5,8 @@ in the same order with -ffp-contract=off, the kernels are built with
 -fmad=false), so positions, velocities, spins and forces are compared
 BIT-EXACTLY -- tighter than the 1e-5 relative bound asked of FP32 -- and the
 FP32 error against the FP64 twin of the oracle is stated and bounded."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -192,6 +194,77 @@ def test_checkpoint_resume_bit_exact(sdlib, orc, tmp_path):
         assert np.array_equal(bits(x), bits(y))
     a.close()
     c.close()
+
+
+def test_set_state_resorts_only_when_keys_change(sdlib, orc):
+    """Uploading the positions just read back keeps every sphere in its cell:
+    no re-sort, and the run is bit-identical to one that never uploaded.
+    Moving one sphere onto another, in a distant cell, re-sorts: the new
+    contact is found and the pair list equals the oracle's for the new state."""
+    from stardust_gb300 import _abi, scenes
+    pos, vel, cfg, dt, phi = scenes.settling_rsa(20_000, box=scenes.scaled_box(20_000), seed=8)
+    a = run_engine(sdlib, pos, vel, cfg, dt, 10, record=False)
+    b = run_engine(sdlib, pos, vel, cfg, dt, 10, record=False)
+    a.set(_abi.SD_FIELD_POSITION, a.positions())
+    a.set(_abi.SD_FIELD_VELOCITY, a.velocities())
+    a.step(dt, 15)
+    b.step(dt, 15)
+    a.sync()
+    b.sync()
+    assert np.array_equal(bits(a.positions()), bits(b.positions()))
+    assert np.array_equal(bits(a.velocities()), bits(b.velocities()))
+    # teleport sphere 0 onto the last sphere (far away: another cell)
+    p = a.positions()
+    far = len(p) - 1
+    assert np.linalg.norm(p[0, :3] - p[far, :3]) > 4 * cfg.cell
+    p[0, :3] = p[far, :3] + np.float32(0.5) * (p[0, 3] + p[far, 3]) * np.float32([1, 0, 0])
+    a.set(_abi.SD_FIELD_POSITION, p)
+    got = a.pairs()
+    assert (np.uint64(0) << np.uint64(32) | np.uint64(far)) in set(got.tolist())
+    prm = orc.params_from_engine(a.params(), dt)
+    sp, sv, sw, _, cs = orc.prepare(prm, p, a.velocities(), orc.with_ids(a.omegas(), np.arange(len(p))))
+    assert np.array_equal(got, orc.contact_pairs(prm, sp, sw, cs))
+    a.close()
+    b.close()
+
+
+def test_pinned_host_buffers_match_pageable(sdlib):
+    """Page-locked host buffers are read and written in place by the kernels;
+    pageable ones are staged through device memory.  Both give the same
+    bits, in both directions, for every settable field."""
+    import torch
+    from stardust_gb300 import _abi, scenes
+    pos, vel, cfg, dt, phi = scenes.settling_rsa(30_000, box=scenes.scaled_box(30_000), seed=9)
+    runs = []
+    for pinned in (False, True):
+        rng = np.random.default_rng(1)
+        eng = run_engine(sdlib, pos, vel, cfg, dt, 5, record=False)
+        new = {f: eng.get(f) for f in (_abi.SD_FIELD_POSITION, _abi.SD_FIELD_VELOCITY, _abi.SD_FIELD_OMEGA)}
+        new[_abi.SD_FIELD_VELOCITY][:, :3] += rng.uniform(-1e-3, 1e-3, (len(pos), 3)).astype(np.float32)
+        new[_abi.SD_FIELD_OMEGA][:, :3] = 3.0
+        for f, arr in new.items():
+            if pinned:
+                t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+                _abi.check(_abi.lib().sd_engine_set_state(eng._h, f, C.c_void_p(t.data_ptr()), t.numel() * 4),
+                           "set_state", eng._h)
+            else:
+                eng.set(f, arr)
+        eng.step(dt, 5)
+        eng.sync()
+        out = []
+        for f in (_abi.SD_FIELD_POSITION, _abi.SD_FIELD_VELOCITY, _abi.SD_FIELD_OMEGA):
+            if pinned:
+                t = torch.empty((len(pos), 4), dtype=torch.float32).pin_memory()
+                _abi.check(_abi.lib().sd_engine_get_state(eng._h, f, C.c_void_p(t.data_ptr()), t.numel() * 4),
+                           "get_state", eng._h)
+                out.append(t.numpy().copy())
+            else:
+                out.append(eng.get(f))
+        runs.append(out)
+        eng.close()
+    for x, y in zip(*runs):
+        assert np.array_equal(bits(x), bits(y))
+    assert np.all(runs[0][2][:, 3] == 0)  # the id lane never leaks out
 
 
 def test_set_state_and_momentum(sdlib):
