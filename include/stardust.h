@@ -186,11 +186,36 @@ sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float
  * face feels one contact.  Sphere-triangle contacts use the sphere contact
  * law against the moving wall.  Candidate triangles come from a static grid
  * in the mesh's own frame (the mesh moves rigidly, so the grid is built
- * once).  One mesh per engine; not in a batch.  Replaces DEMEngine::addMesh
- * (engine.cpp:117-121) with DEMMesh (entity.hpp:64-120), whose triangles the
- * reference never used in a step. */
+ * once).  Static meshes combine: a later static mesh is appended, its
+ * patch ids renumbered after the earlier ones (ids must be >= 0); a rotating
+ * mesh must be the engine's only mesh.  Not in a batch.  Replaces
+ * DEMEngine::addMesh (engine.cpp:117-121) with DEMMesh (entity.hpp:64-120),
+ * whose triangles the reference never used in a step. */
 sd_status sd_engine_add_mesh(sd_engine* h, uint32_t n_tris, const float* tri9, const int32_t* patch,
                              const float centre[3], const float axis[3], float omega);
+/* Triangles of an STL file (ASCII or binary), 9 floats each, as stored.
+ * Call with tri9 = NULL for the count (*n_tris), then with cap >= *n_tris.
+ * Replaces loadAndConvertMesh (src/IO/mesh_loader.cpp:9-45), which reads
+ * through the third-party stl_reader header (external/stl_reader). */
+sd_status sd_stl_read(const char* path, uint64_t cap, float* tri9, uint64_t* n_tris);
+/* Smooth faces of a triangle soup: triangles sharing an edge (bit-identical
+ * endpoints) whose normals, as unoriented lines, differ by less than
+ * angle_deg share a patch id; ids count up from 0 in order of each patch's
+ * first triangle. */
+sd_status sd_mesh_patches(uint64_t n_tris, const float* tri9, float angle_deg, int32_t* patch);
+/* DEMMesh(filename, position, quaternion) (entity.hpp:68-73) as a wall of
+ * the step: the STL's triangles placed at R(quat) v + position (quat = (s,
+ * x, y, z), normalised; NULL = identity; position NULL = 0), grouped into
+ * patches with patch_angle_deg (30 is a good default), then added with
+ * sd_engine_add_mesh (centre NULL = origin; omega 0: static). */
+sd_status sd_engine_add_mesh_stl(sd_engine* h, const char* path, const float position[3], const float quat[4],
+                                 const float centre[3], const float axis[3], float omega, float patch_angle_deg);
+/* The engine's mesh as it steps it (host copy; before or after prepare):
+ * n_tris triangles in the mesh frame -- world at time 0 minus centre --,
+ * 9 floats each, their patch ids, and the centre.  tri9 / patch / centre3
+ * may be NULL; with either array, cap must be >= the triangle count. */
+sd_status sd_engine_get_mesh(sd_engine* h, uint64_t cap, float* tri9, int32_t* patch, float* centre3,
+                             uint64_t* n_tris);
 /* The mesh pose on the device: R[9] (mesh to world, row-major), centre[3],
  * axis[3], omega, q[4] (s, x, y, z), dq[4] (the rotation of one step). */
 sd_status sd_engine_get_mesh_state(sd_engine* h, float* state24);

@@ -531,6 +531,24 @@ def make_mesh(tris, patch, centre, state24):
     return m
 
 
+def make_mesh_frame(tri_frame, patch, state24):
+    """Oracle mesh from triangles already in the mesh frame (as the engine
+    stores them, sd_engine_get_mesh) and the engine's pose state."""
+    t = np.asarray(tri_frame, np.float32).reshape(-1, 3, 3)
+    t4 = np.zeros((len(t), 3, 4), np.float32)
+    t4[:, :, :3] = t
+    t4 = np.ascontiguousarray(t4)
+    pa = np.ascontiguousarray(patch, np.int32)
+    m = Mesh()
+    m.ntri = len(t)
+    m.tri = t4.ctypes.data
+    m.patch = pa.ctypes.data
+    for k in range(24):
+        m.state[k] = float(state24[k])
+    m._keep = (t4, pa)
+    return m
+
+
 def run_full(p: Params, pos, vel, omg, steps: int, bodies=None, r0=None, body_of=None, mesh=None):
     """sdo_run_full: optional clumps (as run_bodies) and an optional mesh."""
     pos = np.array(pos, np.float32, copy=True)

@@ -8,7 +8,8 @@ from . import _abi
 from ._abi import SdError, lib
 from .engine import (BoundingVolumes, DEMEngine, EngineConfig, SpatialPartition, SweepAndPrune, add_hull_scene,
                      scene_lattice, scene_rsa)
+from .meshio import mesh_patches, read_stl, write_stl
 
 __all__ = ["BoundingVolumes", "DEMEngine", "EngineConfig", "SpatialPartition", "SweepAndPrune", "SdError",
-           "add_hull_scene", "lib",
+           "add_hull_scene", "lib", "mesh_patches", "read_stl", "write_stl",
            "scene_lattice", "scene_rsa", "_abi"]

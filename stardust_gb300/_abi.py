@@ -133,6 +133,10 @@ SIGNATURES = {
     "sd_engine_add_scene": [P, U64, P, P, P, P, P, F32],
     "sd_engine_add_mesh": [P, U32, P, P, P, P, F32],
     "sd_engine_get_mesh_state": [P, P],
+    "sd_engine_get_mesh": [P, U64, P, P, P, C.POINTER(U64)],
+    "sd_stl_read": [C.c_char_p, U64, P, C.POINTER(U64)],
+    "sd_mesh_patches": [U64, P, F32, P],
+    "sd_engine_add_mesh_stl": [P, C.c_char_p, P, P, P, P, F32, F32],
     "sd_engine_get_bodies": [P, I32, P, C.c_size_t],
     "sd_engine_add_hull": [P, U32, P, F32, P, P, P, P],
     "sd_engine_get_hull_shapes": [P, P, P, P, U64, C.POINTER(U64)],

@@ -668,32 +668,69 @@ sd_status sd_engine_add_mesh(sd_engine* h, uint32_t n_tris, const float* tri9, c
                              const float centre[3], const float axis[3], float omega) {
     if (!h || (n_tris && !tri9) || !centre) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
     if (h->prepared) return fail(h, SD_ERR_STATE, "meshes cannot be added after prepare");
-    if (!h->mesh.tri.empty()) return fail(h, SD_ERR_UNSUPPORTED, "one mesh per engine");
     if (n_tris == 0 || n_tris >= (1u << 26)) return fail(h, SD_ERR_INVALID_ARG, "n_tris must be in 1..2^26");
     double a[3] = {axis ? axis[0] : 0.0, axis ? axis[1] : 0.0, axis ? axis[2] : 1.0};
     const double an = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
     if (!(an > 0.0)) return fail(h, SD_ERR_INVALID_ARG, "mesh axis is zero");
     if (!std::isfinite(omega)) return fail(h, SD_ERR_INVALID_ARG, "omega must be finite");
     auto& M = h->mesh;
-    M.tri.resize(3 * (size_t)n_tris);
-    M.patch.resize(n_tris);
+    // Static meshes combine into one (triangles appended in the first mesh's
+    // frame, patches renumbered after the ones already there); a rotating
+    // mesh must be the only one.
+    const bool merge = !M.tri.empty();
+    if (merge && (M.omega != 0.0f || omega != 0.0f))
+        return fail(h, SD_ERR_UNSUPPORTED, "a rotating mesh must be the engine's only mesh (static meshes combine)");
+    if (merge && M.patch.size() + n_tris >= (1u << 26))
+        return fail(h, SD_ERR_INVALID_ARG, "the meshes hold 2^26 triangles or more");
+    for (uint32_t t = 0; t < n_tris; ++t) {
+        for (int k = 0; k < 9; ++k)
+            if (!std::isfinite(tri9[9 * (size_t)t + k])) return fail(h, SD_ERR_INVALID_ARG, "mesh vertex not finite");
+        if (patch && patch[t] < 0) return fail(h, SD_ERR_INVALID_ARG, "mesh patch ids must be >= 0");
+    }
+    const float c[3] = {merge ? M.centre[0] : centre[0], merge ? M.centre[1] : centre[1],
+                        merge ? M.centre[2] : centre[2]};
+    int32_t poff = 0;
+    for (int32_t pid : M.patch) poff = std::max(poff, pid + 1);
+    const size_t t0 = M.patch.size();
+    M.tri.resize(3 * (t0 + n_tris));
+    M.patch.resize(t0 + n_tris);
     for (uint32_t t = 0; t < n_tris; ++t) {
         for (int k = 0; k < 3; ++k) {
             const float* v = tri9 + 9 * (size_t)t + 3 * k;
-            if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2])) {
-                M.tri.clear();
-                M.patch.clear();
-                return fail(h, SD_ERR_INVALID_ARG, "mesh vertex not finite");
-            }
-            M.tri[3 * (size_t)t + k] = make_float4(v[0] - centre[0], v[1] - centre[1], v[2] - centre[2], 0.0f);
+            M.tri[3 * (t0 + t) + k] = make_float4(v[0] - c[0], v[1] - c[1], v[2] - c[2], 0.0f);
         }
-        M.patch[t] = patch ? patch[t] : (int32_t)t;
+        M.patch[t0 + t] = poff + (patch ? patch[t] : (int32_t)t);
     }
-    for (int k = 0; k < 3; ++k) {
-        M.centre[k] = centre[k];
-        M.axis[k] = (float)(a[k] / an);
+    if (!merge) {
+        for (int k = 0; k < 3; ++k) {
+            M.centre[k] = centre[k];
+            M.axis[k] = (float)(a[k] / an);
+        }
+        M.omega = omega;
     }
-    M.omega = omega;
+    return SD_OK;
+}
+
+sd_status sd_engine_get_mesh(sd_engine* h, uint64_t cap, float* tri9, int32_t* patch, float* centre3,
+                             uint64_t* n_tris) {
+    if (!h || !n_tris) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    const auto& M = h->mesh;
+    *n_tris = M.patch.size();
+    if (centre3)
+        for (int k = 0; k < 3; ++k) centre3[k] = M.centre[k];
+    if (tri9 || patch) {
+        if (cap < *n_tris) return fail(h, SD_ERR_CAPACITY, "capacity below the mesh's triangle count");
+        for (uint64_t t = 0; t < *n_tris; ++t) {
+            if (tri9)
+                for (int k = 0; k < 3; ++k) {
+                    const float4 v = M.tri[3 * t + k];
+                    tri9[9 * t + 3 * k] = v.x;
+                    tri9[9 * t + 3 * k + 1] = v.y;
+                    tri9[9 * t + 3 * k + 2] = v.z;
+                }
+            if (patch) patch[t] = M.patch[t];
+        }
+    }
     return SD_OK;
 }
 
@@ -917,17 +954,55 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
         float size, diameter, mass, p3[3], v3[3];
     };
     std::vector<Cube> cubes;
+    // mesh entities (DEMMesh): an STL file placed by position + quaternion,
+    // static or rotating; the file name is relative to the JSON file
+    struct MeshEnt {
+        std::string file;
+        float p3[3] = {0, 0, 0}, q4[4] = {1, 0, 0, 0}, centre[3] = {0, 0, 0}, axis[3] = {0, 0, 1};
+        float omega = 0.0f, angle = 30.0f;
+    };
+    std::vector<MeshEnt> meshes;
+    std::string dir(path);
+    dir = dir.find('/') == std::string::npos ? std::string() : dir.substr(0, dir.rfind('/') + 1);
     if (const sd::JsonValue* ents = scene->get("entities")) {
         if (ents->kind != sd::JsonValue::Array) return fail(h, SD_ERR_JSON, "scene.entities must be an array");
         for (size_t i = 0; i < ents->arr.size(); ++i) {
             const sd::JsonValue& e = ents->arr[i];
             std::string where = "scene.entities[" + std::to_string(i) + "]";
             if (e.kind != sd::JsonValue::Object) return fail(h, SD_ERR_JSON, where + " must be an object");
+            const sd::JsonValue* t = e.get("type");
+            if (t && t->kind == sd::JsonValue::String && t->str == "mesh") {
+                if (!keys_subset(e, {"type", "file", "position", "quaternion", "rotation", "patch_angle"}, &bad))
+                    return fail(h, SD_ERR_JSON, "unknown key " + where + "." + bad);
+                MeshEnt me;
+                const sd::JsonValue* fn = e.get("file");
+                if (!fn || fn->kind != sd::JsonValue::String || fn->str.empty())
+                    return fail(h, SD_ERR_JSON, where + ".file must name an STL file");
+                me.file = fn->str[0] == '/' ? fn->str : dir + fn->str;
+                if (e.get("position") && !json_vec3(e.get("position"), me.p3))
+                    return fail(h, SD_ERR_JSON, where + ".position must be [x,y,z]");
+                if (const sd::JsonValue* q = e.get("quaternion")) {
+                    if (q->kind != sd::JsonValue::Array || q->arr.size() != 4)
+                        return fail(h, SD_ERR_JSON, where + ".quaternion must be [s,x,y,z]");
+                    for (int k = 0; k < 4; ++k)
+                        if (!json_num(&q->arr[k], &me.q4[k])) return fail(h, SD_ERR_JSON, where + ".quaternion must be [s,x,y,z]");
+                }
+                if (const sd::JsonValue* r = e.get("rotation")) {
+                    if (r->kind != sd::JsonValue::Object || !keys_subset(*r, {"centre", "axis", "omega"}, &bad) ||
+                        !json_vec3(r->get("centre"), me.centre) || !json_vec3(r->get("axis"), me.axis) ||
+                        !json_num(r->get("omega"), &me.omega))
+                        return fail(h, SD_ERR_JSON, where + ".rotation must be {centre:[3], axis:[3], omega}");
+                }
+                if (e.get("patch_angle") &&
+                    (!json_num(e.get("patch_angle"), &me.angle) || !(me.angle >= 0.0f && me.angle <= 180.0f)))
+                    return fail(h, SD_ERR_JSON, where + ".patch_angle must be in [0, 180] degrees");
+                meshes.push_back(me);
+                continue;
+            }
             if (!keys_subset(e, {"type", "position", "size", "mass", "velocity", "grid_resolution", "diameter"}, &bad))
                 return fail(h, SD_ERR_JSON, "unknown key " + where + "." + bad);
-            const sd::JsonValue* t = e.get("type");
             if (!t || t->kind != sd::JsonValue::String || t->str != "generic")
-                return fail(h, SD_ERR_JSON, where + ".type must be \"generic\"");
+                return fail(h, SD_ERR_JSON, where + ".type must be \"generic\" or \"mesh\"");
             float p3[3], v3[3] = {0, 0, 0}, size, mass;
             if (!json_vec3(e.get("position"), p3)) return fail(h, SD_ERR_JSON, where + ".position must be [x,y,z]");
             if (e.get("velocity") && !json_vec3(e.get("velocity"), v3))
@@ -971,6 +1046,10 @@ sd_status sd_engine_load_scene_json(sd_engine* h, const char* path) {
         if (!(q >= 1.0f)) return fail(h, SD_ERR_JSON, "a cube entity's size is smaller than its diameter");
     }
     h->cfg = c;
+    for (const MeshEnt& me : meshes)
+        if (sd_status s = sd_engine_add_mesh_stl(h, me.file.c_str(), me.p3, me.q4, me.centre, me.axis, me.omega,
+                                                 me.angle))
+            return s;
     size_t done = 0;  // floats of `pos` added so far
     for (const Cube& cb : cubes) {
         if (cb.after > done) {

@@ -135,6 +135,28 @@ class DEMEngine:
         a = (C.c_float * 3)(*axis)
         self._call("sd_engine_add_mesh", len(t), t.ctypes.data, None if pa is None else pa.ctypes.data, c, a, omega)
 
+    def add_mesh_stl(self, path, position=None, quaternion=None, centre=None, axis=(0.0, 0.0, 1.0),
+                     omega: float = 0.0, patch_angle: float = 30.0) -> None:
+        """DEMMesh(filename, position, quaternion): an STL file's triangles
+        placed at R(quaternion) v + position (quaternion (s, x, y, z)), grouped
+        into smooth patches (crease angle patch_angle degrees), static or
+        rotating at omega about the line through centre along axis."""
+        def arr(v, n):
+            return None if v is None else (C.c_float * n)(*v)
+        self._call("sd_engine_add_mesh_stl", str(path).encode(), arr(position, 3), arr(quaternion, 4), arr(centre, 3),
+                   arr(axis, 3), omega, patch_angle)
+
+    def mesh(self):
+        """The engine's mesh as it steps it: (triangles in the mesh frame,
+        (n, 3, 3); patch ids; centre) -- world at time 0 = frame + centre."""
+        n = C.c_uint64()
+        self._call("sd_engine_get_mesh", 0, None, None, None, C.byref(n))
+        t = np.empty((n.value, 3, 3), np.float32)
+        pa = np.empty(n.value, np.int32)
+        c = (C.c_float * 3)()
+        self._call("sd_engine_get_mesh", n.value, t.ctypes.data, pa.ctypes.data, c, C.byref(n))
+        return t, pa, tuple(c)
+
     def mesh_state(self) -> np.ndarray:
         out = np.empty(24, np.float32)
         self._call("sd_engine_get_mesh_state", out.ctypes.data)

@@ -291,10 +291,41 @@ def drum_scene(n_spheres: int = 2_097_152, radius: float = 0.5, length: float = 
             "clumps": clumps, "cfg": cfg, "dt": 2e-6}
 
 
-def add_drum_scene(eng, d) -> None:
-    """Adds drum_scene's clumps (ids first), spheres and mesh."""
+def add_drum_scene(eng, d, stl_path=None) -> None:
+    """Adds drum_scene's clumps (ids first), spheres and mesh.  With
+    stl_path the mesh goes through an STL file: written there (binary) and
+    loaded with add_mesh_stl, whose smooth-face rule recovers the drum's
+    three faces -- the same triangles and patches as the direct route."""
     for rel, mass, com, v, w in d["clumps"]:
         eng.add_clump(rel, mass, com, v, w)
     if len(d["pos"]):
         eng.add_spheres(d["pos"], d["vel"])
-    eng.add_mesh(d["tris"], d["centre"], d["axis"], d["omega"], d["patch"])
+    if stl_path is None:
+        eng.add_mesh(d["tris"], d["centre"], d["axis"], d["omega"], d["patch"])
+    else:
+        from .meshio import write_stl
+        write_stl(stl_path, d["tris"])
+        eng.add_mesh_stl(stl_path, centre=d["centre"], axis=d["axis"], omega=d["omega"], patch_angle=30.0)
+
+
+def hopper_meshes(top: float = 0.12, outlet: float = 0.03, height: float = 0.08, z_outlet: float = 0.06,
+                  tray: float = 0.16, tray_depth: float = 0.02):
+    """A square hopper (four sloped walls, open top and outlet) above an
+    open tray (floor and four low walls), centred on x = y = 0: (funnel
+    (8, 3, 3), tray (10, 3, 3)) triangles, consistently wound."""
+    a, b = 0.5 * top, 0.5 * outlet
+    zt, zb = z_outlet + height, z_outlet
+    ring_t = [(-a, -a, zt), (a, -a, zt), (a, a, zt), (-a, a, zt)]
+    ring_b = [(-b, -b, zb), (b, -b, zb), (b, b, zb), (-b, b, zb)]
+    funnel = []
+    for k in range(4):
+        p0, p1, q0, q1 = ring_b[k], ring_b[(k + 1) % 4], ring_t[k], ring_t[(k + 1) % 4]
+        funnel += [(p0, p1, q1), (p0, q1, q0)]
+    c = 0.5 * tray
+    floor = [(-c, -c, 0.0), (c, -c, 0.0), (c, c, 0.0), (-c, c, 0.0)]
+    rim = [(x, y, tray_depth) for x, y, _ in floor]
+    tray_t = [(floor[0], floor[2], floor[1]), (floor[0], floor[3], floor[2])]
+    for k in range(4):
+        p0, p1, q0, q1 = floor[k], floor[(k + 1) % 4], rim[k], rim[(k + 1) % 4]
+        tray_t += [(p0, p1, q1), (p0, q1, q0)]
+    return np.array(funnel, np.float32), np.array(tray_t, np.float32)

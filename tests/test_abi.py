@@ -200,7 +200,7 @@ def test_scene_json_extensions_and_errors(sdlib, tmp_path):
     assert p["dims"] == (20, 20, 80) and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
     eng.close()
     for bad, what in (({"scene": {"domain": 1, "colour": 3}}, "colour"),
-                      ({"scene": {"entities": [{"type": "mesh", "position": [0, 0, 0], "size": 1, "mass": 1}]}}, "generic"),
+                      ({"scene": {"entities": [{"type": "cloud", "position": [0, 0, 0], "size": 1, "mass": 1}]}}, "generic"),
                       ({"scene": {"entities": [{"type": "generic", "position": [0, 0], "size": 1, "mass": 1}]}}, "position"),
                       ({"nope": {}}, "nope")):
         g = tmp_path / "bad.json"
