@@ -144,6 +144,10 @@ sd_status sd_config_default(sd_config* cfg);
 sd_status sd_engine_create(const sd_config* cfg, sd_engine** out);
 /* ~DEMEngine: engine.hpp:192-296 (frees every device buffer). */
 sd_status sd_engine_destroy(sd_engine* h);
+/* Removes free spheres (not spheres of rigid clumps) by id, before or after
+ * prepare; the remaining spheres keep their order and take ids 0..n-1 in
+ * it (clump tables follow).  Ids must be distinct and in range. */
+sd_status sd_engine_remove_spheres(sd_engine* h, uint64_t n, const uint32_t* ids);
 /* Copies the last error message of h (or of handle-less calls when h is
  * NULL) into buf; always NUL-terminates when len > 0. */
 sd_status sd_last_error(const sd_engine* h, char* buf, size_t len);
@@ -151,7 +155,15 @@ sd_status sd_last_error(const sd_engine* h, char* buf, size_t len);
 /* Adds n free spheres.  pos4 = (x, y, z, r), vel4 = (vx, vy, vz, m) host
  * arrays; omega4 may be NULL (zero spin).  Replaces the bulk of
  * DEMEngine::add(DEMParticle) for one-sphere entities
- * (engine.cpp:601-603, entity_handler.cpp:101-107). */
+ * (engine.cpp:601-603, entity_handler.cpp:101-107).
+ *
+ * Runtime changes (the reference's EntityHandler::addEntityRuntime,
+ * entity_handler.cpp:116, is a stub): on a prepared engine,
+ * sd_engine_add_spheres, sd_engine_add_clump and sd_engine_remove_spheres
+ * bring the state back to the host in sphere-id order, apply the change
+ * and prepare again (new buffers, cell sort, step graph on the next step);
+ * the step count and the mesh pose carry over.  New spheres take the next
+ * ids.  Not for a batch of scenes or convex-hull scenes. */
 sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4,
                                 const float* vel4, const float* omega4);
 
@@ -216,6 +228,19 @@ sd_status sd_engine_add_mesh_stl(sd_engine* h, const char* path, const float pos
  * may be NULL; with either array, cap must be >= the triangle count. */
 sd_status sd_engine_get_mesh(sd_engine* h, uint64_t cap, float* tri9, int32_t* patch, float* centre3,
                              uint64_t* n_tris);
+/* Headless snapshots in place of the reference's OpenGL renderer
+ * (src/graphics/renderer.cpp:15-22, 146-147), which writes nothing to disk.
+ * SD_SNAPSHOT_CSV: one row per sphere in id order, id,x,y,z,r,vx,vy,vz,m,
+ * wx,wy,wz, 9 significant digits (float32 values read back exactly); with
+ * SD_SNAPSHOT_CONTACTS also <path>.contacts.csv (i,j per contact pair).
+ * SD_SNAPSHOT_VTK: legacy VTK, BINARY POLYDATA -- spheres as points (point
+ * i = sphere i, VERTICES cells), contact pairs as LINES, the mesh at its
+ * current pose as POLYGONS over extra points (SD_SNAPSHOT_MESH); point data
+ * radius, mass, id (-1 on mesh points), velocity, spin. */
+typedef enum sd_snapshot_format { SD_SNAPSHOT_CSV = 0, SD_SNAPSHOT_VTK = 1 } sd_snapshot_format;
+#define SD_SNAPSHOT_CONTACTS 0x1u
+#define SD_SNAPSHOT_MESH 0x2u
+sd_status sd_engine_write_snapshot(sd_engine* h, const char* path, int32_t format, uint32_t flags);
 /* The mesh pose on the device: R[9] (mesh to world, row-major), centre[3],
  * axis[3], omega, q[4] (s, x, y, z), dq[4] (the rotation of one step). */
 sd_status sd_engine_get_mesh_state(sd_engine* h, float* state24);

@@ -29,6 +29,10 @@ STATUS_NAMES = {
     8: "SD_ERR_NOMEM", 9: "SD_ERR_UNSUPPORTED",
 }
 
+SD_SNAPSHOT_CSV = 0
+SD_SNAPSHOT_VTK = 1
+SD_SNAPSHOT_CONTACTS = 0x1
+SD_SNAPSHOT_MESH = 0x2
 SD_ENGINE_SAP = 0
 SD_ENGINE_SHP = 1
 SD_DEVICE_CPU = 0
@@ -128,12 +132,14 @@ SIGNATURES = {
     "sd_engine_destroy": [P],
     "sd_last_error": [P, C.c_char_p, C.c_size_t],
     "sd_engine_add_spheres": [P, U64, P, P, P],
+    "sd_engine_remove_spheres": [P, U64, P],
     "sd_engine_add_particle": [P, I32, F32, F32, F32, P, P],
     "sd_engine_add_clump": [P, U32, P, F32, P, P, P],
     "sd_engine_add_scene": [P, U64, P, P, P, P, P, F32],
     "sd_engine_add_mesh": [P, U32, P, P, P, P, F32],
     "sd_engine_get_mesh_state": [P, P],
     "sd_engine_get_mesh": [P, U64, P, P, P, C.POINTER(U64)],
+    "sd_engine_write_snapshot": [P, C.c_char_p, I32, U32],
     "sd_stl_read": [C.c_char_p, U64, P, C.POINTER(U64)],
     "sd_mesh_patches": [U64, P, F32, P],
     "sd_engine_add_mesh_stl": [P, C.c_char_p, P, P, P, P, F32, F32],

@@ -635,10 +635,127 @@ sd_status sd_last_error(const sd_engine* h, char* buf, size_t len) {
     return SD_OK;
 }
 
+// ---------------------------------------------------------- runtime changes
+// The reference declares EntityHandler::addEntityRuntime and leaves it empty
+// (entity_handler.cpp:116-119).  Here a prepared engine takes new spheres and
+// clumps and loses free spheres: its state comes back to the host in sphere-
+// id order (spheres with their id lanes, body states, the mesh pose), the
+// change is applied there, and the engine is prepared again -- new buffers,
+// the cell sort from id order, the step graph rebuilt on the next step.  The
+// step count and the mesh pose carry over.  A batch of scenes and convex-hull
+// scenes do not change at runtime.
+
+// The device state back into the host arrays, in sphere-id order.
+static sd_status pull_state(sd_engine* h, std::vector<float>* mesh_state) {
+    sd::DemBuffers& B = h->B;
+    const uint32_t n = B.n;
+    SD_CUDA(h, cudaSetDevice(h->device));
+    std::vector<float4>* dst[3] = {&h->h_pos, &h->h_vel, &h->h_omg};
+    const float4* src[3] = {B.pos, B.vel, B.omg};
+    for (int f = 0; f < 3; ++f) {
+        dst[f]->resize(n);
+        if (!n) continue;
+        // unsorted by the id lane, which the omega copy keeps (id + clump flag)
+        SD_CUDA(h, sd::dem_unsort_async(src[f], B.omg, h->d_tmp, n, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(dst[f]->data(), h->d_tmp, 16 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    const size_t nb = h->hb_pos.size();
+    std::vector<float4>* bdst[5] = {&h->hb_pos, &h->hb_vel, &h->hb_quat, &h->hb_omg, &h->hb_ang};
+    float4* const bsrc[5] = {B.bpos, B.bvel, B.bquat, B.bomg, B.bang};
+    for (int k = 0; k < 5 && nb; ++k)
+        SD_CUDA(h, cudaMemcpyAsync(bdst[k]->data(), bsrc[k], 16 * nb, cudaMemcpyDeviceToHost, h->stream));
+    mesh_state->clear();
+    if (B.mesh.ntri) {
+        mesh_state->resize(24);
+        SD_CUDA(h, cudaMemcpyAsync(mesh_state->data(), B.mesh.state, 24 * sizeof(float), cudaMemcpyDeviceToHost,
+                                   h->stream));
+    }
+    SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SD_OK;
+}
+
+struct Change {
+    std::vector<float> mesh_state;
+    uint64_t steps = 0;
+    bool active = false;
+};
+
+// A prepared engine's state to the host and its device buffers released.
+static sd_status begin_change(sd_engine* h, Change* c) {
+    if (!h->prepared) return SD_OK;
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "convex-hull scenes do not change after prepare");
+    if (h->scenes.size() > 1) return fail(h, SD_ERR_UNSUPPORTED, "a batch of scenes does not change after prepare");
+    sd_status s = pull_state(h, &c->mesh_state);
+    if (s) return s;
+    c->steps = h->steps;
+    c->active = true;
+    release_device(h);
+    return SD_OK;
+}
+
+// Prepared again on the changed host state (status: the change's own).
+static sd_status finish_change(sd_engine* h, const Change& c, sd_status status) {
+    if (!c.active) return status;
+    sd_status s = prepare_with(h, h->h_pos.data(), h->h_vel.data(), h->h_omg.data(), (uint32_t)h->h_pos.size());
+    if (s) return s;
+    h->steps = c.steps;
+    if (!c.mesh_state.empty() && h->B.mesh.ntri) {
+        SD_CUDA(h, cudaMemcpyAsync(h->B.mesh.state, c.mesh_state.data(), 24 * sizeof(float), cudaMemcpyHostToDevice,
+                                   h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    return status;
+}
+
+sd_status sd_engine_remove_spheres(sd_engine* h, uint64_t n, const uint32_t* ids) {
+    if (!h || (n && !ids)) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
+    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes");
+    if (!h->scenes.empty()) return fail(h, SD_ERR_UNSUPPORTED, "spheres of a batch of scenes cannot be removed");
+    const uint64_t total = h->prepared ? h->B.n : h->h_pos.size();
+    std::vector<char> gone(total, 0);
+    for (uint64_t k = 0; k < n; ++k) {
+        const uint32_t id = ids[k];
+        if (id >= total) return fail(h, SD_ERR_INVALID_ARG, "sphere id " + std::to_string(id) + " out of range");
+        if (gone[id]) return fail(h, SD_ERR_INVALID_ARG, "sphere id " + std::to_string(id) + " listed twice");
+        if (h->h_body_of[id] >= 0)
+            return fail(h, SD_ERR_UNSUPPORTED, "sphere " + std::to_string(id) + " belongs to a rigid clump");
+        gone[id] = 1;
+    }
+    if (n == 0) return SD_OK;
+    Change c;
+    sd_status s = begin_change(h, &c);
+    if (s) return s;
+    // compact in id order; the kept spheres' ids are their ranks
+    std::vector<uint32_t> new_id(total);
+    uint32_t k = 0;
+    for (uint64_t i = 0; i < total; ++i) {
+        new_id[i] = k;
+        if (gone[i]) continue;
+        h->h_pos[k] = h->h_pos[i];
+        h->h_vel[k] = h->h_vel[i];
+        h->h_omg[k] = h->h_omg[i];
+        h->h_body_of[k] = h->h_body_of[i];
+        h->h_r0[k] = h->h_r0[i];
+        const uint32_t bits = id_bits(k) | (h->h_body_of[k] >= 0 ? 0x80000000u : 0u);
+        std::memcpy(&h->h_omg[k].w, &bits, 4);
+        ++k;
+    }
+    for (auto* v : {&h->h_pos, &h->h_vel, &h->h_omg, &h->h_r0}) v->resize(k);
+    h->h_body_of.resize(k);
+    for (uint32_t& f : h->hb_first) f = new_id[f];  // a clump's spheres are all kept, still consecutive
+    return finish_change(h, c, SD_OK);
+}
+
 sd_status sd_engine_add_spheres(sd_engine* h, uint64_t n, const float* pos4, const float* vel4,
                                 const float* omega4) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
-    if (h->prepared) return fail(h, SD_ERR_STATE, "spheres cannot be added after prepare (reference: addEntityRuntime is a stub)");
+    if (h->prepared) {
+        Change c;
+        sd_status s = begin_change(h, &c);
+        if (s) return s;
+        return finish_change(h, c, sd_engine_add_spheres(h, n, pos4, vel4, omega4));
+    }
     if (!h->scenes.empty() && !h->adding_scene)
         return fail(h, SD_ERR_STATE, "spheres added outside a scene of the batch (use sd_engine_add_scene)");
     if (n && (!pos4 || !vel4)) return fail(h, SD_ERR_INVALID_ARG, "pos4/vel4 NULL");
@@ -773,7 +890,12 @@ sd_status sd_engine_add_scene(sd_engine* h, uint64_t n, const float* pos4, const
 sd_status sd_engine_add_clump(sd_engine* h, uint32_t n, const float* rel4, float mass, const float com[3],
                               const float vel[3], const float omega[3]) {
     if (!h || !rel4 || !com || !vel) return fail(h, SD_ERR_INVALID_ARG, "NULL argument");
-    if (h->prepared) return fail(h, SD_ERR_STATE, "bodies cannot be added after prepare");
+    if (h->prepared) {
+        Change c;
+        sd_status s = begin_change(h, &c);
+        if (s) return s;
+        return finish_change(h, c, sd_engine_add_clump(h, n, rel4, mass, com, vel, omega));
+    }
     if (n == 0) return fail(h, SD_ERR_INVALID_ARG, "a clump needs at least one sphere");
     if (!(mass > 0.0f) || !std::isfinite(mass)) return fail(h, SD_ERR_INVALID_ARG, "clump mass must be > 0");
     if (h->h_pos.size() + n >= 0x7fffffffull) return fail(h, SD_ERR_CAPACITY, "more than 2^31-1 spheres");

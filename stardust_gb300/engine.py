@@ -107,6 +107,13 @@ class DEMEngine:
                    None if w is None else w.ctypes.data)
         self._n += len(p)
 
+    def remove_spheres(self, ids) -> None:
+        """Removes free spheres by id (before or after prepare); the others
+        keep their order and take ids 0..n-1 in it."""
+        i = np.ascontiguousarray(ids, np.uint32)
+        self._call("sd_engine_remove_spheres", len(i), i.ctypes.data)
+        self._n -= len(i)
+
     def add(self, grid_resolution: int, size: float, diameter: float, mass: float, position, velocity) -> None:
         """DEMEngine::add(DEMParticle(...)): one sphere, or a rigid cube clump
         of floor(size/diameter)^2 spheres when grid_resolution > 1."""
@@ -156,6 +163,14 @@ class DEMEngine:
         c = (C.c_float * 3)()
         self._call("sd_engine_get_mesh", n.value, t.ctypes.data, pa.ctypes.data, c, C.byref(n))
         return t, pa, tuple(c)
+
+    def write_snapshot(self, path, fmt: str = "vtk", contacts: bool = False, mesh: bool = False) -> None:
+        """Writes the state to a CSV or legacy-VTK file (sd_engine_write_snapshot)."""
+        kinds = {"csv": _abi.SD_SNAPSHOT_CSV, "vtk": _abi.SD_SNAPSHOT_VTK}
+        if fmt not in kinds:
+            raise ValueError("fmt must be 'csv' or 'vtk'")
+        flags = (_abi.SD_SNAPSHOT_CONTACTS if contacts else 0) | (_abi.SD_SNAPSHOT_MESH if mesh else 0)
+        self._call("sd_engine_write_snapshot", str(path).encode(), kinds[fmt], flags)
 
     def mesh_state(self) -> np.ndarray:
         out = np.empty(24, np.float32)
