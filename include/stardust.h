@@ -231,7 +231,7 @@ sd_status sd_engine_get_mesh(sd_engine* h, uint64_t cap, float* tri9, int32_t* p
 /* Headless snapshots in place of the reference's OpenGL renderer
  * (src/graphics/renderer.cpp:15-22, 146-147), which writes nothing to disk.
  * SD_SNAPSHOT_CSV: one row per sphere in id order, id,x,y,z,r,vx,vy,vz,m,
- * wx,wy,wz, 9 significant digits (float32 values read back exactly); with
+ * wx,wy,wz, each the shortest decimal that reads back as the same float32; with
  * SD_SNAPSHOT_CONTACTS also <path>.contacts.csv (i,j per contact pair).
  * SD_SNAPSHOT_VTK: legacy VTK, BINARY POLYDATA -- spheres as points (point
  * i = sphere i, VERTICES cells), contact pairs as LINES, the mesh at its

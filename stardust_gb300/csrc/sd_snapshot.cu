@@ -7,8 +7,8 @@
 // sd_engine_get_pairs, sd_engine_get_mesh, sd_engine_get_mesh_state):
 //
 //   * CSV: one row per sphere in id order --
-//     id,x,y,z,r,vx,vy,vz,m,wx,wy,wz -- with 9 significant digits, so every
-//     float32 reads back exactly; with SD_SNAPSHOT_CONTACTS a second file,
+//     id,x,y,z,r,vx,vy,vz,m,wx,wy,wz -- each value the shortest decimal that
+//     reads back as the same float32; with SD_SNAPSHOT_CONTACTS a second file,
 //     <path>.contacts.csv, lists the contact pairs (i,j with i < j).
 //   * VTK (legacy format, BINARY, POLYDATA): the spheres as points (point i
 //     = sphere i) with VERTICES cells, the contact pairs as LINES
@@ -16,6 +16,7 @@
 //     extra points (SD_SNAPSHOT_MESH), and point data: radius, mass, id,
 //     velocity, spin (zero on mesh points).  Big-endian float32 / int32 as
 //     the format requires.
+#include <charconv>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -58,10 +59,11 @@ std::vector<uint32_t> big_endian(const T* src, size_t n) {
     return out;
 }
 
-std::string fmt9(float v) {
+// The shortest decimal text that reads back as exactly v (std::to_chars).
+void put_float(std::string& out, float v) {
     char b[32];
-    std::snprintf(b, sizeof b, "%.9g", (double)v);
-    return b;
+    const auto r = std::to_chars(b, b + sizeof b, v);
+    out.append(b, r.ptr);
 }
 
 }  // namespace
@@ -114,10 +116,13 @@ extern "C" sd_status sd_engine_write_snapshot(sd_engine* h, const char* path, in
         std::string buf = "id,x,y,z,r,vx,vy,vz,m,wx,wy,wz\n";
         for (uint64_t i = 0; i < n; ++i) {
             buf += std::to_string(i);
-            for (int k = 0; k < 4; ++k) buf += "," + fmt9(pos[4 * i + k]);
-            for (int k = 0; k < 4; ++k) buf += "," + fmt9(vel[4 * i + k]);
-            for (int k = 0; k < 3; ++k) buf += "," + fmt9(omg[4 * i + k]);
-            buf += "\n";
+            const float* row[3] = {&pos[4 * i], &vel[4 * i], &omg[4 * i]};
+            for (int fld = 0; fld < 3; ++fld)
+                for (int k = 0; k < (fld == 2 ? 3 : 4); ++k) {  // spin: no w lane
+                    buf += ',';
+                    put_float(buf, row[fld][k]);
+                }
+            buf += '\n';
             if (buf.size() > (1u << 20)) {
                 if (!f.put(buf)) return sd_fail(h, SD_ERR_IO, "write failed: " + p);
                 buf.clear();
