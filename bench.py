@@ -67,6 +67,15 @@ CONTACT_BYTES_PER_SPHERE = 48 + 48 + 8
 STEP_BYTES_PER_SPHERE = 104 + 4 + 32 + 104
 
 
+def clocks_mhz(clocks) -> float:
+    """Median SM clock seen during the timed region (max clock if unsampled)."""
+    try:
+        v = float(clocks.get("sm_mhz") or 0)
+    except Exception:
+        v = 0.0
+    return v if v > 0 else 2070.0
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -148,16 +157,20 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def recorded_traffic():
-    """Per-launch DRAM bytes of the contact kernel from the committed ncu summary."""
+def recorded_profile():
+    """DRAM bytes and warp instructions per sphere of one contact-kernel
+    launch, from the committed ncu summary (profiles/roofline_traffic.json)."""
     f = ROOT / "profiles" / "roofline_traffic.json"
     if f.exists():
         try:
             d = json.loads(f.read_text())
-            return d.get("contact_integrate_bytes_per_sphere")
+            return d.get("contact_integrate_bytes_per_sphere"), d.get("contact_integrate_warp_instructions_per_sphere")
         except Exception:
-            return None
-    return None
+            pass
+    return None, None
+
+
+SMS, SCHEDULERS_PER_SM = 152, 4  # GB300: one warp instruction per scheduler per clock
 
 
 def cpu_oracle_rate(pos, vel, cfg, dt, seconds: float, threads: int | None):
@@ -491,7 +504,7 @@ def run_ours(args, rank, world, local):
     contact_ms = stage_ms["contact_integrate"]
     peak, peak_kind = measured_peak()
     achieved = n * CONTACT_BYTES_PER_SPHERE / (contact_ms * 1e-3) / 1e9
-    traffic_ps = recorded_traffic()
+    traffic_ps, winst_ps = recorded_profile()
 
     # ---- end to end through the C ABI with host buffers: the host owns the
     # state; every step uploads positions and velocities from pinned memory,
@@ -572,6 +585,15 @@ def run_ours(args, rank, world, local):
                          "traffic": None if traffic_ps is None else traffic_ps * n,
                          "algorithmic_bytes": CONTACT_BYTES_PER_SPHERE * n,
                          "launch_ms": contact_ms},
+            # the contact kernel is bound by instruction issue, not bytes:
+            # its warp instructions per launch (ncu) over the live launch time,
+            # against one warp instruction per scheduler per clock
+            "issue_roofline": None if winst_ps is None else {
+                "kernel": "dem_contact_integrate_kernel", "unit": "warp instructions/s",
+                "achieved": winst_ps * n / (contact_ms * 1e-3),
+                "peak": SMS * SCHEDULERS_PER_SM * clocks_mhz(clocks) * 1e6,
+                "frac": winst_ps * n / (contact_ms * 1e-3) / (SMS * SCHEDULERS_PER_SM * clocks_mhz(clocks) * 1e6),
+                "warp_instructions": winst_ps * n, "sm_mhz": clocks_mhz(clocks)},
             "stages_ms": stage_ms,
             "step_bytes_per_sphere": STEP_BYTES_PER_SPHERE,
             "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
