@@ -25,6 +25,8 @@ reorder + cell_start.  Timings:
              20,480-triangle cylinder (bench_drum);
   batch      512 independent scenes (~2.9M spheres) stepped together, one
              launch per stage (bench_batch), against 16 of them stepped alone;
+  sap        the sweep-and-prune operators on 2,000,000 boxes, beside the
+             reference's recorded SAP run times (bench_sap);
   gjk        the second half of the metric: mean GJK support evaluations per
              candidate pair with the learned warm start vs plain GJK, on a
              65,536-hull scene (bench_hulls), with the contact sets and states
@@ -430,6 +432,50 @@ def bench_drum(steps: int, warmup: int, local: int):
             "scene_generation_s": gen_s}
 
 
+def bench_sap(n: int, steps: int, warmup: int, local: int):
+    """The sweep-and-prune operators on n boxes (centres uniform in the unit
+    cube, half-width 2.5 mm, seeded) -- SAPCollision::processCollisions's
+    bug-compatible rows (sd_sap_process_collisions: boxes, stable sort of the
+    lower x, windowed sweep) and the exact pair set (sd_sap_pairs).  The
+    reference records 6.8-8.6 ms per "blocksweep"/"serialweep" run
+    (profiling/*.txt) for testSAP.cu, whose setup is 2,000,000 objects but
+    whose hardware and initialisation are not recorded.  The exact one-axis
+    sweep is slow on a uniform 3D field (each box sweeps every box whose
+    lower x lies within its x extent); the LBVH operator (sd_lbvh_pairs) gives
+    the same pair set quickly.  CUDA events on the current stream, mean over
+    `steps` calls after `warmup`."""
+    import torch
+    import stardust_gb300 as sd
+    g = torch.Generator(device="cpu").manual_seed(7)
+    pos = torch.empty((n, 4), dtype=torch.float32)
+    pos[:, :3] = torch.rand((n, 3), generator=g)
+    pos[:, 3] = 0.0025
+    pos = pos.to(f"cuda:{local}")
+    lo = (pos[:, :3] - pos[:, 3:]).contiguous()
+    hi = (pos[:, :3] + pos[:, 3:]).contiguous()
+    lo4 = torch.cat([lo, torch.zeros((n, 1), device=lo.device)], 1).contiguous()
+    hi4 = torch.cat([hi, torch.zeros((n, 1), device=hi.device)], 1).contiguous()
+    cap = 1 << 24
+    out = {"workload": f"{n} boxes, centres uniform in the unit cube, half-width 2.5 mm"}
+    for name, fn in (("process_collisions_ms", lambda: sd.SweepAndPrune.process_collisions(pos)),
+                     ("exact_pairs_ms", lambda: sd.SweepAndPrune.pairs(lo4, hi4, cap)),
+                     ("lbvh_pairs_ms", lambda: sd.BoundingVolumes.pairs(lo4, hi4, cap))):
+        for _ in range(warmup):
+            r = fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            r = fn()
+        b.record()
+        torch.cuda.synchronize()
+        out[name] = a.elapsed_time(b) / steps
+        if name != "process_collisions_ms":
+            out[name.replace("_ms", "_count")] = int(r[1])
+    out["reference_recorded_ms"] = {"blocksweep_median": 7.048, "serialweep_median": 7.054}
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -556,6 +602,12 @@ def run_ours(args, rank, world, local):
         drum = bench_drum(args.steps, args.warmup, local)
         log(f"drum: {drum}")
 
+    # ---- sweep and prune on 2,000,000 boxes (rank 0, N = 1)
+    sap = None
+    if rank == 0 and world == 1 and not args.no_sap:
+        sap = bench_sap(2_000_000, 20, 3, local)
+        log(f"sap: {sap}")
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -604,6 +656,7 @@ def run_ours(args, rank, world, local):
             "gjk": gjk,
             "batch": batch,
             "drum": drum,
+            "sap": sap,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -631,6 +684,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--no-drum", action="store_true")
     ap.add_argument("--only-drum", action="store_true", help="run only the rotating-drum section")
+    ap.add_argument("--no-sap", action="store_true")
+    ap.add_argument("--only-sap", action="store_true", help="run only the sweep-and-prune section")
     ap.add_argument("--z-div", type=int, default=None,
                     help="z cells per cell edge for every engine (default: the library's automatic choice)")
     args = ap.parse_args()
@@ -641,6 +696,11 @@ def main():
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.only_sap:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"sap": bench_sap(2_000_000, args.steps, args.warmup, local)}), flush=True)
+        return 0
     if args.only_drum:
         import torch
         torch.cuda.set_device(local)
