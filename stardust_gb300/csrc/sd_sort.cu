@@ -127,12 +127,19 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
     // load + warp-local stable ranking
     uint32_t key[ITEMS], val[ITEMS], rank[ITEMS];
     uint32_t* wh = s_whist + w * BINS;
+    // all of the thread's loads first, so their latencies overlap; read once,
+    // so streaming (evict-first) loads
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         uint32_t idx = tile_base + w * (ITEMS * kWarp) + j * kWarp + lane;
         bool valid = idx < n;
-        key[j] = valid ? keys_in[idx] : 0xffffffffu;
-        val[j] = valid ? vals_in[idx] : 0u;
+        key[j] = valid ? __ldcs(keys_in + idx) : 0xffffffffu;
+        val[j] = valid ? __ldcs(vals_in + idx) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = tile_base + w * (ITEMS * kWarp) + j * kWarp + lane;
+        bool valid = idx < n;
         uint32_t d = valid ? ((key[j] >> shift) & mask) : 0xffffffffu;
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = __popc(peers & lanemask_lt());
