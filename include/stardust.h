@@ -96,6 +96,10 @@ typedef struct sd_stats {
     uint64_t gjk_pairs;
     uint64_t gjk_iters;
     uint64_t epa_iters;
+    /* sphere scenes, last step: slots whose cell key changed (the step
+     * re-sorts incrementally when at most knob "resort_max" changed, else it
+     * runs the radix passes); 0 when the knob is 0 */
+    uint64_t moved_keys;
 } sd_stats;
 
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
@@ -450,7 +454,11 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *   "sort_items"    keys per thread of the sort's digit pass: 8 or 16 (default)
  *   "z_div"         z cells per cell edge for engines prepared afterwards: 1, 2, 4 or 8,
  *                   or 0 (default) = 2 when that keeps keys within 20 bits and the
- *                   sort's pass count, else 1; a batch of scenes always uses 1 */
+ *                   sort's pass count, else 1; a batch of scenes always uses 1
+ *   "resort_max"    most changed cell keys the step re-sorts incrementally (a merge of
+ *                   the changed entries into the previous order) instead of running the
+ *                   radix passes: 0 (always the passes) or a power of two up to 16384;
+ *                   default 4096.  Same result either way (a stable sort by key) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

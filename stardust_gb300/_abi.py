@@ -105,6 +105,7 @@ class SdStats(C.Structure):
         ("gjk_pairs", C.c_uint64),
         ("gjk_iters", C.c_uint64),
         ("epa_iters", C.c_uint64),
+        ("moved_keys", C.c_uint64),
     ]
 
 

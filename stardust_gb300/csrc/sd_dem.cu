@@ -869,7 +869,8 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
                    const uint32_t* __restrict__ vals, const float4* __restrict__ pos_n,
                    const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
                    float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
-                   uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of) {
+                   uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
+                   uint32_t* __restrict__ keys_prev) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
@@ -885,7 +886,9 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
             const uint32_t idb = __float_as_uint(o.w);
             if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
         }
-        s_keys[threadIdx.x + 1] = keys[k];
+        const uint32_t key = keys[k];
+        s_keys[threadIdx.x + 1] = key;
+        keys_prev[k] = key;  // what the next step's incremental re-sort compares against
     }
     if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
     __syncthreads();
@@ -1115,7 +1118,7 @@ __global__ void dem_keys_changed_kernel(DemParams p, uint32_t n, const float4* _
 cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess || b.n == 0) return e;
-    dem_keys_changed_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.sorted_in_tmp ? b.keys_tmp : b.keys,
+    dem_keys_changed_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.keys_prev,
                                                                 Batch{b.scenes, b.scene_first, b.nscenes}, count);
     return cudaGetLastError();
 }
@@ -1146,7 +1149,7 @@ cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
     dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
         b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
-        b.nb ? b.slot_of : nullptr);
+        b.nb ? b.slot_of : nullptr, b.keys_prev);
     return cudaGetLastError();
 }
 
@@ -1229,7 +1232,8 @@ cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool 
 }
 
 // One whole step: clear the sort's scratch, contact + integrate (which also
-// builds the key histograms), the digit passes, reorder.
+// builds the key histograms), the incremental re-sort, the digit passes
+// (which return at once when the re-sort has written the result), reorder.
 cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(dem_key_bits(b.ncells));
@@ -1242,8 +1246,13 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
     if (e != cudaSuccess) return e;
     if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
+    // the passes leave their result in keys/vals for an even pass count,
+    // in keys_tmp/vals_tmp for an odd one; the re-sort writes the same place
+    // (its kernels read the new keys before any of them is overwritten)
+    const bool odd = (plan.passes & 1) != 0;
+    if ((e = resort_async(b, odd ? b.keys_tmp : b.keys, odd ? b.vals_tmp : b.vals, st)) != cudaSuccess) return e;
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
-                               &b.sorted_in_tmp)) != cudaSuccess)
+                               &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
     if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
     return mesh_advance_async(b.mesh, 1, st);

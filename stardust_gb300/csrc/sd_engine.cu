@@ -399,7 +399,10 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &B.vals_tmp, n)) || (s = dev_alloc(h, &B.cell_start, (size_t)B.ncells + 1)) ||
         (s = dev_alloc(h, &B.sort_scratch, sd::sort_scratch_words(n, bits))) ||
         (s = dev_alloc(h, &B.dev_status, 8)) || (s = dev_alloc(h, &h->d_energy, 4)) ||
-        (s = dev_alloc(h, &h->d_tmp, n)))
+        (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
+        (s = dev_alloc(h, &B.rs_mask, ((size_t)n + 31) / 32)) || (s = dev_alloc(h, &B.rs_wbase, ((size_t)n + 31) / 32)) ||
+        (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->cfg.flags & SD_FLAG_RECORD) {
         if ((s = dev_alloc(h, &B.force, n)) || (s = dev_alloc(h, &B.torque, n))) return s;
@@ -410,6 +413,7 @@ sd_status allocate(sd_engine* h, uint32_t n) {
     if ((s = dev_alloc(h, &B.pairs, (size_t)B.pair_cap)) || (s = dev_alloc(h, &B.npairs, 1))) return s;
     SD_CUDA(h, cudaMemsetAsync(B.dev_status, 0, 8 * sizeof(uint32_t), h->stream));
     SD_CUDA(h, cudaMemsetAsync(B.sort_scratch, 0, 16 * sizeof(uint32_t), h->stream));
+    SD_CUDA(h, cudaMemsetAsync(B.rs_scratch, 0, sd::resort_scratch_words(n) * sizeof(uint32_t), h->stream));
     if (!h->mesh.tri.empty()) {
         if ((s = build_mesh(h))) return s;
     }
@@ -494,6 +498,7 @@ sd_status build_graph(sd_engine* h, float dt) {
     }
     cudaGraph_t g = nullptr;
     SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->B.rs_max = sd::dem_resort_max();
     cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
     cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
     if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
@@ -1233,6 +1238,10 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
+    } else if (k == "resort_max") {
+        if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)
+            return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 16384");
+        sd::dem_set_resort_max((uint32_t)value);
     } else {
         return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     }
@@ -1246,6 +1255,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     if (k == "contact_mode") *value = sd::dem_contact_mode();
     else if (k == "sort_items") *value = sd::sort_items();
     else if (k == "z_div") *value = g_z_div;
+    else if (k == "resort_max") *value = (int32_t)sd::dem_resort_max();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }
@@ -1484,7 +1494,11 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
     SD_CUDA(h, sd::dem_pairs_async(h->P, h->B, h->stream));
     unsigned long long np = 0;
     SD_CUDA(h, cudaMemcpyAsync(&np, h->B.npairs, 8, cudaMemcpyDeviceToHost, h->stream));
+    uint32_t moved = 0;
+    if (h->graph_valid && h->B.rs_max && h->B.n)
+        SD_CUDA(h, cudaMemcpyAsync(&moved, h->B.rs_scratch + 1, 4, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
+    out->moved_keys = h->steps ? moved : 0;
     // bodies: the kernel above counted free spheres only
     const size_t nb = h->B.nb;
     if (nb) {

@@ -38,9 +38,11 @@ uint32_t* sort_hist_ptr(uint32_t* scratch);  // global digit histograms, pass q 
 cudaError_t sort_clear_async(uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st);
 cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPlan& plan, uint32_t* scratch,
                                  cudaStream_t st);
+// skip (may be null): the passes return at once when skip[1] <= skip_max
+// (the incremental re-sort has written the result)
 cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                               uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
-                              bool* in_tmp);
+                              bool* in_tmp, const uint32_t* skip = nullptr, uint32_t skip_max = 0);
 cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                              uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
                              bool* in_tmp);
@@ -236,11 +238,26 @@ struct DemBuffers {
     float4 *bpos, *bvel, *bquat, *bomg, *bang;  // per body: (x,y,z,m), v, q=(s,x,y,z), w, L
     float4* binv;                   // per body: 3 rows of the body-frame inverse inertia
     uint32_t *bfirst, *bcount;      // per body: first sphere id, number of spheres
+    // incremental re-sort (sd_resort.cu): rs_max 0 = the step always radix-sorts
+    uint32_t* keys_prev;            // per slot: the sorted key it sits under (written by the reorder)
+    uint32_t *rs_mask, *rs_wbase;   // per 32 slots: moved bits, moved slots before the word
+    unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), rs_max of them
+    uint32_t* rs_scratch;           // ticket, moved count, tile status
+    uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
 
 int dem_key_bits(uint32_t ncells);
+// incremental re-sort (sd_resort.cu): writes the sorted (key, slot) pairs of
+// b.keys into keys_out / vals_out when at most b.rs_max keys changed since
+// the previous sort (the count is rs_scratch[1]); returns at once otherwise
+constexpr uint32_t kResortMaxCap = 16384;  // largest rs_max (the bitonic list fits shared memory)
+uint32_t resort_tiles(uint32_t n);
+uint64_t resort_scratch_words(uint32_t n);
+cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);
+void dem_set_resort_max(uint32_t m);
+uint32_t dem_resort_max();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
 // Counts, into *count (device), the slots whose key from the current position
 // differs from the sorted key they sit under.

@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(kSortThreads)
 sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                  uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                  int shift, int bits, int pass, uint32_t num_tiles, uint32_t stride,
-                 uint32_t* __restrict__ scratch) {
+                 uint32_t* __restrict__ scratch, const uint32_t* __restrict__ skip, uint32_t skip_max) {
+    if (skip && skip[1] <= skip_max) return;  // the incremental re-sort wrote the result
     constexpr int TILE = kSortThreads * ITEMS;
     constexpr int DPT = BINS / kSortThreads;  // digits per thread (1, 2 or 4)
     extern __shared__ __align__(16) uint32_t smem[];
@@ -307,7 +308,7 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
 template <int BINS, int ITEMS>
 static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t* ko, uint32_t* vo,
                                uint32_t n, int shift, int bits, int pass, uint32_t tiles, uint32_t stride,
-                               uint32_t* scratch, cudaStream_t st) {
+                               uint32_t* scratch, cudaStream_t st, const uint32_t* skip, uint32_t skip_max) {
     size_t sm = pass_smem_bytes<BINS, ITEMS>();
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel<BINS, ITEMS>,
@@ -315,7 +316,7 @@ static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t*
         if (e != cudaSuccess) return e;
     }
     sort_pass_kernel<BINS, ITEMS><<<tiles, kSortThreads, sm, st>>>(ki, vi, ko, vo, n, shift, bits,
-                                                                   pass, tiles, stride, scratch);
+                                                                   pass, tiles, stride, scratch, skip, skip_max);
     return cudaGetLastError();
 }
 
@@ -323,7 +324,7 @@ static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t*
 // tile status cleared (sort_clear_async + a histogram producer).
 cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                               uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
-                              bool* in_tmp) {
+                              bool* in_tmp, const uint32_t* skip, uint32_t skip_max) {
     *in_tmp = false;
     if (n == 0) return cudaSuccess;
     const uint32_t tiles = num_tiles(n);
@@ -333,13 +334,13 @@ cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp
         const int b = plan.bits[p], sh = plan.shift[p];
         const uint32_t sd = (uint32_t)plan.stride;
         if (g_sort_items >= 16)
-            e = b > 9   ? launch_pass<1024, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
-                : b > 8 ? launch_pass<512, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
-                        : launch_pass<256, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st);
+            e = b > 9   ? launch_pass<1024, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                : b > 8 ? launch_pass<512, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                        : launch_pass<256, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max);
         else
-            e = b > 9   ? launch_pass<1024, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
-                : b > 8 ? launch_pass<512, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st)
-                        : launch_pass<256, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st);
+            e = b > 9   ? launch_pass<1024, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                : b > 8 ? launch_pass<512, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                        : launch_pass<256, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max);
         if (e != cudaSuccess) return e;
         uint32_t* t;
         t = ki; ki = ko; ko = t;

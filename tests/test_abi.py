@@ -279,3 +279,18 @@ def test_batch_api_rules(sdlib):
         e2.add_scene(pos, vel, (0, 0, 0), (1, 1, 1))
     assert e.value.status == sdlib._abi.SD_ERR_STATE
     e2.close()
+
+
+def test_resort_max_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("resort_max")
+    assert old == 4096
+    try:
+        for v in (0, 1, 2, 256, 16384):
+            _abi.tune_set("resort_max", v)
+            assert _abi.tune_get("resort_max") == v
+        for v in (-1, 3, 6000, 32768):
+            with pytest.raises(Exception):
+                _abi.tune_set("resort_max", v)
+    finally:
+        _abi.tune_set("resort_max", old)
