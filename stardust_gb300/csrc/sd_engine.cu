@@ -1240,7 +1240,7 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         g_z_div = value;
     } else if (k == "resort_max") {
         if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)
-            return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 16384");
+            return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 2048");
         sd::dem_set_resort_max((uint32_t)value);
     } else {
         return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);

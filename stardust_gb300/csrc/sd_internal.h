@@ -251,8 +251,9 @@ constexpr uint32_t kClumpFlag = 0x80000000u;
 int dem_key_bits(uint32_t ncells);
 // incremental re-sort (sd_resort.cu): writes the sorted (key, slot) pairs of
 // b.keys into keys_out / vals_out when at most b.rs_max keys changed since
-// the previous sort (the count is rs_scratch[1]); returns at once otherwise
-constexpr uint32_t kResortMaxCap = 16384;  // largest rs_max (the bitonic list fits shared memory)
+// the previous sort (the count is rs_scratch[1]; b.cell_start must still be
+// the previous sort's table); leaves them alone otherwise
+constexpr uint32_t kResortMaxCap = 2048;  // largest rs_max (the moved list is sorted in 16 KB of shared memory)
 uint32_t resort_tiles(uint32_t n);
 uint64_t resort_scratch_words(uint32_t n);
 cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);

@@ -284,12 +284,12 @@ def test_batch_api_rules(sdlib):
 def test_resort_max_knob(sdlib):
     from stardust_gb300 import _abi
     old = _abi.tune_get("resort_max")
-    assert old == 4096
+    assert old == 1024
     try:
-        for v in (0, 1, 2, 256, 16384):
+        for v in (0, 1, 2, 256, 2048):
             _abi.tune_set("resort_max", v)
             assert _abi.tune_get("resort_max") == v
-        for v in (-1, 3, 6000, 32768):
+        for v in (-1, 3, 1000, 4096, 16384):
             with pytest.raises(Exception):
                 _abi.tune_set("resort_max", v)
     finally:
