@@ -400,8 +400,8 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &B.sort_scratch, sd::sort_scratch_words(n, bits))) ||
         (s = dev_alloc(h, &B.dev_status, 8)) || (s = dev_alloc(h, &h->d_energy, 4)) ||
         (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
-        (s = dev_alloc(h, &B.rs_mask, ((size_t)n + 31) / 32)) || (s = dev_alloc(h, &B.rs_wbase, ((size_t)n + 31) / 32)) ||
-        (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_mask, ((size_t)n + 31) / 32)) || (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_slots, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->cfg.flags & SD_FLAG_RECORD) {

@@ -240,9 +240,10 @@ struct DemBuffers {
     uint32_t *bfirst, *bcount;      // per body: first sphere id, number of spheres
     // incremental re-sort (sd_resort.cu): rs_max 0 = the step always radix-sorts
     uint32_t* keys_prev;            // per slot: the sorted key it sits under (written by the reorder)
-    uint32_t *rs_mask, *rs_wbase;   // per 32 slots: moved bits, moved slots before the word
-    unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), rs_max of them
-    uint32_t* rs_scratch;           // ticket, moved count, tile status
+    uint32_t* rs_mask;              // per 32 slots: moved bits
+    unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), up to kResortMaxCap
+    uint32_t* rs_slots;             // their slots in ascending order
+    uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
 };
 
@@ -254,7 +255,6 @@ int dem_key_bits(uint32_t ncells);
 // the previous sort (the count is rs_scratch[1]; b.cell_start must still be
 // the previous sort's table); leaves them alone otherwise
 constexpr uint32_t kResortMaxCap = 2048;  // largest rs_max (the moved list is sorted in 16 KB of shared memory)
-uint32_t resort_tiles(uint32_t n);
 uint64_t resort_scratch_words(uint32_t n);
 cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);
 void dem_set_resort_max(uint32_t m);
