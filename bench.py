@@ -653,7 +653,7 @@ def run_ours(args, rank, world, local):
             "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": st["step_kernels"] * args.steps,
             "contacts": st["contacts"],
             "gjk": gjk,
             "batch": batch,

@@ -100,6 +100,9 @@ typedef struct sd_stats {
      * re-sorts incrementally when at most knob "resort_max" changed, else it
      * runs the radix passes); 0 when the knob is 0 */
     uint64_t moved_keys;
+    /* kernels one step launches (the kernel nodes of the captured step
+     * graph; 0 before the first step) */
+    uint64_t step_kernels;
 } sd_stats;
 
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u

@@ -106,6 +106,7 @@ class SdStats(C.Structure):
         ("gjk_iters", C.c_uint64),
         ("epa_iters", C.c_uint64),
         ("moved_keys", C.c_uint64),
+        ("step_kernels", C.c_uint64),
     ]
 
 

@@ -125,13 +125,13 @@ static sd_status grid_dims(sd_engine* h, const float* lo, const float* hi, float
     return SD_OK;
 }
 
-// z cells per cell edge (knob "z_div"; 0 = automatic): automatically 2 when
-// the finer grid keeps keys within 20 bits and sorts in as many passes as
-// the plain one (a 50 x 50 x 100 grid: 18-bit keys -> 19 bits, 2 passes
-// either way), else 1.  Measured on 1,048,576 spheres, per step: z_div 1
-// 0.216 ms, 2 0.205 ms, 4 0.208 ms (the 10-bit digits of a 20-bit key cost
-// more than the shorter candidate ranges save); on the 2.1M-sphere drum
-// (23-bit keys) any split was slower.
+// z cells per cell edge (knob "z_div"; 0 = automatic): automatically the
+// largest of 4 and 2 whose finer grid keeps keys within 20 bits and sorts in
+// as many passes as the plain one (a 50 x 50 x 100 grid: 18-bit keys -> 20
+// bits at 4, 2 passes either way), else 1.  Measured on 1,048,576 spheres
+// with the incremental re-sort, per step: z_div 1 0.190 ms, 2 0.174 ms,
+// 4 0.169 ms, 8 0.171 ms; on the 2.1M-sphere drum (23-bit keys) any split
+// was slower (1 0.477 ms, 2 0.495 ms, 4 0.541 ms).
 static int32_t g_z_div = 0;
 static int key_bits_of(uint64_t ncells) {
     int b = 1;
@@ -141,8 +141,11 @@ static int key_bits_of(uint64_t ncells) {
 static int32_t z_div_for(uint64_t ncells) {
     if (g_z_div > 0) return ncells * (uint64_t)g_z_div <= (1ull << 30) ? g_z_div : 1;
     const int p0 = sd::sort_num_passes(key_bits_of(ncells));
-    const uint64_t n2 = ncells * 2;
-    return key_bits_of(n2) <= 20 && sd::sort_num_passes(key_bits_of(n2)) == p0 ? 2 : 1;
+    for (int32_t zd = 4; zd >= 2; zd /= 2) {
+        const int bits = key_bits_of(ncells * (uint64_t)zd);
+        if (bits <= 20 && sd::sort_num_passes(bits) == p0) return zd;
+    }
+    return 1;
 }
 
 // A batch: per scene its grid (cell = given or 2 x its largest radius) at
@@ -504,11 +507,25 @@ sd_status build_graph(sd_engine* h, float dt) {
     if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
     if (e3 != cudaSuccess) return cuda_fail(h, e3, "cudaStreamEndCapture");
     cudaError_t e4 = cudaGraphInstantiate(&h->graph, g, 0);
+    h->graph_kernels = graph_kernel_nodes(g);
     cudaGraphDestroy(g);
     if (e4 != cudaSuccess) return cuda_fail(h, e4, "cudaGraphInstantiate");
     h->graph_dt = dt;
     h->graph_valid = true;
     return SD_OK;
+}
+
+uint32_t graph_kernel_nodes(cudaGraph_t g) {
+    size_t count = 0;
+    if (cudaGraphGetNodes(g, nullptr, &count) != cudaSuccess || count == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(count);
+    if (cudaGraphGetNodes(g, nodes.data(), &count) != cudaSuccess) return 0;
+    uint32_t k = 0;
+    for (size_t i = 0; i < count; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
 }
 
 sd_status resort_if_needed(sd_engine* h) {
@@ -1499,6 +1516,7 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
         SD_CUDA(h, cudaMemcpyAsync(&moved, h->B.rs_scratch + 1, 4, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     out->moved_keys = h->steps ? moved : 0;
+    out->step_kernels = h->graph_valid ? h->graph_kernels : 0;
     // bodies: the kernel above counted free spheres only
     const size_t nb = h->B.nb;
     if (nb) {

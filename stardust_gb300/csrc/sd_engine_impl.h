@@ -32,6 +32,7 @@ struct HullScene {
     float graph_dt = 0.0f;
     bool graph_valid = false;
     uint64_t graph_epoch = 0;
+    uint32_t graph_kernels = 0;                   // kernel nodes of one step's graph
 };
 
 struct sd_engine {
@@ -79,6 +80,7 @@ struct sd_engine {
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.0f;
     bool graph_valid = false;
+    uint32_t graph_kernels = 0;  // kernel nodes of the step graph
     uint64_t steps = 0;
     bool need_resort = false;
     // the sorted key arrays hold the cell key of every slot's sphere (true
@@ -92,6 +94,8 @@ struct sd_engine {
 // shared helpers (sd_engine.cu)
 sd_status sd_fail(sd_engine* h, sd_status code, const std::string& msg);
 sd_status sd_cuda_fail(sd_engine* h, cudaError_t e, const char* where);
+// Kernel nodes in a captured graph (the kernels one launch of it runs).
+uint32_t graph_kernel_nodes(cudaGraph_t g);
 sd_status sd_alloc_bytes(sd_engine* h, void** p, size_t bytes);
 float sd_damp_from(float kn, float e);
 uint64_t sd_tune_epoch();

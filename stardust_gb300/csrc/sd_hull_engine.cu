@@ -139,6 +139,7 @@ sd_status build_hull_graphs(sd_engine* h, float dt) {
         if (e != cudaSuccess) return sd_cuda_fail(h, e, "capturing the hull step");
         if (e2 != cudaSuccess) return sd_cuda_fail(h, e2, "cudaStreamEndCapture");
         cudaError_t e3 = cudaGraphInstantiate(&S.graph[par], g, 0);
+        S.graph_kernels = graph_kernel_nodes(g);
         cudaGraphDestroy(g);
         if (e3 != cudaSuccess) return sd_cuda_fail(h, e3, "cudaGraphInstantiate");
     }
@@ -281,6 +282,7 @@ sd_status hull_stats(sd_engine* h, sd_stats* out) {
     out->n_bodies = nb;
     out->n_spheres = 0;
     out->steps = h->steps;
+    out->step_kernels = S.graph_valid ? S.graph_kernels : 0;
     if (!h->prepared) return SD_OK;
     std::vector<float4> x(nb), v(nb), w(nb), L(nb);
     unsigned long long c[4] = {0, 0, 0, 0};

@@ -351,7 +351,7 @@ class DEMEngine:
             "kinetic_energy": s.kinetic_energy, "momentum": tuple(s.momentum),
             "device_errors": s.device_errors, "n_cells": s.n_cells, "n_bodies": s.n_bodies,
             "gjk_pairs": s.gjk_pairs, "gjk_iters": s.gjk_iters, "epa_iters": s.epa_iters,
-            "moved_keys": s.moved_keys,
+            "moved_keys": s.moved_keys, "step_kernels": s.step_kernels,
         }
 
     def params(self) -> dict:

@@ -97,9 +97,9 @@ def test_params_derivation(sdlib):
     eng = sdlib.DEMEngine(cfg)
     eng.add_spheres(pos, vel)
     p = eng.params()
-    # 32^3 cells, z split 2x finer: 16-bit keys still sort in 2 passes
-    assert p["z_div"] == 2 and p["dims"] == (32, 32, 64)
-    assert p["cell"] == pytest.approx(0.02) and p["cell_z"] == pytest.approx(0.01)
+    # 32^3 cells, z split 4x finer: 17-bit keys still sort in 2 passes
+    assert p["z_div"] == 4 and p["dims"] == (32, 32, 128)
+    assert p["cell"] == pytest.approx(0.02) and p["cell_z"] == pytest.approx(0.005)
     # gamma_n = damp sqrt(m_eff); damp = 2 beta sqrt(kn), beta = -ln e / sqrt(pi^2 + ln^2 e)
     le = np.log(0.5)
     beta = -le / np.sqrt(np.pi ** 2 + le ** 2)
@@ -161,8 +161,9 @@ def test_scene_json_cube_entities(sdlib, tmp_path):
 
 
 @pytest.mark.parametrize("knob, box, want", [
-    (0, (1.0, 1.0, 2.0), 2),    # 50 x 50 x 100: 18-bit keys -> 19-bit, 2 passes (10 + 9 bits)
-    (0, (1.4, 1.4, 1.4), 2),    # 70^3: 19 bits -> 20, 2 passes
+    (0, (1.0, 1.0, 2.0), 4),    # 50 x 50 x 100: 18-bit keys -> 20-bit, 2 passes (10 + 10 bits)
+    (0, (0.5, 0.5, 0.5), 4),    # 25^3: 14 bits -> 16, 2 passes
+    (0, (1.4, 1.4, 1.4), 2),    # 70^3: 19 bits -> 20 at x2 (21 at x4: a third pass)
     (0, (1.8, 1.8, 1.8), 1),    # 90^3: 20 bits; x2 would need 21 bits and a third pass
     (0, (5.0, 5.0, 5.0), 1),    # 250^3: 24-bit keys, no split (measured slower on the drum)
     (1, (1.0, 1.0, 2.0), 1),
@@ -197,7 +198,7 @@ def test_scene_json_extensions_and_errors(sdlib, tmp_path):
     eng = sdlib.DEMEngine()
     eng.load_scene_json(f)
     p = eng.params()
-    assert p["dims"] == (20, 20, 80) and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
+    assert p["dims"] == (20, 20, 160) and p["z_div"] == 4 and p["kn"] == pytest.approx(2e5) and p["mu"] == pytest.approx(0.1)
     eng.close()
     for bad, what in (({"scene": {"domain": 1, "colour": 3}}, "colour"),
                       ({"scene": {"entities": [{"type": "cloud", "position": [0, 0, 0], "size": 1, "mass": 1}]}}, "generic"),

@@ -94,3 +94,25 @@ def test_resort_mixes_with_radix_steps(sdlib, orc):
         eng.close()
     finally:
         _abi.tune_set("resort_max", old)
+
+
+def test_step_kernel_count(sdlib):
+    """The step graph runs two re-sort kernels more than the plain radix
+    step (scan, merge); stats report the graph's kernel nodes."""
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("resort_max")
+    counts = {}
+    try:
+        for rm in (0, 1024):
+            _abi.tune_set("resort_max", rm)
+            pos, vel, cfg, dt = moving_scene(20_000, 50, seed=1)
+            eng = sdlib.DEMEngine(cfg)
+            eng.add_spheres(pos, vel)
+            eng.prepare()
+            assert eng.stats()["step_kernels"] == 0
+            eng.step(dt, 2)
+            counts[rm] = eng.stats()["step_kernels"]
+            eng.close()
+    finally:
+        _abi.tune_set("resort_max", old)
+    assert counts[0] >= 4 and counts[1024] == counts[0] + 2
