@@ -515,19 +515,6 @@ sd_status build_graph(sd_engine* h, float dt) {
     return SD_OK;
 }
 
-uint32_t graph_kernel_nodes(cudaGraph_t g) {
-    size_t count = 0;
-    if (cudaGraphGetNodes(g, nullptr, &count) != cudaSuccess || count == 0) return 0;
-    std::vector<cudaGraphNode_t> nodes(count);
-    if (cudaGraphGetNodes(g, nodes.data(), &count) != cudaSuccess) return 0;
-    uint32_t k = 0;
-    for (size_t i = 0; i < count; ++i) {
-        cudaGraphNodeType t;
-        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
-    }
-    return k;
-}
-
 sd_status resort_if_needed(sd_engine* h) {
     if (!h->need_resort) return SD_OK;
     sd::DemBuffers& B = h->B;
@@ -583,6 +570,19 @@ struct SplitMix {
 };
 
 }  // namespace
+
+uint32_t graph_kernel_nodes(cudaGraph_t g) {
+    size_t count = 0;
+    if (cudaGraphGetNodes(g, nullptr, &count) != cudaSuccess || count == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(count);
+    if (cudaGraphGetNodes(g, nodes.data(), &count) != cudaSuccess) return 0;
+    uint32_t k = 0;
+    for (size_t i = 0; i < count; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
 
 namespace sd {
 // Records the message sd_last_error(NULL, ...) returns, for entry points
