@@ -100,10 +100,8 @@ typedef struct sd_stats {
      * re-sorts incrementally when at most knob "resort_max" changed, else it
      * runs the radix passes); 0 when the knob is 0 */
     uint64_t moved_keys;
-    /* kernels one step launches: the kernel nodes of the captured step
-     * graph (0 before the first step), not counting the radix passes in the
-     * conditional node that runs only when the re-sort cannot place the
-     * changed keys */
+    /* kernels one step launches (the kernel nodes of the captured step
+     * graph; 0 before the first step) */
     uint64_t step_kernels;
 } sd_stats;
 

@@ -1250,48 +1250,10 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     // in keys_tmp/vals_tmp for an odd one; the re-sort writes the same place
     // (its kernels read the new keys before any of them is overwritten)
     const bool odd = (plan.passes & 1) != 0;
-    // under capture, the passes go into the body of an IF node that the
-    // re-sort's scan switches on only when it could not place the moves
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaGraph_t cg = nullptr;
-    cudaGraphConditionalHandle cond = 0;
-    if (b.rs_max && b.side) {
-        if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg)) != cudaSuccess) return e;
-        if (cs == cudaStreamCaptureStatusActive &&
-            (e = cudaGraphConditionalHandleCreate(&cond, cg, 1u, cudaGraphCondAssignDefault)) != cudaSuccess)
-            return e;
-    }
-    if ((e = resort_async(b, odd ? b.keys_tmp : b.keys, odd ? b.vals_tmp : b.vals, cond, st)) != cudaSuccess)
+    if ((e = resort_async(b, odd ? b.keys_tmp : b.keys, odd ? b.vals_tmp : b.vals, st)) != cudaSuccess) return e;
+    if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
+                               &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
-    if (cond) {
-        const cudaGraphNode_t* deps = nullptr;
-        const cudaGraphEdgeData* edges = nullptr;
-        size_t ndeps = 0;
-        if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &edges, &ndeps)) != cudaSuccess) return e;
-        cudaGraphNodeParams np = {};
-        np.type = cudaGraphNodeTypeConditional;
-        np.conditional.handle = cond;
-        np.conditional.type = cudaGraphCondTypeIf;
-        np.conditional.size = 1;
-        cudaGraphNode_t node = nullptr;
-        if ((e = cudaGraphAddNode(&node, cg, deps, edges, ndeps, &np)) != cudaSuccess) return e;
-        if ((e = cudaStreamBeginCaptureToGraph(b.side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                               cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-            return e;
-        cudaError_t ep = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, b.side,
-                                           &b.sorted_in_tmp, b.rs_scratch, b.rs_max);
-        cudaGraph_t body = nullptr;
-        e = cudaStreamEndCapture(b.side, &body);
-        if (ep != cudaSuccess) return ep;
-        if (e != cudaSuccess) return e;
-        if ((e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
-            cudaSuccess)
-            return e;
-    } else if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
-                                      &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) !=
-               cudaSuccess) {
-        return e;
-    }
     if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
     return mesh_advance_async(b.mesh, 1, st);
 }

@@ -100,7 +100,6 @@ void release_device(sd_engine* h) {
     h->graph_valid = false;
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
-    if (h->B.side) cudaStreamDestroy(h->B.side);
     h->B = sd::DemBuffers{};
     h->d_energy = nullptr;
     h->d_tmp = nullptr;
@@ -469,7 +468,6 @@ sd_status prepare_with(sd_engine* h, const float4* pos, const float4* vel, const
     if (h->device >= ndev) return fail(h, SD_ERR_INVALID_ARG, "cuda_device out of range");
     SD_CUDA(h, cudaSetDevice(h->device));
     SD_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-    SD_CUDA(h, cudaStreamCreateWithFlags(&h->B.side, cudaStreamNonBlocking));
     SD_CUDA(h, sd::dem_init_kernels());
     if ((s = allocate(h, n))) {
         release_device(h);

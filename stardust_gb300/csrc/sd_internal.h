@@ -245,7 +245,6 @@ struct DemBuffers {
     uint32_t* rs_slots;             // their slots in ascending order
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
-    cudaStream_t side;              // captures the radix passes into the step graph's conditional body
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
@@ -257,10 +256,7 @@ int dem_key_bits(uint32_t ncells);
 // the previous sort's table); leaves them alone otherwise
 constexpr uint32_t kResortMaxCap = 2048;  // largest rs_max (the moved list is sorted in 16 KB of shared memory)
 uint64_t resort_scratch_words(uint32_t n);
-// cond: a conditional-node handle of the graph being captured, or 0; the
-// scan sets it to 1 when the radix passes must run (more than rs_max moved)
-cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaGraphConditionalHandle cond,
-                         cudaStream_t st);
+cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture

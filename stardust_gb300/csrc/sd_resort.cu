@@ -23,10 +23,8 @@
 //
 // The unmoved slots are already in (key, slot) order, so this is a merge of
 // two sorted sequences and the result is exactly the stable LSD sort's.
-// When more than `mmax` keys change the step's radix passes run instead and
-// the merge returns.  In the step graph the passes sit in the body of a
-// conditional node that the scan's last block switches on; run outside a
-// graph they are launched anyway and return at once when not needed.
+// When more than `mmax` keys change the step's radix passes run instead (they
+// are in the graph and return at once otherwise) and the merge returns.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -65,7 +63,7 @@ __device__ void bitonic_sort(unsigned long long* v, uint32_t P) {
 __global__ void __launch_bounds__(kRsThreads)
 resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __restrict__ keys_prev, uint32_t n,
                    uint32_t* __restrict__ mask, unsigned long long* __restrict__ list, uint32_t* __restrict__ slots,
-                   uint32_t mmax, uint32_t* __restrict__ scratch, cudaGraphConditionalHandle cond) {
+                   uint32_t mmax, uint32_t* __restrict__ scratch) {
     __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
     __shared__ unsigned long long s_list[kResortMaxCap];
     const uint32_t w = threadIdx.x / kWarp, lane = lane_id();
@@ -116,7 +114,6 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
         scratch[1] = M;
         scratch[0] = 0u;
         scratch[2] = 0u;
-        if (cond) cudaGraphSetConditional(cond, M > mmax ? 1u : 0u);  // run the radix passes?
     }
     if (M == 0 || M > mmax) return;
     uint32_t P = 2;
@@ -193,14 +190,13 @@ uint32_t dem_resort_max() { return g_resort_max; }
 
 uint64_t resort_scratch_words(uint32_t) { return 4; }
 
-cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaGraphConditionalHandle cond,
-                         cudaStream_t st) {
+cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st) {
     const uint32_t n = b.n, mmax = b.rs_max;
     if (n == 0 || mmax == 0) return cudaSuccess;
     if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
     const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
     resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, mmax,
-                                                      b.rs_scratch, cond);
+                                                      b.rs_scratch);
     resort_merge_kernel<<<(n + kRsThreads - 1) / kRsThreads, kRsThreads, 0, st>>>(
         b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, b.rs_scratch, mmax, b.cell_start, b.ncells, keys_out,
         vals_out);
