@@ -505,7 +505,7 @@ def run_ours(args, rank, world, local):
         tuned = autotune.tune_engine(eng, dt, reps=5)
         log(f"autotune: {tuned}")
     # the knobs this workload is timed with (later sections tune their own)
-    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max", "pdl")}
+    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max")}
 
     def barrier():
         torch.cuda.synchronize()
@@ -690,16 +690,10 @@ def main():
     ap.add_argument("--only-sap", action="store_true", help="run only the sweep-and-prune section")
     ap.add_argument("--z-div", type=int, default=None,
                     help="z cells per cell edge for every engine (default: the library's automatic choice)")
-    ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
-                    help="set a launch knob (sd_tune_set) before anything runs; repeatable")
     args = ap.parse_args()
-    if args.z_div is not None or args.knob:
+    if args.z_div is not None:
         from stardust_gb300 import _abi
-        if args.z_div is not None:
-            _abi.tune_set("z_div", args.z_div)
-        for kv in args.knob:
-            name, value = kv.split("=", 1)
-            _abi.tune_set(name, int(value))
+        _abi.tune_set("z_div", args.z_div)
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3

@@ -461,10 +461,7 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *   "resort_max"    most changed cell keys the step re-sorts incrementally (a merge of
  *                   the changed entries into the previous order) instead of running the
  *                   radix passes: 0 (always the passes) or a power of two up to 2048;
- *                   default 1024.  Same result either way (a stable sort by key)
- *   "pdl"           1 (default): the step graph's kernels launch as programmatic
- *                   dependents (each starts while its predecessor's last blocks run and
- *                   waits for its completion before reading anything); 0: plain launches */
+ *                   default 1024.  Same result either way (a stable sort by key) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

@@ -11,8 +11,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <utility>
-
 #include "../../include/stardust.h"
 #include "sd_internal.h"
 
@@ -40,36 +38,6 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
-}
-
-// Programmatic dependent launch.  A kernel of the step chain calls
-// pdl_wait() before anything else: it returns once the preceding kernel has
-// completed and its writes are visible (at once when the launch was not
-// programmatic), so completion of any kernel of the chain implies completion
-// of every earlier one.  pdl_trigger() lets the next kernel's blocks be
-// scheduled while this kernel's last blocks still run.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-// Launches k, as a programmatic dependent of the stream's previous kernel
-// when pdl is set.
-template <typename... K, typename... A>
-cudaError_t launch_k(bool pdl, void (*k)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
-    if (!pdl) {
-        k<<<grid, block, smem, st>>>(std::forward<A>(args)...);
-        return cudaGetLastError();
-    }
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & (kWarp - 1); }

@@ -552,7 +552,6 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
                              ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{}) {
     __shared__ uint32_t s_hist[kHistWords];
-    pdl_trigger();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
@@ -635,7 +634,6 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
     __shared__ uint32_t s_hist[kHistWords];
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ uint32_t s_beg[9], s_cnt[9], s_shift[9], s_total;
-    pdl_trigger();
 
     const int32_t X = (int32_t)blockIdx.x / p.ny, Y = (int32_t)blockIdx.x % p.ny;
     if (threadIdx.x < 9) {
@@ -835,8 +833,6 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
                 float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
                 uint32_t hist_spec, uint32_t* __restrict__ ghist) {
     __shared__ uint32_t s_hist[kHistWords];
-    pdl_wait();
-    pdl_trigger();
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
@@ -876,8 +872,6 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
                    uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
                    uint32_t* __restrict__ keys_prev) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
-    pdl_wait();
-    pdl_trigger();
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
     const uint32_t k = b0 + threadIdx.x;
@@ -1055,7 +1049,6 @@ __global__ void dem_energy_kernel(uint32_t n, const float4* __restrict__ pos, co
 // product), then the rotation matrix of q (the expression of the rigid
 // bodies).
 __global__ void mesh_advance_kernel(float* __restrict__ S, int advance) {
-    pdl_wait();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     float qs = S[16], qx = S[17], qy = S[18], qz = S[19];
     if (advance) {
@@ -1087,9 +1080,10 @@ __global__ void mesh_advance_kernel(float* __restrict__ S, int advance) {
 
 static inline unsigned grid_for(uint32_t n, unsigned threads) { return (n + threads - 1) / threads; }
 
-cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st, bool pdl) {
+cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st) {
     if (m.ntri == 0) return cudaSuccess;
-    return launch_k(pdl, mesh_advance_kernel, dim3(1), dim3(32), 0, st, m.state, advance);
+    mesh_advance_kernel<<<1, 32, 0, st>>>(m.state, advance);
+    return cudaGetLastError();
 }
 
 cudaError_t dem_init_kernels() {
@@ -1149,13 +1143,14 @@ cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
                             st, &b.sorted_in_tmp);
 }
 
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool pdl) {
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
     const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
-    return launch_k(pdl, dem_reorder_kernel, dim3(grid_for(b.n, kReorderThreads)), dim3(kReorderThreads), 0, st, b.n,
-                    b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
-                    b.nb ? b.slot_of : nullptr, b.keys_prev);
+    dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
+        b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
+        b.nb ? b.slot_of : nullptr, b.keys_prev);
+    return cudaGetLastError();
 }
 
 cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {
@@ -1225,11 +1220,9 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
         launch_contact_t<false>(p, b, spec, ghist, st);
     }
     if (b.nb) {
-        cudaError_t e = launch_k(b.pdl && ghist, dem_body_kernel, dim3(grid_for(b.nb, 128)), dim3(128), 0, st, p,
-                                 b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0,
-                                 b.slot_of, b.pos, b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n,
-                                 spec, ghist);
-        if (e != cudaSuccess) return e;
+        dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
+            p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
+            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n, spec, ghist);
     }
     return cudaGetLastError();
 }
@@ -1259,10 +1252,10 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     const bool odd = (plan.passes & 1) != 0;
     if ((e = resort_async(b, odd ? b.keys_tmp : b.keys, odd ? b.vals_tmp : b.vals, st)) != cudaSuccess) return e;
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
-                               &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max, b.pdl)) != cudaSuccess)
+                               &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
-    if ((e = dem_reorder_async(b, st, b.pdl)) != cudaSuccess) return e;
-    return mesh_advance_async(b.mesh, 1, st, b.pdl);
+    if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
+    return mesh_advance_async(b.mesh, 1, st);
 }
 
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {

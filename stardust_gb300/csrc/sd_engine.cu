@@ -502,9 +502,7 @@ sd_status build_graph(sd_engine* h, float dt) {
     cudaGraph_t g = nullptr;
     SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     h->B.rs_max = sd::dem_resort_max();
-    h->B.pdl = sd::dem_pdl();
     cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
-    h->B.pdl = false;  // launches outside the step graph stay ordinary
     cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
     if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
     if (e3 != cudaSuccess) return cuda_fail(h, e3, "cudaStreamEndCapture");
@@ -1261,9 +1259,6 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)
             return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 2048");
         sd::dem_set_resort_max((uint32_t)value);
-    } else if (k == "pdl") {
-        if (value != 0 && value != 1) return fail(nullptr, SD_ERR_INVALID_ARG, "pdl must be 0 or 1");
-        sd::dem_set_pdl(value != 0);
     } else {
         return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     }
@@ -1278,7 +1273,6 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "sort_items") *value = sd::sort_items();
     else if (k == "z_div") *value = g_z_div;
     else if (k == "resort_max") *value = (int32_t)sd::dem_resort_max();
-    else if (k == "pdl") *value = sd::dem_pdl() ? 1 : 0;
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }

@@ -42,8 +42,7 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
 // (the incremental re-sort has written the result)
 cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                               uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
-                              bool* in_tmp, const uint32_t* skip = nullptr, uint32_t skip_max = 0,
-                              bool pdl = false);
+                              bool* in_tmp, const uint32_t* skip = nullptr, uint32_t skip_max = 0);
 cudaError_t sort_pairs_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                              uint32_t n, int key_bits, uint32_t* scratch, cudaStream_t st,
                              bool* in_tmp);
@@ -246,7 +245,6 @@ struct DemBuffers {
     uint32_t* rs_slots;             // their slots in ascending order
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
-    bool pdl;                       // the step's kernels launch as programmatic dependents
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
@@ -261,15 +259,13 @@ uint64_t resort_scratch_words(uint32_t n);
 cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
-void dem_set_pdl(bool on);
-bool dem_pdl();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
 // Counts, into *count (device), the slots whose key from the current position
 // differs from the sorted key they sit under.
 cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st);
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool pdl = false);
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record,
                                         cudaStream_t st);
@@ -290,6 +286,6 @@ cudaError_t dem_scatter_in_async(const float4* src_by_id, const float4* omg, flo
                                  cudaStream_t st);
 cudaError_t dem_energy_async(const DemBuffers& b, double* d_out, cudaStream_t st);
 // advance != 0: q <- normalize(dq q); then R <- R(q)
-cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st, bool pdl = false);
+cudaError_t mesh_advance_async(const MeshView& m, int advance, cudaStream_t st);
 
 }  // namespace sd

@@ -66,8 +66,6 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
                    uint32_t mmax, uint32_t* __restrict__ scratch) {
     __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
     __shared__ unsigned long long s_list[kResortMaxCap];
-    pdl_wait();
-    pdl_trigger();
     const uint32_t w = threadIdx.x / kWarp, lane = lane_id();
     const uint32_t nwords = (n + 31) / 32;
     const uint32_t word0 = blockIdx.x * kRsBlockWords + w * kRsWordsPerWarp;
@@ -148,8 +146,6 @@ resort_merge_kernel(const uint32_t* __restrict__ keys_prev, uint32_t n, const ui
                     const unsigned long long* __restrict__ list, const uint32_t* __restrict__ slots,
                     const uint32_t* __restrict__ scratch, uint32_t mmax, const uint32_t* __restrict__ cell_start,
                     uint32_t ncells, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out) {
-    pdl_wait();
-    pdl_trigger();
     const uint32_t M = scratch[1];
     if (M > mmax) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -188,12 +184,9 @@ resort_merge_kernel(const uint32_t* __restrict__ keys_prev, uint32_t n, const ui
 }  // namespace
 
 static uint32_t g_resort_max = 1024;
-static bool g_pdl = true;
 
 void dem_set_resort_max(uint32_t m) { g_resort_max = m; }
 uint32_t dem_resort_max() { return g_resort_max; }
-void dem_set_pdl(bool on) { g_pdl = on; }
-bool dem_pdl() { return g_pdl; }
 
 uint64_t resort_scratch_words(uint32_t) { return 4; }
 
@@ -202,13 +195,12 @@ cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals
     if (n == 0 || mmax == 0) return cudaSuccess;
     if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
     const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
-    cudaError_t e = launch_k(b.pdl, resort_scan_kernel, dim3(blocks), dim3(kRsThreads), 0, st, b.keys, b.keys_prev, n,
-                             b.rs_mask, b.rs_list, b.rs_slots, mmax, b.rs_scratch);
-    if (e != cudaSuccess) return e;
-    return launch_k(b.pdl, resort_merge_kernel, dim3((n + kRsThreads - 1) / kRsThreads), dim3(kRsThreads), 0, st,
-                    (const uint32_t*)b.keys_prev, n, (const uint32_t*)b.rs_mask, (const unsigned long long*)b.rs_list,
-                    (const uint32_t*)b.rs_slots, (const uint32_t*)b.rs_scratch, mmax, (const uint32_t*)b.cell_start,
-                    b.ncells, keys_out, vals_out);
+    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, mmax,
+                                                      b.rs_scratch);
+    resort_merge_kernel<<<(n + kRsThreads - 1) / kRsThreads, kRsThreads, 0, st>>>(
+        b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, b.rs_scratch, mmax, b.cell_start, b.ncells, keys_out,
+        vals_out);
+    return cudaGetLastError();
 }
 
 }  // namespace sd

@@ -104,8 +104,6 @@ sort_pass_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restric
                  uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                  int shift, int bits, int pass, uint32_t num_tiles, uint32_t stride,
                  uint32_t* __restrict__ scratch, const uint32_t* __restrict__ skip, uint32_t skip_max) {
-    pdl_wait();
-    pdl_trigger();
     if (skip && skip[1] <= skip_max) return;  // the incremental re-sort wrote the result
     constexpr int TILE = kSortThreads * ITEMS;
     constexpr int DPT = BINS / kSortThreads;  // digits per thread (1, 2 or 4)
@@ -310,23 +308,23 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
 template <int BINS, int ITEMS>
 static cudaError_t launch_pass(const uint32_t* ki, const uint32_t* vi, uint32_t* ko, uint32_t* vo,
                                uint32_t n, int shift, int bits, int pass, uint32_t tiles, uint32_t stride,
-                               uint32_t* scratch, cudaStream_t st, const uint32_t* skip, uint32_t skip_max,
-                               bool pdl) {
+                               uint32_t* scratch, cudaStream_t st, const uint32_t* skip, uint32_t skip_max) {
     size_t sm = pass_smem_bytes<BINS, ITEMS>();
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel<BINS, ITEMS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    return launch_k(pdl, sort_pass_kernel<BINS, ITEMS>, dim3(tiles), dim3(kSortThreads), sm, st, ki, vi, ko, vo, n,
-                    shift, bits, pass, tiles, stride, scratch, skip, skip_max);
+    sort_pass_kernel<BINS, ITEMS><<<tiles, kSortThreads, sm, st>>>(ki, vi, ko, vo, n, shift, bits,
+                                                                   pass, tiles, stride, scratch, skip, skip_max);
+    return cudaGetLastError();
 }
 
 // The digit passes alone: the histograms in scratch must be complete and the
 // tile status cleared (sort_clear_async + a histogram producer).
 cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                               uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
-                              bool* in_tmp, const uint32_t* skip, uint32_t skip_max, bool pdl) {
+                              bool* in_tmp, const uint32_t* skip, uint32_t skip_max) {
     *in_tmp = false;
     if (n == 0) return cudaSuccess;
     const uint32_t tiles = num_tiles(n);
@@ -336,13 +334,13 @@ cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp
         const int b = plan.bits[p], sh = plan.shift[p];
         const uint32_t sd = (uint32_t)plan.stride;
         if (g_sort_items >= 16)
-            e = b > 9   ? launch_pass<1024, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl)
-                : b > 8 ? launch_pass<512, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl)
-                        : launch_pass<256, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl);
+            e = b > 9   ? launch_pass<1024, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                : b > 8 ? launch_pass<512, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                        : launch_pass<256, 16>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max);
         else
-            e = b > 9   ? launch_pass<1024, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl)
-                : b > 8 ? launch_pass<512, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl)
-                        : launch_pass<256, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max, pdl);
+            e = b > 9   ? launch_pass<1024, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                : b > 8 ? launch_pass<512, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max)
+                        : launch_pass<256, 8>(ki, vi, ko, vo, n, sh, b, p, tiles, sd, scratch, st, skip, skip_max);
         if (e != cudaSuccess) return e;
         uint32_t* t;
         t = ki; ki = ko; ko = t;

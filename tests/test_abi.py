@@ -295,17 +295,3 @@ def test_resort_max_knob(sdlib):
                 _abi.tune_set("resort_max", v)
     finally:
         _abi.tune_set("resort_max", old)
-
-
-def test_pdl_knob(sdlib):
-    from stardust_gb300 import _abi
-    old = _abi.tune_get("pdl")
-    assert old in (0, 1)
-    try:
-        for v in (0, 1):
-            _abi.tune_set("pdl", v)
-            assert _abi.tune_get("pdl") == v
-        with pytest.raises(Exception):
-            _abi.tune_set("pdl", 2)
-    finally:
-        _abi.tune_set("pdl", old)

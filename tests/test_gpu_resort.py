@@ -116,28 +116,3 @@ def test_step_kernel_count(sdlib):
     finally:
         _abi.tune_set("resort_max", old)
     assert counts[0] >= 4 and counts[1024] == counts[0] + 2
-
-
-@pytest.mark.parametrize("pdl", [0, 1])
-def test_programmatic_launch_knob_bit_exact(sdlib, orc, pdl):
-    """The step's kernels launched as programmatic dependents or plainly:
-    the same bits either way (every kernel waits for its predecessor)."""
-    from stardust_gb300 import _abi
-    old = _abi.tune_get("pdl")
-    try:
-        _abi.tune_set("pdl", pdl)
-        n = 30_000
-        pos, vel, cfg, dt = moving_scene(n, 300, seed=4)
-        eng = sdlib.DEMEngine(cfg)
-        eng.add_spheres(pos, vel)
-        eng.prepare()
-        eng.step(dt, 15)
-        eng.sync()
-        assert eng.stats()["device_errors"] == 0
-        p = orc.params_from_engine(eng.params(), dt)
-        op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)), 15)
-        assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
-        assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))
-        eng.close()
-    finally:
-        _abi.tune_set("pdl", old)
