@@ -690,10 +690,16 @@ def main():
     ap.add_argument("--only-sap", action="store_true", help="run only the sweep-and-prune section")
     ap.add_argument("--z-div", type=int, default=None,
                     help="z cells per cell edge for every engine (default: the library's automatic choice)")
+    ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
+                    help="set a launch knob (sd_tune_set) before anything runs; repeatable")
     args = ap.parse_args()
-    if args.z_div is not None:
+    if args.z_div is not None or args.knob:
         from stardust_gb300 import _abi
-        _abi.tune_set("z_div", args.z_div)
+        if args.z_div is not None:
+            _abi.tune_set("z_div", args.z_div)
+        for kv in args.knob:
+            name, value = kv.split("=", 1)
+            _abi.tune_set(name, int(value))
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
