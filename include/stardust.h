@@ -460,7 +460,7 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   sort's pass count, else 1; a batch of scenes always uses 1
  *   "resort_max"    most changed cell keys the step re-sorts incrementally (a merge of
  *                   the changed entries into the previous order) instead of running the
- *                   radix passes: 0 (always the passes) or a power of two up to 2048;
+ *                   radix passes: 0 (always the passes) or a power of two up to 1024;
  *                   default 1024.  Same result either way (a stable sort by key) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);

@@ -859,6 +859,54 @@ __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restric
 
 constexpr int kReorderThreads = 256;
 
+// The order the incremental re-sort found, read in place of sorted arrays:
+// the new keys, and the moved entries in (key, slot) order with their
+// sorted positions and, per moved slot in ascending order, slot - rank.
+struct ResortView {
+    const uint32_t* keys_new;
+    const uint32_t* pos;
+    const uint32_t* q;
+    const unsigned long long* list;
+    const uint32_t* scratch;  // null: read the sorted arrays
+    uint32_t mmax;
+};
+
+// Source slot and key of sorted position k.  From the re-sort: a moved
+// entry sits at its recorded position; the others keep their order, so
+// position k holds unmoved rank u = k - (moved entries placed before k),
+// which is slot u + (moved slots s_j with s_j - j <= u).  An unmoved slot's
+// new key is its previous one.
+__device__ __forceinline__ void sorted_entry(uint32_t k, bool inc, uint32_t M, const ResortView& rv,
+                                             const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                             uint32_t n, uint32_t& src, uint32_t& key) {
+    if (!inc) {
+        src = vals[k];
+        key = keys[k];
+        return;
+    }
+    uint32_t lo = 0, hi = M;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rv.pos[mid] < k) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < M && rv.pos[lo] == k) {
+        const unsigned long long c = rv.list[lo];
+        key = (uint32_t)(c >> 32);
+        src = (uint32_t)c;
+        return;
+    }
+    const uint32_t u = k - lo;
+    uint32_t a = 0, z = M;
+    while (a < z) {
+        const uint32_t mid = (a + z) >> 1;
+        if (rv.q[mid] <= u) a = mid + 1;
+        else z = mid;
+    }
+    src = u + a;
+    key = src < n ? rv.keys_new[src] : 0u;
+}
+
 // Gather the next state into sorted order and write cell_start.  Block b
 // owns slots [b0, b1) and the cells (key[b0-1], key[b1-1]] (the first block
 // starts at cell 0, the last ends at ncells), so every cell's lower bound is
@@ -870,13 +918,16 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
                    const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
                    float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
                    uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
-                   uint32_t* __restrict__ keys_prev) {
+                   uint32_t* __restrict__ keys_prev, ResortView rv) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
     const uint32_t k = b0 + threadIdx.x;
+    const uint32_t M = rv.scratch ? rv.scratch[1] : 0u;
+    const bool inc = rv.scratch && M <= rv.mmax;
     if (k < n) {
-        const uint32_t src = vals[k];
+        uint32_t src, key;
+        sorted_entry(k, inc, M, rv, keys, vals, n, src, key);
         if (src < n) {  // always true for a valid permutation
             pos[k] = pos_n[src];
             vel[k] = vel_n[src];
@@ -886,11 +937,14 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
             const uint32_t idb = __float_as_uint(o.w);
             if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
         }
-        const uint32_t key = keys[k];
         s_keys[threadIdx.x + 1] = key;
         keys_prev[k] = key;  // what the next step's incremental re-sort compares against
     }
-    if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
+    if (threadIdx.x == 0) {
+        uint32_t src0 = 0, key0 = 0;
+        if (b0 > 0) sorted_entry(b0 - 1, inc, M, rv, keys, vals, n, src0, key0);
+        s_keys[0] = key0;
+    }
     __syncthreads();
     const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
     const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
@@ -1143,13 +1197,15 @@ cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
                             st, &b.sorted_in_tmp);
 }
 
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool incremental) {
     if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
     const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
+    ResortView rv{};
+    if (incremental && b.rs_max) rv = ResortView{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
     dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
         b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
-        b.nb ? b.slot_of : nullptr, b.keys_prev);
+        b.nb ? b.slot_of : nullptr, b.keys_prev, rv);
     return cudaGetLastError();
 }
 
@@ -1246,15 +1302,13 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
     if (e != cudaSuccess) return e;
     if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
-    // the passes leave their result in keys/vals for an even pass count,
-    // in keys_tmp/vals_tmp for an odd one; the re-sort writes the same place
-    // (its kernels read the new keys before any of them is overwritten)
-    const bool odd = (plan.passes & 1) != 0;
-    if ((e = resort_async(b, odd ? b.keys_tmp : b.keys, odd ? b.vals_tmp : b.vals, st)) != cudaSuccess) return e;
+    // the re-sort places the moved keys when it can (the passes then return
+    // at once and the reorder reads its order), else the passes sort
+    if ((e = resort_async(b, st)) != cudaSuccess) return e;
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
                                &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
-    if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
+    if ((e = dem_reorder_async(b, st, true)) != cudaSuccess) return e;
     return mesh_advance_async(b.mesh, 1, st);
 }
 

@@ -403,8 +403,8 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &B.sort_scratch, sd::sort_scratch_words(n, bits))) ||
         (s = dev_alloc(h, &B.dev_status, 8)) || (s = dev_alloc(h, &h->d_energy, 4)) ||
         (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
-        (s = dev_alloc(h, &B.rs_mask, ((size_t)n + 31) / 32)) || (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
-        (s = dev_alloc(h, &B.rs_slots, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_pos, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_q, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->cfg.flags & SD_FLAG_RECORD) {
@@ -1257,7 +1257,7 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         g_z_div = value;
     } else if (k == "resort_max") {
         if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)
-            return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 2048");
+            return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 1024");
         sd::dem_set_resort_max((uint32_t)value);
     } else {
         return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);

@@ -240,9 +240,9 @@ struct DemBuffers {
     uint32_t *bfirst, *bcount;      // per body: first sphere id, number of spheres
     // incremental re-sort (sd_resort.cu): rs_max 0 = the step always radix-sorts
     uint32_t* keys_prev;            // per slot: the sorted key it sits under (written by the reorder)
-    uint32_t* rs_mask;              // per 32 slots: moved bits
     unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), up to kResortMaxCap
-    uint32_t* rs_slots;             // their slots in ascending order
+    uint32_t* rs_pos;               // per moved entry (in (key, slot) order): its sorted position
+    uint32_t* rs_q;                 // per moved slot (ascending): slot - rank
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
 };
@@ -250,13 +250,14 @@ struct DemBuffers {
 constexpr uint32_t kClumpFlag = 0x80000000u;
 
 int dem_key_bits(uint32_t ncells);
-// incremental re-sort (sd_resort.cu): writes the sorted (key, slot) pairs of
-// b.keys into keys_out / vals_out when at most b.rs_max keys changed since
-// the previous sort (the count is rs_scratch[1]; b.cell_start must still be
-// the previous sort's table); leaves them alone otherwise
-constexpr uint32_t kResortMaxCap = 2048;  // largest rs_max (the moved list is sorted in 16 KB of shared memory)
+// incremental re-sort (sd_resort.cu): when at most b.rs_max keys of b.keys
+// changed since the previous sort (the count is rs_scratch[1]; b.cell_start
+// must still be the previous sort's table), lists the moved entries in
+// (key, slot) order with their sorted positions, which the reorder turns
+// into the sorted order (ResortView); does nothing else otherwise
+constexpr uint32_t kResortMaxCap = 1024;  // largest rs_max (two sorted lists in 16 KB of shared memory)
 uint64_t resort_scratch_words(uint32_t n);
-cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st);
+cudaError_t resort_async(const DemBuffers& b, cudaStream_t st);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
@@ -265,7 +266,8 @@ cudaError_t dem_init_kernels();  // once per device, outside stream capture
 cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st);
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
+// incremental: take the order from the re-sort when it placed the moves
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool incremental = false);
 cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record,
                                         cudaStream_t st);

@@ -7,24 +7,24 @@
 // it can be built without a radix sort:
 //
 //   1. resort_scan_kernel: per block of 4096 slots, the slots whose new key
-//      differs from the sorted key they sit under ("moved"), as one bit per
-//      slot, and the moved entries (key << 32 | slot) appended to a list
-//      (one atomic per block: the list's order does not matter, it is
-//      sorted next).  The last block to finish (a fence and an arrival
-//      counter, no waiting) publishes the count M and sorts the list twice
-//      in shared memory (bitonic): by (key, slot), and by slot alone;
-//   2. resort_merge_kernel: an unmoved slot i keeps its key; its place is i
-//      minus the moved slots before it (a binary search in the slot-sorted
-//      list) plus the moved entries that sort before (key_i << 32 | i).
-//      Moved entry r (rank r among the moved) goes to r plus the unmoved
-//      slots that sort before it: the previous step's cell table bounds the
-//      slots of its key, so that count is the clamped slot minus the moved
-//      slots before it.
+//      differs from the sorted key they sit under ("moved"), appended to a
+//      list as (key << 32 | slot) (one atomic per block: the list's order
+//      does not matter, it is sorted next).  The last block to finish (a
+//      fence and an arrival counter, no waiting) publishes the count M and,
+//      in shared memory, sorts the list by (key, slot) and the moved slots
+//      alone (bitonic); moved entry r (rank r in (key, slot) order) goes to
+//      r plus the unmoved slots that sort before it -- the previous step's
+//      cell table bounds the slots of its key, so that count is its slot
+//      clamped to that range minus the moved slots below it;
+//   2. the reorder (dem_reorder_kernel) reads the order from these lists:
+//      position k holds a moved entry where one was placed, else the
+//      unmoved slot of rank k - (moved entries placed before k).
 //
 // The unmoved slots are already in (key, slot) order, so this is a merge of
 // two sorted sequences and the result is exactly the stable LSD sort's.
 // When more than `mmax` keys change the step's radix passes run instead (they
-// are in the graph and return at once otherwise) and the merge returns.
+// are in the graph and return at once otherwise) and the reorder reads their
+// sorted arrays.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -62,12 +62,12 @@ __device__ void bitonic_sort(unsigned long long* v, uint32_t P) {
 // [2] arrivals.  [0] and [2] are zero again when the kernel ends.
 __global__ void __launch_bounds__(kRsThreads)
 resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __restrict__ keys_prev, uint32_t n,
-                   uint32_t* __restrict__ mask, unsigned long long* __restrict__ list, uint32_t* __restrict__ slots,
-                   uint32_t mmax, uint32_t* __restrict__ scratch) {
+                   unsigned long long* __restrict__ list, uint32_t* __restrict__ pos_out, uint32_t* __restrict__ q_out,
+                   uint32_t mmax, uint32_t* __restrict__ scratch, const uint32_t* __restrict__ cell_start,
+                   uint32_t ncells) {
     __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
-    __shared__ unsigned long long s_list[kResortMaxCap];
+    __shared__ unsigned long long s_a[kResortMaxCap], s_b[kResortMaxCap];
     const uint32_t w = threadIdx.x / kWarp, lane = lane_id();
-    const uint32_t nwords = (n + 31) / 32;
     const uint32_t word0 = blockIdx.x * kRsBlockWords + w * kRsWordsPerWarp;
     uint32_t m[kRsWordsPerWarp];
     uint32_t cnt = 0;
@@ -86,19 +86,18 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
         s_base = tot ? atomicAdd(&scratch[0], tot) : 0u;
     }
     __syncthreads();
-    uint32_t rank0 = s_base;
-    for (uint32_t v = 0; v < w; ++v) rank0 += s_wcnt[v];
+    if (cnt) {
+        uint32_t rank0 = s_base;
+        for (uint32_t v = 0; v < w; ++v) rank0 += s_wcnt[v];
 #pragma unroll
-    for (uint32_t j = 0; j < kRsWordsPerWarp; ++j) {
-        const uint32_t word = word0 + j;
-        if (word >= nwords) break;
-        if (lane == 0) mask[word] = m[j];
-        if ((m[j] >> lane) & 1u) {
-            const uint32_t rank = rank0 + __popc(m[j] & lanemask_lt());
-            const uint32_t s = word * 32 + lane;
-            if (rank < mmax) list[rank] = ((unsigned long long)keys_new[s] << 32) | s;
+        for (uint32_t j = 0; j < kRsWordsPerWarp; ++j) {
+            if ((m[j] >> lane) & 1u) {
+                const uint32_t rank = rank0 + __popc(m[j] & lanemask_lt());
+                const uint32_t s = (word0 + j) * 32 + lane;
+                if (rank < mmax) list[rank] = ((unsigned long long)keys_new[s] << 32) | s;
+            }
+            rank0 += __popc(m[j]);
         }
-        rank0 += __popc(m[j]);
     }
     // the last block to arrive sees every block's count and list entries
     __syncthreads();
@@ -118,66 +117,30 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
     if (M == 0 || M > mmax) return;
     uint32_t P = 2;
     while (P < M) P <<= 1;
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_list[i] = i < M ? __ldcg(&list[i]) : ~0ull;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_a[i] = i < M ? __ldcg(&list[i]) : ~0ull;
     __syncthreads();
-    bitonic_sort(s_list, P);
-    for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) list[i] = s_list[i];
+    bitonic_sort(s_a, P);
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_b[i] = i < M ? (s_a[i] & 0xffffffffull) : ~0ull;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_list[i] = i < M ? (s_list[i] & 0xffffffffull) : ~0ull;
-    __syncthreads();
-    bitonic_sort(s_list, P);
-    for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) slots[i] = (uint32_t)s_list[i];
-}
-
-// Moved slots below slot x: the first index of the slot-sorted list whose
-// slot is >= x.
-__device__ __forceinline__ uint32_t moved_before(const uint32_t* __restrict__ slots, uint32_t M, uint32_t x) {
-    uint32_t lo = 0, hi = M;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (slots[mid] < x) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(kRsThreads)
-resort_merge_kernel(const uint32_t* __restrict__ keys_prev, uint32_t n, const uint32_t* __restrict__ mask,
-                    const unsigned long long* __restrict__ list, const uint32_t* __restrict__ slots,
-                    const uint32_t* __restrict__ scratch, uint32_t mmax, const uint32_t* __restrict__ cell_start,
-                    uint32_t ncells, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out) {
-    const uint32_t M = scratch[1];
-    if (M > mmax) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && !((mask[i >> 5] >> (i & 31)) & 1u)) {  // unmoved (a moved slot is placed below)
-        const uint32_t key = keys_prev[i];
-        const unsigned long long c = ((unsigned long long)key << 32) | i;
-        uint32_t lo = 0, hi = M;  // moved entries sorting before (key, i)
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (list[mid] < c) lo = mid + 1;
-            else hi = mid;
-        }
-        const uint32_t pos = i - moved_before(slots, M, i) + lo;
-        if (pos < n) {  // always, for consistent tables
-            keys_out[pos] = key;
-            vals_out[pos] = i;
-        }
-    }
-    if (i < M) {
-        const unsigned long long c = list[i];
+    bitonic_sort(s_b, P);
+    for (uint32_t r = threadIdx.x; r < M; r += blockDim.x) {
+        const unsigned long long c = s_a[r];
         const uint32_t key = (uint32_t)(c >> 32), slot = (uint32_t)c;
-        // the previous order's slots of keys below `key` are [0, L), those of
-        // `key` itself [L, U); the unmoved ones among [0, clamp(slot, L, U))
-        // sort before (key, slot)
+        // the previous order's slots of keys below `key` are [0, L), those
+        // of `key` itself [L, U); the unmoved ones among [0, clamp(slot, L,
+        // U)) sort before (key, slot)
         const uint32_t L = min(cell_start[min(key, ncells)], n);
         const uint32_t U = min(cell_start[min(key + 1, ncells)], n);
         const uint32_t x = min(max(slot, L), U);
-        const uint32_t pos = i + x - moved_before(slots, M, x);
-        if (pos < n) {
-            keys_out[pos] = key;
-            vals_out[pos] = slot;
+        uint32_t lo = 0, hi = M;  // moved slots below x
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_b[mid] < x) lo = mid + 1;
+            else hi = mid;
         }
+        list[r] = c;
+        pos_out[r] = r + x - lo;
+        q_out[r] = (uint32_t)s_b[r] - r;
     }
 }
 
@@ -190,16 +153,13 @@ uint32_t dem_resort_max() { return g_resort_max; }
 
 uint64_t resort_scratch_words(uint32_t) { return 4; }
 
-cudaError_t resort_async(const DemBuffers& b, uint32_t* keys_out, uint32_t* vals_out, cudaStream_t st) {
+cudaError_t resort_async(const DemBuffers& b, cudaStream_t st) {
     const uint32_t n = b.n, mmax = b.rs_max;
     if (n == 0 || mmax == 0) return cudaSuccess;
     if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
     const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
-    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, mmax,
-                                                      b.rs_scratch);
-    resort_merge_kernel<<<(n + kRsThreads - 1) / kRsThreads, kRsThreads, 0, st>>>(
-        b.keys_prev, n, b.rs_mask, b.rs_list, b.rs_slots, b.rs_scratch, mmax, b.cell_start, b.ncells, keys_out,
-        vals_out);
+    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_list, b.rs_pos, b.rs_q, mmax,
+                                                      b.rs_scratch, b.cell_start, b.ncells);
     return cudaGetLastError();
 }
 

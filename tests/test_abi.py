@@ -287,10 +287,10 @@ def test_resort_max_knob(sdlib):
     old = _abi.tune_get("resort_max")
     assert old == 1024
     try:
-        for v in (0, 1, 2, 256, 2048):
+        for v in (0, 1, 2, 256, 1024):
             _abi.tune_set("resort_max", v)
             assert _abi.tune_get("resort_max") == v
-        for v in (-1, 3, 1000, 4096, 16384):
+        for v in (-1, 3, 1000, 2048, 4096):
             with pytest.raises(Exception):
                 _abi.tune_set("resort_max", v)
     finally:

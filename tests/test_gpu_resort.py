@@ -30,7 +30,7 @@ def moving_scene(n, moved_per_step, seed):
 
 
 @pytest.mark.parametrize("resort_max,moved", [(0, 200), (2, 200), (256, 200), (1024, 200), (1024, 0),
-                                              (2048, 1500), (2048, 9000)])
+                                              (1024, 700), (512, 9000)])
 def test_incremental_resort_bit_exact(sdlib, orc, resort_max, moved):
     from stardust_gb300 import _abi
     old = _abi.tune_get("resort_max")
