@@ -127,7 +127,7 @@ __device__ __forceinline__ void resort_finish(const ResortArgs& ra, unsigned lon
 // The contact kernel's epilogue, one slot per thread: list the moved slot
 // and, in the last block, sort and place.  Kept out of line so that it does
 // not change the register allocation of the kernel's main loop.
-__device__ __noinline__ void resort_epilogue(ResortArgs ra, bool moved, uint32_t key, uint32_t slot,
+static __device__ __noinline__ void resort_epilogue(ResortArgs ra, bool moved, uint32_t key, uint32_t slot,
                                              unsigned long long* buf) {
     resort_collect_one(ra, moved, key, slot);
     resort_finish(ra, buf);
