@@ -37,7 +37,6 @@
 
 #include "sd_common.cuh"
 #include "sd_internal.h"
-#include "sd_resort.cuh"
 
 namespace sd {
 
@@ -551,9 +550,8 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
-                             ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{},
-                             ResortArgs ra = ResortArgs{}) {
-    __shared__ __align__(8) uint32_t s_hist[kHistWords];
+                             ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{}) {
+    __shared__ uint32_t s_hist[kHistWords];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
@@ -570,22 +568,6 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
         hist_flush(s_hist, hist_spec, ghist);
     }
     if (RECORD) count_contacts(status, contacts);
-    if constexpr (!CLUMPS) {  // the re-sort's listing of moved slots (scenes without clumps)
-        if (!ra.keys_prev) return;
-        static_assert(kHistWords * sizeof(uint32_t) >= kResortMaxCap * sizeof(unsigned long long),
-                      "the histogram's shared memory holds the re-sort's list");
-        unsigned long long* buf = reinterpret_cast<unsigned long long*>(s_hist);
-        const bool moved = i < n && key != ra.keys_prev[i];
-        // out of line for the plain kernel, whose main loop it would push
-        // into spills; inline for the batch and mesh kernels, where the call
-        // would (register counts from ptxas)
-        if constexpr (BATCHED || MESH) {
-            resort_collect_one(ra, moved, key, i);
-            resort_finish(ra, buf);
-        } else {
-            resort_epilogue(ra, moved, key, i, buf);
-        }
-    }
 }
 
 // ------------------------------------- contact_mode 1: TMA column tiles
@@ -1240,8 +1222,7 @@ void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
 int dem_contact_mode() { return g_contact_mode; }
 
 template <bool RECORD>
-static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st,
-                             const ResortArgs& ra) {
+static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st) {
     float4* f = RECORD ? b.force : nullptr;
     float4* t = RECORD ? b.torque : nullptr;
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
@@ -1255,11 +1236,11 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
         else
             dem_contact_integrate_kernel<RECORD, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, ra);
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist, cc, Batch{b.scenes, b.scene_first, b.nscenes}, MeshView{}, ra);
+            b.dev_status, spec, ghist, cc, Batch{b.scenes, b.scene_first, b.nscenes});
     } else if (g_contact_mode == 0) {
         if (b.nb)
             dem_contact_integrate_kernel<RECORD, true><<<grid_for(b.n, 256), 256, 0, st>>>(
@@ -1268,7 +1249,7 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
         else
             dem_contact_integrate_kernel<RECORD, false><<<grid_for(b.n, 256), 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, ra);
+                b.dev_status, spec, ghist, cc);
     } else {
         if (b.nb)
             dem_contact_column_kernel<RECORD, true><<<cols, kColThreads, tile, st>>>(
@@ -1284,15 +1265,15 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
 // Contact + integration of free spheres, then (with clumps) the body
 // kernel, which completes the next state and keys of the clump spheres.
 static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
-                                  uint32_t* ghist, cudaStream_t st, const ResortArgs& ra = ResortArgs{}) {
+                                  uint32_t* ghist, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
     const uint32_t spec = pack_hist_spec(plan);
     if (record) {
         cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        launch_contact_t<true>(p, b, spec, ghist, st, ra);
+        launch_contact_t<true>(p, b, spec, ghist, st);
     } else {
-        launch_contact_t<false>(p, b, spec, ghist, st, ra);
+        launch_contact_t<false>(p, b, spec, ghist, st);
     }
     if (b.nb) {
         dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
@@ -1320,14 +1301,10 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     }
     cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
     if (e != cudaSuccess) return e;
+    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
     // the re-sort places the moved keys when it can (the passes then return
-    // at once and the reorder reads its order), else the passes sort; the
-    // per-slot contact kernel lists the moved slots itself when no clump
-    // sphere's key is left for the body kernel
-    const bool fused = b.rs_max && !b.nb && (b.mesh.ntri || b.nscenes > 1 || g_contact_mode == 0);
-    const ResortArgs ra = fused ? resort_args(b) : ResortArgs{};
-    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st, ra)) != cudaSuccess) return e;
-    if (!fused && (e = resort_async(b, st)) != cudaSuccess) return e;
+    // at once and the reorder reads its order), else the passes sort
+    if ((e = resort_async(b, st)) != cudaSuccess) return e;
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
                                &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;

@@ -4,25 +4,32 @@
 // being the sorted order of the previous step.  Between two steps almost
 // every sphere keeps its cell (1,048,576 settling spheres: 0-3 changes per
 // step), so the result is the previous order with a few entries moved, and
-// it can be built without a radix sort: the moved entries are listed,
-// sorted and placed (sd_resort.cuh), and the reorder reads the order from
-// that list -- position k holds a moved entry where one was placed, else
-// the unmoved slot of rank k - (moved entries placed before k).  The
-// unmoved slots are already in (key, slot) order, so this is a merge of two
-// sorted sequences and the result is exactly the stable LSD sort's.  When
-// more than `mmax` keys change the step's radix passes run instead (they are
-// in the graph and return at once otherwise) and the reorder reads their
-// sorted arrays.
+// it can be built without a radix sort:
 //
-// resort_scan_kernel lists the moved slots for scenes with clumps (whose
-// spheres' keys the body kernel writes after the contact kernel) and for the
-// column contact kernel; the per-slot contact kernel lists them itself.
+//   1. resort_scan_kernel: per block of 4096 slots, the slots whose new key
+//      differs from the sorted key they sit under ("moved"), appended to a
+//      list as (key << 32 | slot) (one atomic per block: the list's order
+//      does not matter, it is sorted next).  The last block to finish (a
+//      fence and an arrival counter, no waiting) publishes the count M and,
+//      in shared memory, sorts the list by (key, slot) and the moved slots
+//      alone (bitonic); moved entry r (rank r in (key, slot) order) goes to
+//      r plus the unmoved slots that sort before it -- the previous step's
+//      cell table bounds the slots of its key, so that count is its slot
+//      clamped to that range minus the moved slots below it;
+//   2. the reorder (dem_reorder_kernel) reads the order from these lists:
+//      position k holds a moved entry where one was placed, else the
+//      unmoved slot of rank k - (moved entries placed before k).
+//
+// The unmoved slots are already in (key, slot) order, so this is a merge of
+// two sorted sequences and the result is exactly the stable LSD sort's.
+// When more than `mmax` keys change the step's radix passes run instead (they
+// are in the graph and return at once otherwise) and the reorder reads their
+// sorted arrays.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "sd_common.cuh"
 #include "sd_internal.h"
-#include "sd_resort.cuh"
 
 namespace sd {
 namespace {
@@ -31,11 +38,35 @@ constexpr int kRsThreads = 256;
 constexpr uint32_t kRsWordsPerWarp = 16;
 constexpr uint32_t kRsBlockWords = kRsWordsPerWarp * kRsThreads / kWarp;  // 128 words: 4096 slots
 
+// Sorts v[0, P) ascending in shared memory (P a power of two; every thread
+// of the block calls it).
+__device__ void bitonic_sort(unsigned long long* v, uint32_t P) {
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                const uint32_t l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = v[i], b = v[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        v[i] = b;
+                        v[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// scratch: [0] running count, [1] M (published by the last block),
+// [2] arrivals.  [0] and [2] are zero again when the kernel ends.
 __global__ void __launch_bounds__(kRsThreads)
-resort_scan_kernel(const uint32_t* __restrict__ keys_new, ResortArgs ra) {
-    __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base;
-    __shared__ unsigned long long s_buf[kResortMaxCap];
-    const uint32_t n = ra.n;
+resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __restrict__ keys_prev, uint32_t n,
+                   unsigned long long* __restrict__ list, uint32_t* __restrict__ pos_out, uint32_t* __restrict__ q_out,
+                   uint32_t mmax, uint32_t* __restrict__ scratch, const uint32_t* __restrict__ cell_start,
+                   uint32_t ncells) {
+    __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
+    __shared__ unsigned long long s_a[kResortMaxCap], s_b[kResortMaxCap];
     const uint32_t w = threadIdx.x / kWarp, lane = lane_id();
     const uint32_t word0 = blockIdx.x * kRsBlockWords + w * kRsWordsPerWarp;
     uint32_t m[kRsWordsPerWarp];
@@ -43,7 +74,7 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, ResortArgs ra) {
 #pragma unroll
     for (uint32_t j = 0; j < kRsWordsPerWarp; ++j) {
         const uint32_t s = (word0 + j) * 32 + lane;
-        const bool moved = s < n && keys_new[s] != ra.keys_prev[s];
+        const bool moved = s < n && keys_new[s] != keys_prev[s];
         m[j] = __ballot_sync(0xffffffffu, moved);
         cnt += __popc(m[j]);
     }
@@ -52,7 +83,7 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, ResortArgs ra) {
     if (threadIdx.x == 0) {
         uint32_t tot = 0;
         for (uint32_t v = 0; v < kRsThreads / kWarp; ++v) tot += s_wcnt[v];
-        s_base = tot ? atomicAdd(&ra.scratch[0], tot) : 0u;
+        s_base = tot ? atomicAdd(&scratch[0], tot) : 0u;
     }
     __syncthreads();
     if (cnt) {
@@ -63,12 +94,54 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, ResortArgs ra) {
             if ((m[j] >> lane) & 1u) {
                 const uint32_t rank = rank0 + __popc(m[j] & lanemask_lt());
                 const uint32_t s = (word0 + j) * 32 + lane;
-                if (rank < ra.mmax) ra.list[rank] = ((unsigned long long)keys_new[s] << 32) | s;
+                if (rank < mmax) list[rank] = ((unsigned long long)keys_new[s] << 32) | s;
             }
             rank0 += __popc(m[j]);
         }
     }
-    resort_finish(ra, s_buf);
+    // the last block to arrive sees every block's count and list entries
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&scratch[2], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t M = ld_relaxed(&scratch[0]);
+    if (threadIdx.x == 0) {
+        scratch[1] = M;
+        scratch[0] = 0u;
+        scratch[2] = 0u;
+    }
+    if (M == 0 || M > mmax) return;
+    uint32_t P = 2;
+    while (P < M) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_a[i] = i < M ? __ldcg(&list[i]) : ~0ull;
+    __syncthreads();
+    bitonic_sort(s_a, P);
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_b[i] = i < M ? (s_a[i] & 0xffffffffull) : ~0ull;
+    __syncthreads();
+    bitonic_sort(s_b, P);
+    for (uint32_t r = threadIdx.x; r < M; r += blockDim.x) {
+        const unsigned long long c = s_a[r];
+        const uint32_t key = (uint32_t)(c >> 32), slot = (uint32_t)c;
+        // the previous order's slots of keys below `key` are [0, L), those
+        // of `key` itself [L, U); the unmoved ones among [0, clamp(slot, L,
+        // U)) sort before (key, slot)
+        const uint32_t L = min(cell_start[min(key, ncells)], n);
+        const uint32_t U = min(cell_start[min(key + 1, ncells)], n);
+        const uint32_t x = min(max(slot, L), U);
+        uint32_t lo = 0, hi = M;  // moved slots below x
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_b[mid] < x) lo = mid + 1;
+            else hi = mid;
+        }
+        list[r] = c;
+        pos_out[r] = r + x - lo;
+        q_out[r] = (uint32_t)s_b[r] - r;
+    }
 }
 
 }  // namespace
@@ -80,18 +153,13 @@ uint32_t dem_resort_max() { return g_resort_max; }
 
 uint64_t resort_scratch_words(uint32_t) { return 4; }
 
-ResortArgs resort_args(const DemBuffers& b) {
-    ResortArgs ra{};
-    if (b.n == 0 || b.rs_max == 0 || b.rs_max > kResortMaxCap || (b.rs_max & (b.rs_max - 1)) != 0) return ra;
-    ra = ResortArgs{b.keys_prev, b.rs_list, b.rs_pos, b.rs_q, b.rs_scratch, b.cell_start, b.n, b.ncells, b.rs_max};
-    return ra;
-}
-
 cudaError_t resort_async(const DemBuffers& b, cudaStream_t st) {
-    const ResortArgs ra = resort_args(b);
-    if (!ra.keys_prev) return b.rs_max == 0 || b.n == 0 ? cudaSuccess : cudaErrorInvalidValue;
-    const uint32_t blocks = ((b.n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
-    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, ra);
+    const uint32_t n = b.n, mmax = b.rs_max;
+    if (n == 0 || mmax == 0) return cudaSuccess;
+    if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
+    const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
+    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_list, b.rs_pos, b.rs_q, mmax,
+                                                      b.rs_scratch, b.cell_start, b.ncells);
     return cudaGetLastError();
 }
 

@@ -97,10 +97,9 @@ def test_resort_mixes_with_radix_steps(sdlib, orc):
 
 
 def test_step_kernel_count(sdlib):
-    """Without clumps the contact kernel lists the moved slots itself and
-    the reorder reads the order from that list, so the step graph has as
-    many kernels as the plain radix step (contact, two passes that return at
-    once, reorder); stats report the graph's kernel nodes."""
+    """The step graph runs one kernel more than the plain radix step (the
+    re-sort's scan; the reorder reads its order); stats report the graph's
+    kernel nodes."""
     from stardust_gb300 import _abi
     old = _abi.tune_get("resort_max")
     counts = {}
@@ -117,4 +116,4 @@ def test_step_kernel_count(sdlib):
             eng.close()
     finally:
         _abi.tune_set("resort_max", old)
-    assert counts[0] == 4 and counts[1024] == 4
+    assert counts[0] >= 4 and counts[1024] == counts[0] + 1
