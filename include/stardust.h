@@ -424,7 +424,9 @@ sd_status sd_lbvh_morton(uint64_t n, const float* d_lo4, const float* d_hi4, uin
  * original sphere order.  The engine re-sorts before the next step. */
 sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src, size_t bytes);
 /* Device pointer of a field in current SORTED slot order (headless
- * replacement of the GL VBO interop, engine.hpp:165-168). */
+ * replacement of the GL VBO interop, engine.hpp:165-168).  Valid until the
+ * next step: the step alternates between two state buffers, so ask again
+ * after stepping, as the reference maps its VBO each frame. */
 sd_status sd_engine_device_ptr(sd_engine* h, int32_t field, void** out);
 /* The engine's CUDA stream (cudaStream_t as void*). */
 sd_status sd_engine_stream(sd_engine* h, void** out);

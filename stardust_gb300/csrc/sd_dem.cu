@@ -876,12 +876,13 @@ struct ResortView {
 // position k holds unmoved rank u = k - (moved entries placed before k),
 // which is slot u + (moved slots s_j with s_j - j <= u).  An unmoved slot's
 // new key is its previous one.
+template <bool KEY = true>
 __device__ __forceinline__ void sorted_entry(uint32_t k, bool inc, uint32_t M, const ResortView& rv,
                                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                                              uint32_t n, uint32_t& src, uint32_t& key) {
     if (!inc) {
         src = vals[k];
-        key = keys[k];
+        if (KEY) key = keys[k];
         return;
     }
     uint32_t lo = 0, hi = M;
@@ -904,7 +905,7 @@ __device__ __forceinline__ void sorted_entry(uint32_t k, bool inc, uint32_t M, c
         else z = mid;
     }
     src = u + a;
-    key = src < n ? rv.keys_new[src] : 0u;
+    if (KEY) key = src < n ? rv.keys_new[src] : 0u;
 }
 
 // Gather the next state into sorted order and write cell_start.  Block b
@@ -960,6 +961,106 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
             continue;
         }
         uint32_t a = 0, z = cnt;  // first index in [0, cnt) with key >= c, else cnt
+        while (a < z) {
+            uint32_t m = (a + z) >> 1;
+            if ((int64_t)s_keys[m + 1] < c) a = m + 1;
+            else z = m;
+        }
+        cell_start[c] = b0 + a;
+    }
+}
+
+// The in-place reorder of a step whose next state stays where the contact
+// kernel wrote it (S, the *_n buffers, in the previous slot order).  Sorted
+// position k needs the entry of slot src(k); where src(k) == k -- every
+// slot but those shifted by the few moved keys -- nothing moves.  Phase 1
+// gathers the others into the free buffer T (the step's input state, no
+// longer read) and, with the re-sort's order, shifts the cell table by the
+// moved keys: cell_start[c] counts the entries with key < c, so it changes
+// by (moved entries whose new key < c) - (moved entries whose old key < c).
+// Phase 2 copies the gathered entries back, records every position's key
+// and, for the radix passes' order, rebuilds the cell table as the plain
+// reorder does.
+__global__ void __launch_bounds__(kReorderThreads)
+dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
+                      const uint32_t* __restrict__ vals, const float4* __restrict__ s_pos,
+                      const float4* __restrict__ s_vel, const float4* __restrict__ s_omg, float4* __restrict__ t_pos,
+                      float4* __restrict__ t_vel, float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start,
+                      const uint32_t* __restrict__ oldk, ResortView rv) {
+    const uint32_t M = rv.scratch[1];
+    const bool inc = M <= rv.mmax;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        uint32_t src, key;
+        sorted_entry<false>(k, inc, M, rv, keys, vals, n, src, key);
+        if (src != k && src < n) {
+            t_pos[k] = s_pos[src];
+            t_vel[k] = s_vel[src];
+            t_omg[k] = s_omg[src];
+        }
+    }
+    if (inc && M) {
+        for (uint32_t c = k; c <= ncells; c += gridDim.x * blockDim.x) {
+            uint32_t a = 0, z = M;  // moved entries with new key < c (the list is in key order)
+            while (a < z) {
+                const uint32_t mid = (a + z) >> 1;
+                if ((uint32_t)(rv.list[mid] >> 32) < c) a = mid + 1;
+                else z = mid;
+            }
+            uint32_t b = 0, y = M;  // moved entries with old key < c
+            while (b < y) {
+                const uint32_t mid = (b + y) >> 1;
+                if (oldk[mid] < c) b = mid + 1;
+                else y = mid;
+            }
+            if (a != b) cell_start[c] = cell_start[c] + a - b;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kReorderThreads)
+dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
+                     const uint32_t* __restrict__ vals, const float4* __restrict__ t_pos,
+                     const float4* __restrict__ t_vel, const float4* __restrict__ t_omg, float4* __restrict__ s_pos,
+                     float4* __restrict__ s_vel, float4* __restrict__ s_omg, uint32_t* __restrict__ cell_start,
+                     uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv) {
+    __shared__ uint32_t s_keys[kReorderThreads + 1];
+    const uint32_t M = rv.scratch[1];
+    const bool inc = M <= rv.mmax;
+    const uint32_t b0 = blockIdx.x * kReorderThreads;
+    const uint32_t b1 = min(b0 + kReorderThreads, n);
+    const uint32_t k = b0 + threadIdx.x;
+    if (k < n) {
+        uint32_t src, key;
+        sorted_entry(k, inc, M, rv, keys, vals, n, src, key);
+        if (src != k && src < n) {
+            s_pos[k] = t_pos[k];
+            s_vel[k] = t_vel[k];
+            const float4 o = t_omg[k];
+            s_omg[k] = o;
+            const uint32_t idb = __float_as_uint(o.w);
+            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
+        }
+        s_keys[threadIdx.x + 1] = key;
+        keys_prev[k] = key;
+    }
+    if (inc) return;  // the gather phase shifted the cell table
+    if (threadIdx.x == 0) {
+        uint32_t src0 = 0, key0 = 0;
+        if (b0 > 0) sorted_entry(b0 - 1, inc, M, rv, keys, vals, n, src0, key0);
+        s_keys[0] = key0;
+    }
+    __syncthreads();
+    const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
+    const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
+    const uint32_t cnt = b1 - b0;
+    const int64_t kfirst = cnt ? (int64_t)s_keys[1] : hi, klast = cnt ? (int64_t)s_keys[cnt] : lo;
+    for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += kReorderThreads) {
+        if (c <= kfirst || c > klast) {
+            cell_start[c] = c <= kfirst ? b0 : b1;
+            continue;
+        }
+        uint32_t a = 0, z = cnt;
         while (a < z) {
             uint32_t m = (a + z) >> 1;
             if ((int64_t)s_keys[m + 1] < c) a = m + 1;
@@ -1308,8 +1409,26 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
                                &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
-    if ((e = dem_reorder_async(b, st, true)) != cudaSuccess) return e;
+    if (dem_step_swaps(b)) {  // sorted in place: the next state stays in the *_n buffers
+        const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
+        const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
+        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
+        const unsigned grid = grid_for(b.n, kReorderThreads);
+        dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n,
+                                                                b.pos, b.vel, b.omg, b.cell_start, b.rs_oldk, rv);
+        dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
+                                                               b.vel_n, b.omg_n, b.cell_start,
+                                                               b.nb ? b.slot_of : nullptr, b.keys_prev, rv);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    } else if ((e = dem_reorder_async(b, st, true)) != cudaSuccess) {
+        return e;
+    }
     return mesh_advance_async(b.mesh, 1, st);
+}
+
+bool dem_step_swaps(const DemBuffers& b) {
+    return b.n > 0 && b.rs_max > 0 && b.rs_max <= kResortMaxCap && (b.rs_max & (b.rs_max - 1)) == 0 &&
+           sort_plan(dem_key_bits(b.ncells)).passes <= kFusedPasses;
 }
 
 cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) {

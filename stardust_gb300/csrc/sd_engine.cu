@@ -96,7 +96,9 @@ sd_status dev_alloc(sd_engine* h, T** p, size_t count) {
 void release_device(sd_engine* h) {
     hull_release(h);
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->graph_alt) cudaGraphExecDestroy(h->graph_alt);
     h->graph = nullptr;
+    h->graph_alt = nullptr;
     h->graph_valid = false;
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
@@ -405,6 +407,7 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
         (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_pos, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_q, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_oldk, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->cfg.flags & SD_FLAG_RECORD) {
@@ -483,10 +486,20 @@ sd_status prepare_with(sd_engine* h, const float4* pos, const float4* vel, const
     return SD_OK;
 }
 
+static void swap_state(sd::DemBuffers& B) {
+    std::swap(B.pos, B.pos_n);
+    std::swap(B.vel, B.vel_n);
+    std::swap(B.omg, B.omg_n);
+}
+
 sd_status build_graph(sd_engine* h, float dt) {
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
+    }
+    if (h->graph_alt) {
+        cudaGraphExecDestroy(h->graph_alt);
+        h->graph_alt = nullptr;
     }
     h->P.dt = dt;
     bool record = (h->cfg.flags & SD_FLAG_RECORD) != 0;
@@ -499,17 +512,34 @@ sd_status build_graph(sd_engine* h, float dt) {
         SD_CUDA(h, cudaStreamSynchronize(h->stream));
         h->mesh.dt = dt;
     }
-    cudaGraph_t g = nullptr;
-    SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     h->B.rs_max = sd::dem_resort_max();
-    cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
-    cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
-    if (e2 != cudaSuccess) return cuda_fail(h, e2, "capturing the step");
-    if (e3 != cudaSuccess) return cuda_fail(h, e3, "cudaStreamEndCapture");
-    cudaError_t e4 = cudaGraphInstantiate(&h->graph, g, 0);
-    h->graph_kernels = graph_kernel_nodes(g);
-    cudaGraphDestroy(g);
-    if (e4 != cudaSuccess) return cuda_fail(h, e4, "cudaGraphInstantiate");
+    h->graph_swaps = sd::dem_step_swaps(h->B);
+    h->graph_parity = 0;
+    // with swaps: the graph on the current buffers, then the one on the
+    // swapped buffers (the state after one step); the second swap restores B
+    for (int par = 0; par < (h->graph_swaps ? 2 : 1); ++par) {
+        cudaGraph_t g = nullptr;
+        SD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e2 = sd::dem_step_async(h->P, h->B, record, h->stream);
+        cudaError_t e3 = cudaStreamEndCapture(h->stream, &g);
+        if (h->graph_swaps) swap_state(h->B);
+        if (e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (h->graph_swaps && par == 0) swap_state(h->B);
+            return cuda_fail(h, e2, "capturing the step");
+        }
+        if (e3 != cudaSuccess) {
+            if (h->graph_swaps && par == 0) swap_state(h->B);
+            return cuda_fail(h, e3, "cudaStreamEndCapture");
+        }
+        cudaError_t e4 = cudaGraphInstantiate(par == 0 ? &h->graph : &h->graph_alt, g, 0);
+        h->graph_kernels = graph_kernel_nodes(g);
+        cudaGraphDestroy(g);
+        if (e4 != cudaSuccess) {
+            if (h->graph_swaps && par == 0) swap_state(h->B);
+            return cuda_fail(h, e4, "cudaGraphInstantiate");
+        }
+    }
     h->graph_dt = dt;
     h->graph_valid = true;
     return SD_OK;
@@ -1234,7 +1264,13 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
         h->graph_epoch = g_tune_epoch.load();
         if ((s = build_graph(h, dt))) return s;
     }
-    for (int32_t i = 0; i < n_steps; ++i) SD_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+    for (int32_t i = 0; i < n_steps; ++i) {
+        SD_CUDA(h, cudaGraphLaunch(h->graph_parity ? h->graph_alt : h->graph, h->stream));
+        if (h->graph_swaps) {  // the next state was sorted in place in the *_n buffers
+            swap_state(h->B);
+            h->graph_parity ^= 1;
+        }
+    }
     if (n_steps > 0 && !h->hull_mode()) h->keys_current = true;  // every step ends with a sort + reorder
     h->steps += (uint64_t)n_steps;
     return SD_OK;

@@ -78,6 +78,12 @@ struct sd_engine {
     double* d_energy = nullptr;
     float4* d_tmp = nullptr;
     cudaGraphExec_t graph = nullptr;
+    // when the step leaves the next state in the *_n buffers (graph_swaps),
+    // a second graph captured on the swapped buffers alternates with the
+    // first; graph_parity names the one whose input is the current state
+    cudaGraphExec_t graph_alt = nullptr;
+    bool graph_swaps = false;
+    int graph_parity = 0;
     float graph_dt = 0.0f;
     bool graph_valid = false;
     uint32_t graph_kernels = 0;  // kernel nodes of the step graph
