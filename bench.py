@@ -384,7 +384,7 @@ def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
             "per_scene_particle_steps_per_s_median": float(np.median(counts)) / (ms * 1e-3),
             "alone_16_scenes": {"spheres": alone_n, "ms_per_step_sum": alone_ms,
                                 "particle_steps_per_s": alone_n / (alone_ms * 1e-3)},
-            "device_errors": st["device_errors"], "autotune": tuned}
+            "device_errors": st["device_errors"], "moved_keys_last_step": st["moved_keys"], "autotune": tuned}
 
 
 def bench_drum(steps: int, warmup: int, local: int):
@@ -429,7 +429,7 @@ def bench_drum(steps: int, warmup: int, local: int):
                         f"{len(d['tris'])} triangles loaded from a binary STL, R 0.5 m, L 0.5 m, 2 rad/s, dt 2e-6 s",
             "spheres": n, "bodies": int(stt["n_bodies"]), "triangles": int(len(d["tris"])), "ms_per_step": ms,
             "particle_steps_per_s": n / (ms * 1e-3), "device_errors": stt["device_errors"],
-            "scene_generation_s": gen_s}
+            "moved_keys_last_step": stt["moved_keys"], "scene_generation_s": gen_s}
 
 
 def bench_sap(n: int, steps: int, warmup: int, local: int):
@@ -655,6 +655,7 @@ def run_ours(args, rank, world, local):
             "clocks": clocks,
             "gpu_launches": st["step_kernels"] * args.steps,
             "contacts": st["contacts"],
+            "moved_keys_last_step": st["moved_keys"],
             "gjk": gjk,
             "batch": batch,
             "drum": drum,
