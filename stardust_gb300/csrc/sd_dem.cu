@@ -859,103 +859,21 @@ __global__ void dem_keys_kernel(DemParams p, uint32_t n, const float4* __restric
 
 constexpr int kReorderThreads = 256;
 
-// The order the incremental re-sort found, read in place of sorted arrays:
-// the new keys, and the moved entries in (key, slot) order with their
-// sorted positions and, per moved slot in ascending order, slot - rank.
-struct ResortView {
-    const uint32_t* keys_new;
-    const uint32_t* pos;
-    const uint32_t* q;
-    const unsigned long long* list;
-    const uint32_t* scratch;  // null: read the sorted arrays
-    uint32_t mmax;
-};
-
-// Source slot and key of sorted position k.  From the re-sort: a moved
-// entry sits at its recorded position; the others keep their order, so
-// position k holds unmoved rank u = k - (moved entries placed before k),
-// which is slot u + (moved slots s_j with s_j - j <= u).  An unmoved slot's
-// new key is its previous one.
-template <bool KEY = true>
-__device__ __forceinline__ void sorted_entry(uint32_t k, bool inc, uint32_t M, const ResortView& rv,
-                                             const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                             uint32_t n, uint32_t& src, uint32_t& key) {
-    if (!inc) {
-        src = vals[k];
-        if (KEY) key = keys[k];
-        return;
-    }
-    uint32_t lo = 0, hi = M;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (rv.pos[mid] < k) lo = mid + 1;
-        else hi = mid;
-    }
-    if (lo < M && rv.pos[lo] == k) {
-        const unsigned long long c = rv.list[lo];
-        key = (uint32_t)(c >> 32);
-        src = (uint32_t)c;
-        return;
-    }
-    const uint32_t u = k - lo;
-    uint32_t a = 0, z = M;
-    while (a < z) {
-        const uint32_t mid = (a + z) >> 1;
-        if (rv.q[mid] <= u) a = mid + 1;
-        else z = mid;
-    }
-    src = u + a;
-    if (KEY) key = src < n ? rv.keys_new[src] : 0u;
-}
-
-// Gather the next state into sorted order and write cell_start.  Block b
-// owns slots [b0, b1) and the cells (key[b0-1], key[b1-1]] (the first block
-// starts at cell 0, the last ends at ncells), so every cell's lower bound is
-// written exactly once, by binary search over the block's keys in shared
-// memory.
-__global__ void __launch_bounds__(kReorderThreads)
-dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
-                   const uint32_t* __restrict__ vals, const float4* __restrict__ pos_n,
-                   const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
-                   float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
-                   uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
-                   uint32_t* __restrict__ keys_prev, ResortView rv) {
-    __shared__ uint32_t s_keys[kReorderThreads + 1];
-    const uint32_t b0 = blockIdx.x * kReorderThreads;
-    const uint32_t b1 = min(b0 + kReorderThreads, n);
-    const uint32_t k = b0 + threadIdx.x;
-    const uint32_t M = rv.scratch ? rv.scratch[1] : 0u;
-    const bool inc = rv.scratch && M <= rv.mmax;
-    if (k < n) {
-        uint32_t src, key;
-        sorted_entry(k, inc, M, rv, keys, vals, n, src, key);
-        if (src < n) {  // always true for a valid permutation
-            pos[k] = pos_n[src];
-            vel[k] = vel_n[src];
-            const float4 o = omg_n[src];
-            omg[k] = o;
-            // clump spheres: where their body finds them next step
-            const uint32_t idb = __float_as_uint(o.w);
-            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
-        }
-        s_keys[threadIdx.x + 1] = key;
-        keys_prev[k] = key;  // what the next step's incremental re-sort compares against
-    }
-    if (threadIdx.x == 0) {
-        uint32_t src0 = 0, key0 = 0;
-        if (b0 > 0) sorted_entry(b0 - 1, inc, M, rv, keys, vals, n, src0, key0);
-        s_keys[0] = key0;
-    }
-    __syncthreads();
+// Writes cell_start for the cells block [b0, b1) owns, (s_keys[0],
+// s_keys[cnt]] (the first block starts at cell 0, the last ends at ncells),
+// by binary search over the block's sorted keys s_keys[1..cnt] in shared
+// memory, so that every cell's lower bound is written exactly once.  Cells
+// at or before the block's first key take b0 and cells after its last key
+// (only the last block has them: the tail up to ncells) take b1 without a
+// search -- an empty region past the last sphere can be tens of thousands
+// of cells, all in that one block.
+__device__ __forceinline__ void block_cell_starts(const uint32_t* s_keys, uint32_t b0, uint32_t b1, uint32_t n,
+                                                  uint32_t ncells, uint32_t* __restrict__ cell_start) {
     const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
     const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
     const uint32_t cnt = b1 - b0;
-    // cells at or before the block's first key take b0 and cells after its
-    // last key (only the last block has them: the tail up to ncells) take
-    // b1, without a search -- an empty region past the last sphere can be
-    // tens of thousands of cells, all in that one block
     const int64_t kfirst = cnt ? (int64_t)s_keys[1] : hi, klast = cnt ? (int64_t)s_keys[cnt] : lo;
-    for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += kReorderThreads) {
+    for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += blockDim.x) {
         if (c <= kfirst || c > klast) {
             cell_start[c] = c <= kfirst ? b0 : b1;
             continue;
@@ -970,49 +888,160 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
     }
 }
 
+// Gather the next state into sorted order and write cell_start.
+__global__ void __launch_bounds__(kReorderThreads)
+dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
+                   const uint32_t* __restrict__ vals, const float4* __restrict__ pos_n,
+                   const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
+                   float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
+                   uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
+                   uint32_t* __restrict__ keys_prev) {
+    __shared__ uint32_t s_keys[kReorderThreads + 1];
+    const uint32_t b0 = blockIdx.x * kReorderThreads;
+    const uint32_t b1 = min(b0 + kReorderThreads, n);
+    const uint32_t k = b0 + threadIdx.x;
+    if (k < n) {
+        const uint32_t src = vals[k];
+        if (src < n) {  // always true for a valid permutation
+            pos[k] = pos_n[src];
+            vel[k] = vel_n[src];
+            const float4 o = omg_n[src];
+            omg[k] = o;
+            // clump spheres: where their body finds them next step
+            const uint32_t idb = __float_as_uint(o.w);
+            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
+        }
+        const uint32_t key = keys[k];
+        s_keys[threadIdx.x + 1] = key;
+        keys_prev[k] = key;  // what the next step's incremental re-sort compares against
+    }
+    if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
+    __syncthreads();
+    block_cell_starts(s_keys, b0, b1, n, ncells, cell_start);
+}
+
+// The order the incremental re-sort found: the new keys, and the M moved
+// entries in (key, slot) order with their new keys and sorted positions
+// and, per moved slot in ascending order, slot - rank and its old key.
+struct ResortView {
+    const uint32_t* keys_new;
+    const uint32_t* pos;
+    const uint32_t* q;
+    const unsigned long long* list;
+    const uint32_t* newk;
+    const uint32_t* oldk;
+    const uint32_t* scratch;  // [1] = M
+    uint32_t mmax;
+};
+
+// First index in [lo, hi) of ascending a with a[i] >= x (hi if none).
+__device__ __forceinline__ uint32_t lower_idx(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// First index in [lo, hi) of ascending a with a[i] > x (hi if none).
+__device__ __forceinline__ uint32_t upper_idx(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Sorted positions [b0, b1) (b0 < b1) read the re-sort's lists only in a
+// window: moved entries placed in the block are pos[p0, p1); position k
+// holds, if no moved entry, unmoved rank u = k - lo(k) with lo(k) in
+// [p0, p1], so u in [b0 - p1, b1 - 1 - p0], and its slot is u + t(u), where
+// t(u) = #{j : q_j <= u} is monotone and so lies in [t(umin), t(umax)].
+// Thread 0 finds the window; each thread then searches a few entries.
+struct SortedWindow {
+    uint32_t p0, p1, q0, q1;
+};
+
+__device__ __forceinline__ SortedWindow sorted_window(uint32_t b0, uint32_t b1, uint32_t M, const ResortView& rv) {
+    SortedWindow w;
+    w.p0 = lower_idx(rv.pos, 0, M, b0);
+    w.p1 = lower_idx(rv.pos, w.p0, M, b1);
+    const uint32_t umin = b0 > w.p1 ? b0 - w.p1 : 0u;
+    const uint32_t umax = b1 - 1 - w.p0;
+    w.q0 = upper_idx(rv.q, 0, M, umin);
+    w.q1 = upper_idx(rv.q, w.q0, M, umax);
+    return w;
+}
+
+// Source slot and key of sorted position k in its block's window.  An
+// unmoved slot's new key is its previous one.
+template <bool KEY>
+__device__ __forceinline__ void sorted_entry(uint32_t k, const SortedWindow& w, const ResortView& rv, uint32_t n,
+                                             uint32_t& src, uint32_t& key) {
+    const uint32_t lo = lower_idx(rv.pos, w.p0, w.p1, k);
+    if (lo < w.p1 && rv.pos[lo] == k) {
+        const unsigned long long c = rv.list[lo];
+        src = (uint32_t)c;
+        if (KEY) key = (uint32_t)(c >> 32);
+        return;
+    }
+    const uint32_t u = k - lo;
+    src = u + upper_idx(rv.q, w.q0, w.q1, u);
+    if (KEY) key = src < n ? rv.keys_new[src] : 0u;
+}
+
 // The in-place reorder of a step whose next state stays where the contact
 // kernel wrote it (S, the *_n buffers, in the previous slot order).  Sorted
 // position k needs the entry of slot src(k); where src(k) == k -- every
-// slot but those shifted by the few moved keys -- nothing moves.  Phase 1
+// slot but those shifted by the moved keys -- nothing moves.  Phase 1
 // gathers the others into the free buffer T (the step's input state, no
 // longer read) and, with the re-sort's order, shifts the cell table by the
 // moved keys: cell_start[c] counts the entries with key < c, so it changes
 // by (moved entries whose new key < c) - (moved entries whose old key < c).
 // Phase 2 copies the gathered entries back, records every position's key
-// and, for the radix passes' order, rebuilds the cell table as the plain
-// reorder does.
+// and, for the radix passes' order (more moves than the re-sort takes),
+// rebuilds the cell table as the plain reorder does.
 __global__ void __launch_bounds__(kReorderThreads)
-dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
-                      const uint32_t* __restrict__ vals, const float4* __restrict__ s_pos,
-                      const float4* __restrict__ s_vel, const float4* __restrict__ s_omg, float4* __restrict__ t_pos,
-                      float4* __restrict__ t_vel, float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start,
-                      const uint32_t* __restrict__ oldk, ResortView rv) {
+dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ vals,
+                      const float4* __restrict__ s_pos, const float4* __restrict__ s_vel,
+                      const float4* __restrict__ s_omg, float4* __restrict__ t_pos, float4* __restrict__ t_vel,
+                      float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start, ResortView rv) {
+    __shared__ SortedWindow s_w;
+    __shared__ uint32_t s_a0, s_a1, s_o0, s_o1;
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t b0 = blockIdx.x * kReorderThreads;
+    const uint32_t k = b0 + threadIdx.x;
+    if (inc) {
+        if (threadIdx.x == 0 && b0 < n) s_w = sorted_window(b0, min(b0 + kReorderThreads, n), M, rv);
+        __syncthreads();
+    }
     if (k < n) {
         uint32_t src, key;
-        sorted_entry<false>(k, inc, M, rv, keys, vals, n, src, key);
+        if (inc) sorted_entry<false>(k, s_w, rv, n, src, key);
+        else src = vals[k];
         if (src != k && src < n) {
             t_pos[k] = s_pos[src];
             t_vel[k] = s_vel[src];
             t_omg[k] = s_omg[src];
         }
     }
-    if (inc && M) {
-        for (uint32_t c = k; c <= ncells; c += gridDim.x * blockDim.x) {
-            uint32_t a = 0, z = M;  // moved entries with new key < c (the list is in key order)
-            while (a < z) {
-                const uint32_t mid = (a + z) >> 1;
-                if ((uint32_t)(rv.list[mid] >> 32) < c) a = mid + 1;
-                else z = mid;
-            }
-            uint32_t b = 0, y = M;  // moved entries with old key < c
-            while (b < y) {
-                const uint32_t mid = (b + y) >> 1;
-                if (oldk[mid] < c) b = mid + 1;
-                else y = mid;
-            }
+    if (!inc || M == 0) return;
+    for (uint32_t base = b0; base <= ncells; base += gridDim.x * kReorderThreads) {
+        const uint32_t c = base + threadIdx.x, c1 = base + kReorderThreads;
+        __syncthreads();
+        if (threadIdx.x == 0) {  // the block's windows in the new and old key lists
+            s_a0 = lower_idx(rv.newk, 0, M, base);
+            s_a1 = lower_idx(rv.newk, s_a0, M, c1);
+            s_o0 = lower_idx(rv.oldk, 0, M, base);
+            s_o1 = lower_idx(rv.oldk, s_o0, M, c1);
+        }
+        __syncthreads();
+        if (c <= ncells) {
+            const uint32_t a = lower_idx(rv.newk, s_a0, s_a1, c);
+            const uint32_t b = lower_idx(rv.oldk, s_o0, s_o1, c);
             if (a != b) cell_start[c] = cell_start[c] + a - b;
         }
     }
@@ -1025,14 +1054,24 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
                      float4* __restrict__ s_vel, float4* __restrict__ s_omg, uint32_t* __restrict__ cell_start,
                      uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
+    __shared__ SortedWindow s_w;
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
     const uint32_t k = b0 + threadIdx.x;
+    if (inc) {
+        if (threadIdx.x == 0) s_w = sorted_window(b0, b1, M, rv);
+        __syncthreads();
+    }
     if (k < n) {
         uint32_t src, key;
-        sorted_entry(k, inc, M, rv, keys, vals, n, src, key);
+        if (inc) {
+            sorted_entry<true>(k, s_w, rv, n, src, key);
+        } else {
+            src = vals[k];
+            key = keys[k];
+        }
         if (src != k && src < n) {
             s_pos[k] = t_pos[k];
             s_vel[k] = t_vel[k];
@@ -1045,29 +1084,9 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
         keys_prev[k] = key;
     }
     if (inc) return;  // the gather phase shifted the cell table
-    if (threadIdx.x == 0) {
-        uint32_t src0 = 0, key0 = 0;
-        if (b0 > 0) sorted_entry(b0 - 1, inc, M, rv, keys, vals, n, src0, key0);
-        s_keys[0] = key0;
-    }
+    if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
     __syncthreads();
-    const int64_t lo = b0 == 0 ? -1 : (int64_t)s_keys[0];
-    const int64_t hi = b1 == n ? (int64_t)ncells : min((int64_t)s_keys[b1 - b0], (int64_t)ncells);
-    const uint32_t cnt = b1 - b0;
-    const int64_t kfirst = cnt ? (int64_t)s_keys[1] : hi, klast = cnt ? (int64_t)s_keys[cnt] : lo;
-    for (int64_t c = lo + 1 + threadIdx.x; c <= hi; c += kReorderThreads) {
-        if (c <= kfirst || c > klast) {
-            cell_start[c] = c <= kfirst ? b0 : b1;
-            continue;
-        }
-        uint32_t a = 0, z = cnt;
-        while (a < z) {
-            uint32_t m = (a + z) >> 1;
-            if ((int64_t)s_keys[m + 1] < c) a = m + 1;
-            else z = m;
-        }
-        cell_start[c] = b0 + a;
-    }
+    block_cell_starts(s_keys, b0, b1, n, ncells, cell_start);
 }
 
 __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
@@ -1298,15 +1317,13 @@ cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
                             st, &b.sorted_in_tmp);
 }
 
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool incremental) {
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
     const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
-    ResortView rv{};
-    if (incremental && b.rs_max) rv = ResortView{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
     dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
         b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
-        b.nb ? b.slot_of : nullptr, b.keys_prev, rv);
+        b.nb ? b.slot_of : nullptr, b.keys_prev);
     return cudaGetLastError();
 }
 
@@ -1412,15 +1429,15 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     if (dem_step_swaps(b)) {  // sorted in place: the next state stays in the *_n buffers
         const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
         const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
-        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
+        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_newk, b.rs_oldk, b.rs_scratch, b.rs_max};
         const unsigned grid = grid_for(b.n, kReorderThreads);
-        dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n,
-                                                                b.pos, b.vel, b.omg, b.cell_start, b.rs_oldk, rv);
+        dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, v, b.pos_n, b.vel_n, b.omg_n, b.pos,
+                                                                b.vel, b.omg, b.cell_start, rv);
         dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
                                                                b.vel_n, b.omg_n, b.cell_start,
                                                                b.nb ? b.slot_of : nullptr, b.keys_prev, rv);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    } else if ((e = dem_reorder_async(b, st, true)) != cudaSuccess) {
+    } else if ((e = dem_reorder_async(b, st)) != cudaSuccess) {
         return e;
     }
     return mesh_advance_async(b.mesh, 1, st);

@@ -243,6 +243,7 @@ struct DemBuffers {
     unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), up to kResortMaxCap
     uint32_t* rs_pos;               // per moved entry (in (key, slot) order): its sorted position
     uint32_t* rs_q;                 // per moved slot (ascending): slot - rank
+    uint32_t* rs_newk;              // per moved entry (in (key, slot) order): its new key
     uint32_t* rs_oldk;              // per moved slot (ascending): its previous key
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
@@ -267,8 +268,7 @@ cudaError_t dem_init_kernels();  // once per device, outside stream capture
 cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st);
 cudaError_t dem_keys_from_state_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st);
-// incremental: take the order from the re-sort when it placed the moves
-cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st, bool incremental = false);
+cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
 // True when dem_step_async leaves the next state in the *_n buffers (sorted
 // in place there): the caller then swaps pos/pos_n, vel/vel_n, omg/omg_n.
 bool dem_step_swaps(const DemBuffers& b);
