@@ -921,21 +921,20 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
 }
 
 // The order the incremental re-sort found: the new keys, and the M moved
-// entries in (key, slot) order with their new keys and sorted positions
-// and, per moved slot in ascending order, slot - rank and its old key.
+// entries in (key, slot) order with their sorted positions and, per moved
+// slot in ascending order, slot - rank.
 struct ResortView {
     const uint32_t* keys_new;
     const uint32_t* pos;
     const uint32_t* q;
     const unsigned long long* list;
-    const uint32_t* newk;
-    const uint32_t* oldk;
     const uint32_t* scratch;  // [1] = M
     uint32_t mmax;
 };
 
-// First index in [lo, hi) of ascending a with a[i] >= x (hi if none).
-__device__ __forceinline__ uint32_t lower_idx(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+// First index in [0, m) of ascending a with a[i] >= x (m if none).
+__device__ __forceinline__ uint32_t lower_idx(const uint32_t* a, uint32_t m, uint32_t x) {
+    uint32_t lo = 0, hi = m;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (a[mid] < x) lo = mid + 1;
@@ -944,8 +943,9 @@ __device__ __forceinline__ uint32_t lower_idx(const uint32_t* __restrict__ a, ui
     return lo;
 }
 
-// First index in [lo, hi) of ascending a with a[i] > x (hi if none).
-__device__ __forceinline__ uint32_t upper_idx(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+// First index in [0, m) of ascending a with a[i] > x (m if none).
+__device__ __forceinline__ uint32_t upper_idx(const uint32_t* a, uint32_t m, uint32_t x) {
+    uint32_t lo = 0, hi = m;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (a[mid] <= x) lo = mid + 1;
@@ -954,41 +954,32 @@ __device__ __forceinline__ uint32_t upper_idx(const uint32_t* __restrict__ a, ui
     return lo;
 }
 
-// Sorted positions [b0, b1) (b0 < b1) read the re-sort's lists only in a
-// window: moved entries placed in the block are pos[p0, p1); position k
-// holds, if no moved entry, unmoved rank u = k - lo(k) with lo(k) in
-// [p0, p1], so u in [b0 - p1, b1 - 1 - p0], and its slot is u + t(u), where
-// t(u) = #{j : q_j <= u} is monotone and so lies in [t(umin), t(umax)].
-// Thread 0 finds the window; each thread then searches a few entries.
-struct SortedWindow {
-    uint32_t p0, p1, q0, q1;
-};
-
-__device__ __forceinline__ SortedWindow sorted_window(uint32_t b0, uint32_t b1, uint32_t M, const ResortView& rv) {
-    SortedWindow w;
-    w.p0 = lower_idx(rv.pos, 0, M, b0);
-    w.p1 = lower_idx(rv.pos, w.p0, M, b1);
-    const uint32_t umin = b0 > w.p1 ? b0 - w.p1 : 0u;
-    const uint32_t umax = b1 - 1 - w.p0;
-    w.q0 = upper_idx(rv.q, 0, M, umin);
-    w.q1 = upper_idx(rv.q, w.q0, M, umax);
-    return w;
+// Copies the re-sort's positions and slot - rank lists (M <= kResortMaxCap)
+// into the block's shared memory; every thread calls it.
+__device__ __forceinline__ void load_resort_lists(const ResortView& rv, uint32_t M, uint32_t* s_pos, uint32_t* s_q) {
+    for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
+        s_pos[i] = rv.pos[i];
+        s_q[i] = rv.q[i];
+    }
+    __syncthreads();
 }
 
-// Source slot and key of sorted position k in its block's window.  An
-// unmoved slot's new key is its previous one.
+// Source slot and key of sorted position k: a moved entry where one was
+// placed, else the unmoved slot of rank u = k - (moved entries placed
+// before k), which is u + #{moved slots s_j with s_j - j <= u}.  An unmoved
+// slot's new key is its previous one.
 template <bool KEY>
-__device__ __forceinline__ void sorted_entry(uint32_t k, const SortedWindow& w, const ResortView& rv, uint32_t n,
-                                             uint32_t& src, uint32_t& key) {
-    const uint32_t lo = lower_idx(rv.pos, w.p0, w.p1, k);
-    if (lo < w.p1 && rv.pos[lo] == k) {
+__device__ __forceinline__ void sorted_entry(uint32_t k, uint32_t M, const uint32_t* s_pos, const uint32_t* s_q,
+                                             const ResortView& rv, uint32_t n, uint32_t& src, uint32_t& key) {
+    const uint32_t lo = lower_idx(s_pos, M, k);
+    if (lo < M && s_pos[lo] == k) {
         const unsigned long long c = rv.list[lo];
         src = (uint32_t)c;
         if (KEY) key = (uint32_t)(c >> 32);
         return;
     }
     const uint32_t u = k - lo;
-    src = u + upper_idx(rv.q, w.q0, w.q1, u);
+    src = u + upper_idx(s_q, M, u);
     if (KEY) key = src < n ? rv.keys_new[src] : 0u;
 }
 
@@ -997,83 +988,69 @@ __device__ __forceinline__ void sorted_entry(uint32_t k, const SortedWindow& w, 
 // position k needs the entry of slot src(k); where src(k) == k -- every
 // slot but those shifted by the moved keys -- nothing moves.  Phase 1
 // gathers the others into the free buffer T (the step's input state, no
-// longer read) and, with the re-sort's order, shifts the cell table by the
-// moved keys: cell_start[c] counts the entries with key < c, so it changes
-// by (moved entries whose new key < c) - (moved entries whose old key < c).
+// longer read) and, with the re-sort's order, shifts the cell table:
+// cell_start[c] counts the entries with key < c, so an entry moving from
+// key a to key b takes one from the cells (a, b] when b > a and adds one to
+// (b, a] when b < a (atomic adds: several entries may share cells).
 // Phase 2 copies the gathered entries back, records every position's key
 // and, for the radix passes' order (more moves than the re-sort takes),
 // rebuilds the cell table as the plain reorder does.
 __global__ void __launch_bounds__(kReorderThreads)
 dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ vals,
-                      const float4* __restrict__ s_pos, const float4* __restrict__ s_vel,
+                      const float4* __restrict__ s_pos4, const float4* __restrict__ s_vel,
                       const float4* __restrict__ s_omg, float4* __restrict__ t_pos, float4* __restrict__ t_vel,
-                      float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start, ResortView rv) {
-    __shared__ SortedWindow s_w;
-    __shared__ uint32_t s_a0, s_a1, s_o0, s_o1;
+                      float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start,
+                      const uint32_t* __restrict__ keys_prev, ResortView rv) {
+    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
-    const uint32_t b0 = blockIdx.x * kReorderThreads;
-    const uint32_t k = b0 + threadIdx.x;
-    if (inc) {
-        if (threadIdx.x == 0 && b0 < n) s_w = sorted_window(b0, min(b0 + kReorderThreads, n), M, rv);
-        __syncthreads();
-    }
+    const uint32_t k = blockIdx.x * kReorderThreads + threadIdx.x;
+    if (inc) load_resort_lists(rv, M, s_pos, s_q);
     if (k < n) {
         uint32_t src, key;
-        if (inc) sorted_entry<false>(k, s_w, rv, n, src, key);
+        if (inc) sorted_entry<false>(k, M, s_pos, s_q, rv, n, src, key);
         else src = vals[k];
         if (src != k && src < n) {
-            t_pos[k] = s_pos[src];
+            t_pos[k] = s_pos4[src];
             t_vel[k] = s_vel[src];
             t_omg[k] = s_omg[src];
         }
     }
-    if (!inc || M == 0) return;
-    for (uint32_t base = b0; base <= ncells; base += gridDim.x * kReorderThreads) {
-        const uint32_t c = base + threadIdx.x, c1 = base + kReorderThreads;
-        __syncthreads();
-        if (threadIdx.x == 0) {  // the block's windows in the new and old key lists
-            s_a0 = lower_idx(rv.newk, 0, M, base);
-            s_a1 = lower_idx(rv.newk, s_a0, M, c1);
-            s_o0 = lower_idx(rv.oldk, 0, M, base);
-            s_o1 = lower_idx(rv.oldk, s_o0, M, c1);
-        }
-        __syncthreads();
-        if (c <= ncells) {
-            const uint32_t a = lower_idx(rv.newk, s_a0, s_a1, c);
-            const uint32_t b = lower_idx(rv.oldk, s_o0, s_o1, c);
-            if (a != b) cell_start[c] = cell_start[c] + a - b;
-        }
+    if (!inc) return;
+    for (uint32_t r = blockIdx.x; r < M; r += gridDim.x) {  // one moved entry per block
+        const unsigned long long c = rv.list[r];
+        const uint32_t b = min((uint32_t)(c >> 32), ncells), slot = (uint32_t)c;
+        const uint32_t a = slot < n ? min(keys_prev[slot], ncells) : b;
+        const uint32_t lo = min(a, b) + 1, hi = max(a, b);  // cells [lo, hi]
+        const uint32_t d = b > a ? 0xffffffffu : 1u;          // -1 or +1
+        for (uint32_t cc = lo + threadIdx.x; cc <= hi; cc += kReorderThreads) atomicAdd(&cell_start[cc], d);
     }
 }
 
 __global__ void __launch_bounds__(kReorderThreads)
 dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ keys,
                      const uint32_t* __restrict__ vals, const float4* __restrict__ t_pos,
-                     const float4* __restrict__ t_vel, const float4* __restrict__ t_omg, float4* __restrict__ s_pos,
+                     const float4* __restrict__ t_vel, const float4* __restrict__ t_omg, float4* __restrict__ s_pos4,
                      float4* __restrict__ s_vel, float4* __restrict__ s_omg, uint32_t* __restrict__ cell_start,
                      uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
-    __shared__ SortedWindow s_w;
+    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
     const uint32_t k = b0 + threadIdx.x;
-    if (inc) {
-        if (threadIdx.x == 0) s_w = sorted_window(b0, b1, M, rv);
-        __syncthreads();
-    }
+    if (inc) load_resort_lists(rv, M, s_pos, s_q);
     if (k < n) {
         uint32_t src, key;
         if (inc) {
-            sorted_entry<true>(k, s_w, rv, n, src, key);
+            sorted_entry<true>(k, M, s_pos, s_q, rv, n, src, key);
         } else {
             src = vals[k];
             key = keys[k];
         }
         if (src != k && src < n) {
-            s_pos[k] = t_pos[k];
+            s_pos4[k] = t_pos[k];
             s_vel[k] = t_vel[k];
             const float4 o = t_omg[k];
             s_omg[k] = o;
@@ -1429,10 +1406,10 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     if (dem_step_swaps(b)) {  // sorted in place: the next state stays in the *_n buffers
         const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
         const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
-        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_newk, b.rs_oldk, b.rs_scratch, b.rs_max};
+        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
         const unsigned grid = grid_for(b.n, kReorderThreads);
         dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, v, b.pos_n, b.vel_n, b.omg_n, b.pos,
-                                                                b.vel, b.omg, b.cell_start, rv);
+                                                                b.vel, b.omg, b.cell_start, b.keys_prev, rv);
         dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
                                                                b.vel_n, b.omg_n, b.cell_start,
                                                                b.nb ? b.slot_of : nullptr, b.keys_prev, rv);

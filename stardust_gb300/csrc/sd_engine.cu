@@ -407,7 +407,6 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
         (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_pos, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_q, (size_t)sd::kResortMaxCap)) ||
-        (s = dev_alloc(h, &B.rs_oldk, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_newk, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->cfg.flags & SD_FLAG_RECORD) {

@@ -243,8 +243,6 @@ struct DemBuffers {
     unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), up to kResortMaxCap
     uint32_t* rs_pos;               // per moved entry (in (key, slot) order): its sorted position
     uint32_t* rs_q;                 // per moved slot (ascending): slot - rank
-    uint32_t* rs_newk;              // per moved entry (in (key, slot) order): its new key
-    uint32_t* rs_oldk;              // per moved slot (ascending): its previous key
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
 };

@@ -63,7 +63,6 @@ __device__ void bitonic_sort(unsigned long long* v, uint32_t P) {
 __global__ void __launch_bounds__(kRsThreads)
 resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __restrict__ keys_prev, uint32_t n,
                    unsigned long long* __restrict__ list, uint32_t* __restrict__ pos_out, uint32_t* __restrict__ q_out,
-                   uint32_t* __restrict__ oldk_out, uint32_t* __restrict__ newk_out,
                    uint32_t mmax, uint32_t* __restrict__ scratch, const uint32_t* __restrict__ cell_start,
                    uint32_t ncells) {
     __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
@@ -140,12 +139,8 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
             else hi = mid;
         }
         list[r] = c;
-        newk_out[r] = key;
         pos_out[r] = r + x - lo;
         q_out[r] = (uint32_t)s_b[r] - r;
-        // the previous keys of the moved slots, ascending (slots ascending,
-        // keys_prev sorted): the cell table's shift subtracts them
-        oldk_out[r] = keys_prev[(uint32_t)s_b[r]];
     }
 }
 
@@ -163,9 +158,8 @@ cudaError_t resort_async(const DemBuffers& b, cudaStream_t st) {
     if (n == 0 || mmax == 0) return cudaSuccess;
     if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
     const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
-    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_list, b.rs_pos, b.rs_q,
-                                                      b.rs_oldk, b.rs_newk, mmax, b.rs_scratch, b.cell_start,
-                                                      b.ncells);
+    resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_list, b.rs_pos, b.rs_q, mmax,
+                                                      b.rs_scratch, b.cell_start, b.ncells);
     return cudaGetLastError();
 }
 
