@@ -34,8 +34,10 @@
 namespace sd {
 namespace {
 
-constexpr int kRsThreads = 256;
-constexpr uint32_t kRsWordsPerWarp = 16;
+// 1024 threads, so that the last block sorts the moved list with 1024
+// threads; 4 words of 32 slots per warp, 4096 slots per block
+constexpr int kRsThreads = 1024;
+constexpr uint32_t kRsWordsPerWarp = 4;
 constexpr uint32_t kRsBlockWords = kRsWordsPerWarp * kRsThreads / kWarp;  // 128 words: 4096 slots
 
 // Sorts v[0, P) ascending in shared memory (P a power of two; every thread
