@@ -229,6 +229,15 @@ struct ClumpCtx {
     float4* __restrict__ st;               // per slot: torque handed to the body
 };
 
+// Contact partner lists of the two-kernel contact stage (scenes without
+// clumps or meshes): per slot a count and up to kNbrCap partner slots,
+// appended in any order by dem_pair_lists_kernel.
+constexpr uint32_t kNbrCap = 16;
+struct NbrLists {
+    uint32_t* cnt;
+    const uint32_t* nbr;
+};
+
 // True when slot s holds a sphere of the same rigid body as the clump sphere
 // with id bits `idb` (such pairs are skipped, collision_resolution.cu:69).
 __device__ __forceinline__ bool same_body(const ClumpCtx& cc, uint32_t idb, const float4* __restrict__ omg,
@@ -342,7 +351,7 @@ __device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView
 // the next-state write.  Returns the new cell key; a clump sphere hands its
 // force and torque to its body instead (the body kernel writes its next
 // state and key) and *has_key is false.
-template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false, bool MESH = false>
+template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false, bool MESH = false, bool LISTED = false>
 __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                   const float4* __restrict__ omg,
@@ -352,7 +361,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   uint32_t* __restrict__ vals, float4* __restrict__ force,
                                                   float4* __restrict__ torque, uint32_t& contacts,
                                                   const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{},
-                                                  const MeshView* mesh = nullptr) {
+                                                  const MeshView* mesh = nullptr, const NbrLists* nl = nullptr) {
     const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
@@ -381,6 +390,35 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
         axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
         axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
         axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
+    }
+    if constexpr (LISTED) {
+        // the partners found by the pair kernel, applied in ascending slot
+        // order -- the order of the scan below (columns in key order, slots
+        // ascending in each) -- unless the list overflowed
+        const uint32_t c = nl->cnt[i];
+        nl->cnt[i] = 0u;  // cleared for the next step's pair kernel
+        if (c <= kNbrCap) {
+            x1 = x0 - 1;  // no scan
+            uint32_t js[kNbrCap];
+            for (uint32_t k = 0; k < c; ++k) {
+                const uint32_t v = nl->nbr[(size_t)i * kNbrCap + k];
+                uint32_t m = k;
+                for (; m > 0 && js[m - 1] > v; --m) js[m] = js[m - 1];
+                js[m] = v;
+            }
+            for (uint32_t k = 0; k < c; ++k) {
+                const uint32_t s = js[k];
+                if (s >= n) continue;
+                const float4 pa = src.load(s);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float da = dist2(ax, ay, az);
+                const float ra = ri + pa.w;
+                if (da < ra * ra && da != 0.0f) {
+                    ++contacts;
+                    pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                }
+            }
+        }
     }
     for (int32_t X = x0; X <= x1; ++X) {
         for (int32_t Y = y0; Y <= y1; ++Y) {
@@ -541,7 +579,52 @@ __device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contac
 }
 
 // ---------------------------------------------- contact_mode 0: per slot
-template <bool RECORD, bool CLUMPS, bool BATCHED = false, bool MESH = false>
+// The first kernel of the two-kernel contact stage: each candidate pair is
+// tested once, by its lower slot, over the upper part of that sphere's
+// candidate window (the columns after its own, and its own column above
+// it).  The test is symmetric -- x_j - x_i is the exact negation of
+// x_i - x_j and r_i + r_j commutes -- so it decides exactly as the
+// partner's own scan would, and every pair in contact lies in the lower
+// slot's window.  A contact is appended to both spheres' lists.
+template <bool BATCHED>
+__global__ void __launch_bounds__(256)
+dem_pair_lists_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
+                      const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ cnt,
+                      uint32_t* __restrict__ nbr, Batch bt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
+    const float4 pi = __ldg(&pos[i]);
+    const float ri = pi.w;
+    const float reach = (ri + p.rmax) * 1.00001f;
+    int32_t x0, x1, y0, y1, z0, z1;
+    const float ic = 1.0f / g.cell;
+    axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
+    axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
+    axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
+    for (int32_t X = x0; X <= x1; ++X) {
+        for (int32_t Y = y0; Y <= y1; ++Y) {
+            const uint32_t col = g.base + (uint32_t)((X * g.ny + Y) * g.nz);
+            const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)z1 + 1]), n);
+            if (s1 <= i + 1) continue;  // the column holds no slot above i
+            uint32_t s = max(__ldg(&cell_start[col + (uint32_t)z0]), i + 1);
+            for (; s < s1; ++s) {
+                const float4 pa = __ldg(&pos[s]);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float da = dist2(ax, ay, az);
+                const float ra = ri + pa.w;
+                if (__builtin_expect(da < ra * ra && da != 0.0f, 0)) {
+                    const uint32_t a = atomicAdd(&cnt[i], 1u);
+                    if (a < kNbrCap) nbr[(size_t)i * kNbrCap + a] = s;
+                    const uint32_t b = atomicAdd(&cnt[s], 1u);
+                    if (b < kNbrCap) nbr[(size_t)s * kNbrCap + b] = i;
+                }
+            }
+        }
+    }
+}
+
+template <bool RECORD, bool CLUMPS, bool BATCHED = false, bool MESH = false, bool LISTED = false>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -550,16 +633,16 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
-                             ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{}) {
+                             ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{},
+                             NbrLists nl = NbrLists{}) {
     __shared__ uint32_t s_hist[kHistWords];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     if (i < n)
-        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH>(p, n, i, GlobalSource{pos}, pos, vel, omg,
-                                                                          cell_start, pos_n, vel_n, omg_n, keys, vals,
-                                                                          force, torque, contacts, cc, &has_key, bt,
-                                                                          &mesh);
+        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, LISTED>(
+            p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
+            contacts, cc, &has_key, bt, &mesh, &nl);
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
@@ -1312,6 +1395,10 @@ cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream
 }
 
 static int g_contact_mode = 0;  // 0: per slot (default), 1: TMA column tiles
+static int g_pair_lists = 1;    // scenes without clumps or meshes: pair kernel + listed contacts
+
+void dem_set_pair_lists(int on) { g_pair_lists = on ? 1 : 0; }
+int dem_pair_lists() { return g_pair_lists; }
 
 void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
 int dem_contact_mode() { return g_contact_mode; }
@@ -1333,9 +1420,24 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
-        dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+        const Batch bt{b.scenes, b.scene_first, b.nscenes};
+        if (g_pair_lists && b.nbr_cnt) {
+            dem_pair_lists_kernel<true><<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt,
+                                                                             b.nbr, bt);
+            dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{b.nbr_cnt, b.nbr});
+        } else {
+            dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                b.dev_status, spec, ghist, cc, bt);
+        }
+    } else if (g_contact_mode == 0 && !b.nb && g_pair_lists && b.nbr_cnt) {
+        dem_pair_lists_kernel<false><<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt,
+                                                                          b.nbr, Batch{});
+        dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist, cc, Batch{b.scenes, b.scene_first, b.nscenes});
+            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{b.nbr_cnt, b.nbr});
     } else if (g_contact_mode == 0) {
         if (b.nb)
             dem_contact_integrate_kernel<RECORD, true><<<grid_for(b.n, 256), 256, 0, st>>>(

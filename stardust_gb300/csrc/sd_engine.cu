@@ -409,6 +409,10 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &B.rs_pos, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_q, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
+    if (h->hb_pos.empty() && h->mesh.tri.empty() && n) {  // the two-kernel contact stage's partner lists
+        if ((s = dev_alloc(h, &B.nbr_cnt, n)) || (s = dev_alloc(h, &B.nbr, (size_t)n * 16))) return s;
+        SD_CUDA(h, cudaMemsetAsync(B.nbr_cnt, 0, sizeof(uint32_t) * n, h->stream));
+    }
     if (h->cfg.flags & SD_FLAG_RECORD) {
         if ((s = dev_alloc(h, &B.force, n)) || (s = dev_alloc(h, &B.torque, n))) return s;
         SD_CUDA(h, cudaMemsetAsync(B.force, 0, sizeof(float4) * std::max<uint32_t>(n, 1), h->stream));
@@ -1290,6 +1294,9 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
+    } else if (k == "pair_lists") {
+        if (value != 0 && value != 1) return fail(nullptr, SD_ERR_INVALID_ARG, "pair_lists must be 0 or 1");
+        sd::dem_set_pair_lists(value);
     } else if (k == "resort_max") {
         if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)
             return fail(nullptr, SD_ERR_INVALID_ARG, "resort_max must be 0 or a power of two up to 1024");
@@ -1308,6 +1315,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "sort_items") *value = sd::sort_items();
     else if (k == "z_div") *value = g_z_div;
     else if (k == "resort_max") *value = (int32_t)sd::dem_resort_max();
+    else if (k == "pair_lists") *value = sd::dem_pair_lists();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }

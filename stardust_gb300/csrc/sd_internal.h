@@ -245,6 +245,9 @@ struct DemBuffers {
     uint32_t* rs_q;                 // per moved slot (ascending): slot - rank
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
+    // contact partner lists (scenes without clumps): per slot a count, zero
+    // between steps, and 16 partner slots; null when not allocated
+    uint32_t *nbr_cnt, *nbr;
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
@@ -260,6 +263,8 @@ uint64_t resort_scratch_words(uint32_t n);
 cudaError_t resort_async(const DemBuffers& b, cudaStream_t st);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
+void dem_set_pair_lists(int on);
+int dem_pair_lists();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
 // Counts, into *count (device), the slots whose key from the current position
 // differs from the sorted key they sit under.

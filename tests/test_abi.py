@@ -295,3 +295,16 @@ def test_resort_max_knob(sdlib):
                 _abi.tune_set("resort_max", v)
     finally:
         _abi.tune_set("resort_max", old)
+
+
+def test_pair_lists_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("pair_lists")
+    assert old == 1
+    try:
+        _abi.tune_set("pair_lists", 0)
+        assert _abi.tune_get("pair_lists") == 0
+        with pytest.raises(Exception):
+            _abi.tune_set("pair_lists", 2)
+    finally:
+        _abi.tune_set("pair_lists", old)
