@@ -1395,7 +1395,7 @@ cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream
 }
 
 static int g_contact_mode = 0;  // 0: per slot (default), 1: TMA column tiles
-static int g_pair_lists = 1;    // scenes without clumps or meshes: pair kernel + listed contacts
+static int g_pair_lists = 0;    // scenes without clumps or meshes: pair kernel + listed contacts
 
 void dem_set_pair_lists(int on) { g_pair_lists = on ? 1 : 0; }
 int dem_pair_lists() { return g_pair_lists; }

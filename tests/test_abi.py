@@ -300,10 +300,10 @@ def test_resort_max_knob(sdlib):
 def test_pair_lists_knob(sdlib):
     from stardust_gb300 import _abi
     old = _abi.tune_get("pair_lists")
-    assert old == 1
+    assert old == 0
     try:
-        _abi.tune_set("pair_lists", 0)
-        assert _abi.tune_get("pair_lists") == 0
+        _abi.tune_set("pair_lists", 1)
+        assert _abi.tune_get("pair_lists") == 1
         with pytest.raises(Exception):
             _abi.tune_set("pair_lists", 2)
     finally:
