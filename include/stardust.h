@@ -463,7 +463,12 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *   "resort_max"    most changed cell keys the step re-sorts incrementally (a merge of
  *                   the changed entries into the previous order) instead of running the
  *                   radix passes: 0 (always the passes) or a power of two up to 1024;
- *                   default 1024.  Same result either way (a stable sort by key) */
+ *                   default 1024.  Same result either way (a stable sort by key)
+ *   "pair_lists"    scenes without clumps or meshes: 1 = a pair kernel tests each candidate
+ *                   pair once and lists up to 16 contacts per sphere, which the contact
+ *                   kernel applies in slot order (a full scan for an overflowed list);
+ *                   0 = one scan kernel; 2 (default) = lists for batches of scenes only.
+ *                   Same bits either way */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

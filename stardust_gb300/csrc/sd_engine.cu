@@ -1295,7 +1295,7 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
     } else if (k == "pair_lists") {
-        if (value != 0 && value != 1) return fail(nullptr, SD_ERR_INVALID_ARG, "pair_lists must be 0 or 1");
+        if (value < 0 || value > 2) return fail(nullptr, SD_ERR_INVALID_ARG, "pair_lists must be 0, 1 or 2");
         sd::dem_set_pair_lists(value);
     } else if (k == "resort_max") {
         if (value < 0 || value > (int32_t)sd::kResortMaxCap || (value & (value - 1)) != 0)

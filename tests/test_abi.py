@@ -300,11 +300,12 @@ def test_resort_max_knob(sdlib):
 def test_pair_lists_knob(sdlib):
     from stardust_gb300 import _abi
     old = _abi.tune_get("pair_lists")
-    assert old == 0
+    assert old == 2
     try:
-        _abi.tune_set("pair_lists", 1)
-        assert _abi.tune_get("pair_lists") == 1
+        for v in (0, 1, 2):
+            _abi.tune_set("pair_lists", v)
+            assert _abi.tune_get("pair_lists") == v
         with pytest.raises(Exception):
-            _abi.tune_set("pair_lists", 2)
+            _abi.tune_set("pair_lists", 3)
     finally:
         _abi.tune_set("pair_lists", old)
