@@ -505,7 +505,7 @@ def run_ours(args, rank, world, local):
         tuned = autotune.tune_engine(eng, dt, reps=5)
         log(f"autotune: {tuned}")
     # the knobs this workload is timed with (later sections tune their own)
-    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max")}
+    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max", "pair_lists")}
 
     def barrier():
         torch.cuda.synchronize()
