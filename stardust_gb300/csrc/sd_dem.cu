@@ -1048,22 +1048,23 @@ __device__ __forceinline__ void load_resort_lists(const ResortView& rv, uint32_t
 }
 
 // Source slot and key of sorted position k: a moved entry where one was
-// placed, else the unmoved slot of rank u = k - (moved entries placed
-// before k), which is u + #{moved slots s_j with s_j - j <= u}.  An unmoved
-// slot's new key is its previous one.
+// placed (returns true), else the unmoved slot of rank u = k - (moved
+// entries placed before k), which is u + #{moved slots s_j with s_j - j <=
+// u}.  An unmoved slot's new key is its previous one.
 template <bool KEY>
-__device__ __forceinline__ void sorted_entry(uint32_t k, uint32_t M, const uint32_t* s_pos, const uint32_t* s_q,
+__device__ __forceinline__ bool sorted_entry(uint32_t k, uint32_t M, const uint32_t* s_pos, const uint32_t* s_q,
                                              const ResortView& rv, uint32_t n, uint32_t& src, uint32_t& key) {
     const uint32_t lo = lower_idx(s_pos, M, k);
     if (lo < M && s_pos[lo] == k) {
         const unsigned long long c = rv.list[lo];
         src = (uint32_t)c;
         if (KEY) key = (uint32_t)(c >> 32);
-        return;
+        return true;
     }
     const uint32_t u = k - lo;
     src = u + upper_idx(s_q, M, u);
     if (KEY) key = src < n ? rv.keys_new[src] : 0u;
+    return false;
 }
 
 // The in-place reorder of a step whose next state stays where the contact
@@ -1125,9 +1126,13 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
     const uint32_t k = b0 + threadIdx.x;
     if (inc) load_resort_lists(rv, M, s_pos, s_q);
     if (k < n) {
-        uint32_t src, key;
+        uint32_t src, key = 0;
         if (inc) {
-            sorted_entry<true>(k, M, s_pos, s_q, rv, n, src, key);
+            // a position that keeps its unmoved entry keeps its key too:
+            // nothing to write there
+            const bool moved = sorted_entry<false>(k, M, s_pos, s_q, rv, n, src, key);
+            if (src == k && !moved) return;  // no block-wide step follows in this mode
+            key = moved ? (uint32_t)(rv.list[lower_idx(s_pos, M, k)] >> 32) : (src < n ? rv.keys_new[src] : 0u);
         } else {
             src = vals[k];
             key = keys[k];
