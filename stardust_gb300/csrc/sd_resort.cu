@@ -16,9 +16,10 @@
 //      r plus the unmoved slots that sort before it -- the previous step's
 //      cell table bounds the slots of its key, so that count is its slot
 //      clamped to that range minus the moved slots below it;
-//   2. the reorder (dem_reorder_kernel) reads the order from these lists:
-//      position k holds a moved entry where one was placed, else the
-//      unmoved slot of rank k - (moved entries placed before k).
+//   2. the in-place reorder (dem_fix_gather_kernel, dem_fix_place_kernel in
+//      sd_dem.cu) reads the order from these lists: position k holds a moved
+//      entry where one was placed, else the unmoved slot of rank
+//      k - (moved entries placed before k).
 //
 // The unmoved slots are already in (key, slot) order, so this is a merge of
 // two sorted sequences and the result is exactly the stable LSD sort's.
