@@ -201,3 +201,32 @@ def test_cube_particle_drop(sdlib):
     assert np.linalg.norm(v) < 0.05
     assert eng.stats()["device_errors"] == 0
     eng.close()
+
+
+def test_clumps_under_every_resort_setting(sdlib):
+    """Clump scenes through the re-sort's both orders: radix passes only
+    (resort_max 0), mostly the passes with the in-place reorder's fallback
+    copy (2), and the incremental order (1024) -- the same bits, body states
+    included (the slot table the body kernel reads follows every order)."""
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("resort_max")
+    outs = []
+    try:
+        for rm in (0, 2, 1024):
+            _abi.tune_set("resort_max", rm)
+            eng, dt, *_ = build(sdlib, n_side=7, seed=3)
+            moved = []
+            for _ in range(30):
+                eng.step(dt, 2)
+                moved.append(eng.stats()["moved_keys"])
+            eng.sync()
+            assert eng.stats()["device_errors"] == 0
+            outs.append((eng.positions(), eng.velocities(), eng.bodies(_abi.SD_BODY_QUATERNION),
+                         eng.bodies(_abi.SD_BODY_POSITION), moved))
+            eng.close()
+    finally:
+        _abi.tune_set("resort_max", old)
+    assert max(outs[1][4]) > 2  # the fallback ran
+    for o in outs[1:]:
+        for a, b in zip(outs[0][:4], o[:4]):
+            assert np.array_equal(bits(a), bits(b))
