@@ -536,8 +536,12 @@ def run_ours(args, rank, world, local):
     kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     stage_ms = {}
-    for name, stage in (("contact_integrate", _abi.SD_STAGE_CONTACT), ("sort", _abi.SD_STAGE_SORT),
-                        ("reorder", _abi.SD_STAGE_REORDER)):
+    # the stage API's stages, each timed alone: the step graph runs the
+    # contact stage as is, but replaces the full radix sort and the gather
+    # reorder with the incremental re-sort and the in-place reorder when few
+    # cell keys changed (stages_note in the JSON line)
+    for name, stage in (("contact_integrate", _abi.SD_STAGE_CONTACT), ("radix_sort", _abi.SD_STAGE_SORT),
+                        ("gather_reorder", _abi.SD_STAGE_REORDER)):
         ms = []
         for k in range(args.steps):
             with torch.cuda.stream(stream):
@@ -649,6 +653,9 @@ def run_ours(args, rank, world, local):
                 "frac": winst_ps * n / (contact_ms * 1e-3) / (SMS * SCHEDULERS_PER_SM * clocks_mhz(clocks) * 1e6),
                 "warp_instructions": winst_ps * n, "sm_mhz": clocks_mhz(clocks)},
             "stages_ms": stage_ms,
+            "stages_note": "sd_engine_launch_stage stages timed alone; in the step graph the radix sort and gather "
+                           "reorder give way to the incremental re-sort (scan) and in-place reorder while at most "
+                           "resort_max keys change (profiles/dem_step_1M_launches.md has the step's kernels)",
             "step_bytes_per_sphere": STEP_BYTES_PER_SPHERE,
             "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
             "cpu_baseline": cpu,
