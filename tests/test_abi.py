@@ -309,3 +309,27 @@ def test_pair_lists_knob(sdlib):
             _abi.tune_set("pair_lists", 3)
     finally:
         _abi.tune_set("pair_lists", old)
+
+
+@pytest.mark.parametrize("cname,pyname", [("sd_config", "SdConfig"), ("sd_stats", "SdStats"),
+                                          ("sd_params", "SdParams")])
+def test_struct_layouts_match_the_header(tmp_path, cname, pyname):
+    """The ctypes mirrors of the C structs have the header's size and every
+    field at the header's offset (compiled with the host C compiler)."""
+    import shutil
+    import subprocess
+    from stardust_gb300 import _abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    py = getattr(_abi, pyname)
+    fields = [f[0] for f in py._fields_]
+    lines = [f'printf("%zu\\n", sizeof({cname}));'] + [f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "stardust.h"\nint main(void) {\n'
+                   + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert out[0] == C.sizeof(py)
+    assert out[1:] == [getattr(py, f).offset for f in fields]
