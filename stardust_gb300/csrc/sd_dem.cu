@@ -232,7 +232,6 @@ struct ClumpCtx {
 // Contact partner lists of the two-kernel contact stage (scenes without
 // clumps or meshes): per slot a count and up to kNbrCap partner slots,
 // appended in any order by dem_pair_lists_kernel.
-constexpr uint32_t kNbrCap = 16;
 struct NbrLists {
     uint32_t* cnt;
     const uint32_t* nbr;

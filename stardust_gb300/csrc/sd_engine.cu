@@ -410,7 +410,7 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->hb_pos.empty() && h->mesh.tri.empty() && n) {  // the two-kernel contact stage's partner lists
-        if ((s = dev_alloc(h, &B.nbr_cnt, n)) || (s = dev_alloc(h, &B.nbr, (size_t)n * 16))) return s;
+        if ((s = dev_alloc(h, &B.nbr_cnt, n)) || (s = dev_alloc(h, &B.nbr, (size_t)n * sd::kNbrCap))) return s;
         SD_CUDA(h, cudaMemsetAsync(B.nbr_cnt, 0, sizeof(uint32_t) * n, h->stream));
     }
     if (h->cfg.flags & SD_FLAG_RECORD) {

@@ -246,11 +246,12 @@ struct DemBuffers {
     uint32_t* rs_scratch;           // running count, moved count, arrivals
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
     // contact partner lists (scenes without clumps): per slot a count, zero
-    // between steps, and 16 partner slots; null when not allocated
+    // between steps, and kNbrCap partner slots; null when not allocated
     uint32_t *nbr_cnt, *nbr;
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
+constexpr uint32_t kNbrCap = 16;  // contact partners listed per sphere by the pair kernel
 
 int dem_key_bits(uint32_t ncells);
 // incremental re-sort (sd_resort.cu): when at most b.rs_max keys of b.keys
