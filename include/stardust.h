@@ -468,7 +468,13 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   pair once and lists up to 16 contacts per sphere, which the contact
  *                   kernel applies in slot order (a full scan for an overflowed list);
  *                   0 = one scan kernel; 2 (default) = lists for batches of scenes only.
- *                   Same bits either way */
+ *                   Same bits either way
+ *   "skin_um"       single scenes of free spheres prepared afterwards: contact lists with a
+ *                   skin of this many micrometres (0, the default, = none).  A step that
+ *                   follows a sphere moving 0.45 skin from its position at the last build
+ *                   scans the window widened by the skin and lists each sphere's neighbours
+ *                   within r_i + r_j + skin; other steps test only the listed neighbours.
+ *                   Same contact set and order as the scan, so the same bits */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

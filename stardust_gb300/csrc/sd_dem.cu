@@ -237,6 +237,19 @@ struct NbrLists {
     const uint32_t* nbr;
 };
 
+// Skin lists of the single-scene free-sphere step: per sphere id its
+// neighbour ids within r_i + r_j + skin at the last build, the position
+// then, and the slot of every id this step.
+struct SkinLists {
+    uint32_t* cnt;            // per id; kVlCap + 1 = overflowed (the sphere scans)
+    uint32_t* nbr;            // per id, kVlCap neighbour ids
+    float4* ref;              // per id: position at the build
+    const uint32_t* flags;    // [0]: build this step
+    uint32_t* next;           // = flags + 1: set when a sphere left its skin
+    const uint32_t* slot_of;  // per id: slot this step
+    float skin, thr2;         // skin; (0.45 skin)^2, the displacement that forces a build
+};
+
 // True when slot s holds a sphere of the same rigid body as the clump sphere
 // with id bits `idb` (such pairs are skipped, collision_resolution.cu:69).
 __device__ __forceinline__ bool same_body(const ClumpCtx& cc, uint32_t idb, const float4* __restrict__ omg,
@@ -350,7 +363,8 @@ __device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView
 // the next-state write.  Returns the new cell key; a clump sphere hands its
 // force and torque to its body instead (the body kernel writes its next
 // state and key) and *has_key is false.
-template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false, bool MESH = false, bool LISTED = false>
+template <bool RECORD, bool CLUMPS, class SRC, bool BATCHED = false, bool MESH = false, bool LISTED = false,
+          bool SKIN = false>
 __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n, uint32_t i, const SRC& src,
                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                   const float4* __restrict__ omg,
@@ -360,7 +374,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   uint32_t* __restrict__ vals, float4* __restrict__ force,
                                                   float4* __restrict__ torque, uint32_t& contacts,
                                                   const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{},
-                                                  const MeshView* mesh = nullptr, const NbrLists* nl = nullptr) {
+                                                  const MeshView* mesh = nullptr, const NbrLists* nl = nullptr,
+                                                  const SkinLists* sk = nullptr) {
     const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
@@ -389,6 +404,82 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
         axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
         axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
         axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
+    }
+    if constexpr (SKIN) {
+        // A pair in contact now was within r_i + r_j + skin at the build:
+        // every sphere has moved less than 0.45 skin since (checked at the
+        // end of every step), so the distance changed by less than 0.9
+        // skin.  Contacts are applied in ascending slot order, the scan's.
+        const uint32_t id = idb & kIdMask;
+        if (sk->flags[0] != 0u) {  // build: the scan over the window widened by the skin
+            const float reach_b = (ri + p.rmax + sk->skin) * 1.00001f;
+            int32_t bx0, bx1, by0, by1, bz0, bz1;
+            axis_window(pi.x, reach_b, g.lo[0], 1.0f / g.cell, g.nx, bx0, bx1);
+            axis_window(pi.y, reach_b, g.lo[1], 1.0f / g.cell, g.ny, by0, by1);
+            axis_window(pi.z, reach_b, g.lo[2], 1.0f / g.cellz, g.nz, bz0, bz1);
+            uint32_t c = 0;
+            for (int32_t X = bx0; X <= bx1; ++X) {
+                for (int32_t Y = by0; Y <= by1; ++Y) {
+                    const uint32_t col = g.base + (uint32_t)((X * g.ny + Y) * g.nz);
+                    const uint32_t s0 = __ldg(&cell_start[col + (uint32_t)bz0]);
+                    const uint32_t s1 = min(__ldg(&cell_start[col + (uint32_t)bz1 + 1]), n);
+                    for (uint32_t s = s0; s < s1; ++s) {
+                        const float4 pa = src.load(s);
+                        const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                        const float da = dist2(ax, ay, az);
+                        if (da == 0.0f) continue;  // the sphere itself (or a coincident one: never a contact)
+                        const float rl = ri + pa.w + sk->skin;
+                        if (da < rl * rl) {
+                            if (c < kVlCap && id < n)
+                                sk->nbr[(size_t)id * kVlCap + c] =
+                                    __float_as_uint(__ldg(reinterpret_cast<const float*>(omg) + 4 * (size_t)s + 3)) &
+                                    kIdMask;
+                            ++c;
+                            const float ra = ri + pa.w;
+                            if (da < ra * ra) {
+                                ++contacts;
+                                pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                            }
+                        }
+                    }
+                }
+            }
+            if (id < n) {
+                sk->cnt[id] = min(c, kVlCap + 1);
+                sk->ref[id] = pi;
+            }
+            x1 = x0 - 1;  // no second scan
+        } else if (id < n && sk->cnt[id] <= kVlCap) {
+            const uint32_t c = sk->cnt[id];
+            uint32_t js[kVlCap];
+            uint32_t m = 0;
+            for (uint32_t k = 0; k < c; ++k) {  // the listed neighbours in contact, by ascending slot
+                const uint32_t jd = sk->nbr[(size_t)id * kVlCap + k];
+                if (jd >= n) continue;
+                const uint32_t s = sk->slot_of[jd];
+                if (s >= n) continue;
+                const float4 pa = src.load(s);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float da = dist2(ax, ay, az);
+                const float ra = ri + pa.w;
+                if (da < ra * ra && da != 0.0f) {
+                    uint32_t q = m++;
+                    for (; q > 0 && js[q - 1] > s; --q) js[q] = js[q - 1];
+                    js[q] = s;
+                }
+            }
+            for (uint32_t k = 0; k < m; ++k) {
+                const uint32_t s = js[k];
+                const float4 pa = src.load(s);
+                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+                const float da = dist2(ax, ay, az);
+                const float ra = ri + pa.w;
+                ++contacts;
+                pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+            }
+            x1 = x0 - 1;  // no scan
+        }
+        // else: an overflowed list -- the scan below
     }
     if constexpr (LISTED) {
         // the partners found by the pair kernel, applied in ascending slot
@@ -520,6 +611,13 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     vel_n[i] = make_float4(nvx, nvy, nvz, mi);
     omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia), wi.z + dt * (t.z / inertia),
                            wi.w);
+    if constexpr (SKIN) {  // left 0.45 skin of the build position: build next step
+        const uint32_t id = idb & kIdMask;
+        if (id < n) {
+            const float4 r = sk->ref[id];
+            if (dist2(nxp - r.x, nyp - r.y, nzp - r.z) > sk->thr2) atomicOr(sk->next, 1u);
+        }
+    }
     const uint32_t key = cell_key_g(g, nxp, nyp, nzp);
     keys[i] = key;
     vals[i] = i;
@@ -623,7 +721,8 @@ dem_pair_lists_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
     }
 }
 
-template <bool RECORD, bool CLUMPS, bool BATCHED = false, bool MESH = false, bool LISTED = false>
+template <bool RECORD, bool CLUMPS, bool BATCHED = false, bool MESH = false, bool LISTED = false,
+          bool SKIN = false>
 __global__ void __launch_bounds__(256)
 dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
                              const float4* __restrict__ vel, const float4* __restrict__ omg,
@@ -633,15 +732,15 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
                              ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{},
-                             NbrLists nl = NbrLists{}) {
+                             NbrLists nl = NbrLists{}, SkinLists sk = SkinLists{}) {
     __shared__ uint32_t s_hist[kHistWords];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     if (i < n)
-        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, LISTED>(
+        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, LISTED, SKIN>(
             p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
-            contacts, cc, &has_key, bt, &mesh, &nl);
+            contacts, cc, &has_key, bt, &mesh, &nl, &sk);
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
@@ -977,7 +1076,7 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
                    const float4* __restrict__ vel_n, const float4* __restrict__ omg_n,
                    float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ omg,
                    uint32_t* __restrict__ cell_start, uint32_t* __restrict__ slot_of,
-                   uint32_t* __restrict__ keys_prev) {
+                   uint32_t* __restrict__ keys_prev, bool slot_all) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     const uint32_t b0 = blockIdx.x * kReorderThreads;
     const uint32_t b1 = min(b0 + kReorderThreads, n);
@@ -991,7 +1090,7 @@ dem_reorder_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ key
             omg[k] = o;
             // clump spheres: where their body finds them next step
             const uint32_t idb = __float_as_uint(o.w);
-            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
+            if (slot_of && (slot_all || (idb & kClumpFlag)) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
         }
         const uint32_t key = keys[k];
         s_keys[threadIdx.x + 1] = key;
@@ -1115,7 +1214,8 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
                      const uint32_t* __restrict__ vals, const float4* __restrict__ t_pos,
                      const float4* __restrict__ t_vel, const float4* __restrict__ t_omg, float4* __restrict__ s_pos4,
                      float4* __restrict__ s_vel, float4* __restrict__ s_omg, uint32_t* __restrict__ cell_start,
-                     uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv) {
+                     uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv,
+                     bool slot_all) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
@@ -1142,7 +1242,7 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
             const float4 o = t_omg[k];
             s_omg[k] = o;
             const uint32_t idb = __float_as_uint(o.w);
-            if (slot_of && (idb & kClumpFlag) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
+            if (slot_of && (slot_all || (idb & kClumpFlag)) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
         }
         s_keys[threadIdx.x + 1] = key;
         keys_prev[k] = key;
@@ -1381,13 +1481,17 @@ cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
                             st, &b.sorted_in_tmp);
 }
 
+// The slot table covers every sphere when the skin lists use it, else only
+// clump spheres (null without clumps or lists).
+static bool slot_all_of(const DemBuffers& b) { return b.vl_skin > 0.0f && b.vl_cnt && !b.nb; }
+
 cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
     const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
     const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
     dem_reorder_kernel<<<grid_for(b.n, kReorderThreads), kReorderThreads, 0, st>>>(
         b.n, b.ncells, k, v, b.pos_n, b.vel_n, b.omg_n, b.pos, b.vel, b.omg, b.cell_start,
-        b.nb ? b.slot_of : nullptr, b.keys_prev);
+        b.slot_of, b.keys_prev, slot_all_of(b));
     return cudaGetLastError();
 }
 
@@ -1413,7 +1517,8 @@ void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
 int dem_contact_mode() { return g_contact_mode; }
 
 template <bool RECORD>
-static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st) {
+static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st,
+                             bool skin) {
     float4* f = RECORD ? b.force : nullptr;
     float4* t = RECORD ? b.torque : nullptr;
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
@@ -1441,6 +1546,12 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
                 b.dev_status, spec, ghist, cc, bt);
         }
+    } else if (skin) {  // single scene of free spheres, skin lists
+        const float thr = 0.45f * b.vl_skin;
+        const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
+        dem_contact_integrate_kernel<RECORD, false, false, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, sk);
     } else if (g_contact_mode == 0 && !b.nb && g_pair_lists == 1 && b.nbr_cnt) {
         dem_pair_lists_kernel<false><<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt,
                                                                           b.nbr, Batch{});
@@ -1471,15 +1582,15 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
 // Contact + integration of free spheres, then (with clumps) the body
 // kernel, which completes the next state and keys of the clump spheres.
 static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
-                                  uint32_t* ghist, cudaStream_t st) {
+                                  uint32_t* ghist, cudaStream_t st, bool skin = false) {
     if (b.n == 0) return cudaSuccess;
     const uint32_t spec = pack_hist_spec(plan);
     if (record) {
         cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        launch_contact_t<true>(p, b, spec, ghist, st);
+        launch_contact_t<true>(p, b, spec, ghist, st, skin);
     } else {
-        launch_contact_t<false>(p, b, spec, ghist, st);
+        launch_contact_t<false>(p, b, spec, ghist, st, skin);
     }
     if (b.nb) {
         dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
@@ -1507,10 +1618,11 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
     }
     cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
     if (e != cudaSuccess) return e;
-    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
+    const bool skin = dem_step_skin(b);
+    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st, skin)) != cudaSuccess) return e;
     // the re-sort places the moved keys when it can (the passes then return
     // at once and the reorder reads its order), else the passes sort
-    if ((e = resort_async(b, st)) != cudaSuccess) return e;
+    if ((e = resort_async(b, st, skin ? b.vl_flags : nullptr)) != cudaSuccess) return e;
     if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
                                &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
         return e;
@@ -1523,12 +1635,17 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
                                                                 b.vel, b.omg, b.cell_start, b.keys_prev, rv);
         dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
                                                                b.vel_n, b.omg_n, b.cell_start,
-                                                               b.nb ? b.slot_of : nullptr, b.keys_prev, rv);
+                                                               b.slot_of, b.keys_prev, rv, slot_all_of(b));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     } else if ((e = dem_reorder_async(b, st)) != cudaSuccess) {
         return e;
     }
     return mesh_advance_async(b.mesh, 1, st);
+}
+
+bool dem_step_skin(const DemBuffers& b) {
+    return b.vl_skin > 0.0f && b.vl_cnt && b.slot_of && !b.nb && !b.mesh.ntri && b.nscenes <= 1 &&
+           g_contact_mode == 0 && dem_step_swaps(b);
 }
 
 bool dem_step_swaps(const DemBuffers& b) {

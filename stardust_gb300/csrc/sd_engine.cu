@@ -135,6 +135,7 @@ static sd_status grid_dims(sd_engine* h, const float* lo, const float* hi, float
 // 4 0.169 ms, 8 0.171 ms; on the 2.1M-sphere drum (23-bit keys) any split
 // was slower (1 0.477 ms, 2 0.495 ms, 4 0.541 ms).
 static int32_t g_z_div = 0;
+static int32_t g_skin_um = 0;  // skin of the contact lists in micrometres (0: no lists), read at prepare
 static int key_bits_of(uint64_t ncells) {
     int b = 1;
     while (b < 32 && (1ull << b) < ncells) ++b;
@@ -437,6 +438,18 @@ sd_status allocate(sd_engine* h, uint32_t n) {
                                    h->stream));
         B.scenes = g;
         B.scene_first = f;
+    }
+    // skin lists (knob skin_um): single scenes of free spheres
+    B.vl_skin = 0.0f;
+    if (g_skin_um > 0 && h->hb_pos.empty() && h->mesh.tri.empty() && h->scenes.size() <= 1 && n) {
+        if ((s = dev_alloc(h, &B.vl_cnt, n)) || (s = dev_alloc(h, &B.vl_nbr, (size_t)n * sd::kVlCap)) ||
+            (s = dev_alloc(h, &B.vl_ref, n)) || (s = dev_alloc(h, &B.vl_flags, 4)) ||
+            (s = dev_alloc(h, &B.slot_of, n)))
+            return s;
+        const uint32_t build[4] = {1u, 0u, 0u, 0u};  // build on the first step
+        SD_CUDA(h, cudaMemcpyAsync(B.vl_flags, build, sizeof build, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+        B.vl_skin = 1e-6f * (float)g_skin_um;
     }
     const uint32_t nb = (uint32_t)h->hb_pos.size();
     B.nb = nb;
@@ -1294,6 +1307,9 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
+    } else if (k == "skin_um") {
+        if (value < 0 || value > 100000) return fail(nullptr, SD_ERR_INVALID_ARG, "skin_um must be in [0, 100000]");
+        g_skin_um = value;
     } else if (k == "pair_lists") {
         if (value < 0 || value > 2) return fail(nullptr, SD_ERR_INVALID_ARG, "pair_lists must be 0, 1 or 2");
         sd::dem_set_pair_lists(value);
@@ -1316,6 +1332,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "z_div") *value = g_z_div;
     else if (k == "resort_max") *value = (int32_t)sd::dem_resort_max();
     else if (k == "pair_lists") *value = sd::dem_pair_lists();
+    else if (k == "skin_um") *value = g_skin_um;
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }
@@ -1418,6 +1435,10 @@ sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src,
         uint32_t* d_changed = h->B.dev_status + 4;
         SD_CUDA(h, sd::dem_keys_changed_async(h->P, h->B, d_changed, h->stream));
         SD_CUDA(h, cudaMemcpyAsync(&changed, d_changed, 4, cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (field == SD_FIELD_POSITION && h->B.vl_flags) {  // new positions: the skin lists are rebuilt
+        const uint32_t build = 1u;
+        SD_CUDA(h, cudaMemcpyAsync(h->B.vl_flags, &build, 4, cudaMemcpyHostToDevice, h->stream));
     }
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     if (field == SD_FIELD_POSITION && changed != 0) h->need_resort = true;

@@ -248,10 +248,17 @@ struct DemBuffers {
     // contact partner lists (scenes without clumps): per slot a count, zero
     // between steps, and kNbrCap partner slots; null when not allocated
     uint32_t *nbr_cnt, *nbr;
+    // skin lists (single scenes of free spheres, vl_skin > 0): per sphere id
+    // its neighbours within r_i + r_j + skin at the last build and the
+    // position then; vl_flags[0] = build this step, [1] = build next step
+    uint32_t *vl_cnt, *vl_nbr, *vl_flags;
+    float4* vl_ref;
+    float vl_skin;
 };
 
 constexpr uint32_t kClumpFlag = 0x80000000u;
 constexpr uint32_t kNbrCap = 16;  // contact partners listed per sphere by the pair kernel
+constexpr uint32_t kVlCap = 24;   // skin-list neighbours per sphere (more: the sphere scans)
 
 int dem_key_bits(uint32_t ncells);
 // incremental re-sort (sd_resort.cu): when at most b.rs_max keys of b.keys
@@ -261,7 +268,9 @@ int dem_key_bits(uint32_t ncells);
 // into the sorted order (ResortView); does nothing else otherwise
 constexpr uint32_t kResortMaxCap = 1024;  // largest rs_max (two sorted lists in 16 KB of shared memory)
 uint64_t resort_scratch_words(uint32_t n);
-cudaError_t resort_async(const DemBuffers& b, cudaStream_t st);
+// vl_flags (may be null): the skin lists' flags, [0] <- [1], [1] <- 0, by the
+// scan's last block
+cudaError_t resort_async(const DemBuffers& b, cudaStream_t st, uint32_t* vl_flags = nullptr);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 void dem_set_pair_lists(int on);
@@ -276,6 +285,9 @@ cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st);
 // True when dem_step_async leaves the next state in the *_n buffers (sorted
 // in place there): the caller then swaps pos/pos_n, vel/vel_n, omg/omg_n.
 bool dem_step_swaps(const DemBuffers& b);
+// True when the step uses the skin lists (single scene of free spheres, knob
+// skin_um > 0, re-sort on).
+bool dem_step_skin(const DemBuffers& b);
 cudaError_t dem_sort_reorder_async(const DemParams& p, DemBuffers& b, cudaStream_t st);
 cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record,
                                         cudaStream_t st);

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kRsThreads)
 resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __restrict__ keys_prev, uint32_t n,
                    unsigned long long* __restrict__ list, uint32_t* __restrict__ pos_out, uint32_t* __restrict__ q_out,
                    uint32_t mmax, uint32_t* __restrict__ scratch, const uint32_t* __restrict__ cell_start,
-                   uint32_t ncells) {
+                   uint32_t ncells, uint32_t* __restrict__ vl_flags) {
     __shared__ uint32_t s_wcnt[kRsThreads / kWarp], s_base, s_last;
     __shared__ unsigned long long s_a[kResortMaxCap], s_b[kResortMaxCap];
     const uint32_t w = threadIdx.x / kWarp, lane = lane_id();
@@ -116,6 +116,10 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
         scratch[1] = M;
         scratch[0] = 0u;
         scratch[2] = 0u;
+        if (vl_flags) {  // the skin lists: build next step if a sphere left its skin this step
+            vl_flags[0] = vl_flags[1];
+            vl_flags[1] = 0u;
+        }
     }
     if (M == 0 || M > mmax) return;
     uint32_t P = 2;
@@ -156,13 +160,13 @@ uint32_t dem_resort_max() { return g_resort_max; }
 
 uint64_t resort_scratch_words(uint32_t) { return 4; }
 
-cudaError_t resort_async(const DemBuffers& b, cudaStream_t st) {
+cudaError_t resort_async(const DemBuffers& b, cudaStream_t st, uint32_t* vl_flags) {
     const uint32_t n = b.n, mmax = b.rs_max;
     if (n == 0 || mmax == 0) return cudaSuccess;
     if (mmax > kResortMaxCap || (mmax & (mmax - 1)) != 0) return cudaErrorInvalidValue;
     const uint32_t blocks = ((n + 31) / 32 + kRsBlockWords - 1) / kRsBlockWords;
     resort_scan_kernel<<<blocks, kRsThreads, 0, st>>>(b.keys, b.keys_prev, n, b.rs_list, b.rs_pos, b.rs_q, mmax,
-                                                      b.rs_scratch, b.cell_start, b.ncells);
+                                                      b.rs_scratch, b.cell_start, b.ncells, vl_flags);
     return cudaGetLastError();
 }
 

@@ -333,3 +333,17 @@ def test_struct_layouts_match_the_header(tmp_path, cname, pyname):
     out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert out[0] == C.sizeof(py)
     assert out[1:] == [getattr(py, f).offset for f in fields]
+
+
+def test_skin_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("skin_um")
+    assert old == 0
+    try:
+        _abi.tune_set("skin_um", 500)
+        assert _abi.tune_get("skin_um") == 500
+        for v in (-1, 100001):
+            with pytest.raises(Exception):
+                _abi.tune_set("skin_um", v)
+    finally:
+        _abi.tune_set("skin_um", old)
