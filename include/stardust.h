@@ -103,6 +103,11 @@ typedef struct sd_stats {
     /* kernels one step launches (the kernel nodes of the captured step
      * graph; 0 before the first step) */
     uint64_t step_kernels;
+    /* sphere scenes with contact lists (knob "skin_um"), since prepare:
+     * steps that built the lists (a scan over the window widened by the
+     * skin) and steps that tested only the listed neighbours */
+    uint64_t list_builds;
+    uint64_t listed_steps;
 } sd_stats;
 
 #define SD_DEVERR_LOOKBACK_TIMEOUT 0x1u
@@ -526,8 +531,9 @@ sd_status sd_sort_status(const void* d_scratch, void* stream, uint32_t* errors);
  * a fixed 8 MiB array in the library's device memory, held on every GPU
  * that loads the library until exit.  Sorts whose scratch need
  * (sd_sort_scratch_bytes) exceeds 8 MiB return SD_ERR_CAPACITY -- up to
- * 2,093,056 keys of 32 bits, 4,188,160 keys of at most 18 bits.  The first
- * call on a device looks up the array's device address (make that first
+ * 2,093,056 keys of 32 bits, 4,188,160 keys of at most 18 bits.  Every call
+ * looks up the array's device address on the current device; the first call
+ * on a device also loads the library's device code there (make that first
  * call before any stream capture).  All calls share the array, so calls
  * that overlap on the GPU race; each call re-clears what must start at zero.
  * Same result layout as sd_sort_pairs (sorted pairs in d_keys/d_vals);

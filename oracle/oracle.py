@@ -7,6 +7,7 @@ product library never loads it.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from pathlib import Path
 
 import numpy as np
@@ -50,6 +51,7 @@ def lib() -> C.CDLL:
             "sdo_contact_integrate_f64": (C.c_uint64, [P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]),
             "sdo_contact_pairs": (C.c_uint64, [P, C.c_uint32, P, P, P, P, C.c_uint64]),
             "sdo_run": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_int]),
+            "sdo_run_f64": (C.c_int, [P, C.c_uint32, P, P, P, P, C.c_int, P]),
             "sdo_contact_integrate_bodies": (C.c_uint64, [P, C.c_uint32] + [P] * 13),
             "sdo_slot_of": (None, [C.c_uint32, P, P]),
             "sdo_body_step": (None, [P, C.c_uint32] + [P] * 18),
@@ -64,6 +66,10 @@ def lib() -> C.CDLL:
             "sdo_sap_process": (None, [C.c_uint32, P, P, P]),
             "sdo_run_full": (C.c_int, [P, C.c_uint32, P, P, P, C.c_int, C.c_uint32] + [P] * 11),
             "sdo_mesh_advance": (None, [P, C.c_int]),
+            "sdo_scene_lattice": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, P, C.c_float,
+                                            C.c_float, C.c_float, C.c_uint64, P, P]),
+            "sdo_scene_rsa": (C.c_int, [C.c_uint64, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                        C.c_float, C.c_uint64, C.c_uint64, P, P, C.POINTER(C.c_double)]),
             "sdo_num_threads": (C.c_int, []),
             "sdo_set_num_threads": (None, [C.c_int]),
         }
@@ -77,6 +83,32 @@ def lib() -> C.CDLL:
 
 def _p(a: np.ndarray | None):
     return None if a is None else a.ctypes.data
+
+
+# ------------------------------------------------------------ scene inputs
+def scene_lattice(nx, ny, nz, spacing, jitter, origin, radius, mass, vmax, seed):
+    """The library's seeded lattice builder, compiled into the oracle
+    (stardust_gb300/csrc/sd_scenes.cu): same arguments and output."""
+    n = nx * ny * nz
+    pos = np.empty((n, 4), np.float32)
+    vel = np.empty((n, 4), np.float32)
+    rc = lib().sdo_scene_lattice(nx, ny, nz, spacing, jitter, (C.c_float * 3)(*origin), radius, mass, vmax, seed,
+                                 _p(pos), _p(vel))
+    if rc != 0:
+        raise RuntimeError(f"scene_lattice failed ({rc})")
+    return pos, vel
+
+
+def scene_rsa(n, lo, hi, r_median, r_sigma, r_min, r_max, density, vmax, seed, max_attempts=50_000_000):
+    """The library's seeded RSA packing, compiled into the oracle."""
+    pos = np.empty((n, 4), np.float32)
+    vel = np.empty((n, 4), np.float32)
+    phi = C.c_double()
+    rc = lib().sdo_scene_rsa(n, (C.c_float * 3)(*lo), (C.c_float * 3)(*hi), r_median, r_sigma, r_min, r_max,
+                             density, vmax, seed, max_attempts, _p(pos), _p(vel), C.byref(phi))
+    if rc != 0:
+        raise RuntimeError(f"scene_rsa failed ({rc})")
+    return pos, vel, phi.value
 
 
 # ---------------------------------------------------------------- ref_compat
@@ -122,21 +154,103 @@ def ref_resolve_forces(cells, spheres, count, pos4, vel4, body_of=None):
 
 
 # ------------------------------------------------------------------- physics
-def params_from_engine(ep: dict, dt: float) -> Params:
-    """Oracle parameters equal to the engine's derived ones (sd_engine_params)."""
+def _key_bits(ncells: int) -> int:
+    """Bits of a cell key over ncells cells (at least 1, at most 32)."""
+    b = 1
+    while b < 32 and (1 << b) < ncells:
+        b += 1
+    return b
+
+
+def _sort_passes(bits: int) -> int:
+    """Digit passes of the step's radix sort for keys of `bits` bits: 9-bit
+    digits, except that 19- and 20-bit keys take two 10-bit passes."""
+    bits = min(max(bits, 1), 32)
+    return 2 if bits in (19, 20) else (bits + 8) // 9
+
+
+def auto_z_div(ncells: int) -> int:
+    """The automatic z split of a single scene's grid: the larger of 4 and 2
+    whose finer grid keeps keys within 20 bits and sorts in as many passes
+    as the plain grid, else 1."""
+    p0 = _sort_passes(_key_bits(ncells))
+    for zd in (4, 2):
+        bits = _key_bits(ncells * zd)
+        if bits <= 20 and _sort_passes(bits) == p0:
+            return zd
+    return 1
+
+
+def derive_params(cfg, radii, dt: float, z_div: int | None = None) -> Params:
+    """The step parameters of a single scene, derived here from the scene
+    config and the sphere radii (not read back from the engine).
+
+    cfg: an object with box_lo, box_hi, domain, cell, kn, restitution, mu,
+    gravity, walls (the engine config's fields).  Box: box_lo..box_hi, or
+    0..domain on every axis when box_hi is all zero.  Cell edge: cfg.cell,
+    or 2 x the largest radius when it is 0.  Cells per axis:
+    ceil(edge / cell * (1 - 1e-6)) in double (at least 1), so a float cell
+    that divides the edge gives the exact count.  z split: z_div when given
+    (1 when the finer grid would exceed 2^30 cells), else auto_z_div.
+    cell_z = cell / z_div in float.  Normal damping: damp_from(kn, e)."""
+    f32 = np.float32
+    given = any(float(v) != 0.0 for v in cfg.box_hi)
+    lo = [f32(cfg.box_lo[a]) if given else f32(0.0) for a in range(3)]
+    hi = [f32(cfg.box_hi[a]) if given else f32(cfg.domain) for a in range(3)]
+    r = np.asarray(radii, np.float32)
+    rmax = f32(r.max()) if r.size else f32(0.0)
+    cell = f32(cfg.cell) if cfg.cell > 0 else f32(2.0) * rmax
+    if not cell > 0:
+        cell = hi[0] - lo[0]
+    dims = [max(1, int(math.ceil((float(hi[a]) - float(lo[a])) / float(cell) * (1.0 - 1e-6)))) for a in range(3)]
+    ncells = dims[0] * dims[1] * dims[2]
+    if z_div is not None and z_div > 0:
+        zd = z_div if ncells * z_div <= (1 << 30) else 1
+    else:
+        zd = auto_z_div(ncells)
     p = Params()
     for a in range(3):
-        p.lo[a] = ep["lo"][a]
-        p.hi[a] = ep["hi"][a]
-        p.g[a] = ep["gravity"][a]
-    p.cell = ep["cell"]
-    p.cell_z = ep.get("cell_z", 0.0)
-    p.nx, p.ny, p.nz = ep["dims"]
-    p.kn = ep["kn"]
-    p.damp = ep["damp"]
-    p.mu = ep["mu"]
+        p.lo[a] = lo[a]
+        p.hi[a] = hi[a]
+        p.g[a] = cfg.gravity[a]
+    p.cell = cell
+    p.nx, p.ny, p.nz = dims[0], dims[1], dims[2] * zd
+    p.cell_z = f32(cell / f32(zd))
+    p.kn = cfg.kn
+    p.damp = damp_from(cfg.kn, cfg.restitution)
+    p.mu = cfg.mu
     p.dt = dt
-    p.walls = ep["walls"]
+    p.walls = cfg.walls
+    return p
+
+
+def params_checked(cfg, radii, dt: float, engine_params: dict, z_div: int | None = None) -> Params:
+    """derive_params, then a check that the engine derived the same grid and
+    contact-law constants (engine_params = its sd_engine_params): box, cell,
+    cells per axis, cell_z, kn, damp, mu, gravity, walls, bit for bit.
+    Raises AssertionError naming every field that differs."""
+    p = derive_params(cfg, radii, dt, z_div)
+    f = lambda x: np.float32(x).view(np.uint32)  # noqa: E731
+    ep = engine_params
+    bad = []
+    for a in range(3):
+        if f(p.lo[a]) != f(ep["lo"][a]) or f(p.hi[a]) != f(ep["hi"][a]):
+            bad.append(f"box axis {a}: oracle {p.lo[a]}..{p.hi[a]}, engine {ep['lo'][a]}..{ep['hi'][a]}")
+        if f(p.g[a]) != f(ep["gravity"][a]):
+            bad.append(f"gravity {a}")
+    if f(p.cell) != f(ep["cell"]):
+        bad.append(f"cell: oracle {p.cell}, engine {ep['cell']}")
+    if (p.nx, p.ny, p.nz) != tuple(ep["dims"]):
+        bad.append(f"dims: oracle {(p.nx, p.ny, p.nz)}, engine {tuple(ep['dims'])}")
+    if f(p.cell_z) != f(ep["cell_z"]):
+        bad.append(f"cell_z: oracle {p.cell_z}, engine {ep['cell_z']}")
+    for k in ("kn", "damp", "mu"):
+        if f(getattr(p, k)) != f(ep[k]):
+            bad.append(f"{k}: oracle {getattr(p, k)}, engine {ep[k]}")
+    if p.walls != ep["walls"]:
+        bad.append("walls")
+    if bad:
+        raise AssertionError("engine parameters differ from the oracle's: " + "; ".join(bad))
     return p
 
 
@@ -239,6 +353,50 @@ def run(p: Params, pos, vel, omg, steps: int, prepare_first: bool = True):
     if rc != 0:
         raise RuntimeError("oracle run failed")
     return pos, vel, omg
+
+
+def run_f64(p: Params, pos, vel, omg, steps: int):
+    """The FP64 twin of run(): the same step in double from the given state
+    (insertion order; omg.w holds no id here).  Returns (pos, vel, omg) as
+    float64 n x 4 arrays in the input's row order (not cell-sorted) and the
+    contact pairs of every state 0..steps-1 (the state each step integrates
+    from)."""
+    n = len(pos)
+    P = np.array(pos, np.float64, copy=True)
+    V = np.array(vel, np.float64, copy=True)
+    W = np.array(omg, np.float64, copy=True)
+    W[:, 3] = 0.0
+    ids = np.arange(n, dtype=np.uint32)
+    counts = np.zeros(max(steps, 1), np.uint64)
+    rc = lib().sdo_run_f64(C.byref(p), n, _p(P), _p(V), _p(W), _p(ids), steps, _p(counts))
+    if rc != 0:
+        raise RuntimeError("oracle FP64 run failed")
+    out = [np.empty_like(P), np.empty_like(V), np.empty_like(W)]
+    for a, b in zip(out, (P, V, W)):
+        a[ids] = b
+    return out[0], out[1], out[2], counts[:steps].astype(np.int64)
+
+
+def ensemble(pos, vel, omg):
+    """Kinetic energy (translational + rotational, I = 0.4 m r^2), packing
+    fraction (sphere volume over the volume of the spheres' bounding box)
+    and contact count (pairs with |x_i - x_j| < r_i + r_j) of a sphere
+    state, in double."""
+    from scipy.spatial import cKDTree
+    x = np.asarray(pos, np.float64)[:, :3]
+    r = np.asarray(pos, np.float64)[:, 3]
+    m = np.asarray(vel, np.float64)[:, 3]
+    v = np.asarray(vel, np.float64)[:, :3]
+    w = np.asarray(omg, np.float64)[:, :3]
+    ke = float(0.5 * np.sum(m * np.sum(v * v, 1)) + 0.5 * np.sum(0.4 * m * r * r * np.sum(w * w, 1)))
+    box = (x + r[:, None]).max(0) - (x - r[:, None]).min(0)
+    phi = float(np.sum(4.0 / 3.0 * np.pi * r ** 3) / np.prod(box))
+    pairs = np.array(sorted(cKDTree(x).query_pairs(2.0 * float(r.max()), output_type="ndarray").tolist()),
+                     np.int64).reshape(-1, 2)
+    if len(pairs):
+        d = np.linalg.norm(x[pairs[:, 0]] - x[pairs[:, 1]], axis=1)
+        pairs = pairs[d < r[pairs[:, 0]] + r[pairs[:, 1]]]
+    return {"kinetic_energy": ke, "packing_fraction": phi, "contacts": int(len(pairs))}
 
 
 def run_bodies(p: Params, pos, vel, omg, steps: int, bodies: dict, r0, body_of):

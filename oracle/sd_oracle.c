@@ -822,6 +822,58 @@ int sdo_run(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg,
     return 0;
 }
 
+/* The FP64 twin of sdo_run, for the error statement of long runs: the same
+ * contact law, walls and integrator in double (SDO_DEFINE_STEP), the cell
+ * order taken from the float-rounded positions (the order only fixes the
+ * summation order).  pos/vel/omg: n x 4 doubles in any order, ids[i] the
+ * sphere id of row i; on return the state is cell-sorted and ids permuted
+ * with it.  contacts (may be NULL) receives per step s < steps the
+ * contact pairs of state s (the one that step integrates from). */
+int sdo_run_f64(const sdo_params* p, uint32_t n, double* pos, double* vel, double* omg, uint32_t* ids, int steps,
+                uint64_t* contacts) {
+    /* contacts (may be NULL): steps entries, [s] = contact pairs of state s */
+    size_t nc = (size_t)p->nx * p->ny * p->nz;
+    double* pn = (double*)malloc(sizeof(double) * 12 * (size_t)(n ? n : 1));
+    double *vn = pn + 4 * (size_t)n, *wn = vn + 4 * (size_t)n;
+    uint32_t* k = (uint32_t*)malloc(sizeof(uint32_t) * 5 * (size_t)(n ? n : 1));
+    uint32_t* cs = (uint32_t*)malloc(sizeof(uint32_t) * (nc + 1));
+    if (!pn || !k || !cs) {
+        free(pn); free(k); free(cs);
+        return -1;
+    }
+    uint32_t *v = k + n, *tk = v + n, *tv = tk + n, *idn = tv + n;
+    memcpy(pn, pos, 32 * (size_t)n);
+    memcpy(vn, vel, 32 * (size_t)n);
+    memcpy(wn, omg, 32 * (size_t)n);
+    memcpy(idn, ids, 4 * (size_t)n);
+    for (int s = 0; s <= steps; ++s) {
+        /* sort the (next) state into cell order */
+        for (uint32_t i = 0; i < n; ++i) {
+            k[i] = sdo_cell_key(p, (float)pn[4 * i], (float)pn[4 * i + 1], (float)pn[4 * i + 2]);
+            v[i] = i;
+        }
+        sdo_radix_sort_pairs(k, v, n, key_bits(p), tk, tv);
+        for (uint32_t i = 0; i < n; ++i) {
+            memcpy(pos + 4 * (size_t)i, pn + 4 * (size_t)v[i], 32);
+            memcpy(vel + 4 * (size_t)i, vn + 4 * (size_t)v[i], 32);
+            memcpy(omg + 4 * (size_t)i, wn + 4 * (size_t)v[i], 32);
+            ids[i] = idn[v[i]];
+        }
+        memcpy(idn, ids, 4 * (size_t)n);
+        uint32_t q = 0;
+        for (uint32_t cc = 0; cc <= (uint32_t)nc; ++cc) {
+            while (q < n && k[q] < cc) ++q;
+            cs[cc] = q;
+        }
+        if (s == steps) break;
+        uint64_t c = contact_integrate_f64(p, n, pos, vel, omg, cs, pn, vn, wn, NULL, NULL, NULL, NULL, NULL, NULL,
+                                           NULL);
+        if (contacts) contacts[s] = c / 2;
+    }
+    free(pn); free(k); free(cs);
+    return 0;
+}
+
 /* ------------------------------------------------------ rigid clumps ----- */
 
 uint64_t sdo_contact_integrate_bodies(const sdo_params* p, uint32_t n, const float* pos, const float* vel,

@@ -157,6 +157,11 @@ uint64_t sdo_contact_pairs(const sdo_params* p, uint32_t n, const float* pos,
  * updated in place.  Scratch is allocated internally. */
 int sdo_run(const sdo_params* p, uint32_t n, float* pos, float* vel, float* omg,
             int steps, int prepare);
+/* FP64 twin of sdo_run (error statement of long runs): n x 4 doubles, ids
+ * permuted with the cell sort; contacts[s] (s < steps, may be NULL) = the
+ * contact pairs of state s. */
+int sdo_run_f64(const sdo_params* p, uint32_t n, double* pos, double* vel, double* omg, uint32_t* ids, int steps,
+                uint64_t* contacts);
 
 /* A rigid triangle mesh: tri holds 12 floats per triangle (3 rows x, y, z,
  * unused) in the mesh frame, patch a face id per triangle, state 24 floats

@@ -107,6 +107,8 @@ class SdStats(C.Structure):
         ("epa_iters", C.c_uint64),
         ("moved_keys", C.c_uint64),
         ("step_kernels", C.c_uint64),
+        ("list_builds", C.c_uint64),
+        ("listed_steps", C.c_uint64),
     ]
 
 

@@ -427,7 +427,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                         const float4 pa = src.load(s);
                         const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
                         const float da = dist2(ax, ay, az);
-                        if (da == 0.0f) continue;  // the sphere itself (or a coincident one: never a contact)
+                        if (s == i) continue;  // the sphere itself; a coincident partner is listed
                         const float rl = ri + pa.w + sk->skin;
                         if (da < rl * rl) {
                             if (c < kVlCap && id < n)
@@ -436,7 +436,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                     kIdMask;
                             ++c;
                             const float ra = ri + pa.w;
-                            if (da < ra * ra) {
+                            if (da < ra * ra && da != 0.0f) {  // coincident centres: no normal, no contact
                                 ++contacts;
                                 pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
                             }

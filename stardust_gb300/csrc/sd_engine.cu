@@ -508,6 +508,15 @@ static void swap_state(sd::DemBuffers& B) {
     std::swap(B.omg, B.omg_n);
 }
 
+// Makes the next step build the contact lists (knob skin_um) from a scan
+// over the widened window, whatever the lists' state.
+static sd_status force_list_build(sd_engine* h) {
+    if (!h->B.vl_flags) return SD_OK;
+    const uint32_t build[2] = {1u, 0u};
+    SD_CUDA(h, cudaMemcpyAsync(h->B.vl_flags, build, sizeof build, cudaMemcpyHostToDevice, h->stream));
+    return SD_OK;
+}
+
 sd_status build_graph(sd_engine* h, float dt) {
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
@@ -603,17 +612,6 @@ sd_status errors_to_status(sd_engine* h, uint32_t bits) {
     return SD_OK;
 }
 
-// ------------------------------------------------------------ RNG + scenes
-struct SplitMix {
-    uint64_t s;
-    uint64_t next() {
-        uint64_t z = (s += 0x9e3779b97f4a7c15ull);
-        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-        return z ^ (z >> 31);
-    }
-    double u01() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
-};
 
 }  // namespace
 
@@ -1279,6 +1277,10 @@ sd_status sd_engine_step(sd_engine* h, float dt, int32_t n_steps) {
     if (!h->graph_valid || h->graph_dt != dt || h->graph_epoch != g_tune_epoch.load()) {
         h->graph_epoch = g_tune_epoch.load();
         if ((s = build_graph(h, dt))) return s;
+        // steps of the previous graph may have used no lists (a knob change
+        // turned them off) and moved spheres without checking their skin:
+        // the first step of a list graph builds them again
+        if ((s = force_list_build(h))) return s;
     }
     for (int32_t i = 0; i < n_steps; ++i) {
         SD_CUDA(h, cudaGraphLaunch(h->graph_parity ? h->graph_alt : h->graph, h->stream));
@@ -1453,6 +1455,9 @@ sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
     sd_status s = resort_if_needed(h);
     if (s) return s;
     h->keys_current = false;  // a lone stage can leave keys and slots apart
+    // a lone stage neither uses nor maintains the contact lists: the next
+    // step builds them again
+    if ((s = force_list_build(h))) return s;
     switch (stage) {
         case SD_STAGE_CONTACT: {
             if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(h, SD_ERR_INVALID_ARG, "dt must be positive");
@@ -1575,11 +1580,14 @@ sd_status sd_engine_stats(sd_engine* h, sd_stats* out) {
     SD_CUDA(h, sd::dem_pairs_async(h->P, h->B, h->stream));
     unsigned long long np = 0;
     SD_CUDA(h, cudaMemcpyAsync(&np, h->B.npairs, 8, cudaMemcpyDeviceToHost, h->stream));
-    uint32_t moved = 0;
+    uint32_t moved = 0, vl[4] = {0u, 0u, 0u, 0u};
     if (h->graph_valid && h->B.rs_max && h->B.n)
         SD_CUDA(h, cudaMemcpyAsync(&moved, h->B.rs_scratch + 1, 4, cudaMemcpyDeviceToHost, h->stream));
+    if (h->B.vl_flags) SD_CUDA(h, cudaMemcpyAsync(vl, h->B.vl_flags, sizeof vl, cudaMemcpyDeviceToHost, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     out->moved_keys = h->steps ? moved : 0;
+    out->list_builds = vl[2];
+    out->listed_steps = vl[3];
     out->step_kernels = h->graph_valid ? h->graph_kernels : 0;
     // bodies: the kernel above counted free spheres only
     const size_t nb = h->B.nb;
@@ -1839,96 +1847,6 @@ sd_status sd_hash_candidate_pairs(const uint32_t* d_cells, const uint32_t* d_sph
                                                   d_pair_b, cap, reinterpret_cast<unsigned long long*>(d_npairs),
                                                   static_cast<uint32_t*>(d_scratch), static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "candidate_pairs");
-    return SD_OK;
-}
-
-// ------------------------------------------------------------ scene builders
-sd_status sd_scene_lattice(int32_t nx, int32_t ny, int32_t nz, float spacing, float jitter, const float origin[3],
-                           float radius, float mass, float vmax, uint64_t seed, float* pos4, float* vel4) {
-    if (nx < 0 || ny < 0 || nz < 0 || !origin || !pos4 || !vel4)
-        return fail(nullptr, SD_ERR_INVALID_ARG, "bad lattice arguments");
-    SplitMix rng{seed};
-    size_t i = 0;
-    for (int32_t x = 0; x < nx; ++x)
-        for (int32_t y = 0; y < ny; ++y)
-            for (int32_t z = 0; z < nz; ++z, ++i) {
-                int32_t idx[3] = {x, y, z};
-                for (int a = 0; a < 3; ++a) {
-                    double j = (2.0 * rng.u01() - 1.0) * jitter;
-                    pos4[4 * i + a] = (float)((double)origin[a] + (double)idx[a] * spacing + j);
-                }
-                pos4[4 * i + 3] = radius;
-                for (int a = 0; a < 3; ++a) vel4[4 * i + a] = (float)((2.0 * rng.u01() - 1.0) * vmax);
-                vel4[4 * i + 3] = mass;
-            }
-    return SD_OK;
-}
-
-sd_status sd_scene_rsa(uint64_t n, const float lo[3], const float hi[3], float r_median, float r_sigma, float r_min,
-                       float r_max, float density, float vmax, uint64_t seed, uint64_t max_attempts, float* pos4,
-                       float* vel4, double* volume_fraction) {
-    if (!lo || !hi || (n && (!pos4 || !vel4)) || !(r_min > 0) || !(r_max >= r_min) || !(density > 0))
-        return fail(nullptr, SD_ERR_INVALID_ARG, "bad RSA arguments");
-    for (int a = 0; a < 3; ++a)
-        if (!(hi[a] - lo[a] > 2 * r_max)) return fail(nullptr, SD_ERR_INVALID_ARG, "box smaller than a sphere");
-    SplitMix rng{seed};
-    std::vector<double> r(n);
-    for (uint64_t i = 0; i < n; ++i) {
-        double u1 = rng.u01(), u2 = rng.u01();
-        double g = std::sqrt(-2.0 * std::log(u1 + 1e-300)) * std::cos(2.0 * M_PI * u2);
-        double x = (double)r_median * std::exp((double)r_sigma * g);
-        r[i] = std::min<double>(std::max<double>(x, r_min), r_max);
-    }
-    std::sort(r.begin(), r.end(), [](double a, double b) { return a > b; });
-    const double c = 2.0 * r_max;
-    int dims[3];
-    for (int a = 0; a < 3; ++a) dims[a] = std::max(1, (int)std::ceil((hi[a] - lo[a]) / c));
-    size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
-    // cell-binned occupancy; a cell of edge 2*r_max holds few spheres
-    std::vector<std::vector<uint32_t>> bins(ncell);
-    std::vector<double> P(3 * n);
-    double vol = 0;
-    for (uint64_t i = 0; i < n; ++i) {
-        double ri = r[i];
-        bool placed = false;
-        for (uint64_t att = 0; att < max_attempts && !placed; ++att) {
-            double x[3];
-            for (int a = 0; a < 3; ++a) x[a] = lo[a] + ri + rng.u01() * ((double)hi[a] - lo[a] - 2 * ri);
-            int ci[3];
-            for (int a = 0; a < 3; ++a) ci[a] = std::min(dims[a] - 1, (int)((x[a] - lo[a]) / c));
-            bool clash = false;
-            for (int dx = -1; dx <= 1 && !clash; ++dx)
-                for (int dy = -1; dy <= 1 && !clash; ++dy)
-                    for (int dz = -1; dz <= 1 && !clash; ++dz) {
-                        int X = ci[0] + dx, Y = ci[1] + dy, Z = ci[2] + dz;
-                        if (X < 0 || Y < 0 || Z < 0 || X >= dims[0] || Y >= dims[1] || Z >= dims[2]) continue;
-                        for (uint32_t j : bins[((size_t)X * dims[1] + Y) * dims[2] + Z]) {
-                            double ex = x[0] - P[3 * j], ey = x[1] - P[3 * j + 1], ez = x[2] - P[3 * j + 2];
-                            double rr = ri + r[j];
-                            if (ex * ex + ey * ey + ez * ez < rr * rr) {
-                                clash = true;
-                                break;
-                            }
-                        }
-                    }
-            if (clash) continue;
-            for (int a = 0; a < 3; ++a) P[3 * i + a] = x[a];
-            bins[((size_t)ci[0] * dims[1] + ci[1]) * dims[2] + ci[2]].push_back((uint32_t)i);
-            placed = true;
-        }
-        if (!placed)
-            return fail(nullptr, SD_ERR_CAPACITY, "RSA could not place sphere " + std::to_string(i) + " within max_attempts");
-        double vi = 4.0 / 3.0 * M_PI * ri * ri * ri;
-        vol += vi;
-        for (int a = 0; a < 3; ++a) {
-            pos4[4 * i + a] = (float)P[3 * i + a];
-            vel4[4 * i + a] = (float)((2.0 * rng.u01() - 1.0) * vmax);
-        }
-        pos4[4 * i + 3] = (float)ri;
-        vel4[4 * i + 3] = (float)(density * vi);
-    }
-    if (volume_fraction)
-        *volume_fraction = vol / (((double)hi[0] - lo[0]) * ((double)hi[1] - lo[1]) * ((double)hi[2] - lo[2]));
     return SD_OK;
 }
 

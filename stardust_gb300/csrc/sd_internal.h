@@ -250,7 +250,8 @@ struct DemBuffers {
     uint32_t *nbr_cnt, *nbr;
     // skin lists (single scenes of free spheres, vl_skin > 0): per sphere id
     // its neighbours within r_i + r_j + skin at the last build and the
-    // position then; vl_flags[0] = build this step, [1] = build next step
+    // position then; vl_flags[0] = build this step, [1] = build next step,
+    // [2] = steps that built the lists, [3] = steps that used them
     uint32_t *vl_cnt, *vl_nbr, *vl_flags;
     float4* vl_ref;
     float vl_skin;

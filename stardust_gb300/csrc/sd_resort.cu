@@ -117,6 +117,8 @@ resort_scan_kernel(const uint32_t* __restrict__ keys_new, const uint32_t* __rest
         scratch[0] = 0u;
         scratch[2] = 0u;
         if (vl_flags) {  // the skin lists: build next step if a sphere left its skin this step
+            if (vl_flags[0]) ++vl_flags[2];  // steps that built the lists
+            else ++vl_flags[3];              // steps that used them
             vl_flags[0] = vl_flags[1];
             vl_flags[1] = 0u;
         }

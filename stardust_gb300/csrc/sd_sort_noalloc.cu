@@ -23,7 +23,6 @@
 //     carries over from the previous call.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/stardust.h"
@@ -33,15 +32,10 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
 constexpr size_t kNoAllocScratchWords = kNoAllocScratchBytes / sizeof(uint32_t);
-constexpr int kMaxDevices = 64;
-
 // The scratch.  Host code must not use this name as an address (on the host
 // it is only a stand-in for the device symbol); its device address comes from
-// cudaGetSymbolAddress, per device.
+// cudaGetSymbolAddress with the device current.
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
-
-std::mutex g_addr_mutex;
-uint32_t* g_addr[kMaxDevices] = {};
 
 // failures are reported through sd_last_error(NULL, ...)
 sd_status noalloc_fail(sd_status code, const std::string& msg) {
@@ -66,24 +60,15 @@ extern "C" sd_status sd_sort_pairs_noalloc(uint32_t* d_keys, uint32_t* d_vals, u
     if (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp)
         return noalloc_fail(SD_ERR_INVALID_ARG, "NULL key/value buffer");
 
-    // one-time set-up per device, with that device current: resolve the
-    // array's device address
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return noalloc_fail(SD_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(SD_ERR_UNSUPPORTED, "device ordinal above 63");
-    uint32_t* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_addr_mutex);
-        if (!g_addr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess)
-                return noalloc_fail(SD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_addr[dev] = static_cast<uint32_t*>(p);
-        }
-        scratch = g_addr[dev];
-    }
+    // the array's device address on the current device, looked up on every
+    // call: once the module is loaded this is a table lookup, and it stays
+    // right across a cudaDeviceReset (which unloads the module and may place
+    // the array elsewhere when it is loaded again)
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return noalloc_fail(SD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    uint32_t* scratch = static_cast<uint32_t*>(p);
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the status word (error bits) starts at zero on every call; the sort

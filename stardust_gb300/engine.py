@@ -352,6 +352,7 @@ class DEMEngine:
             "device_errors": s.device_errors, "n_cells": s.n_cells, "n_bodies": s.n_bodies,
             "gjk_pairs": s.gjk_pairs, "gjk_iters": s.gjk_iters, "epa_iters": s.epa_iters,
             "moved_keys": s.moved_keys, "step_kernels": s.step_kernels,
+            "list_builds": s.list_builds, "listed_steps": s.listed_steps,
         }
 
     def params(self) -> dict:

@@ -28,25 +28,30 @@ M_BOX = 1e-3
 DENSITY = M_BOX / (4.0 / 3.0 * math.pi * R_BOX ** 3)
 
 
-def box_lattice(n_side: int = 16, seed: int = 0):
-    """(pos4, vel4, EngineConfig, dt) of the jittered-lattice box."""
+def box_lattice(n_side: int = 16, seed: int = 0, lattice=None):
+    """(pos4, vel4, EngineConfig, dt) of the jittered-lattice box.  lattice:
+    the builder (default the library's sd_scene_lattice; the oracle's copy
+    gives the same spheres without loading the library)."""
     edge = 0.64
     spacing = 2.2 * R_BOX
     extent = (n_side - 1) * spacing
     o = (edge - extent) / 2.0
-    pos, vel = scene_lattice(n_side, n_side, n_side, spacing, 0.05 * R_BOX, (o, o, o), R_BOX, M_BOX, 0.1, seed)
+    pos, vel = (lattice or scene_lattice)(n_side, n_side, n_side, spacing, 0.05 * R_BOX, (o, o, o), R_BOX, M_BOX,
+                                          0.1, seed)
     cfg = EngineConfig(box_lo=(0.0, 0.0, 0.0), box_hi=(edge, edge, edge), walls=0x3F, cell=2 * R_BOX,
                        kn=1e5, restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81))
     return pos, vel, cfg, 1e-5
 
 
-def settling_rsa(n: int = 1 << 20, box=(1.0, 1.0, 2.0), seed: int = 0):
+def settling_rsa(n: int = 1 << 20, box=(1.0, 1.0, 2.0), seed: int = 0, rsa=None):
     """(pos4, vel4, EngineConfig, dt, volume_fraction) of the polydisperse settling box.
 
     Smaller n with a proportionally smaller box keeps the packing fraction.
+    rsa: the packing builder (default the library's sd_scene_rsa; the
+    oracle's copy gives the same spheres without loading the library).
     """
     rmed, sig, rmin, rmax = 0.005, 0.25, 0.0025, 0.01
-    pos, vel, phi = scene_rsa(n, (0.0, 0.0, 0.0), box, rmed, sig, rmin, rmax, DENSITY, 0.0, seed)
+    pos, vel, phi = (rsa or scene_rsa)(n, (0.0, 0.0, 0.0), box, rmed, sig, rmin, rmax, DENSITY, 0.0, seed)
     cfg = EngineConfig(box_lo=(0.0, 0.0, 0.0), box_hi=tuple(box), walls=0x3F, cell=2 * rmax, kn=1e5,
                        restitution=0.5, mu=0.3, gravity=(0.0, 0.0, -9.81))
     return pos, vel, cfg, 5e-6, phi

@@ -74,7 +74,7 @@ def test_clumps_bit_exact(sdlib, orc, steps):
     pos, vel, omg = oracle_input(orc, eng, body_of)
     b0 = body_state(sdlib, eng)
     b0.update(first=first, count=count)
-    p = orc.params_from_engine(eng.params(), dt)
+    p = orc.params_checked(eng.config, pos[:, 3], dt, eng.params())
     op, ov, ow, ob = orc.run_bodies(p, pos, vel, omg, steps, b0, r0, body_of)
     eng.step(dt, steps)
     eng.sync()

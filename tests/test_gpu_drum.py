@@ -52,7 +52,7 @@ def test_drum_bit_exact(sdlib, orc, steps):
           "angmom": eng.bodies(_abi.SD_BODY_ANGMOM), "inv": eng.bodies(_abi.SD_BODY_INV_INERTIA),
           "first": first, "count": count}
     mesh = orc.make_mesh(d["tris"], d["patch"], d["centre"], eng.mesh_state())
-    p = orc.params_from_engine(eng.params(), d["dt"])
+    p = orc.params_checked(d["cfg"], pos[:, 3], d["dt"], eng.params())
     op, ov, ow, ob = orc.run_full(p, pos, vel, omg, steps, b0, r0, body_of, mesh)
     eng.step(d["dt"], steps)
     eng.sync()

@@ -36,7 +36,7 @@ def test_single_sphere_comes_to_rest_on_the_floor(sdlib, orc):
     vel = np.array([[0.0, 0.0, 0.0, 1e-3]], np.float32)
     eng.add_spheres(pos, vel)
     eng.prepare()
-    p = orc.params_from_engine(eng.params(), 1e-5)
+    p = orc.params_checked(eng.config, pos[:, 3], 1e-5, eng.params())
     op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), [0]), 50000)
     eng.step(1e-5, 50000)
     eng.sync()
@@ -60,7 +60,7 @@ def test_spheres_outside_the_box(sdlib, orc):
     eng = sdlib.DEMEngine(cfg_box(sdlib))
     eng.add_spheres(pos, vel)
     eng.prepare()
-    p = orc.params_from_engine(eng.params(), 1e-5)
+    p = orc.params_checked(eng.config, pos[:, 3], 1e-5, eng.params())
     op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(len(pos))), 50)
     eng.step(1e-5, 50)
     eng.sync()

@@ -25,8 +25,8 @@ def run_engine(sd, pos, vel, cfg, dt, steps, record=True, omega=None):
     return eng
 
 
-def oracle_state(orc, eng, pos, vel, dt, steps, omega=None):
-    p = orc.params_from_engine(eng.params(), dt)
+def oracle_state(orc, eng, pos, vel, dt, steps, omega=None, z_div=None):
+    p = orc.params_checked(eng.config, pos[:, 3], dt, eng.params(), z_div)
     omg = orc.with_ids(np.zeros_like(pos) if omega is None else omega, np.arange(len(pos)))
     return p, orc.run(p, pos, vel, omg, steps)
 
@@ -90,7 +90,7 @@ def test_z_division_is_bit_exact(sdlib, orc, z_div):
         cfg.cell = float(2 * pos[:, 3].max())
         eng = run_engine(sdlib, pos, vel, cfg, dt, 20)
         assert eng.params()["z_div"] == z_div
-        p, (op, ov, ow) = oracle_state(orc, eng, pos, vel, dt, 20)
+        p, (op, ov, ow) = oracle_state(orc, eng, pos, vel, dt, 20, z_div=z_div)
         assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
         assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))
         assert np.array_equal(bits(eng.omegas())[:, :3], bits(orc.unsort(ow, ow))[:, :3])
@@ -147,7 +147,7 @@ def test_dense_pack_forces_torques_pairs(sdlib, orc):
     omega = np.zeros((n, 4), np.float32)
     omega[:, :3] = rng.uniform(-30, 30, (n, 3))
     eng = run_engine(sdlib, pos, vel, cfg, dt, 0, omega=omega)
-    p = orc.params_from_engine(eng.params(), dt)
+    p = orc.params_checked(eng.config, pos[:, 3], dt, eng.params())
     omg = orc.with_ids(omega, np.arange(n))
     sp, sv, sw, _, cs = orc.prepare(p, pos, vel, omg)
     pairs_o = orc.contact_pairs(p, sp, sw, cs)
@@ -221,7 +221,7 @@ def test_set_state_resorts_only_when_keys_change(sdlib, orc):
     a.set(_abi.SD_FIELD_POSITION, p)
     got = a.pairs()
     assert (np.uint64(0) << np.uint64(32) | np.uint64(far)) in set(got.tolist())
-    prm = orc.params_from_engine(a.params(), dt)
+    prm = orc.params_checked(cfg, pos[:, 3], dt, a.params())
     sp, sv, sw, _, cs = orc.prepare(prm, p, a.velocities(), orc.with_ids(a.omegas(), np.arange(len(p))))
     assert np.array_equal(got, orc.contact_pairs(prm, sp, sw, cs))
     a.close()

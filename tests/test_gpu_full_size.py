@@ -26,7 +26,7 @@ def test_settling_box_1m_bit_exact(sdlib, orc, inflate):
     eng.add_spheres(pos, vel)
     eng.prepare()
     steps = 4
-    p = orc.params_from_engine(eng.params(), dt)
+    p = orc.params_checked(cfg, pos[:, 3], dt, eng.params())
     n = len(pos)
     if inflate > 1.0:  # the dense state's contact list first
         sp, sv, sw, _, cs = orc.prepare(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)))
@@ -73,7 +73,7 @@ def test_drum_2m_bit_exact(sdlib, orc):
           "first": np.array(first, np.uint32), "count": np.array(count, np.uint32)}
     t, pa, c = eng.mesh()
     mesh = orc.make_mesh_frame(t, pa, eng.mesh_state())
-    p = orc.params_from_engine(eng.params(), d["dt"])
+    p = orc.params_checked(d["cfg"], pos[:, 3], d["dt"], eng.params())
     steps = 3
     op, ov, ow, ob = orc.run_full(p, pos, vel, omg, steps, b0, r0, body_of, mesh)
     eng.step(d["dt"], steps)

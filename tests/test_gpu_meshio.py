@@ -69,7 +69,7 @@ def test_stl_hopper_bit_exact_vs_oracle(sdlib, orc, tmp_path):
     eng.step(dt, 0)
     eng.sync()
     mesh = orc.make_mesh_frame(t, pa, eng.mesh_state())
-    p = orc.params_from_engine(eng.params(), dt)
+    p = orc.params_checked(eng.config, pos[:, 3], dt, eng.params())
     n = len(pos)
     omg = orc.with_ids(np.zeros_like(pos), np.arange(n))
     steps = 4000

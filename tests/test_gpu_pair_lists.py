@@ -46,7 +46,7 @@ def test_pair_lists_bit_exact(sdlib, orc, pair_lists, inflate):
         eng.step(dt, steps)
         eng.sync()
         assert eng.stats()["device_errors"] == 0
-        p = orc.params_from_engine(eng.params(), dt)
+        p = orc.params_checked(cfg, pos[:, 3], dt, eng.params())
         op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)), steps)
         assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
         assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))

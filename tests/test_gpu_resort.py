@@ -54,7 +54,7 @@ def test_incremental_resort_bit_exact(sdlib, orc, resort_max, moved):
             assert max(seen) <= 8
         else:
             assert 0.3 * moved < np.median(seen) < 3 * moved
-        p = orc.params_from_engine(eng.params(), dt)
+        p = orc.params_checked(cfg, pos[:, 3], dt, eng.params())
         op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)), steps)
         assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
         assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))
@@ -87,7 +87,7 @@ def test_resort_mixes_with_radix_steps(sdlib, orc):
             eng.step(dt, 1)
             seen.append(eng.stats()["moved_keys"])
         assert min(seen) <= 256 < max(seen)
-        p = orc.params_from_engine(eng.params(), dt)
+        p = orc.params_checked(cfg, pos[:, 3], dt, eng.params())
         op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)), 30)
         assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
         assert np.array_equal(bits(eng.velocities()), bits(orc.unsort(ov, ow)))

@@ -31,7 +31,7 @@ def test_remove_before_prepare_and_argument_checks(sdlib):
 
 
 def run_oracle(orc, eng, dt, steps):
-    p = orc.params_from_engine(eng.params(), dt)
+    p = orc.params_checked(eng.config, eng.positions()[:, 3], dt, eng.params())
     n = eng.n
     return orc.run(p, eng.positions(), eng.velocities(), orc.with_ids(eng.omegas(), np.arange(n)), steps)
 
@@ -114,7 +114,7 @@ def test_runtime_change_keeps_bodies_and_mesh_pose(sdlib, orc):
           "first": np.array(first, np.uint32), "count": np.array(count, np.uint32)}
     t, pa, c = eng.mesh()
     mesh = orc.make_mesh_frame(t, pa, eng.mesh_state())
-    p = orc.params_from_engine(eng.params(), d["dt"])
+    p = orc.params_checked(d["cfg"], pos[:, 3], d["dt"], eng.params())
     op, ov, ow, ob = orc.run_full(p, pos, vel, omg, 150, b0, r0, body_of, mesh)
     eng.step(d["dt"], 150)
     eng.sync()
