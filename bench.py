@@ -4,14 +4,21 @@ Workload: the settling box -- 1,048,576 spheres, radii lognormal (median
 5 mm, sigma 0.25) clipped to [2.5, 10] mm, random sequential addition in a
 walled 1 x 1 x 2 m box, linear spring-dashpot kn = 1e5, restitution 0.5,
 Coulomb mu = 0.3, gravity, dt = 5e-6 s, hash cell 2 x max radius (50 x 50 x
-100 cells), cell keys radix sorted every step.  Synthetic, seeded.
+100 cells), cell keys sorted every step, a 2,000-step run.  Synthetic,
+seeded.
 
-One step = contact gather + integration, (cell key, slot) onesweep sort,
-reorder + cell_start.  Timings:
+One step = contact gather + integration (over contact lists with a skin
+between list builds), a stable sort of the (cell key, slot) pairs -- an
+incremental re-sort of the keys that changed, or the onesweep radix passes
+--, reorder + cell_start.  The scene is first advanced (untimed) to step
+`--advance` (1,000) of the run, so the timed window sits in the middle of
+the settling run rather than right after the packing.  Timings:
 
   value      device time per step (CUDA events on the engine's stream, one
              event pair per step, the L2 flushed by a 256 MB write before
-             every timed step), whole job over ranks;
+             every timed step), whole job over ranks; also the first steps
+             after the packing (early_window), the same state without
+             contact lists and with the full radix sort every step;
   e2e        the same steps through the public C ABI with the state in
              pinned host memory: per step, upload positions + velocities
              (sd_engine_set_state), step, read positions + velocities back
@@ -21,6 +28,8 @@ reorder + cell_start.  Timings:
              measured HBM peak;
   cpu_baseline  the CPU oracle (the restated step, OpenMP on the host cores)
              on a bounded sample of the same scene;
+  dense_bed  the same spheres with radii x1.2 (~2.5M contact pairs), after
+             1,000 steps;
   drum       the rotating drum: 2.1M spheres and clumps against a turning
              20,480-triangle cylinder (bench_drum);
   batch      512 independent scenes (~2.9M spheres) stepped together, one
@@ -63,6 +72,11 @@ N_FULL = 1 << 20
 # spin (48) + cell key + slot (8); the cell_start table (250,001 words for
 # 1,048,576 spheres) adds ~1 B/sphere
 CONTACT_BYTES_PER_SPHERE = 48 + 48 + 8
+# with contact lists (knob skin_um), a listed step also reads the sphere's
+# list count (4) and its position at the last build (16) for the skin check;
+# the listed neighbours' ids and slots add 8 B per entry (not counted: a
+# sphere of the settling box lists ~1-2 neighbours)
+LIST_BYTES_PER_SPHERE = 4 + 16
 # algorithmic HBM bytes per sphere-step of the whole step (2 sort passes of
 # 18-bit keys):  contact 104 + histogram 4 + 2 x (8 read + 8 write) + reorder
 # (slot 4 + key 4 + gather 48 + write 48)
@@ -89,11 +103,11 @@ def dist_env():
     return rank, world, local
 
 
-def build_scene(n: int, seed: int):
+def build_scene(n: int, seed: int, rsa=None):
     from stardust_gb300 import scenes
     box = (1.0, 1.0, 2.0) if n == N_FULL else scenes.scaled_box(n)
     t0 = time.time()
-    pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=box, seed=seed)
+    pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=box, seed=seed, rsa=rsa)
     log(f"scene: {n} spheres, volume fraction {phi:.4f}, generated in {time.time() - t0:.1f}s")
     return pos, vel, cfg, dt, phi
 
@@ -159,14 +173,16 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def recorded_profile():
+def recorded_profile(kind: str = "scan"):
     """DRAM bytes and warp instructions per sphere of one contact-kernel
-    launch, from the committed ncu summary (profiles/roofline_traffic.json)."""
+    launch, from the committed ncu summary (profiles/roofline_traffic.json):
+    kind "scan" (the candidate scan) or "listed" (contact lists)."""
     f = ROOT / "profiles" / "roofline_traffic.json"
     if f.exists():
         try:
             d = json.loads(f.read_text())
-            return d.get("contact_integrate_bytes_per_sphere"), d.get("contact_integrate_warp_instructions_per_sphere")
+            pre = "contact_integrate" if kind == "scan" else "contact_listed"
+            return d.get(f"{pre}_bytes_per_sphere"), d.get(f"{pre}_warp_instructions_per_sphere")
         except Exception:
             pass
     return None, None
@@ -175,15 +191,10 @@ def recorded_profile():
 SMS, SCHEDULERS_PER_SM = 152, 4  # GB300: one warp instruction per scheduler per clock
 
 
-def cpu_oracle_rate(pos, vel, cfg, dt, seconds: float, threads: int | None):
+def cpu_oracle_rate(pos, vel, cfg, dt, seconds: float, threads: int | None, z_div: int | None = None):
     """Oracle steps on the host cores until ~`seconds` of work: particle-steps/s."""
     from oracle import oracle as orc
-    from stardust_gb300 import DEMEngine
-    # the engine's derived parameters (host-only, no GPU call)
-    eng = DEMEngine(cfg)
-    eng.add_spheres(pos, vel)
-    p = orc.params_from_engine(eng.params(), dt)
-    eng.close()
+    p = orc.derive_params(cfg, pos[:, 3], dt, z_div)
     if threads:
         orc.lib().sdo_set_num_threads(threads)
     used = orc.lib().sdo_num_threads()
@@ -203,19 +214,22 @@ def cpu_oracle_rate(pos, vel, cfg, dt, seconds: float, threads: int | None):
 
 
 def run_reference_arm(args, rank, world):
+    """The CPU restatement of the step on all host threads, on the same
+    scene; the scene comes from the oracle's copy of the seeded builders and
+    the parameters from the oracle's own derivation, so this arm loads
+    nothing of the library."""
     if rank != 0:
         return 0
     n = args.n
-    pos, vel, cfg, dt, phi = build_scene(n, args.seed)
     from oracle import oracle as orc
-    from stardust_gb300 import DEMEngine
-    eng = DEMEngine(cfg)
-    eng.add_spheres(pos, vel)
-    p = orc.params_from_engine(eng.params(), dt)
-    eng.close()
+    pos, vel, cfg, dt, phi = build_scene(n, args.seed, rsa=orc.scene_rsa)
+    p = orc.derive_params(cfg, pos[:, 3], dt, args.z_div)
     used = orc.lib().sdo_num_threads()
     omg = orc.with_ids(np.zeros_like(pos), np.arange(n))
-    sp, sv, sw, _, cs = orc.prepare(p, pos, vel, omg)
+    # the same window of the settling run as the GPU arm: advanced untimed
+    # (sdo_run) to step `advance`, then warm-up and the timed steps
+    sp, sv, sw = orc.run(p, pos, vel, omg, args.advance)
+    sp, sv, sw, _, cs = orc.prepare(p, sp, sv, sw)
     for _ in range(args.warmup):
         pn, vn, wn, keys, _, _, _ = orc.contact_integrate(p, sp, sv, sw, cs, record=False)
         sp, sv, sw, _, cs = orc.sort_reorder(p, pn, vn, wn, keys)
@@ -229,11 +243,14 @@ def run_reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s",
-                   "n_spheres": n, "volume_fraction": round(phi, 4), "l2": "n/a (host cores)"},
+        "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s, 2000-step run",
+                   "n_spheres": n, "volume_fraction": round(phi, 4), "l2": "n/a (host cores)",
+                   "timed_window": f"steps {args.advance + args.warmup + 1}-{args.advance + args.warmup + args.steps} "
+                                   "of the run"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": used, "kind": "port",
-                         "sample": f"{args.steps} full steps of the {n}-sphere scene, CPU restatement of the "
-                                   "step (the reference has no CPU DEM path), OpenMP on all host threads"},
+                         "sample": f"{args.steps} full steps (after {args.advance + args.warmup}) of the {n}-sphere "
+                                   "scene, CPU restatement of the step (the reference has no CPU DEM path), OpenMP "
+                                   "on all host threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -357,7 +374,7 @@ def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
     tuned = None
     if tune:
         from stardust_gb300 import autotune
-        tuned = autotune.tune_engine(eng, dt, reps=3)
+        tuned = autotune.tune_engine(eng, dt, reps=3, knobs=autotune.BATCH_KNOBS)
     ms = timed(eng, steps)
     st = eng.stats()
     eng.close()
@@ -476,6 +493,64 @@ def bench_sap(n: int, steps: int, warmup: int, local: int):
     return out
 
 
+def timed_steps(eng, dt: float, k: int, stream, flush) -> list:
+    """k steps, each after a 256 MB write that flushes the L2, one CUDA event
+    pair per step on the engine's stream: the per-step device times (ms)."""
+    import torch
+    a = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    b = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    for i in range(k):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+        a[i].record(stream)
+        eng.step(dt, 1)
+        b[i].record(stream)
+    torch.cuda.synchronize()
+    return [x.elapsed_time(y) for x, y in zip(a, b)]
+
+
+def with_knobs(knobs: dict, fn):
+    """Runs fn() with launch knobs set, then restores them."""
+    from stardust_gb300 import _abi
+    old = {k: _abi.tune_get(k) for k in knobs}
+    try:
+        for k, v in knobs.items():
+            _abi.tune_set(k, v)
+        return fn()
+    finally:
+        for k, v in old.items():
+            _abi.tune_set(k, v)
+
+
+def bench_dense_bed(pos, vel, cfg, dt, steps: int, advance: int, local: int):
+    """The same 1,048,576 spheres with radii inflated by 1.2: an overlapping
+    contact network of ~2.5M pairs, advanced `advance` steps (the explosive
+    start relaxes), then `steps` device-timed steps (L2 flushed before each),
+    with the knobs the settling box was tuned to and without contact lists."""
+    import torch
+    import stardust_gb300 as sd
+    p = pos.copy()
+    p[:, 3] *= np.float32(1.2)
+    c = sd.EngineConfig(**{**cfg.__dict__})
+    c.cell = float(2 * p[:, 3].max())
+    c.cuda_device = local
+    eng = sd.DEMEngine(c)
+    eng.add_spheres(p, vel)
+    eng.prepare()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    eng.step(dt, advance)
+    ms = statistics.mean(timed_steps(eng, dt, steps, stream, flush))
+    no_lists = statistics.mean(with_knobs({"skin_um": 0}, lambda: timed_steps(eng, dt, steps, stream, flush)))
+    st = eng.stats()
+    eng.close()
+    n = len(p)
+    return {"workload": f"{n} spheres of the settling box with radii x1.2, after {advance} steps",
+            "contacts": st["contacts"], "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3),
+            "ms_per_step_without_contact_lists": no_lists, "moved_keys_last_step": st["moved_keys"],
+            "device_errors": st["device_errors"]}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -495,9 +570,17 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    # warm-up (graph capture happens on the first step), then the autotuner
-    # picks the launch knobs on this scene (its steps are warm-up too)
+    # the first steps after the packing (graph capture happens on the first
+    # step): a short window kept as an extra key
     eng.step(dt, args.warmup)
+    eng.sync()
+    early_ms = statistics.mean(timed_steps(eng, dt, 10, stream, flush))
+    early = eng.stats()
+    # the timed window lies inside the config's 2,000-step settling run: the
+    # scene is advanced (untimed) to step `advance` first, then the
+    # autotuner picks the launch knobs on that state (its steps advance the
+    # run too), then warm-up
+    eng.step(dt, max(0, args.advance - int(early["steps"])))
     eng.sync()
     tuned = None
     if not args.no_tune:
@@ -505,7 +588,11 @@ def run_ours(args, rank, world, local):
         tuned = autotune.tune_engine(eng, dt, reps=5)
         log(f"autotune: {tuned}")
     # the knobs this workload is timed with (later sections tune their own)
-    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max", "pair_lists")}
+    knobs = {k: _abi.tune_get(k) for k in ("contact_mode", "sort_items", "z_div", "resort_max", "pair_lists",
+                                           "skin_um")}
+    eng.step(dt, args.warmup)
+    eng.sync()
+    first_step = int(eng.stats()["steps"]) + 1
 
     def barrier():
         torch.cuda.synchronize()
@@ -514,25 +601,29 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
 
     # ---- device-timed steps (value)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier()
     with Clocks(local) as clk:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xFF)
-            starts[k].record(stream)
-            eng.step(dt, 1)
-            ends[k].record(stream)
+        step_ms = timed_steps(eng, dt, args.steps, stream, flush)
         barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     clocks = clk.summary()
     eng.sync()
+    st = eng.stats()
     from stardust_gb300 import replicas
     total_ms = replicas.max_over_ranks(sum(step_ms), device=f"cuda:{local}")
     value = replicas.job_rate(n * args.steps, total_ms * 1e-3, device=f"cuda:{local}")
+    window = {"first_step": first_step, "last_step": int(st["steps"]), "contacts": st["contacts"],
+              "moved_keys_last_step": st["moved_keys"], "list_builds": st["list_builds"],
+              "listed_steps": st["listed_steps"]}
 
-    # ---- dominant kernel alone: contact + integrate (idempotent stage)
+    # ---- the same state without the contact lists, and with the full radix
+    # sort every step (no incremental re-sort, hence no lists either)
+    k_cmp = max(10, args.steps // 2)
+    no_lists_ms = statistics.mean(with_knobs({"skin_um": 0}, lambda: timed_steps(eng, dt, k_cmp, stream, flush)))
+    full_sort_ms = statistics.mean(with_knobs({"resort_max": 0},
+                                              lambda: timed_steps(eng, dt, k_cmp, stream, flush)))
+
+    # ---- dominant kernel alone: contact + integrate (idempotent stage: the
+    # step's own variant, i.e. the listed contacts between list builds)
     kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     stage_ms = {}
@@ -542,7 +633,6 @@ def run_ours(args, rank, world, local):
     # cell keys changed (stages_note in the JSON line)
     for name, stage in (("contact_integrate", _abi.SD_STAGE_CONTACT), ("radix_sort", _abi.SD_STAGE_SORT),
                         ("gather_reorder", _abi.SD_STAGE_REORDER)):
-        ms = []
         for k in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xFF)
@@ -554,9 +644,11 @@ def run_ours(args, rank, world, local):
         stage_ms[name] = sum(ms) / len(ms)
     eng.sync()
     contact_ms = stage_ms["contact_integrate"]
+    lists_on = knobs["skin_um"] > 0 and knobs["resort_max"] > 0 and knobs["contact_mode"] == 0
+    contact_bytes = CONTACT_BYTES_PER_SPHERE + (LIST_BYTES_PER_SPHERE if lists_on else 0)
     peak, peak_kind = measured_peak()
-    achieved = n * CONTACT_BYTES_PER_SPHERE / (contact_ms * 1e-3) / 1e9
-    traffic_ps, winst_ps = recorded_profile()
+    achieved = n * contact_bytes / (contact_ms * 1e-3) / 1e9
+    traffic_ps, winst_ps = recorded_profile("listed" if lists_on else "scan")
 
     # ---- end to end through the C ABI with host buffers: the host owns the
     # state; every step uploads positions and velocities from pinned memory,
@@ -587,8 +679,13 @@ def run_ours(args, rank, world, local):
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e = replicas.job_rate(n * args.steps, e2e_s, device=f"cuda:{local}")
-    st = eng.stats()
     eng.close()
+
+    # ---- a dense contact network of the same spheres (rank 0, N = 1)
+    dense = None
+    if rank == 0 and world == 1 and not args.no_dense:
+        dense = bench_dense_bed(pos, vel, cfg, dt, 20, 1000, local)
+        log(f"dense bed: {dense}")
 
     # ---- learned GJK warm start on the convex-hull step (rank 0, N = 1)
     gjk = None
@@ -622,40 +719,47 @@ def run_ours(args, rank, world, local):
             cp, cv, ccfg, cdt = pos, vel, cfg, dt
         else:
             cp, cv, ccfg, cdt, _ = build_scene(n_cpu, args.seed)
-        rate, used, csteps, cel = cpu_oracle_rate(cp, cv, ccfg, cdt, args.cpu_seconds, None)
+        rate, used, csteps, cel = cpu_oracle_rate(cp, cv, ccfg, cdt, args.cpu_seconds, None, args.z_div)
         cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
                "sample": f"{csteps} steps of the {n_cpu}-sphere scene in {cel:.1f}s, CPU restatement of the step "
                          f"(oracle/, OpenMP, {used} threads)"}
 
     if rank == 0:
+        sm_mhz = clocks_mhz(clocks)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s",
+            "config": {"workload": f"settling box, {n} polydisperse spheres, 1x1x2 m, dt 5e-6 s, 2000-step run",
                        "n_spheres": n, "volume_fraction": round(phi, 4), "cells": st["n_cells"],
+                       "timed_window": f"steps {window['first_step']}-{window['last_step']} of the run",
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas{world}",
                        "knobs": knobs},
+            "timed_window": window,
+            "early_window": {"steps": f"{args.warmup + 1}-{args.warmup + 10}", "ms_per_step": early_ms,
+                             "contacts": early["contacts"], "moved_keys_last_step": early["moved_keys"]},
+            "ms_per_step_without_contact_lists": no_lists_ms,
+            "ms_per_step_full_radix_sort": full_sort_ms,
             "autotune": tuned,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes},
-            "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel" + (" (listed)" if lists_on else ""),
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind,
                          "traffic": None if traffic_ps is None else traffic_ps * n,
-                         "algorithmic_bytes": CONTACT_BYTES_PER_SPHERE * n,
-                         "launch_ms": contact_ms},
-            # the contact kernel is bound by instruction issue, not bytes:
-            # its warp instructions per launch (ncu) over the live launch time,
-            # against one warp instruction per scheduler per clock
+                         "algorithmic_bytes": contact_bytes * n, "launch_ms": contact_ms},
+            # a scan-bound contact kernel is bound by instruction issue, not
+            # bytes: its warp instructions per launch (ncu) over the live
+            # launch time, against one warp instruction per scheduler per clock
             "issue_roofline": None if winst_ps is None else {
                 "kernel": "dem_contact_integrate_kernel", "unit": "warp instructions/s",
                 "achieved": winst_ps * n / (contact_ms * 1e-3),
-                "peak": SMS * SCHEDULERS_PER_SM * clocks_mhz(clocks) * 1e6,
-                "frac": winst_ps * n / (contact_ms * 1e-3) / (SMS * SCHEDULERS_PER_SM * clocks_mhz(clocks) * 1e6),
-                "warp_instructions": winst_ps * n, "sm_mhz": clocks_mhz(clocks)},
+                "peak": SMS * SCHEDULERS_PER_SM * sm_mhz * 1e6,
+                "frac": winst_ps * n / (contact_ms * 1e-3) / (SMS * SCHEDULERS_PER_SM * sm_mhz * 1e6),
+                "warp_instructions": winst_ps * n, "sm_mhz": sm_mhz},
             "stages_ms": stage_ms,
             "stages_note": "sd_engine_launch_stage stages timed alone; in the step graph the radix sort and gather "
                            "reorder give way to the incremental re-sort (scan) and in-place reorder while at most "
-                           "resort_max keys change (profiles/dem_step_1M_launches.md has the step's kernels)",
+                           "resort_max keys change",
             "step_bytes_per_sphere": STEP_BYTES_PER_SPHERE,
             "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
             "cpu_baseline": cpu,
@@ -663,6 +767,7 @@ def run_ours(args, rank, world, local):
             "gpu_launches": st["step_kernels"] * args.steps,
             "contacts": st["contacts"],
             "moved_keys_last_step": st["moved_keys"],
+            "dense_bed": dense,
             "gjk": gjk,
             "batch": batch,
             "drum": drum,
@@ -685,6 +790,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--advance", type=int, default=1000,
+                    help="untimed steps of the settling run before tuning and timing (the timed window's start)")
+    ap.add_argument("--no-dense", action="store_true", help="skip the dense contact network (radii x1.2)")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-hulls", action="store_true")
     ap.add_argument("--only-hulls", action="store_true", help="run only the convex-hull GJK section")

@@ -474,8 +474,8 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   kernel applies in slot order (a full scan for an overflowed list);
  *                   0 = one scan kernel; 2 (default) = lists for batches of scenes only.
  *                   Same bits either way
- *   "skin_um"       single scenes of free spheres prepared afterwards: contact lists with a
- *                   skin of this many micrometres (0, the default, = none).  A step that
+ *   "skin_um"       single scenes of free spheres, from the next step: contact lists with a
+ *                   skin of this many micrometres (0 = none; default 50).  A step that
  *                   follows a sphere moving 0.45 skin from its position at the last build
  *                   scans the window widened by the skin and lists each sphere's neighbours
  *                   within r_i + r_j + skin; other steps test only the listed neighbours.

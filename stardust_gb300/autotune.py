@@ -13,7 +13,9 @@ import itertools
 
 from . import _abi
 
-KNOBS = {"contact_mode": (0, 1), "sort_items": (8, 16)}
+KNOBS = {"contact_mode": (0, 1), "sort_items": (8, 16), "skin_um": (0, 20, 50, 100, 200)}
+# a batch of scenes takes no contact lists; its pair lists are a choice
+BATCH_KNOBS = {"sort_items": (8, 16), "pair_lists": (0, 2)}
 
 
 def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, flush_bytes: int = 256 << 20) -> dict:

@@ -1601,7 +1601,9 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
 }
 
 cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
-    return launch_contact(p, b, record, SortPlan{}, nullptr, st);
+    // the step's own variant: with contact lists on, the listed kernel (or
+    // the build scan when a build is due)
+    return launch_contact(p, b, record, SortPlan{}, nullptr, st, dem_step_skin(b));
 }
 
 // One whole step: clear the sort's scratch, contact + integrate (which also
@@ -1665,6 +1667,12 @@ cudaError_t dem_pairs_async(const DemParams& p, DemBuffers& b, cudaStream_t st) 
 cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, uint32_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     dem_unsort_kernel<<<grid_for(n, 256), 256, 0, st>>>(src, omg, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t dem_slot_of_all_async(const float4* omg, uint32_t* slot_of, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dem_slot_of_id_kernel<<<grid_for(n, 256), 256, 0, st>>>(omg, slot_of, n);
     return cudaGetLastError();
 }
 

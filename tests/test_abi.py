@@ -338,7 +338,7 @@ def test_struct_layouts_match_the_header(tmp_path, cname, pyname):
 def test_skin_knob(sdlib):
     from stardust_gb300 import _abi
     old = _abi.tune_get("skin_um")
-    assert old == 0
+    assert old == 50  # the default
     try:
         _abi.tune_set("skin_um", 500)
         assert _abi.tune_get("skin_um") == 500

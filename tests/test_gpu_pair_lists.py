@@ -29,8 +29,9 @@ def packed(n, inflate, seed):
 @pytest.mark.parametrize("inflate", [1.0, 1.3, 1.9])
 def test_pair_lists_bit_exact(sdlib, orc, pair_lists, inflate):
     from stardust_gb300 import _abi
-    old = _abi.tune_get("pair_lists")
+    old = (_abi.tune_get("pair_lists"), _abi.tune_get("skin_um"))
     try:
+        _abi.tune_set("skin_um", 0)  # single scenes take the skin lists first
         _abi.tune_set("pair_lists", pair_lists)
         n = 20_000
         pos, vel, cfg, dt = packed(n, inflate, seed=21)
@@ -53,16 +54,18 @@ def test_pair_lists_bit_exact(sdlib, orc, pair_lists, inflate):
         assert np.array_equal(bits(eng.omegas())[:, :3], bits(orc.unsort(ow, ow))[:, :3])
         eng.close()
     finally:
-        _abi.tune_set("pair_lists", old)
+        _abi.tune_set("pair_lists", old[0])
+        _abi.tune_set("skin_um", old[1])
 
 
 def test_pair_lists_forces_match_single_kernel(sdlib):
     """Recorded forces and torques of a dense pack: the two-kernel stage
     gives the same bits as the single scan kernel."""
     from stardust_gb300 import _abi
-    old = _abi.tune_get("pair_lists")
+    old = (_abi.tune_get("pair_lists"), _abi.tune_get("skin_um"))
     out = {}
     try:
+        _abi.tune_set("skin_um", 0)
         for pl in (0, 1):
             _abi.tune_set("pair_lists", pl)
             pos, vel, cfg, dt = packed(20_000, 1.4, seed=5)
@@ -75,7 +78,8 @@ def test_pair_lists_forces_match_single_kernel(sdlib):
             out[pl] = (eng.forces(), eng.torques(), eng.positions(), eng.stats()["contacts"])
             eng.close()
     finally:
-        _abi.tune_set("pair_lists", old)
+        _abi.tune_set("pair_lists", old[0])
+        _abi.tune_set("skin_um", old[1])
     for a, b in zip(out[0][:3], out[1][:3]):
         assert np.array_equal(bits(a), bits(b))
     assert out[0][3] == out[1][3] > 0

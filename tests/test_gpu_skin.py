@@ -41,9 +41,11 @@ def test_skin_lists_bit_exact(sdlib, orc, skin_um, inflate, speed):
         eng.sync()
         st = eng.stats()
         assert st["device_errors"] == 0
-        # the lists were built and used (not a silent fall-back to the scan)
-        assert st["list_builds"] >= 1 and st["listed_steps"] >= 1
-        assert st["list_builds"] + st["listed_steps"] == steps
+        # every step ran the list path (not a silent fall-back to the scan);
+        # the fast scenes rebuild at every step, the slow ones use the lists
+        assert st["list_builds"] >= 1 and st["list_builds"] + st["listed_steps"] == steps
+        if speed * dt * 4 < 0.45e-6 * skin_um:
+            assert st["listed_steps"] >= 1
         p = orc.params_checked(cfg, pos[:, 3], dt, eng.params())
         op, ov, ow = orc.run(p, pos, vel, orc.with_ids(np.zeros_like(pos), np.arange(n)), steps)
         assert np.array_equal(bits(eng.positions()), bits(orc.unsort(op, ow)))
