@@ -522,11 +522,12 @@ def with_knobs(knobs: dict, fn):
             _abi.tune_set(k, v)
 
 
-def bench_dense_bed(pos, vel, cfg, dt, steps: int, advance: int, local: int):
+def bench_dense_bed(pos, vel, cfg, dt, steps: int, advance: int, local: int, tune: bool):
     """The same 1,048,576 spheres with radii inflated by 1.2: an overlapping
     contact network of ~2.5M pairs, advanced `advance` steps (the explosive
-    start relaxes), then `steps` device-timed steps (L2 flushed before each),
-    with the knobs the settling box was tuned to and without contact lists."""
+    start relaxes), the contact-list skin chosen by the autotuner on that
+    state, then `steps` device-timed steps (L2 flushed before each), with
+    and without contact lists."""
     import torch
     import stardust_gb300 as sd
     p = pos.copy()
@@ -539,16 +540,25 @@ def bench_dense_bed(pos, vel, cfg, dt, steps: int, advance: int, local: int):
     eng.prepare()
     stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    from stardust_gb300 import _abi, autotune
     eng.step(dt, advance)
+    old = _abi.tune_get("skin_um")
+    tuned = None
+    if tune:
+        tuned = autotune.tune_engine(eng, dt, reps=3, knobs={"skin_um": (0, 50, 200, 500)})
+    skin = _abi.tune_get("skin_um")
+    eng.step(dt, 3)
     ms = statistics.mean(timed_steps(eng, dt, steps, stream, flush))
     no_lists = statistics.mean(with_knobs({"skin_um": 0}, lambda: timed_steps(eng, dt, steps, stream, flush)))
+    _abi.tune_set("skin_um", old)
     st = eng.stats()
     eng.close()
     n = len(p)
     return {"workload": f"{n} spheres of the settling box with radii x1.2, after {advance} steps",
             "contacts": st["contacts"], "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3),
-            "ms_per_step_without_contact_lists": no_lists, "moved_keys_last_step": st["moved_keys"],
-            "device_errors": st["device_errors"]}
+            "skin_um": skin, "ms_per_step_without_contact_lists": no_lists,
+            "moved_keys_last_step": st["moved_keys"], "device_errors": st["device_errors"],
+            "autotune": None if tuned is None else tuned["choice"]}
 
 
 def run_ours(args, rank, world, local):
@@ -621,6 +631,8 @@ def run_ours(args, rank, world, local):
     no_lists_ms = statistics.mean(with_knobs({"skin_um": 0}, lambda: timed_steps(eng, dt, k_cmp, stream, flush)))
     full_sort_ms = statistics.mean(with_knobs({"resort_max": 0},
                                               lambda: timed_steps(eng, dt, k_cmp, stream, flush)))
+    eng.step(dt, 2)  # the step graph of the timed knobs again (the stages below run its variant)
+    eng.sync()
 
     # ---- dominant kernel alone: contact + integrate (idempotent stage: the
     # step's own variant, i.e. the listed contacts between list builds)
@@ -684,7 +696,7 @@ def run_ours(args, rank, world, local):
     # ---- a dense contact network of the same spheres (rank 0, N = 1)
     dense = None
     if rank == 0 and world == 1 and not args.no_dense:
-        dense = bench_dense_bed(pos, vel, cfg, dt, 20, 1000, local)
+        dense = bench_dense_bed(pos, vel, cfg, dt, 20, 1000, local, not args.no_tune)
         log(f"dense bed: {dense}")
 
     # ---- learned GJK warm start on the convex-hull step (rank 0, N = 1)

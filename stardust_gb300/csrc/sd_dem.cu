@@ -1453,6 +1453,33 @@ __global__ void dem_keys_changed_kernel(DemParams p, uint32_t n, const float4* _
     if (lane_id() == 0 && m) atomicAdd(count, __popc(m));
 }
 
+// Positions written by the host: a sphere now more than 0.45 skin from its
+// position at the last list build makes the next step build the lists (the
+// steps' own check runs only after integration).
+__global__ void dem_skin_check_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ omg,
+                                      const float4* __restrict__ ref, float thr2, uint32_t* __restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool far = false;
+    if (i < n) {
+        const float4 q = pos[i];
+        const uint32_t id = __float_as_uint(omg[i].w) & kIdMask;
+        if (id < n) {
+            const float4 r = ref[id];
+            far = dist2(q.x - r.x, q.y - r.y, q.z - r.z) > thr2;
+        } else {
+            far = true;
+        }
+    }
+    if (__ballot_sync(0xffffffffu, far) && lane_id() == 0) flags[0] = 1u;
+}
+
+cudaError_t dem_skin_check_async(const DemBuffers& b, cudaStream_t st) {
+    if (b.n == 0 || !b.vl_flags || !(b.vl_skin > 0.0f)) return cudaSuccess;
+    const float thr = 0.45f * b.vl_skin;
+    dem_skin_check_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(b.n, b.pos, b.omg, b.vl_ref, thr * thr, b.vl_flags);
+    return cudaGetLastError();
+}
+
 cudaError_t dem_keys_changed_async(const DemParams& p, const DemBuffers& b, uint32_t* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess || b.n == 0) return e;

@@ -1461,10 +1461,10 @@ sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src,
         SD_CUDA(h, sd::dem_keys_changed_async(h->P, h->B, d_changed, h->stream));
         SD_CUDA(h, cudaMemcpyAsync(&changed, d_changed, 4, cudaMemcpyDeviceToHost, h->stream));
     }
-    if (field == SD_FIELD_POSITION && h->B.vl_flags) {  // new positions: the skin lists are rebuilt
-        const uint32_t build = 1u;
-        SD_CUDA(h, cudaMemcpyAsync(h->B.vl_flags, &build, 4, cudaMemcpyHostToDevice, h->stream));
-    }
+    // new positions: the contact lists are built again at the next step if
+    // a sphere left its skin (lists that are off are rebuilt when they come
+    // back on)
+    if (field == SD_FIELD_POSITION) SD_CUDA(h, sd::dem_skin_check_async(h->B, h->stream));
     SD_CUDA(h, cudaStreamSynchronize(h->stream));
     if (field == SD_FIELD_POSITION && changed != 0) h->need_resort = true;
     return SD_OK;

@@ -301,6 +301,9 @@ cudaError_t dem_unsort_async(const float4* src, const float4* omg, float4* dst, 
 // State fields between a host buffer in sphere-id order that the device can
 // address (mapped page-locked memory) and the slot-ordered device arrays;
 // slot_of_id (n words) receives the id -> slot table.
+// After the host wrote positions: sets the lists' build flag when a sphere
+// left 0.45 skin of its position at the last build (no-op without lists).
+cudaError_t dem_skin_check_async(const DemBuffers& b, cudaStream_t st);
 // slot_of[id] = slot of every sphere of the current state (ids in omg.w).
 cudaError_t dem_slot_of_all_async(const float4* omg, uint32_t* slot_of, uint32_t n, cudaStream_t st);
 cudaError_t dem_host_in_async(const float4* host_src, const float4* omg, float4* dst, uint32_t* slot_of_id,

@@ -110,11 +110,12 @@ def test_dense_pack_1000_steps_ensemble(sdlib, orc):
 def test_hull_600_steps_with_learned_seeds(sdlib, orc):
     """3,000 convex hulls: the warm-start network is trained on the GPU on
     the separating directions plain GJK logs in the first 20 steps, then
-    the scene runs 600 steps with learned seeds.  Seeds change only the
-    iteration count, so the state equals the plain-GJK oracle's bit for bit
-    after 600 steps (the oracle starts from the point sets, not from the
-    engine), and the learned run needs fewer support evaluations per pair
-    than plain GJK over the whole run."""
+    the scene runs 600 steps with learned seeds beside a plain-GJK engine.
+    Seeds change only the iteration count, so both states equal the
+    plain-GJK oracle's bit for bit after 600 steps (the oracle starts from
+    the engine's initial bodies and principal-frame shapes), and the
+    learned run needs fewer support evaluations per pair than plain GJK
+    over the whole run."""
     import torch
     from stardust_gb300 import _abi, scenes
     pts, pos, quat, vel, mass, cfg, dt = scenes.hull_box(3000, seed=1, box=(0.4, 0.4, 0.4), spacing=0.0195,
@@ -147,6 +148,11 @@ def test_hull_600_steps_with_learned_seeds(sdlib, orc):
 
     learned = engine(_abi.SD_GJK_SEED_LEARNED, params)
     plain = engine(_abi.SD_GJK_SEED_PLAIN)
+    vs, vc, verts = learned.hull_shapes()
+    b = {k: learned.bodies(f) for k, f in (("pos", _abi.SD_BODY_POSITION), ("vel", _abi.SD_BODY_VELOCITY),
+                                             ("quat", _abi.SD_BODY_QUATERNION), ("omg", _abi.SD_BODY_OMEGA),
+                                             ("ang", _abi.SD_BODY_ANGMOM), ("iinv", _abi.SD_BODY_HULL_INV_INERTIA))}
+    H = orc.Hulls(b["pos"], b["vel"], b["quat"], b["omg"], b["ang"], b["iinv"], vs, vc, verts)
     it = {"plain": 0, "learned": 0}
     pairs = {"plain": 0, "learned": 0}
     for _ in range(steps):
@@ -157,7 +163,6 @@ def test_hull_600_steps_with_learned_seeds(sdlib, orc):
             pairs[name] += st["gjk_pairs"]
     learned.sync()
     assert learned.stats()["device_errors"] == 0
-    H = orc.hulls_from_points(pts, pos, quat, vel, mass)
     p = orc.hull_params(cfg.box_lo, cfg.box_hi, cfg.kn, orc.damp_from(cfg.kn, cfg.restitution), cfg.mu, cfg.gravity,
                         dt, cfg.walls)
     for _ in range(steps):
