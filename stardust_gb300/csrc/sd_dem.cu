@@ -237,13 +237,14 @@ struct NbrLists {
     const uint32_t* nbr;
 };
 
-// Skin lists of the single-scene free-sphere step: per sphere id its
-// neighbour ids within r_i + r_j + skin at the last build, the position
-// then, and the slot of every id this step.
+// Skin lists of the single-scene free-sphere step, in slot order (the
+// in-place reorder moves them with the state): per slot its neighbours'
+// ids within r_i + r_j + skin at the last build, the position then, and
+// the slot of every id this step.
 struct SkinLists {
-    uint32_t* cnt;            // per id; kVlCap + 1 = overflowed (the sphere scans)
-    uint32_t* nbr;            // per id, kVlCap neighbour ids
-    float4* ref;              // per id: position at the build
+    uint32_t* cnt;            // per slot; kVlCap + 1 = overflowed (the sphere scans)
+    uint32_t* nbr;            // kVlCap rows of n ids: entry q of slot s at nbr[q * n + s]
+    float4* ref;              // per slot: position at the build
     const uint32_t* flags;    // [0]: build this step
     uint32_t* next;           // = flags + 1: set when a sphere left its skin
     const uint32_t* slot_of;  // per id: slot this step
@@ -410,7 +411,6 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
         // every sphere has moved less than 0.45 skin since (checked at the
         // end of every step), so the distance changed by less than 0.9
         // skin.  Contacts are applied in ascending slot order, the scan's.
-        const uint32_t id = idb & kIdMask;
         if (sk->flags[0] != 0u) {  // build: the scan over the window widened by the skin
             const float reach_b = (ri + p.rmax + sk->skin) * 1.00001f;
             int32_t bx0, bx1, by0, by1, bz0, bz1;
@@ -430,8 +430,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                         if (s == i) continue;  // the sphere itself; a coincident partner is listed
                         const float rl = ri + pa.w + sk->skin;
                         if (da < rl * rl) {
-                            if (c < kVlCap && id < n)
-                                sk->nbr[(size_t)id * kVlCap + c] =
+                            if (c < kVlCap)
+                                sk->nbr[(size_t)c * n + i] =
                                     __float_as_uint(__ldg(reinterpret_cast<const float*>(omg) + 4 * (size_t)s + 3)) &
                                     kIdMask;
                             ++c;
@@ -444,17 +444,15 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                     }
                 }
             }
-            if (id < n) {
-                sk->cnt[id] = min(c, kVlCap + 1);
-                sk->ref[id] = pi;
-            }
+            sk->cnt[i] = min(c, kVlCap + 1);
+            sk->ref[i] = pi;
             x1 = x0 - 1;  // no second scan
-        } else if (id < n && sk->cnt[id] <= kVlCap) {
-            const uint32_t c = sk->cnt[id];
+        } else if (sk->cnt[i] <= kVlCap) {
+            const uint32_t c = sk->cnt[i];
             uint32_t js[kVlCap];
             uint32_t m = 0;
             for (uint32_t k = 0; k < c; ++k) {  // the listed neighbours in contact, by ascending slot
-                const uint32_t jd = sk->nbr[(size_t)id * kVlCap + k];
+                const uint32_t jd = sk->nbr[(size_t)k * n + i];
                 if (jd >= n) continue;
                 const uint32_t s = sk->slot_of[jd];
                 if (s >= n) continue;
@@ -612,11 +610,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia), wi.z + dt * (t.z / inertia),
                            wi.w);
     if constexpr (SKIN) {  // left 0.45 skin of the build position: build next step
-        const uint32_t id = idb & kIdMask;
-        if (id < n) {
-            const float4 r = sk->ref[id];
-            if (dist2(nxp - r.x, nyp - r.y, nzp - r.z) > sk->thr2) atomicOr(sk->next, 1u);
-        }
+        const float4 r = sk->ref[i];
+        if (dist2(nxp - r.x, nyp - r.y, nzp - r.z) > sk->thr2) atomicOr(sk->next, 1u);
     }
     const uint32_t key = cell_key_g(g, nxp, nyp, nzp);
     keys[i] = key;
@@ -1165,6 +1160,18 @@ __device__ __forceinline__ bool sorted_entry(uint32_t k, uint32_t M, const uint3
     return false;
 }
 
+// The contact lists the in-place reorder moves with the state (all null
+// when the step uses none): per slot count, build position and kVlCap rows
+// of neighbour ids, and same-sized buffers for the gathered entries.
+struct ListView {
+    uint32_t* cnt;
+    float4* ref;
+    uint32_t* nbr;
+    uint32_t* cnt_t;
+    float4* ref_t;
+    uint32_t* nbr_t;
+};
+
 // The in-place reorder of a step whose next state stays where the contact
 // kernel wrote it (S, the *_n buffers, in the previous slot order).  Sorted
 // position k needs the entry of slot src(k); where src(k) == k -- every
@@ -1182,7 +1189,7 @@ dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ 
                       const float4* __restrict__ s_pos4, const float4* __restrict__ s_vel,
                       const float4* __restrict__ s_omg, float4* __restrict__ t_pos, float4* __restrict__ t_vel,
                       float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start,
-                      const uint32_t* __restrict__ keys_prev, ResortView rv) {
+                      const uint32_t* __restrict__ keys_prev, ResortView rv, ListView lv) {
     __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
@@ -1196,6 +1203,12 @@ dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ 
             t_pos[k] = s_pos4[src];
             t_vel[k] = s_vel[src];
             t_omg[k] = s_omg[src];
+            if (lv.cnt) {
+                const uint32_t c = lv.cnt[src];
+                lv.cnt_t[k] = c;
+                lv.ref_t[k] = lv.ref[src];
+                for (uint32_t q = 0; q < min(c, kVlCap); ++q) lv.nbr_t[(size_t)q * n + k] = lv.nbr[(size_t)q * n + src];
+            }
         }
     }
     if (!inc) return;
@@ -1215,7 +1228,7 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
                      const float4* __restrict__ t_vel, const float4* __restrict__ t_omg, float4* __restrict__ s_pos4,
                      float4* __restrict__ s_vel, float4* __restrict__ s_omg, uint32_t* __restrict__ cell_start,
                      uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv,
-                     bool slot_all) {
+                     bool slot_all, ListView lv) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
     __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
@@ -1243,6 +1256,12 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
             s_omg[k] = o;
             const uint32_t idb = __float_as_uint(o.w);
             if (slot_of && (slot_all || (idb & kClumpFlag)) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
+            if (lv.cnt) {
+                const uint32_t c = lv.cnt_t[k];
+                lv.cnt[k] = c;
+                lv.ref[k] = lv.ref_t[k];
+                for (uint32_t q = 0; q < min(c, kVlCap); ++q) lv.nbr[(size_t)q * n + k] = lv.nbr_t[(size_t)q * n + k];
+            }
         }
         s_keys[threadIdx.x + 1] = key;
         keys_prev[k] = key;
@@ -1456,19 +1475,13 @@ __global__ void dem_keys_changed_kernel(DemParams p, uint32_t n, const float4* _
 // Positions written by the host: a sphere now more than 0.45 skin from its
 // position at the last list build makes the next step build the lists (the
 // steps' own check runs only after integration).
-__global__ void dem_skin_check_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ omg,
-                                      const float4* __restrict__ ref, float thr2, uint32_t* __restrict__ flags) {
+__global__ void dem_skin_check_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ ref,
+                                      float thr2, uint32_t* __restrict__ flags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool far = false;
     if (i < n) {
-        const float4 q = pos[i];
-        const uint32_t id = __float_as_uint(omg[i].w) & kIdMask;
-        if (id < n) {
-            const float4 r = ref[id];
-            far = dist2(q.x - r.x, q.y - r.y, q.z - r.z) > thr2;
-        } else {
-            far = true;
-        }
+        const float4 q = pos[i], r = ref[i];
+        far = dist2(q.x - r.x, q.y - r.y, q.z - r.z) > thr2;
     }
     if (__ballot_sync(0xffffffffu, far) && lane_id() == 0) flags[0] = 1u;
 }
@@ -1476,7 +1489,7 @@ __global__ void dem_skin_check_kernel(uint32_t n, const float4* __restrict__ pos
 cudaError_t dem_skin_check_async(const DemBuffers& b, cudaStream_t st) {
     if (b.n == 0 || !b.vl_flags || !(b.vl_skin > 0.0f)) return cudaSuccess;
     const float thr = 0.45f * b.vl_skin;
-    dem_skin_check_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(b.n, b.pos, b.omg, b.vl_ref, thr * thr, b.vl_flags);
+    dem_skin_check_kernel<<<grid_for(b.n, 256), 256, 0, st>>>(b.n, b.pos, b.vl_ref, thr * thr, b.vl_flags);
     return cudaGetLastError();
 }
 
@@ -1659,12 +1672,14 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
         const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
         const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
         const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
+        const ListView lv = skin ? ListView{b.vl_cnt, b.vl_ref, b.vl_nbr, b.vl_cnt_t, b.vl_ref_t, b.vl_nbr_t}
+                                 : ListView{};
         const unsigned grid = grid_for(b.n, kReorderThreads);
         dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, v, b.pos_n, b.vel_n, b.omg_n, b.pos,
-                                                                b.vel, b.omg, b.cell_start, b.keys_prev, rv);
+                                                                b.vel, b.omg, b.cell_start, b.keys_prev, rv, lv);
         dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
                                                                b.vel_n, b.omg_n, b.cell_start,
-                                                               b.slot_of, b.keys_prev, rv, slot_all_of(b));
+                                                               b.slot_of, b.keys_prev, rv, slot_all_of(b), lv);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     } else if ((e = dem_reorder_async(b, st)) != cudaSuccess) {
         return e;

@@ -517,7 +517,9 @@ static sd_status ensure_contact_lists(sd_engine* h) {
     sd_status s;
     if (!B.vl_cnt) {
         if ((s = dev_alloc(h, &B.vl_cnt, n)) || (s = dev_alloc(h, &B.vl_nbr, (size_t)n * sd::kVlCap)) ||
-            (s = dev_alloc(h, &B.vl_ref, n)) || (s = dev_alloc(h, &B.vl_flags, 4)))
+            (s = dev_alloc(h, &B.vl_ref, n)) || (s = dev_alloc(h, &B.vl_flags, 4)) ||
+            (s = dev_alloc(h, &B.vl_cnt_t, n)) || (s = dev_alloc(h, &B.vl_nbr_t, (size_t)n * sd::kVlCap)) ||
+            (s = dev_alloc(h, &B.vl_ref_t, n)))
             return s;
         SD_CUDA(h, cudaMemsetAsync(B.vl_flags, 0, 4 * sizeof(uint32_t), h->stream));
     }
@@ -605,7 +607,8 @@ sd_status resort_if_needed(sd_engine* h) {
     SD_CUDA(h, sd::dem_sort_reorder_async(h->P, B, h->stream));
     h->need_resort = false;
     h->keys_current = true;
-    return SD_OK;
+    // the plain reorder does not carry the contact lists: build them again
+    return force_list_build(h);
 }
 
 sd_status read_device_errors(sd_engine* h, uint32_t* bits) {

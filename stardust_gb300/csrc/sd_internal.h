@@ -254,6 +254,9 @@ struct DemBuffers {
     // [2] = steps that built the lists, [3] = steps that used them
     uint32_t *vl_cnt, *vl_nbr, *vl_flags;
     float4* vl_ref;
+    // the reorder's buffers for the list entries it moves (same sizes)
+    uint32_t *vl_cnt_t, *vl_nbr_t;
+    float4* vl_ref_t;
     float vl_skin;
 };
 

