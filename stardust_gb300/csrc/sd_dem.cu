@@ -229,6 +229,18 @@ struct ClumpCtx {
     float4* __restrict__ st;               // per slot: torque handed to the body
 };
 
+// The incremental re-sort's list of moved slots (sd_resort.cu): the step's
+// key writers append (key << 32 | slot) for every slot whose new key
+// differs from the sorted key it sits under, keys_prev[slot]; entries past
+// mmax are counted, not written (the radix fallback sorts then).  A null
+// list: the step builds the radix sort's histograms instead.
+struct MoveSink {
+    const uint32_t* keys_prev;
+    unsigned long long* list;
+    uint32_t* count;
+    uint32_t mmax;
+};
+
 // Contact partner lists of the two-kernel contact stage (scenes without
 // clumps or meshes): per slot a count and up to kNbrCap partner slots,
 // appended in any order by dem_pair_lists_kernel.
@@ -360,6 +372,21 @@ __device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView
     }
 }
 
+// Listed neighbour k of slot i: its slot this step and position, and
+// whether it is in contact (|x_i - x_j| < r_i + r_j, centres apart).
+template <class SRC>
+__device__ __forceinline__ bool listed_hit(const SkinLists* sk, uint32_t n, uint32_t i, uint32_t k, const SRC& src,
+                                           const float4& pi, float ri, uint32_t& s, float4& pa) {
+    const uint32_t jd = sk->nbr[(size_t)k * n + i];
+    if (jd >= n) return false;
+    s = sk->slot_of[jd];
+    if (s >= n) return false;
+    pa = src.load(s);
+    const float da = dist2(pi.x - pa.x, pi.y - pa.y, pi.z - pa.z);
+    const float ra = ri + pa.w;
+    return da < ra * ra && da != 0.0f;
+}
+
 // Contacts of slot i over its candidate cells, then walls, integration and
 // the next-state write.  Returns the new cell key; a clump sphere hands its
 // force and torque to its body instead (the body kernel writes its next
@@ -383,29 +410,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     const uint32_t idb = __float_as_uint(wi.w);
     const bool clump_i = CLUMPS && (idb & kClumpFlag);
     float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
-    // The candidate cells: the 3x3x3 block around i's cell, cut per axis to
-    // the cells a partner's centre can occupy, |x_j - x_i| < r_i + r_max
-    // (padded by 1e-5 against rounding).  Only non-contacts are dropped, and
-    // the surviving candidates keep the block's visiting order -- columns (x
-    // outer, y inner), slots ascending -- so the force sums are identical to
-    // a full 27-cell scan.
-    const float reach = (ri + p.rmax) * 1.00001f;
-    int32_t cx = 0, cy = 0, x0, x1, y0, y1, z0, z1;
-    if constexpr (SRC::kExactWindow) {
-        cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
-        cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
-        x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
-        x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
-        y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
-        y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
-        z0 = axis_cell(pi.z - reach, g.lo[2], g.cellz, g.nz);
-        z1 = axis_cell(pi.z + reach, g.lo[2], g.cellz, g.nz);
-    } else {
-        const float ic = 1.0f / g.cell;
-        axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
-        axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
-        axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
-    }
+    int32_t cx = 0, cy = 0, x0 = 0, x1 = -1, y0 = 0, y1 = -1, z0 = 0, z1 = -1;
+    bool scan = true;  // false once the contacts came from a list
     if constexpr (SKIN) {
         // A pair in contact now was within r_i + r_j + skin at the build:
         // every sphere has moved less than 0.45 skin since (checked at the
@@ -446,36 +452,50 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             }
             sk->cnt[i] = min(c, kVlCap + 1);
             sk->ref[i] = pi;
-            x1 = x0 - 1;  // no second scan
+            scan = false;
         } else if (sk->cnt[i] <= kVlCap) {
+            // the listed neighbours in contact, applied by ascending slot (the
+            // scan's order).  A first pass finds them and whether list order
+            // already ascends -- the usual case: the list was written in scan
+            // order and few slots cross between builds; otherwise each is
+            // picked as the smallest slot above the last one applied.
             const uint32_t c = sk->cnt[i];
-            uint32_t js[kVlCap];
-            uint32_t m = 0;
-            for (uint32_t k = 0; k < c; ++k) {  // the listed neighbours in contact, by ascending slot
-                const uint32_t jd = sk->nbr[(size_t)k * n + i];
-                if (jd >= n) continue;
-                const uint32_t s = sk->slot_of[jd];
-                if (s >= n) continue;
-                const float4 pa = src.load(s);
-                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
-                const float da = dist2(ax, ay, az);
-                const float ra = ri + pa.w;
-                if (da < ra * ra && da != 0.0f) {
-                    uint32_t q = m++;
-                    for (; q > 0 && js[q - 1] > s; --q) js[q] = js[q - 1];
-                    js[q] = s;
+            uint32_t m = 0, last = 0;
+            bool asc = true;
+            for (uint32_t k = 0; k < c; ++k) {
+                uint32_t s;
+                float4 pa;
+                if (listed_hit(sk, n, i, k, src, pi, ri, s, pa)) {
+                    if (m && s < last) asc = false;
+                    last = s;
+                    ++m;
                 }
             }
-            for (uint32_t k = 0; k < m; ++k) {
-                const uint32_t s = js[k];
-                const float4 pa = src.load(s);
-                const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
+            uint32_t lo = 0, k0 = 0;  // slots below lo are applied; asc: entries below k0 too
+            for (uint32_t r = 0; r < m; ++r) {
+                uint32_t best = 0xffffffffu;
+                float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (uint32_t k = asc ? k0 : 0u; k < c; ++k) {
+                    uint32_t s;
+                    float4 pa;
+                    if (listed_hit(sk, n, i, k, src, pi, ri, s, pa) && s >= lo && s < best) {
+                        best = s;
+                        pb = pa;
+                        if (asc) {  // list order ascends: the next hit is the next to apply
+                            k0 = k + 1u;
+                            break;
+                        }
+                    }
+                }
+                if (best >= n) break;  // not reached: m hits were found above
+                const float ax = pi.x - pb.x, ay = pi.y - pb.y, az = pi.z - pb.z;
                 const float da = dist2(ax, ay, az);
-                const float ra = ri + pa.w;
+                const float ra = ri + pb.w;
                 ++contacts;
-                pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
+                pair_contact(p, ax, ay, az, da, ra, pb.w, ri, mi, vi, wi, vel, omg, best, f, t);
+                lo = best + 1u;
             }
-            x1 = x0 - 1;  // no scan
+            scan = false;
         }
         // else: an overflowed list -- the scan below
     }
@@ -486,7 +506,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
         const uint32_t c = nl->cnt[i];
         nl->cnt[i] = 0u;  // cleared for the next step's pair kernel
         if (c <= kNbrCap) {
-            x1 = x0 - 1;  // no scan
+            scan = false;
             uint32_t js[kNbrCap];
             for (uint32_t k = 0; k < c; ++k) {
                 const uint32_t v = nl->nbr[(size_t)i * kNbrCap + k];
@@ -506,6 +526,30 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                     pair_contact(p, ax, ay, az, da, ra, pa.w, ri, mi, vi, wi, vel, omg, s, f, t);
                 }
             }
+        }
+    }
+    if (scan) {
+        // The candidate cells: the 3x3x3 block around i's cell, cut per axis
+        // to the cells a partner's centre can occupy, |x_j - x_i| < r_i +
+        // r_max (padded by 1e-5 against rounding).  Only non-contacts are
+        // dropped, and the surviving candidates keep the block's visiting
+        // order -- columns (x outer, y inner), slots ascending -- so the
+        // force sums are identical to a full 27-cell scan.
+        const float reach = (ri + p.rmax) * 1.00001f;
+        if constexpr (SRC::kExactWindow) {
+            cx = axis_cell(pi.x, g.lo[0], g.cell, g.nx);
+            cy = axis_cell(pi.y, g.lo[1], g.cell, g.ny);
+            x0 = max(cx - 1, axis_cell(pi.x - reach, g.lo[0], g.cell, g.nx));
+            x1 = min(cx + 1, axis_cell(pi.x + reach, g.lo[0], g.cell, g.nx));
+            y0 = max(cy - 1, axis_cell(pi.y - reach, g.lo[1], g.cell, g.ny));
+            y1 = min(cy + 1, axis_cell(pi.y + reach, g.lo[1], g.cell, g.ny));
+            z0 = axis_cell(pi.z - reach, g.lo[2], g.cellz, g.nz);
+            z1 = axis_cell(pi.z + reach, g.lo[2], g.cellz, g.nz);
+        } else {
+            const float ic = 1.0f / g.cell;
+            axis_window(pi.x, reach, g.lo[0], ic, g.nx, x0, x1);
+            axis_window(pi.y, reach, g.lo[1], ic, g.ny, y0, y1);
+            axis_window(pi.z, reach, g.lo[2], 1.0f / g.cellz, g.nz, z0, z1);
         }
     }
     for (int32_t X = x0; X <= x1; ++X) {
@@ -600,15 +644,27 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     }
     *has_key = true;
     const float dt = p.dt;
-    const float nvx = vi.x + dt * (f.x / mi + p.g[0]);
-    const float nvy = vi.y + dt * (f.y / mi + p.g[1]);
-    const float nvz = vi.z + dt * (f.z / mi + p.g[2]);
+    // force / mass and torque / inertia; a sphere with no contact and no
+    // wall has f = t = +0 exactly, and +0 / m = +0 for any mass, so its six
+    // divisions are skipped with the same bits
+    float ax = 0.0f, ay = 0.0f, az = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
+    if ((__float_as_uint(f.x) | __float_as_uint(f.y) | __float_as_uint(f.z) | __float_as_uint(t.x) |
+         __float_as_uint(t.y) | __float_as_uint(t.z)) != 0u) {
+        const float inertia = ((0.4f * mi) * ri) * ri;
+        ax = f.x / mi;
+        ay = f.y / mi;
+        az = f.z / mi;
+        bx = t.x / inertia;
+        by = t.y / inertia;
+        bz = t.z / inertia;
+    }
+    const float nvx = vi.x + dt * (ax + p.g[0]);
+    const float nvy = vi.y + dt * (ay + p.g[1]);
+    const float nvz = vi.z + dt * (az + p.g[2]);
     const float nxp = pi.x + dt * nvx, nyp = pi.y + dt * nvy, nzp = pi.z + dt * nvz;
-    const float inertia = ((0.4f * mi) * ri) * ri;
     pos_n[i] = make_float4(nxp, nyp, nzp, ri);
     vel_n[i] = make_float4(nvx, nvy, nvz, mi);
-    omg_n[i] = make_float4(wi.x + dt * (t.x / inertia), wi.y + dt * (t.y / inertia), wi.z + dt * (t.z / inertia),
-                           wi.w);
+    omg_n[i] = make_float4(wi.x + dt * bx, wi.y + dt * by, wi.z + dt * bz, wi.w);
     if constexpr (SKIN) {  // left 0.45 skin of the build position: build next step
         const float4 r = sk->ref[i];
         if (dist2(nxp - r.x, nyp - r.y, nzp - r.z) > sk->thr2) atomicOr(sk->next, 1u);
@@ -661,6 +717,29 @@ __device__ __forceinline__ void hist_flush(const uint32_t* s_hist, uint32_t spec
         for (uint32_t d = threadIdx.x; d < (1u << bits); d += blockDim.x)
             if (s_hist[q * stride + d]) atomicAdd(&ghist[q * stride + d], s_hist[q * stride + d]);
     }
+}
+
+// Appends the moved slots among a warp's (all 32 lanes call it): one atomic
+// per warp that holds any.
+__device__ __forceinline__ void move_append_warp(const MoveSink& ms, uint32_t slot, uint32_t key, bool valid) {
+    const bool mv = valid && key != ms.keys_prev[slot];
+    const uint32_t m = __ballot_sync(0xffffffffu, mv);
+    if (!m) return;
+    const uint32_t leader = (uint32_t)__ffs(m) - 1u;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(ms.count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, (int)leader);
+    if (mv) {
+        const uint32_t r = base + (uint32_t)__popc(m & lanemask_lt());
+        if (r < ms.mmax) ms.list[r] = ((unsigned long long)key << 32) | slot;
+    }
+}
+
+// One slot, from a thread that may be alone in its branch.
+__device__ __forceinline__ void move_append_one(const MoveSink& ms, uint32_t slot, uint32_t key) {
+    if (key == ms.keys_prev[slot]) return;
+    const uint32_t r = atomicAdd(ms.count, 1u);
+    if (r < ms.mmax) ms.list[r] = ((unsigned long long)key << 32) | slot;
 }
 
 __device__ __forceinline__ void count_contacts(uint32_t* status, uint32_t contacts) {
@@ -727,7 +806,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
                              float4* __restrict__ force, float4* __restrict__ torque,
                              uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
                              ClumpCtx cc, Batch bt = Batch{}, MeshView mesh = MeshView{},
-                             NbrLists nl = NbrLists{}, SkinLists sk = SkinLists{}) {
+                             NbrLists nl = NbrLists{}, SkinLists sk = SkinLists{}, MoveSink ms = MoveSink{}) {
     __shared__ uint32_t s_hist[kHistWords];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
@@ -743,6 +822,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
     }
+    if (ms.list) move_append_warp(ms, i, key, has_key);
     if (RECORD) count_contacts(status, contacts);
 }
 
@@ -805,7 +885,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
                           float4* __restrict__ vel_n, float4* __restrict__ omg_n, uint32_t* __restrict__ keys,
                           uint32_t* __restrict__ vals, float4* __restrict__ force, float4* __restrict__ torque,
                           uint32_t* __restrict__ status, uint32_t hist_spec, uint32_t* __restrict__ ghist,
-                          ClumpCtx cc) {
+                          ClumpCtx cc, MoveSink ms) {
     extern __shared__ __align__(128) float4 s_tile[];
     __shared__ uint32_t s_hist[kHistWords];
     __shared__ __align__(8) unsigned long long s_bar;
@@ -875,6 +955,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
                                               vals, force, torque, contacts, cc, &has_key);
         }
         if (ghist) hist_add(s_hist, hist_spec, key, has_key);
+        if (ms.list) move_append_warp(ms, own_beg + k, key, has_key);
     }
     if (ghist) {
         __syncthreads();
@@ -913,7 +994,7 @@ __device__ __forceinline__ void body_step(
     const float4* __restrict__ omg, const float4* __restrict__ sf, const float4* __restrict__ st,
     float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n, uint32_t hist_spec,
-    uint32_t* s_hist) {
+    uint32_t* s_hist, const MoveSink& ms) {
     const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
     const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
     const uint32_t first = bfirst[b], cnt = bcount[b];
@@ -979,6 +1060,7 @@ __device__ __forceinline__ void body_step(
         const uint32_t key = cell_key(p, po.x, po.y, po.z);
         keys[s] = key;
         vals[s] = s;
+        if (ms.list) move_append_one(ms, s, key);
         if (s_hist) {
             const int passes = (int)(hist_spec & 3u);
             const uint32_t stride = spec_stride(hist_spec);
@@ -1007,7 +1089,7 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
                 const float4* __restrict__ pos, const float4* __restrict__ omg, const float4* __restrict__ sf,
                 const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
                 float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
-                uint32_t hist_spec, uint32_t* __restrict__ ghist) {
+                uint32_t hist_spec, uint32_t* __restrict__ ghist, MoveSink ms) {
     __shared__ uint32_t s_hist[kHistWords];
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
@@ -1016,7 +1098,7 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nb)
         body_step(p, b, bpos, bvel, bquat, bomg, bang, binv, bfirst, bcount, r0, slot_of, pos, omg, sf, st, pos_n,
-                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr);
+                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr, ms);
     if (ghist) {
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
@@ -1104,8 +1186,10 @@ struct ResortView {
     const uint32_t* pos;
     const uint32_t* q;
     const unsigned long long* list;
-    const uint32_t* scratch;  // [1] = M
+    const uint32_t* scratch;  // [1] = M, [3] = T
     uint32_t mmax;
+    const uint32_t* iv_lo;    // per moved entry: first position of the interval its move shifts
+    const uint32_t* iv_pre;   // exclusive prefix sums of the intervals' lengths (T = iv_pre[M])
 };
 
 // First index in [0, m) of ascending a with a[i] >= x (m if none).
@@ -1175,27 +1259,60 @@ struct ListView {
 // The in-place reorder of a step whose next state stays where the contact
 // kernel wrote it (S, the *_n buffers, in the previous slot order).  Sorted
 // position k needs the entry of slot src(k); where src(k) == k -- every
-// slot but those shifted by the moved keys -- nothing moves.  Phase 1
-// gathers the others into the free buffer T (the step's input state, no
-// longer read) and, with the re-sort's order, shifts the cell table:
-// cell_start[c] counts the entries with key < c, so an entry moving from
-// key a to key b takes one from the cells (a, b] when b > a and adds one to
-// (b, a] when b < a (atomic adds: several entries may share cells).
-// Phase 2 copies the gathered entries back, records every position's key
-// and, for the radix passes' order (more moves than the re-sort takes),
-// rebuilds the cell table as the plain reorder does.
+// slot but those shifted by the moved keys -- nothing moves.  Only
+// positions between a moved entry's old slot and its new position can
+// change hands, so with the re-sort's order the kernels visit those
+// intervals (T positions in all; a position in several is visited by each,
+// writing the same values) rather than all n, unless T is above n / 4.
+// Phase 1 gathers the positions that change hands into the free buffer T
+// (the step's input state, no longer read) and, with the re-sort's order,
+// shifts the cell table: cell_start[c] counts the entries with key < c, so
+// an entry moving from key a to key b takes one from the cells (a, b] when
+// b > a and adds one to (b, a] when b < a (atomic adds: several entries may
+// share cells).  Phase 2 copies the gathered entries back and records
+// their keys; for the radix passes' order (more moves than the re-sort
+// takes) every position is visited and the cell table is rebuilt as the
+// plain reorder does.  Both kernels run on a fixed grid (grid-stride).
+
+// Position visited by work item t: in interval mode the position of item t
+// among the intervals' concatenation, else t itself.
+__device__ __forceinline__ uint32_t visit_position(uint32_t t, bool iv, uint32_t M, const uint32_t* s_ivlo,
+                                                   const uint32_t* s_ivpre) {
+    if (!iv) return t;
+    const uint32_t r = upper_idx(s_ivpre, M, t) - 1u;  // s_ivpre[0] = 0 <= t
+    return s_ivlo[r] + (t - s_ivpre[r]);
+}
+
+// Loads the re-sort's lists (and the intervals when iv) into shared memory.
+__device__ __forceinline__ void load_fix_lists(const ResortView& rv, uint32_t M, bool iv, uint32_t* s_pos,
+                                               uint32_t* s_q, uint32_t* s_ivlo, uint32_t* s_ivpre) {
+    for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) {
+        s_pos[i] = rv.pos[i];
+        s_q[i] = rv.q[i];
+        if (iv) {
+            s_ivlo[i] = rv.iv_lo[i];
+            s_ivpre[i] = rv.iv_pre[i];
+        }
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(kReorderThreads)
 dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ vals,
                       const float4* __restrict__ s_pos4, const float4* __restrict__ s_vel,
                       const float4* __restrict__ s_omg, float4* __restrict__ t_pos, float4* __restrict__ t_vel,
                       float4* __restrict__ t_omg, uint32_t* __restrict__ cell_start,
                       const uint32_t* __restrict__ keys_prev, ResortView rv, ListView lv) {
-    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
+    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap], s_ivlo[kResortMaxCap], s_ivpre[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
-    const uint32_t k = blockIdx.x * kReorderThreads + threadIdx.x;
-    if (inc) load_resort_lists(rv, M, s_pos, s_q);
-    if (k < n) {
+    const uint32_t T = inc ? (M ? rv.scratch[3] : 0u) : n;
+    const bool iv = inc && T <= n / 4;
+    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
+    const uint32_t total = iv ? T : n;
+    for (uint32_t t = blockIdx.x * kReorderThreads + threadIdx.x; t < total; t += gridDim.x * kReorderThreads) {
+        const uint32_t k = visit_position(t, iv, M, s_ivlo, s_ivpre);
+        if (k >= n) continue;
         uint32_t src, key;
         if (inc) sorted_entry<false>(k, M, s_pos, s_q, rv, n, src, key);
         else src = vals[k];
@@ -1230,46 +1347,61 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
                      uint32_t* __restrict__ slot_of, uint32_t* __restrict__ keys_prev, ResortView rv,
                      bool slot_all, ListView lv) {
     __shared__ uint32_t s_keys[kReorderThreads + 1];
-    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap];
+    __shared__ uint32_t s_pos[kResortMaxCap], s_q[kResortMaxCap], s_ivlo[kResortMaxCap], s_ivpre[kResortMaxCap];
     const uint32_t M = rv.scratch[1];
     const bool inc = M <= rv.mmax;
-    const uint32_t b0 = blockIdx.x * kReorderThreads;
-    const uint32_t b1 = min(b0 + kReorderThreads, n);
-    const uint32_t k = b0 + threadIdx.x;
-    if (inc) load_resort_lists(rv, M, s_pos, s_q);
-    if (k < n) {
-        uint32_t src, key = 0;
-        if (inc) {
-            // a position that keeps its unmoved entry keeps its key too:
-            // nothing to write there
-            const bool moved = sorted_entry<false>(k, M, s_pos, s_q, rv, n, src, key);
-            if (src == k && !moved) return;  // no block-wide step follows in this mode
-            key = moved ? (uint32_t)(rv.list[lower_idx(s_pos, M, k)] >> 32) : (src < n ? rv.keys_new[src] : 0u);
-        } else {
-            src = vals[k];
-            key = keys[k];
-        }
-        if (src != k && src < n) {
-            s_pos4[k] = t_pos[k];
-            s_vel[k] = t_vel[k];
-            const float4 o = t_omg[k];
-            s_omg[k] = o;
-            const uint32_t idb = __float_as_uint(o.w);
-            if (slot_of && (slot_all || (idb & kClumpFlag)) && (idb & kIdMask) < n) slot_of[idb & kIdMask] = k;
-            if (lv.cnt) {
-                const uint32_t c = lv.cnt_t[k];
-                lv.cnt[k] = c;
-                lv.ref[k] = lv.ref_t[k];
-                for (uint32_t q = 0; q < min(c, kVlCap); ++q) lv.nbr[(size_t)q * n + k] = lv.nbr_t[(size_t)q * n + k];
+    const uint32_t T = inc ? (M ? rv.scratch[3] : 0u) : n;
+    const bool iv = inc && T <= n / 4;
+    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
+    // the radix order: chunks of kReorderThreads consecutive positions per
+    // block iteration, so that each chunk rebuilds its part of the cell table
+    const uint32_t total = inc ? (iv ? T : n) : (n + kReorderThreads - 1) / kReorderThreads * kReorderThreads;
+    for (uint32_t t0 = blockIdx.x * kReorderThreads; t0 < total; t0 += gridDim.x * kReorderThreads) {
+        const uint32_t t = t0 + threadIdx.x;
+        const uint32_t k = t < total ? visit_position(t, iv, M, s_ivlo, s_ivpre) : n;
+        if (k < n) {
+            uint32_t src, key = 0;
+            bool write = true;
+            if (inc) {
+                // a position that keeps its unmoved entry keeps its key too:
+                // nothing to write there
+                const bool moved = sorted_entry<false>(k, M, s_pos, s_q, rv, n, src, key);
+                if (src == k && !moved) write = false;
+                else key = moved ? (uint32_t)(rv.list[lower_idx(s_pos, M, k)] >> 32)
+                                 : (src < n ? rv.keys_new[src] : 0u);
+            } else {
+                src = vals[k];
+                key = keys[k];
             }
+            if (write) {
+                if (src != k && src < n) {
+                    s_pos4[k] = t_pos[k];
+                    s_vel[k] = t_vel[k];
+                    const float4 o = t_omg[k];
+                    s_omg[k] = o;
+                    const uint32_t idb = __float_as_uint(o.w);
+                    if (slot_of && (slot_all || (idb & kClumpFlag)) && (idb & kIdMask) < n)
+                        slot_of[idb & kIdMask] = k;
+                    if (lv.cnt) {
+                        const uint32_t c = lv.cnt_t[k];
+                        lv.cnt[k] = c;
+                        lv.ref[k] = lv.ref_t[k];
+                        for (uint32_t q = 0; q < min(c, kVlCap); ++q)
+                            lv.nbr[(size_t)q * n + k] = lv.nbr_t[(size_t)q * n + k];
+                    }
+                }
+                keys_prev[k] = key;
+            }
+            if (!inc) s_keys[threadIdx.x + 1] = key;
         }
-        s_keys[threadIdx.x + 1] = key;
-        keys_prev[k] = key;
+        if (!inc) {  // uniform: the radix order rebuilds the cell table chunk by chunk
+            const uint32_t b0 = t0, b1 = min(t0 + kReorderThreads, n);
+            if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
+            __syncthreads();
+            block_cell_starts(s_keys, b0, b1, n, ncells, cell_start);
+            __syncthreads();
+        }
     }
-    if (inc) return;  // the gather phase shifted the cell table
-    if (threadIdx.x == 0) s_keys[0] = b0 == 0 ? 0u : keys[b0 - 1];
-    __syncthreads();
-    block_cell_starts(s_keys, b0, b1, n, ncells, cell_start);
 }
 
 __global__ void dem_pairs_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos,
@@ -1558,84 +1690,86 @@ int dem_contact_mode() { return g_contact_mode; }
 
 template <bool RECORD>
 static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, uint32_t* ghist, cudaStream_t st,
-                             bool skin) {
+                             bool skin, const MoveSink& ms) {
     float4* f = RECORD ? b.force : nullptr;
     float4* t = RECORD ? b.torque : nullptr;
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
     const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
     const size_t tile = kTileSlots * sizeof(float4);
+    const unsigned grid = grid_for(b.n, 256);
     if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
         if (b.nb)
-            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
         else
-            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, b.mesh);
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         const Batch bt{b.scenes, b.scene_first, b.nscenes};
         if (g_pair_lists != 0 && b.nbr_cnt) {
-            dem_pair_lists_kernel<true><<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt,
-                                                                             b.nbr, bt);
-            dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_pair_lists_kernel<true><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, bt);
+            dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{b.nbr_cnt, b.nbr});
+                b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
         } else {
-            dem_contact_integrate_kernel<RECORD, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false, true><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc, bt);
+                b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{}, SkinLists{}, ms);
         }
     } else if (skin) {  // single scene of free spheres, skin lists
         const float thr = 0.45f * b.vl_skin;
         const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
-        dem_contact_integrate_kernel<RECORD, false, false, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+        dem_contact_integrate_kernel<RECORD, false, false, false, false, true><<<grid, 256, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, sk);
+            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, sk, ms);
     } else if (g_contact_mode == 0 && !b.nb && g_pair_lists == 1 && b.nbr_cnt) {
-        dem_pair_lists_kernel<false><<<grid_for(b.n, 256), 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt,
-                                                                          b.nbr, Batch{});
-        dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+        dem_pair_lists_kernel<false><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, Batch{});
+        dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid, 256, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{b.nbr_cnt, b.nbr});
+            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
     } else if (g_contact_mode == 0) {
         if (b.nb)
-            dem_contact_integrate_kernel<RECORD, true><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, true><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc);
+                b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
         else
-            dem_contact_integrate_kernel<RECORD, false><<<grid_for(b.n, 256), 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false><<<grid, 256, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc);
+                b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
     } else {
         if (b.nb)
             dem_contact_column_kernel<RECORD, true><<<cols, kColThreads, tile, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc);
+                b.dev_status, spec, ghist, cc, ms);
         else
             dem_contact_column_kernel<RECORD, false><<<cols, kColThreads, tile, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
-                b.dev_status, spec, ghist, cc);
+                b.dev_status, spec, ghist, cc, ms);
     }
 }
 
 // Contact + integration of free spheres, then (with clumps) the body
 // kernel, which completes the next state and keys of the clump spheres.
+// The new keys feed either the radix sort's histograms (ghist) or the
+// incremental re-sort's list of moved slots (ms.list).
 static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record, const SortPlan& plan,
-                                  uint32_t* ghist, cudaStream_t st, bool skin = false) {
+                                  uint32_t* ghist, cudaStream_t st, bool skin = false,
+                                  const MoveSink& ms = MoveSink{}) {
     if (b.n == 0) return cudaSuccess;
     const uint32_t spec = pack_hist_spec(plan);
     if (record) {
         cudaError_t e = cudaMemsetAsync(b.dev_status + 2, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        launch_contact_t<true>(p, b, spec, ghist, st, skin);
+        launch_contact_t<true>(p, b, spec, ghist, st, skin, ms);
     } else {
-        launch_contact_t<false>(p, b, spec, ghist, st, skin);
+        launch_contact_t<false>(p, b, spec, ghist, st, skin, ms);
     }
     if (b.nb) {
         dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
             p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
-            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n, spec, ghist);
+            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n, spec, ghist, ms);
     }
     return cudaGetLastError();
 }
@@ -1646,9 +1780,19 @@ cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool 
     return launch_contact(p, b, record, SortPlan{}, nullptr, st, dem_step_skin(b));
 }
 
-// One whole step: clear the sort's scratch, contact + integrate (which also
-// builds the key histograms), the incremental re-sort, the digit passes
-// (which return at once when the re-sort has written the result), reorder.
+// Fixed grid of the in-place reorder's kernels (grid-stride loops): most
+// steps touch a few thousand positions, the radix fallback all of them.
+static unsigned fix_grid(uint32_t n) {
+    const unsigned g = grid_for(n, kReorderThreads);
+    return g < 152u * 8u ? g : 152u * 8u;
+}
+
+// One whole step.  With the incremental re-sort (dem_step_swaps): contact +
+// integrate (which lists the slots whose key changed), the re-sort's plan,
+// the radix fallback (histogram + passes, returning at once when the plan
+// placed the moves), the in-place reorder.  Otherwise: clear the sort's
+// scratch, contact + integrate (which builds the key histograms), the
+// digit passes, the reorder.
 cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(dem_key_bits(b.ncells));
@@ -1658,32 +1802,36 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
         if ((e = dem_sort_reorder_async(p, b, st)) != cudaSuccess) return e;
         return mesh_advance_async(b.mesh, 1, st);
     }
-    cudaError_t e = sort_clear_async(b.n, plan, b.sort_scratch, st);
-    if (e != cudaSuccess) return e;
-    const bool skin = dem_step_skin(b);
-    if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st, skin)) != cudaSuccess) return e;
-    // the re-sort places the moved keys when it can (the passes then return
-    // at once and the reorder reads its order), else the passes sort
-    if ((e = resort_async(b, st, skin ? b.vl_flags : nullptr)) != cudaSuccess) return e;
-    if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
-                               &b.sorted_in_tmp, b.rs_max ? b.rs_scratch : nullptr, b.rs_max)) != cudaSuccess)
-        return e;
-    if (dem_step_swaps(b)) {  // sorted in place: the next state stays in the *_n buffers
-        const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
-        const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
-        const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max};
-        const ListView lv = skin ? ListView{b.vl_cnt, b.vl_ref, b.vl_nbr, b.vl_cnt_t, b.vl_ref_t, b.vl_nbr_t}
-                                 : ListView{};
-        const unsigned grid = grid_for(b.n, kReorderThreads);
-        dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, v, b.pos_n, b.vel_n, b.omg_n, b.pos,
-                                                                b.vel, b.omg, b.cell_start, b.keys_prev, rv, lv);
-        dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
-                                                               b.vel_n, b.omg_n, b.cell_start,
-                                                               b.slot_of, b.keys_prev, rv, slot_all_of(b), lv);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    } else if ((e = dem_reorder_async(b, st)) != cudaSuccess) {
-        return e;
+    cudaError_t e;
+    if (!dem_step_swaps(b)) {
+        if ((e = sort_clear_async(b.n, plan, b.sort_scratch, st)) != cudaSuccess) return e;
+        if ((e = launch_contact(p, b, record, plan, sort_hist_ptr(b.sort_scratch), st)) != cudaSuccess) return e;
+        if ((e = sort_passes_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
+                                   &b.sorted_in_tmp, nullptr, 0)) != cudaSuccess)
+            return e;
+        if ((e = dem_reorder_async(b, st)) != cudaSuccess) return e;
+        return mesh_advance_async(b.mesh, 1, st);
     }
+    const bool skin = dem_step_skin(b);
+    const MoveSink ms{b.keys_prev, b.rs_list, b.rs_scratch, b.rs_max};
+    if ((e = launch_contact(p, b, record, plan, nullptr, st, skin, ms)) != cudaSuccess) return e;
+    if ((e = resort_plan_async(b, st, skin ? b.vl_flags : nullptr)) != cudaSuccess) return e;
+    if ((e = sort_fallback_async(b.keys, b.vals, b.keys_tmp, b.vals_tmp, b.n, plan, b.sort_scratch, st,
+                                 &b.sorted_in_tmp, b.rs_scratch, b.rs_max)) != cudaSuccess)
+        return e;
+    // sorted in place: the next state stays in the *_n buffers
+    const uint32_t* k = b.sorted_in_tmp ? b.keys_tmp : b.keys;
+    const uint32_t* v = b.sorted_in_tmp ? b.vals_tmp : b.vals;
+    const ResortView rv{b.keys, b.rs_pos, b.rs_q, b.rs_list, b.rs_scratch, b.rs_max, b.rs_iv_lo, b.rs_iv_pre};
+    const ListView lv = skin ? ListView{b.vl_cnt, b.vl_ref, b.vl_nbr, b.vl_cnt_t, b.vl_ref_t, b.vl_nbr_t}
+                             : ListView{};
+    const unsigned grid = fix_grid(b.n);
+    dem_fix_gather_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, v, b.pos_n, b.vel_n, b.omg_n, b.pos,
+                                                            b.vel, b.omg, b.cell_start, b.keys_prev, rv, lv);
+    dem_fix_place_kernel<<<grid, kReorderThreads, 0, st>>>(b.n, b.ncells, k, v, b.pos, b.vel, b.omg, b.pos_n,
+                                                           b.vel_n, b.omg_n, b.cell_start, b.slot_of, b.keys_prev,
+                                                           rv, slot_all_of(b), lv);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return mesh_advance_async(b.mesh, 1, st);
 }
 

@@ -412,6 +412,8 @@ sd_status allocate(sd_engine* h, uint32_t n) {
         (s = dev_alloc(h, &h->d_tmp, n)) || (s = dev_alloc(h, &B.keys_prev, n)) ||
         (s = dev_alloc(h, &B.rs_list, (size_t)sd::kResortMaxCap)) ||
         (s = dev_alloc(h, &B.rs_pos, (size_t)sd::kResortMaxCap)) || (s = dev_alloc(h, &B.rs_q, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_iv_lo, (size_t)sd::kResortMaxCap)) ||
+        (s = dev_alloc(h, &B.rs_iv_pre, (size_t)sd::kResortMaxCap + 1)) ||
         (s = dev_alloc(h, &B.rs_scratch, sd::resort_scratch_words(n))))
         return s;
     if (h->hb_pos.empty() && h->mesh.tri.empty() && n) {  // the two-kernel contact stage's partner lists

@@ -40,6 +40,15 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
                                  cudaStream_t st);
 // skip (may be null): the passes return at once when skip[1] <= skip_max
 // (the incremental re-sort has written the result)
+// The radix fallback of the incremental re-sort: when skip[1] > skip_max,
+// clears the tile status, builds the histograms (tile counters and
+// histograms -- the first sort_fallback_clear_words() words after word 4 of
+// the scratch -- must be zero) and runs the passes; otherwise its kernels
+// return at once.
+uint64_t sort_fallback_clear_words();
+cudaError_t sort_fallback_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t n,
+                                const SortPlan& plan, uint32_t* scratch, cudaStream_t st, bool* in_tmp,
+                                const uint32_t* skip, uint32_t skip_max);
 cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                               uint32_t n, const SortPlan& plan, uint32_t* scratch, cudaStream_t st,
                               bool* in_tmp, const uint32_t* skip = nullptr, uint32_t skip_max = 0);
@@ -243,7 +252,9 @@ struct DemBuffers {
     unsigned long long* rs_list;    // the moved entries, (key << 32 | slot), up to kResortMaxCap
     uint32_t* rs_pos;               // per moved entry (in (key, slot) order): its sorted position
     uint32_t* rs_q;                 // per moved slot (ascending): slot - rank
-    uint32_t* rs_scratch;           // running count, moved count, arrivals
+    uint32_t* rs_iv_lo;             // per moved entry: first position its move shifts
+    uint32_t* rs_iv_pre;            // exclusive prefix sums of those intervals' lengths (M + 1 entries)
+    uint32_t* rs_scratch;           // [0] moved count, [1] M of the step, [3] total interval length
     uint32_t rs_max;                // most moved entries re-sorted incrementally (power of two, or 0)
     // contact partner lists (scenes without clumps): per slot a count, zero
     // between steps, and kNbrCap partner slots; null when not allocated
@@ -265,16 +276,17 @@ constexpr uint32_t kNbrCap = 16;  // contact partners listed per sphere by the p
 constexpr uint32_t kVlCap = 24;   // skin-list neighbours per sphere (more: the sphere scans)
 
 int dem_key_bits(uint32_t ncells);
-// incremental re-sort (sd_resort.cu): when at most b.rs_max keys of b.keys
-// changed since the previous sort (the count is rs_scratch[1]; b.cell_start
-// must still be the previous sort's table), lists the moved entries in
-// (key, slot) order with their sorted positions, which the reorder turns
-// into the sorted order (ResortView); does nothing else otherwise
+// incremental re-sort (sd_resort.cu): the step's key writers append the
+// slots whose key changed to rs_list (count in rs_scratch[0]); when at most
+// b.rs_max did (the count is published in rs_scratch[1]; b.cell_start must
+// still be the previous sort's table), the plan kernel orders the moved
+// entries by (key, slot) with their sorted positions and the intervals of
+// positions they shift, which the reorder turns into the sorted order
+// (ResortView); otherwise it clears the radix fallback's counters
 constexpr uint32_t kResortMaxCap = 1024;  // largest rs_max (two sorted lists in 16 KB of shared memory)
 uint64_t resort_scratch_words(uint32_t n);
-// vl_flags (may be null): the skin lists' flags, [0] <- [1], [1] <- 0, by the
-// scan's last block
-cudaError_t resort_async(const DemBuffers& b, cudaStream_t st, uint32_t* vl_flags = nullptr);
+// vl_flags (may be null): the skin lists' flags, [0] <- [1], [1] <- 0
+cudaError_t resort_plan_async(const DemBuffers& b, cudaStream_t st, uint32_t* vl_flags = nullptr);
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 void dem_set_pair_lists(int on);

@@ -94,6 +94,44 @@ sort_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan pl
     }
 }
 
+// The radix fallback of the incremental re-sort.  When more keys changed
+// than the re-sort takes (skip[1] > skip_max) it clears the passes' tile
+// status and builds the digit histograms -- the re-sort's plan kernel has
+// cleared the tile counters and histograms -- else it returns at once, so
+// that a step whose moves the re-sort placed pays no histogram.
+__global__ void __launch_bounds__(kSortThreads)
+sort_hist_fallback_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan plan,
+                          uint32_t* __restrict__ scratch, const uint32_t* __restrict__ skip, uint32_t skip_max,
+                          uint64_t status_words) {
+    if (skip[1] <= skip_max) return;
+    const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < status_words; w += gstride)
+        scratch[kStatusOff + w] = 0u;
+    __shared__ uint32_t hist[2048];  // pass p at p * plan.stride
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t k = valid ? keys[i] : 0u;
+        const uint32_t active = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            if (p >= plan.passes) break;
+            const uint32_t d = (k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1u);
+            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
+            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&hist[p * plan.stride + d], __popc(peers & active));
+        }
+    }
+    __syncthreads();
+    for (int p = 0; p < plan.passes; ++p) {
+        const uint32_t nb = 1u << plan.bits[p];
+        for (uint32_t d = threadIdx.x; d < nb; d += blockDim.x)
+            if (hist[p * plan.stride + d]) atomicAdd(&scratch[kHistOff + p * plan.stride + d], hist[p * plan.stride + d]);
+    }
+}
+
 // ------------------------------------------------------------ onesweep pass
 // BINS: 256, 512 or 1024 digit bins (template so narrow passes do less
 // per-digit work).  ITEMS: keys per thread (tile = 256 * ITEMS keys).
@@ -348,6 +386,23 @@ cudaError_t sort_passes_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp
     }
     *in_tmp = (plan.passes & 1) != 0;
     return cudaSuccess;
+}
+
+uint64_t sort_fallback_clear_words() { return kStatusOff - 4; }
+
+cudaError_t sort_fallback_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t n,
+                                const SortPlan& plan, uint32_t* scratch, cudaStream_t st, bool* in_tmp,
+                                const uint32_t* skip, uint32_t skip_max) {
+    *in_tmp = false;
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)((n + kSortThreads * 16 - 1) / (kSortThreads * 16));
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    if (blocks < 1) blocks = 1;
+    const uint64_t status_words = (uint64_t)plan.passes * num_tiles(n) * (uint64_t)plan.stride;
+    sort_hist_fallback_kernel<<<blocks, kSortThreads, 0, st>>>(keys, n, plan, scratch, skip, skip_max, status_words);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return sort_passes_async(keys, vals, keys_tmp, vals_tmp, n, plan, scratch, st, in_tmp, skip, skip_max);
 }
 
 // Sorts (keys, vals) by bits [0, key_bits).  Returns via *in_tmp whether
