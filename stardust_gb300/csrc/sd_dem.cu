@@ -671,7 +671,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     }
     const uint32_t key = cell_key_g(g, nxp, nyp, nzp);
     keys[i] = key;
-    vals[i] = i;
+    if (vals) vals[i] = i;  // the slot identity, for a radix sort (null: the re-sort step)
     return key;
 }
 
@@ -1059,7 +1059,7 @@ __device__ __forceinline__ void body_step(
         omg_n[s] = make_float4(wx, wy, wz, omg[s].w);
         const uint32_t key = cell_key(p, po.x, po.y, po.z);
         keys[s] = key;
-        vals[s] = s;
+        if (vals) vals[s] = s;
         if (ms.list) move_append_one(ms, s, key);
         if (s_hist) {
             const int passes = (int)(hist_spec & 3u);
@@ -1308,8 +1308,10 @@ dem_fix_gather_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ 
     const bool inc = M <= rv.mmax;
     const uint32_t T = inc ? (M ? rv.scratch[3] : 0u) : n;
     const bool iv = inc && T <= n / 4;
-    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
     const uint32_t total = iv ? T : n;
+    // a block with neither positions nor a moved entry (cell shifts) to take
+    if (blockIdx.x * kReorderThreads >= total && !(inc && blockIdx.x < M)) return;
+    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
     for (uint32_t t = blockIdx.x * kReorderThreads + threadIdx.x; t < total; t += gridDim.x * kReorderThreads) {
         const uint32_t k = visit_position(t, iv, M, s_ivlo, s_ivpre);
         if (k >= n) continue;
@@ -1352,10 +1354,11 @@ dem_fix_place_kernel(uint32_t n, uint32_t ncells, const uint32_t* __restrict__ k
     const bool inc = M <= rv.mmax;
     const uint32_t T = inc ? (M ? rv.scratch[3] : 0u) : n;
     const bool iv = inc && T <= n / 4;
-    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
     // the radix order: chunks of kReorderThreads consecutive positions per
     // block iteration, so that each chunk rebuilds its part of the cell table
     const uint32_t total = inc ? (iv ? T : n) : (n + kReorderThreads - 1) / kReorderThreads * kReorderThreads;
+    if (blockIdx.x * kReorderThreads >= total) return;  // no positions for this block
+    if (inc) load_fix_lists(rv, M, iv, s_pos, s_q, s_ivlo, s_ivpre);
     for (uint32_t t0 = blockIdx.x * kReorderThreads; t0 < total; t0 += gridDim.x * kReorderThreads) {
         const uint32_t t = t0 + threadIdx.x;
         const uint32_t k = t < total ? visit_position(t, iv, M, s_ivlo, s_ivpre) : n;
@@ -1697,55 +1700,57 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
     const size_t tile = kTileSlots * sizeof(float4);
     const unsigned grid = grid_for(b.n, 256);
+    // the re-sort step needs no slot identity (its radix fallback writes it)
+    uint32_t* const vals = ms.list ? nullptr : b.vals;
     if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
         if (b.nb)
             dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
         else
             dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         const Batch bt{b.scenes, b.scene_first, b.nscenes};
         if (g_pair_lists != 0 && b.nbr_cnt) {
             dem_pair_lists_kernel<true><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, bt);
             dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
         } else {
             dem_contact_integrate_kernel<RECORD, false, true><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{}, SkinLists{}, ms);
         }
     } else if (skin) {  // single scene of free spheres, skin lists
         const float thr = 0.45f * b.vl_skin;
         const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
         dem_contact_integrate_kernel<RECORD, false, false, false, false, true><<<grid, 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
             b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, sk, ms);
     } else if (g_contact_mode == 0 && !b.nb && g_pair_lists == 1 && b.nbr_cnt) {
         dem_pair_lists_kernel<false><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, Batch{});
         dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid, 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
             b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
     } else if (g_contact_mode == 0) {
         if (b.nb)
             dem_contact_integrate_kernel<RECORD, true><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
         else
             dem_contact_integrate_kernel<RECORD, false><<<grid, 256, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
     } else {
         if (b.nb)
             dem_contact_column_kernel<RECORD, true><<<cols, kColThreads, tile, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, ms);
         else
             dem_contact_column_kernel<RECORD, false><<<cols, kColThreads, tile, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, f, t,
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, ms);
     }
 }
@@ -1769,7 +1774,7 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
     if (b.nb) {
         dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
             p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
-            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, b.vals, b.n, spec, ghist, ms);
+            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, ms.list ? nullptr : b.vals, b.n, spec, ghist, ms);
     }
     return cudaGetLastError();
 }

@@ -41,7 +41,7 @@ cudaError_t sort_histogram_async(const uint32_t* keys, uint32_t n, const SortPla
 // skip (may be null): the passes return at once when skip[1] <= skip_max
 // (the incremental re-sort has written the result)
 // The radix fallback of the incremental re-sort: when skip[1] > skip_max,
-// clears the tile status, builds the histograms (tile counters and
+// clears the tile status, sets vals[i] = i, builds the histograms (tile counters and
 // histograms -- the first sort_fallback_clear_words() words after word 4 of
 // the scratch -- must be zero) and runs the passes; otherwise its kernels
 // return at once.

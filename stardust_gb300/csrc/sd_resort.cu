@@ -41,6 +41,9 @@ namespace {
 
 // one block of 1024 threads: one thread per moved entry of a full list
 constexpr int kRsThreads = 1024;
+// lists up to this long are sorted by counting ranks (M^2 / 1024 shared
+// reads per thread), longer ones by a bitonic sort
+constexpr uint32_t kRankSortMax = 256;
 static_assert(kResortMaxCap <= (uint32_t)kRsThreads, "one thread per moved entry");
 
 // Sorts v[0, P) ascending in shared memory (P a power of two; every thread
@@ -97,14 +100,37 @@ resort_plan_kernel(unsigned long long* __restrict__ list, uint32_t* __restrict__
         if (threadIdx.x == 0) scratch[3] = 0u;
         return;
     }
-    uint32_t P = 2;
-    while (P < M) P <<= 1;
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_a[i] = i < M ? list[i] : ~0ull;
-    __syncthreads();
-    bitonic_sort(s_a, P);
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_b[i] = i < M ? (s_a[i] & 0xffffffffull) : ~0ull;
-    __syncthreads();
-    bitonic_sort(s_b, P);
+    if (M <= kRankSortMax) {
+        // few entries: each thread places its own by counting the smaller
+        // ones (entries and slots are distinct), two barriers in all
+        const uint32_t r = threadIdx.x;
+        unsigned long long c = 0;
+        if (r < M) s_b[r] = list[r];
+        __syncthreads();
+        if (r < M) {
+            c = s_b[r];
+            uint32_t ra = 0, rs = 0;
+            for (uint32_t j = 0; j < M; ++j) {
+                const unsigned long long o = s_b[j];
+                ra += o < c;
+                rs += (o & 0xffffffffull) < (c & 0xffffffffull);
+            }
+            s_a[ra] = c;
+            c = (c & 0xffffffffull) | ((unsigned long long)rs << 32);  // slot, its rank among the slots
+        }
+        __syncthreads();
+        if (r < M) s_b[(uint32_t)(c >> 32)] = c & 0xffffffffull;
+        __syncthreads();
+    } else {
+        uint32_t P = 2;
+        while (P < M) P <<= 1;
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_a[i] = i < M ? list[i] : ~0ull;
+        __syncthreads();
+        bitonic_sort(s_a, P);
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_b[i] = i < M ? (s_a[i] & 0xffffffffull) : ~0ull;
+        __syncthreads();
+        bitonic_sort(s_b, P);
+    }
     // one moved entry per thread (M <= kResortMaxCap = blockDim.x)
     const uint32_t r = threadIdx.x;
     uint32_t len = 0, lo = 0;

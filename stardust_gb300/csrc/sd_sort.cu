@@ -96,13 +96,14 @@ sort_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan pl
 
 // The radix fallback of the incremental re-sort.  When more keys changed
 // than the re-sort takes (skip[1] > skip_max) it clears the passes' tile
-// status and builds the digit histograms -- the re-sort's plan kernel has
-// cleared the tile counters and histograms -- else it returns at once, so
-// that a step whose moves the re-sort placed pays no histogram.
+// status, writes the slot identity into vals and builds the digit
+// histograms -- the re-sort's plan kernel has cleared the tile counters and
+// histograms -- else it returns at once, so that a step whose moves the
+// re-sort placed pays for neither.
 __global__ void __launch_bounds__(kSortThreads)
-sort_hist_fallback_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan plan,
-                          uint32_t* __restrict__ scratch, const uint32_t* __restrict__ skip, uint32_t skip_max,
-                          uint64_t status_words) {
+sort_hist_fallback_kernel(const uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
+                          SortPlan plan, uint32_t* __restrict__ scratch, const uint32_t* __restrict__ skip,
+                          uint32_t skip_max, uint64_t status_words) {
     if (skip[1] <= skip_max) return;
     const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < status_words; w += gstride)
@@ -115,6 +116,7 @@ sort_hist_fallback_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPla
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < n;
         const uint32_t k = valid ? keys[i] : 0u;
+        if (valid) vals[i] = i;  // the slot identity the passes carry
         const uint32_t active = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
@@ -399,7 +401,8 @@ cudaError_t sort_fallback_async(uint32_t* keys, uint32_t* vals, uint32_t* keys_t
     if (blocks > 152 * 4) blocks = 152 * 4;
     if (blocks < 1) blocks = 1;
     const uint64_t status_words = (uint64_t)plan.passes * num_tiles(n) * (uint64_t)plan.stride;
-    sort_hist_fallback_kernel<<<blocks, kSortThreads, 0, st>>>(keys, n, plan, scratch, skip, skip_max, status_words);
+    sort_hist_fallback_kernel<<<blocks, kSortThreads, 0, st>>>(keys, vals, n, plan, scratch, skip, skip_max,
+                                                               status_words);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return sort_passes_async(keys, vals, keys_tmp, vals_tmp, n, plan, scratch, st, in_tmp, skip, skip_max);
