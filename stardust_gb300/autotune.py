@@ -13,7 +13,7 @@ import itertools
 
 from . import _abi
 
-KNOBS = {"contact_mode": (0, 1), "sort_items": (8, 16), "skin_um": (0, 20, 50, 100, 200)}
+KNOBS = {"contact_mode": (0, 1), "sort_items": (8, 16), "skin_um": (0, 20, 50, 100, 200), "listed_blocks": (4, 5)}
 # a batch of scenes takes no contact lists; its pair lists are a choice
 BATCH_KNOBS = {"sort_items": (8, 16), "pair_lists": (0, 2)}
 
@@ -29,6 +29,14 @@ def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, flush_
     names = list(knobs)
     table = []
     for combo in itertools.product(*(knobs[k] for k in names)):
+        c = dict(zip(names, combo))
+        # combinations that run the same kernels as one already timed: the
+        # column kernel takes no contact lists, and the list kernel's
+        # register cap matters only with lists
+        if c.get("contact_mode", 0) == 1 and (c.get("skin_um", 0) != 0 or c.get("listed_blocks", 4) != 4):
+            continue
+        if c.get("skin_um", 1) == 0 and c.get("listed_blocks", 4) != 4:
+            continue
         for k, v in zip(names, combo):
             _abi.tune_set(k, v)
         eng.step(dt, 2)  # re-capture + warm

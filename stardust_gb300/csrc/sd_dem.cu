@@ -412,12 +412,22 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     float3 f = make_float3(0.f, 0.f, 0.f), t = make_float3(0.f, 0.f, 0.f);
     int32_t cx = 0, cy = 0, x0 = 0, x1 = -1, y0 = 0, y1 = -1, z0 = 0, z1 = -1;
     bool scan = true;  // false once the contacts came from a list
+    // the list state of slot i, loaded with the sphere's own state so that
+    // the loads overlap (the build flag is one word every thread reads)
+    uint32_t sk_cnt = 0;
+    float4 sk_ref = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool sk_build = false;
+    if constexpr (SKIN) {
+        sk_build = sk->flags[0] != 0u;
+        sk_cnt = sk->cnt[i];
+        sk_ref = sk->ref[i];
+    }
     if constexpr (SKIN) {
         // A pair in contact now was within r_i + r_j + skin at the build:
         // every sphere has moved less than 0.45 skin since (checked at the
         // end of every step), so the distance changed by less than 0.9
         // skin.  Contacts are applied in ascending slot order, the scan's.
-        if (sk->flags[0] != 0u) {  // build: the scan over the window widened by the skin
+        if (sk_build) {  // build: the scan over the window widened by the skin
             const float reach_b = (ri + p.rmax + sk->skin) * 1.00001f;
             int32_t bx0, bx1, by0, by1, bz0, bz1;
             axis_window(pi.x, reach_b, g.lo[0], 1.0f / g.cell, g.nx, bx0, bx1);
@@ -453,13 +463,13 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             sk->cnt[i] = min(c, kVlCap + 1);
             sk->ref[i] = pi;
             scan = false;
-        } else if (sk->cnt[i] <= kVlCap) {
+        } else if (sk_cnt <= kVlCap) {
             // the listed neighbours in contact, applied by ascending slot (the
             // scan's order).  A first pass finds them and whether list order
             // already ascends -- the usual case: the list was written in scan
             // order and few slots cross between builds; otherwise each is
             // picked as the smallest slot above the last one applied.
-            const uint32_t c = sk->cnt[i];
+            const uint32_t c = sk_cnt;
             uint32_t m = 0, last = 0;
             bool asc = true;
             for (uint32_t k = 0; k < c; ++k) {
@@ -666,7 +676,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
     vel_n[i] = make_float4(nvx, nvy, nvz, mi);
     omg_n[i] = make_float4(wi.x + dt * bx, wi.y + dt * by, wi.z + dt * bz, wi.w);
     if constexpr (SKIN) {  // left 0.45 skin of the build position: build next step
-        const float4 r = sk->ref[i];
+        const float4 r = sk_build ? pi : sk_ref;  // a build step recorded pi
         if (dist2(nxp - r.x, nyp - r.y, nzp - r.z) > sk->thr2) atomicOr(sk->next, 1u);
     }
     const uint32_t key = cell_key_g(g, nxp, nyp, nzp);
@@ -719,10 +729,11 @@ __device__ __forceinline__ void hist_flush(const uint32_t* s_hist, uint32_t spec
     }
 }
 
-// Appends the moved slots among a warp's (all 32 lanes call it): one atomic
-// per warp that holds any.
-__device__ __forceinline__ void move_append_warp(const MoveSink& ms, uint32_t slot, uint32_t key, bool valid) {
-    const bool mv = valid && key != ms.keys_prev[slot];
+// Appends the moved slots among a warp's (all 32 lanes call it; kprev =
+// keys_prev[slot] where valid): one atomic per warp that holds any.
+__device__ __forceinline__ void move_append_warp(const MoveSink& ms, uint32_t slot, uint32_t key, bool valid,
+                                                 uint32_t kprev) {
+    const bool mv = valid && key != kprev;
     const uint32_t m = __ballot_sync(0xffffffffu, mv);
     if (!m) return;
     const uint32_t leader = (uint32_t)__ffs(m) - 1u;
@@ -811,6 +822,8 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
+    // the key this slot sits under, loaded up front with the slot's state
+    const uint32_t kprev = ms.list && i < n ? __ldg(ms.keys_prev + i) : 0u;
     if (i < n)
         key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, LISTED, SKIN>(
             p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
@@ -822,7 +835,34 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
     }
-    if (ms.list) move_append_warp(ms, i, key, has_key);
+    if (ms.list) move_append_warp(ms, i, key, has_key, kprev);
+    if (RECORD) count_contacts(status, contacts);
+}
+
+// The single-scene free-sphere step over contact lists (knob skin_um): one
+// thread per slot, the listed neighbours between builds, the widened scan
+// at a build.  Its own kernel so that the registers are capped for the
+// listed steps' occupancy (they are bound by load latency): MINB resident
+// blocks of 256 per SM (4: 64 registers; 5: 48, with spills in the build
+// scan; knob "listed_blocks").  It never builds radix histograms (the lists
+// run only with the incremental re-sort).
+template <bool RECORD, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+dem_contact_listed_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                          const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
+                          float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
+                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, float4* __restrict__ force,
+                          float4* __restrict__ torque, uint32_t* __restrict__ status, SkinLists sk, MoveSink ms) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t contacts = 0, key = 0;
+    bool has_key = false;
+    const uint32_t kprev = ms.list && i < n ? __ldg(ms.keys_prev + i) : 0u;
+    const ClumpCtx cc{nullptr, nullptr, nullptr};
+    if (i < n)
+        key = particle_step<RECORD, false, GlobalSource, false, false, false, true>(
+            p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
+            contacts, cc, &has_key, Batch{}, nullptr, nullptr, &sk);
+    if (ms.list) move_append_warp(ms, i, key, has_key, kprev);
     if (RECORD) count_contacts(status, contacts);
 }
 
@@ -955,7 +995,7 @@ dem_contact_column_kernel(DemParams p, uint32_t n, const float4* __restrict__ po
                                               vals, force, torque, contacts, cc, &has_key);
         }
         if (ghist) hist_add(s_hist, hist_spec, key, has_key);
-        if (ms.list) move_append_warp(ms, own_beg + k, key, has_key);
+        if (ms.list) move_append_warp(ms, own_beg + k, key, has_key, has_key ? ms.keys_prev[own_beg + k] : 0u);
     }
     if (ghist) {
         __syncthreads();
@@ -1686,6 +1726,10 @@ static int g_contact_mode = 0;  // 0: per slot (default), 1: TMA column tiles
 static int g_pair_lists = 2;
 
 void dem_set_pair_lists(int mode) { g_pair_lists = mode; }
+
+static int g_listed_blocks = 4;  // resident blocks per SM the listed kernel is compiled for: 4 or 5
+void dem_set_listed_blocks(int b) { g_listed_blocks = b == 5 ? 5 : 4; }
+int dem_listed_blocks() { return g_listed_blocks; }
 int dem_pair_lists() { return g_pair_lists; }
 
 void dem_set_contact_mode(int mode) { g_contact_mode = mode == 0 ? 0 : 1; }
@@ -1726,9 +1770,14 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     } else if (skin) {  // single scene of free spheres, skin lists
         const float thr = 0.45f * b.vl_skin;
         const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
-        dem_contact_integrate_kernel<RECORD, false, false, false, false, true><<<grid, 256, 0, st>>>(
-            p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
-            b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, sk, ms);
+        if (g_listed_blocks == 5)
+            dem_contact_listed_kernel<RECORD, 5><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.vel, b.omg, b.cell_start,
+                                                                        b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                                                                        b.dev_status, sk, ms);
+        else
+            dem_contact_listed_kernel<RECORD, 4><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.vel, b.omg, b.cell_start,
+                                                                        b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                                                                        b.dev_status, sk, ms);
     } else if (g_contact_mode == 0 && !b.nb && g_pair_lists == 1 && b.nbr_cnt) {
         dem_pair_lists_kernel<false><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, Batch{});
         dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid, 256, 0, st>>>(

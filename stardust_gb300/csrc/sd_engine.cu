@@ -1337,6 +1337,9 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
+    } else if (k == "listed_blocks") {
+        if (value != 4 && value != 5) return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4 or 5");
+        sd::dem_set_listed_blocks(value);
     } else if (k == "skin_um") {
         if (value < 0 || value > 100000) return fail(nullptr, SD_ERR_INVALID_ARG, "skin_um must be in [0, 100000]");
         g_skin_um = value;
@@ -1363,6 +1366,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "resort_max") *value = (int32_t)sd::dem_resort_max();
     else if (k == "pair_lists") *value = sd::dem_pair_lists();
     else if (k == "skin_um") *value = g_skin_um;
+    else if (k == "listed_blocks") *value = sd::dem_listed_blocks();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }

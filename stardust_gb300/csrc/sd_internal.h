@@ -290,6 +290,8 @@ cudaError_t resort_plan_async(const DemBuffers& b, cudaStream_t st, uint32_t* vl
 void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 void dem_set_pair_lists(int on);
+void dem_set_listed_blocks(int b);
+int dem_listed_blocks();
 int dem_pair_lists();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture
 // Counts, into *count (device), the slots whose key from the current position
