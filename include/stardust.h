@@ -481,7 +481,7 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   within r_i + r_j + skin; other steps test only the listed neighbours.
  *                   Same contact set and order as the scan, so the same bits
  *   "listed_blocks" resident 256-thread blocks per SM the contact-list kernel is compiled
- *                   for: 4 (64 registers, the default) or 5 (48 registers) */
+ *                   for: 4 (64 registers) or 5 (48 registers, the default) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 
