@@ -374,7 +374,7 @@ def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
     tuned = None
     if tune:
         from stardust_gb300 import autotune
-        tuned = autotune.tune_engine(eng, dt, reps=3, knobs=autotune.BATCH_KNOBS)
+        tuned = autotune.tune_engine(eng, dt, reps=3)
     ms = timed(eng, steps)
     st = eng.stats()
     eng.close()
@@ -507,6 +507,12 @@ def timed_steps(eng, dt: float, k: int, stream, flush) -> list:
         b[i].record(stream)
     torch.cuda.synchronize()
     return [x.elapsed_time(y) for x, y in zip(a, b)]
+
+
+def autotune_table() -> dict:
+    """The launch knobs chosen per size bucket in this run."""
+    from stardust_gb300 import autotune
+    return autotune.table()
 
 
 def with_knobs(knobs: dict, fn):
@@ -753,6 +759,7 @@ def run_ours(args, rank, world, local):
             "ms_per_step_without_contact_lists": no_lists_ms,
             "ms_per_step_full_radix_sort": full_sort_ms,
             "autotune": tuned,
+            "autotune_table": None if args.no_tune else autotune_table(),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes},
             "roofline": {"bound": "hbm", "kernel": "dem_contact_integrate_kernel" + (" (listed)" if lists_on else ""),
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

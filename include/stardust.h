@@ -473,15 +473,19 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   pair once and lists up to 16 contacts per sphere, which the contact
  *                   kernel applies in slot order (a full scan for an overflowed list);
  *                   0 = one scan kernel; 2 (default) = lists for batches of scenes only.
+ *                   Steps with contact lists (knob skin_um) use those instead.
  *                   Same bits either way
- *   "skin_um"       single scenes of free spheres, from the next step: contact lists with a
+ *   "skin_um"       scenes of free spheres (one, or a batch), from the next step: contact lists with a
  *                   skin of this many micrometres (0 = none; default 50).  A step that
  *                   follows a sphere moving 0.45 skin from its position at the last build
  *                   scans the window widened by the skin and lists each sphere's neighbours
  *                   within r_i + r_j + skin; other steps test only the listed neighbours.
  *                   Same contact set and order as the scan, so the same bits
  *   "listed_blocks" resident 256-thread blocks per SM the contact-list kernel is compiled
- *                   for: 4 (64 registers) or 5 (48 registers, the default) */
+ *                   for: 4 (64 registers) or 5 (48 registers, the default)
+ *   "contact_block" threads per block of the per-sphere contact kernels: 64, 128 or 256
+ *                   (default)
+ *   "fix_blocks"    blocks per SM of the in-place reorder's fixed grid: 2, 4 or 8 (default) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

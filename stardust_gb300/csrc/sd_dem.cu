@@ -846,22 +846,23 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
 // blocks of 256 per SM (4: 64 registers; 5: 48, with spills in the build
 // scan; knob "listed_blocks", default 5).  It never builds radix histograms (the lists
 // run only with the incremental re-sort).
-template <bool RECORD, int MINB>
+template <bool RECORD, int MINB, bool BATCHED>
 __global__ void __launch_bounds__(256, MINB)
 dem_contact_listed_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ vel,
                           const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
                           float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
                           uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, float4* __restrict__ force,
-                          float4* __restrict__ torque, uint32_t* __restrict__ status, SkinLists sk, MoveSink ms) {
+                          float4* __restrict__ torque, uint32_t* __restrict__ status, SkinLists sk, MoveSink ms,
+                          Batch bt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     const uint32_t kprev = ms.list && i < n ? __ldg(ms.keys_prev + i) : 0u;
     const ClumpCtx cc{nullptr, nullptr, nullptr};
     if (i < n)
-        key = particle_step<RECORD, false, GlobalSource, false, false, false, true>(
+        key = particle_step<RECORD, false, GlobalSource, BATCHED, false, false, true>(
             p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
-            contacts, cc, &has_key, Batch{}, nullptr, nullptr, &sk);
+            contacts, cc, &has_key, bt, nullptr, nullptr, &sk);
     if (ms.list) move_append_warp(ms, i, key, has_key, kprev);
     if (RECORD) count_contacts(status, contacts);
 }
@@ -1727,6 +1728,16 @@ static int g_pair_lists = 2;
 
 void dem_set_pair_lists(int mode) { g_pair_lists = mode; }
 
+// launch shapes (knobs "contact_block", "fix_blocks"): threads per block of
+// the per-slot contact kernels (64, 128 or 256) and blocks per SM of the
+// in-place reorder's fixed grid (2, 4 or 8)
+static int g_contact_block = 256;
+static int g_fix_blocks = 8;
+void dem_set_contact_block(int t) { g_contact_block = t; }
+int dem_contact_block() { return g_contact_block; }
+void dem_set_fix_blocks(int b) { g_fix_blocks = b; }
+int dem_fix_blocks() { return g_fix_blocks; }
+
 // resident blocks per SM the listed kernel is compiled for: 4 or 5.  Five
 // (48 registers, spills only in the build scan) measured 0.0632 ms per
 // step at 1,048,576 spheres against 0.0668 ms with four (64 registers)
@@ -1746,53 +1757,65 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     const ClumpCtx cc{b.nb ? b.body_of : nullptr, b.sf, b.st};
     const unsigned cols = (unsigned)p.nx * (unsigned)p.ny;
     const size_t tile = kTileSlots * sizeof(float4);
-    const unsigned grid = grid_for(b.n, 256);
+    const unsigned cb = (unsigned)g_contact_block;  // threads per block of the per-slot kernels
+    const unsigned grid = grid_for(b.n, cb);
     // the re-sort step needs no slot identity (its radix fallback writes it)
     uint32_t* const vals = ms.list ? nullptr : b.vals;
     if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
         if (b.nb)
-            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
         else
-            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
+    } else if (skin) {  // free spheres, one scene or a batch, contact lists
+        const float thr = 0.45f * b.vl_skin;
+        const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
+        const Batch bt{b.scenes, b.scene_first, b.nscenes};
+        if (b.nscenes > 1) {
+            if (g_listed_blocks == 5)
+                dem_contact_listed_kernel<RECORD, 5, true><<<grid, cb, 0, st>>>(
+                    p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                    b.dev_status, sk, ms, bt);
+            else
+                dem_contact_listed_kernel<RECORD, 4, true><<<grid, cb, 0, st>>>(
+                    p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                    b.dev_status, sk, ms, bt);
+        } else if (g_listed_blocks == 5) {
+            dem_contact_listed_kernel<RECORD, 5, false><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{});
+        } else {
+            dem_contact_listed_kernel<RECORD, 4, false><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{});
+        }
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         const Batch bt{b.scenes, b.scene_first, b.nscenes};
         if (g_pair_lists != 0 && b.nbr_cnt) {
-            dem_pair_lists_kernel<true><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, bt);
-            dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid, 256, 0, st>>>(
+            dem_pair_lists_kernel<true><<<grid, cb, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, bt);
+            dem_contact_integrate_kernel<RECORD, false, true, false, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
         } else {
-            dem_contact_integrate_kernel<RECORD, false, true><<<grid, 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, bt, MeshView{}, NbrLists{}, SkinLists{}, ms);
         }
-    } else if (skin) {  // single scene of free spheres, skin lists
-        const float thr = 0.45f * b.vl_skin;
-        const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
-        if (g_listed_blocks == 5)
-            dem_contact_listed_kernel<RECORD, 5><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.vel, b.omg, b.cell_start,
-                                                                        b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
-                                                                        b.dev_status, sk, ms);
-        else
-            dem_contact_listed_kernel<RECORD, 4><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.vel, b.omg, b.cell_start,
-                                                                        b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
-                                                                        b.dev_status, sk, ms);
     } else if (g_contact_mode == 0 && !b.nb && g_pair_lists == 1 && b.nbr_cnt) {
-        dem_pair_lists_kernel<false><<<grid, 256, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, Batch{});
-        dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid, 256, 0, st>>>(
+        dem_pair_lists_kernel<false><<<grid, cb, 0, st>>>(p, b.n, b.pos, b.cell_start, b.nbr_cnt, b.nbr, Batch{});
+        dem_contact_integrate_kernel<RECORD, false, false, false, true><<<grid, cb, 0, st>>>(
             p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
             b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{b.nbr_cnt, b.nbr}, SkinLists{}, ms);
     } else if (g_contact_mode == 0) {
         if (b.nb)
-            dem_contact_integrate_kernel<RECORD, true><<<grid, 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
         else
-            dem_contact_integrate_kernel<RECORD, false><<<grid, 256, 0, st>>>(
+            dem_contact_integrate_kernel<RECORD, false><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, spec, ghist, cc, Batch{}, MeshView{}, NbrLists{}, SkinLists{}, ms);
     } else {
@@ -1840,8 +1863,8 @@ cudaError_t dem_contact_integrate_async(const DemParams& p, DemBuffers& b, bool 
 // Fixed grid of the in-place reorder's kernels (grid-stride loops): most
 // steps touch a few thousand positions, the radix fallback all of them.
 static unsigned fix_grid(uint32_t n) {
-    const unsigned g = grid_for(n, kReorderThreads);
-    return g < 152u * 8u ? g : 152u * 8u;
+    const unsigned g = grid_for(n, kReorderThreads), cap = 152u * (unsigned)g_fix_blocks;
+    return g < cap ? g : cap;
 }
 
 // One whole step.  With the incremental re-sort (dem_step_swaps): contact +
@@ -1893,7 +1916,7 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
 }
 
 bool dem_step_skin(const DemBuffers& b) {
-    return b.vl_skin > 0.0f && b.vl_cnt && b.slot_of && !b.nb && !b.mesh.ntri && b.nscenes <= 1 &&
+    return b.vl_skin > 0.0f && b.vl_cnt && b.slot_of && !b.nb && !b.mesh.ntri &&
            g_contact_mode == 0 && dem_step_swaps(b);
 }
 

@@ -504,15 +504,15 @@ static void swap_state(sd::DemBuffers& B) {
     std::swap(B.omg, B.omg_n);
 }
 
-// Contact lists with a skin (knob skin_um) for single scenes of free
-// spheres: allocated when a step graph first uses them, then kept; the skin
+// Contact lists with a skin (knob skin_um) for scenes of free spheres (one
+// or a batch): allocated when a step graph first uses them, then kept; the skin
 // follows the knob at every graph build (0: no lists).  The slot table
 // covers every sphere while the lists are on and is rebuilt here, since
 // steps without lists keep it for clump spheres only.
 static sd_status ensure_contact_lists(sd_engine* h) {
     sd::DemBuffers& B = h->B;
     const uint32_t n = B.n;
-    if (!(g_skin_um > 0 && h->hb_pos.empty() && h->mesh.tri.empty() && h->scenes.size() <= 1 && n)) {
+    if (!(g_skin_um > 0 && h->hb_pos.empty() && h->mesh.tri.empty() && n)) {
         B.vl_skin = 0.0f;
         return SD_OK;
     }
@@ -1337,6 +1337,13 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return fail(nullptr, SD_ERR_INVALID_ARG, "z_div must be 0, 1, 2, 4 or 8");
         g_z_div = value;
+    } else if (k == "contact_block") {
+        if (value != 64 && value != 128 && value != 256)
+            return fail(nullptr, SD_ERR_INVALID_ARG, "contact_block must be 64, 128 or 256");
+        sd::dem_set_contact_block(value);
+    } else if (k == "fix_blocks") {
+        if (value != 2 && value != 4 && value != 8) return fail(nullptr, SD_ERR_INVALID_ARG, "fix_blocks must be 2, 4 or 8");
+        sd::dem_set_fix_blocks(value);
     } else if (k == "listed_blocks") {
         if (value != 4 && value != 5) return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4 or 5");
         sd::dem_set_listed_blocks(value);
@@ -1367,6 +1374,8 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "pair_lists") *value = sd::dem_pair_lists();
     else if (k == "skin_um") *value = g_skin_um;
     else if (k == "listed_blocks") *value = sd::dem_listed_blocks();
+    else if (k == "contact_block") *value = sd::dem_contact_block();
+    else if (k == "fix_blocks") *value = sd::dem_fix_blocks();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }

@@ -291,6 +291,10 @@ void dem_set_resort_max(uint32_t m);
 uint32_t dem_resort_max();
 void dem_set_pair_lists(int on);
 void dem_set_listed_blocks(int b);
+void dem_set_contact_block(int t);
+int dem_contact_block();
+void dem_set_fix_blocks(int b);
+int dem_fix_blocks();
 int dem_listed_blocks();
 int dem_pair_lists();
 cudaError_t dem_init_kernels();  // once per device, outside stream capture

@@ -132,6 +132,7 @@ class DEMEngine:
         self._call("sd_engine_add_scene", len(p), p.ctypes.data, v.ctypes.data, None if w is None else w.ctypes.data,
                    lo3, hi3, cell)
         self._n += len(p)
+        self.n_scenes = getattr(self, "n_scenes", 0) + 1
 
     def add_mesh(self, tris, centre, axis=(0.0, 0.0, 1.0), omega: float = 0.0, patch=None) -> None:
         """A rigid triangle mesh (tris: (n, 3, 3) world vertices at time 0)

@@ -26,16 +26,28 @@ def oracle_scene_params(orc, lo, hi, cell, cfg, dt):
 
 
 @pytest.mark.parametrize("steps", [1, 30])
-def test_batch_matches_scenes_run_alone(sdlib, orc, steps):
-    from stardust_gb300 import scenes
+@pytest.mark.parametrize("skin_um,pair_lists", [(50, 2), (0, 2), (0, 0)])
+def test_batch_matches_scenes_run_alone(sdlib, orc, steps, skin_um, pair_lists):
+    """Three contact stages: contact lists with a skin, the pair kernel's
+    lists, the plain scan."""
+    from stardust_gb300 import _abi, scenes
+    old = (_abi.tune_get("skin_um"), _abi.tune_get("pair_lists"))
     batch, cfg, dt = scenes.batch_boxes(n_scenes=14, seed=4, n_min=5, n_max=3000, median=400)
-    eng = sdlib.DEMEngine(cfg)
-    for pos, vel, lo, hi in batch:
-        eng.add_scene(pos, vel, lo, hi)
-    eng.prepare()
-    eng.step(dt, steps)
-    eng.sync()
-    assert eng.stats()["device_errors"] == 0
+    try:
+        _abi.tune_set("skin_um", skin_um)
+        _abi.tune_set("pair_lists", pair_lists)
+        eng = sdlib.DEMEngine(cfg)
+        for pos, vel, lo, hi in batch:
+            eng.add_scene(pos, vel, lo, hi)
+        eng.prepare()
+        eng.step(dt, steps)
+        eng.sync()
+    finally:
+        _abi.tune_set("skin_um", old[0])
+        _abi.tune_set("pair_lists", old[1])
+    st = eng.stats()
+    assert st["device_errors"] == 0
+    assert st["list_builds"] + st["listed_steps"] == (steps if skin_um else 0)
     P, V = eng.positions(), eng.velocities()
     first = 0
     for pos, vel, lo, hi in batch:
