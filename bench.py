@@ -551,7 +551,8 @@ def bench_dense_bed(pos, vel, cfg, dt, steps: int, advance: int, local: int, tun
     old = _abi.tune_get("skin_um")
     tuned = None
     if tune:
-        tuned = autotune.tune_engine(eng, dt, reps=3, knobs={"skin_um": (0, 50, 200, 500)})
+        tuned = autotune.tune_engine(eng, dt, reps=3, knobs={"skin_um": (0, 50, 200, 500)},
+                                     label=autotune.bucket_of(eng) + ":dense")
     skin = _abi.tune_get("skin_um")
     eng.step(dt, 3)
     ms = statistics.mean(timed_steps(eng, dt, steps, stream, flush))

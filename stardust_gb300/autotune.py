@@ -72,13 +72,14 @@ def _time(eng, dt: float, reps: int, stream, flush) -> float:
 
 
 def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, rounds: int = 2,
-                flush_bytes: int = 256 << 20) -> dict:
+                flush_bytes: int = 256 << 20, label: str | None = None) -> dict:
     """Coordinate descent over `knobs` (default: the bucket kind's set) on
-    the live engine; sets the best and records it for the engine's bucket.
-    Returns {"bucket", "choice", "ms", "table"}: every timed setting."""
+    the live engine; sets the best and records it for the engine's bucket
+    (or under `label`, for a regime of one bucket tuned apart, e.g. a dense
+    bed).  Returns {"bucket", "choice", "ms", "table"}: every timed setting."""
     import torch
 
-    bucket = bucket_of(eng)
+    bucket = label or bucket_of(eng)
     if knobs is None:
         knobs = BATCH_KNOBS if bucket.startswith("batch") else SCENE_KNOBS
     dev = torch.device("cuda", torch.cuda.current_device())
