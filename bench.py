@@ -257,13 +257,19 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+ONLINE_EVERY, ONLINE_ITERS, ONLINE_LR = 5, 10, 2e-3
+
+
 def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
     """GJK support evaluations per candidate pair, plain vs learned seed, on
     the convex-hull step (65,536 hulls of 8-32 points, 0.02 m across, random
-    orientations, packed at 1.95 radii in a walled 1 m box): plain GJK logs
-    its separating directions for a few steps, the warm-start network is
-    trained on them on the GPU, then a plain and a learned engine step the
-    same scene, timed with CUDA events."""
+    orientations, packed at 1.95 radii in a walled 1 m box).  Four engines
+    step the same scene: plain GJK; the previous step's direction as seed
+    (the untrained residual network); the network trained offline on the
+    separating directions plain GJK logged in 10 steps; the network trained
+    online from scratch during the run (every ONLINE_EVERY steps, ONLINE_ITERS
+    Adam steps on that step's max-margin targets, timed steps included).
+    After `warmup` steps each, `steps` steps are timed with CUDA events."""
     import torch
     import stardust_gb300 as sd
     from stardust_gb300 import _abi, scenes
@@ -301,10 +307,16 @@ def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
     params = plain.mlp_params()
     plain.close()
     out = {"workload": f"{n_hulls} convex hulls (8-32 points, 0.02 m across), packed in a walled 1 m box, dt 1e-5 s",
-           "train_samples": int(Xt.shape[0]), "train_iters": 400, "train_s": train_s}
+           "train_samples": int(Xt.shape[0]), "train_iters": 400, "train_s": train_s,
+           "online": {"every": ONLINE_EVERY, "iters": ONLINE_ITERS, "lr": ONLINE_LR, "warmup_steps": warmup}}
     engines = {k: engine(m, params) for k, m in (("plain", _abi.SD_GJK_SEED_PLAIN),
                                                    ("learned", _abi.SD_GJK_SEED_LEARNED),
                                                    ("previous", _abi.SD_GJK_SEED_PREVIOUS))}
+    # the network trained online from scratch (untrained = the previous
+    # direction), on max-margin targets of the run's own pairs; it keeps
+    # training through the timed steps
+    engines["online"] = engine(_abi.SD_GJK_SEED_LEARNED)
+    engines["online"].set_gjk_training(ONLINE_EVERY, ONLINE_ITERS, ONLINE_LR)
     for k, e in engines.items():
         e.step(dt, warmup)
         e.sync()
@@ -331,7 +343,11 @@ def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
     out["identical_contacts"] = bool(np.array_equal(hp["status"] == 1, hl["status"] == 1))
     out["identical_state"] = bool(np.array_equal(engines["plain"].bodies(_abi.SD_BODY_POSITION).view(np.uint32),
                                                  engines["learned"].bodies(_abi.SD_BODY_POSITION).view(np.uint32)))
+    ho = engines["online"].hull_entries()
+    out["identical_contacts_online"] = bool(np.array_equal(hp["status"] == 1, ho["status"] == 1))
     out["ratio_plain_over_learned"] = out["iters_per_pair_plain"] / out["iters_per_pair_learned"]
+    out["ratio_plain_over_online"] = out["iters_per_pair_plain"] / out["iters_per_pair_online"]
+    out["ratio_previous_over_online"] = out["iters_per_pair_previous"] / out["iters_per_pair_online"]
     out["hull_steps_per_s_learned"] = n_hulls / (out["ms_per_step_learned"] * 1e-3)
     for e in engines.values():
         e.close()
@@ -709,7 +725,7 @@ def run_ours(args, rank, world, local):
     # ---- learned GJK warm start on the convex-hull step (rank 0, N = 1)
     gjk = None
     if rank == 0 and world == 1 and not args.no_hulls:
-        gjk = bench_hulls(args.hulls, 20, 5, local)
+        gjk = bench_hulls(args.hulls, 20, 100, local)
         log(f"gjk: {gjk}")
 
     # ---- batched scenes (rank 0, N = 1)

@@ -344,13 +344,23 @@ sd_status sd_engine_get_hull_shapes(sd_engine* h, uint32_t* vstart, uint32_t* vc
  * (testGJK.cu:266).  PREVIOUS: the pair's final search direction of the
  * previous step (in A's body frame) when it was separated then.  LEARNED:
  * the warm-start network's direction for pairs seen in the previous step.
- * GJK always runs to its own termination test, and a seeded run that does
- * not converge is rerun from the plain seed, so the seed changes only the
- * iteration count. */
+ * A seeded run has two support evaluations to certify separation; any other
+ * outcome is decided by GJK rerun from the plain seed to its own
+ * termination test, so the seed changes only the iteration count. */
 #define SD_GJK_SEED_PLAIN 0
 #define SD_GJK_SEED_LEARNED 1
 #define SD_GJK_SEED_PREVIOUS 2
 sd_status sd_engine_set_gjk_seed(sd_engine* h, int32_t mode);
+
+/* Online training of the warm-start network while the scene steps (seed mode
+ * LEARNED): every `every` steps (0 = off) the step also logs, per separated
+ * pair that the network seeds, the separating direction of largest margin
+ * (the closest-point direction, GJK run to convergence) in A's frame, and
+ * then `iters` Adam steps of rate `lr` on that step's inputs and targets run
+ * on the GPU before the next step.  Trains on the simulation's own pairs;
+ * contact results are unchanged (seeds only move the iteration count).  No
+ * counterpart in the reference. */
+sd_status sd_engine_set_gjk_training(sd_engine* h, int32_t every, int32_t iters, float lr);
 
 /* The candidate entries of the last step: off[n_bodies+1] (CSR), partner
  * ids (ascending per body), info (status | GJK iterations << 8 | EPA

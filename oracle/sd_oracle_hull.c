@@ -223,6 +223,9 @@ static inline csop cso(const hpair* P, v3 d) {
 
 enum { GJK_SEP = 0, GJK_HIT = 1, GJK_TOUCH = 2, GJK_NOCONV = 3 };
 #define GJK_MAX_IT 64
+/* support evaluations a seeded run gets to certify separation before the
+ * plain run takes over */
+#define GJK_SEED_MAX_IT 2
 #define EPA_MAXV 48
 #define EPA_MAXF 96
 #define EPA_MAX_IT 48
@@ -352,7 +355,7 @@ static int closest_simplex(simplex_t* S, v3* v) {
  * -v, and the reference's test dot(w, d) < 0 ends it as separated.  Returns
  * the status, the number of support evaluations in *iters and, for a
  * separated pair, the separating search direction in *dir. */
-static int gjk(const hpair* P, v3 d0, simplex_t* S, int* iters, v3* dir) {
+static int gjk(const hpair* P, v3 d0, simplex_t* S, int* iters, v3* dir, int max_it) {
     v3 d = d0;
     if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
     csop p = cso(P, d);
@@ -373,7 +376,7 @@ static int gjk(const hpair* P, v3 d0, simplex_t* S, int* iters, v3* dir) {
             *iters = it;
             return GJK_TOUCH;
         }
-        if (it >= GJK_MAX_IT) {
+        if (it >= max_it) {
             *iters = it;
             return GJK_NOCONV;
         }
@@ -567,7 +570,7 @@ void sdo_gjk_epa(const float* pos4, const float* quat4, const float* iinv4, cons
     simplex_t S;
     int iters = 0;
     v3 dir;
-    const int st = gjk(&P, d0, &S, &iters, &dir);
+    const int st = gjk(&P, d0, &S, &iters, &dir, GJK_MAX_IT);
     contact_t c;
     memset(&c, 0, sizeof c);
     if (st == GJK_HIT) epa(&P, &S, epa_tol(iinv4, A, B), &c);
@@ -623,10 +626,12 @@ static int hull_entry(const sdo_hull_params* p, const float* pos4, const float* 
     if (seeded) d0 = rot(P.A.R, ld3(seed4));
     simplex_t S;
     v3 dir;
-    int st = gjk(&P, d0, &S, iters, &dir);
-    if (seeded && st != GJK_SEP) { /* only a separation certificate is taken from a seeded run */
+    /* a seeded run has GJK_SEED_MAX_IT supports to certify separation; only
+     * that certificate is taken from it, any other outcome is the plain run's */
+    int st = gjk(&P, d0, &S, iters, &dir, seeded ? GJK_SEED_MAX_IT : GJK_MAX_IT);
+    if (seeded && st != GJK_SEP) {
         int it2 = 0;
-        st = gjk(&P, vneg(P.off), &S, &it2, &dir);
+        st = gjk(&P, vneg(P.off), &S, &it2, &dir, GJK_MAX_IT);
         *iters += it2;
     }
     *f = mk(0.0f, 0.0f, 0.0f);

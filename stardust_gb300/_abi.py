@@ -151,6 +151,7 @@ SIGNATURES = {
     "sd_engine_add_hull": [P, U32, P, F32, P, P, P, P],
     "sd_engine_get_hull_shapes": [P, P, P, P, U64, C.POINTER(U64)],
     "sd_engine_set_gjk_seed": [P, I32],
+    "sd_engine_set_gjk_training": [P, I32, I32, F32],
     "sd_engine_hull_entries": [P, P, P, P, P, P, P, U64, C.POINTER(U64)],
     "sd_engine_mlp_params": [P, P, U64, I32],
     "sd_engine_mlp_forward": [P, P, P, U64],

@@ -26,6 +26,12 @@ struct HullScene {
     unsigned long long* stats = nullptr;          // 4 counters of the last step
     sd::MlpState mlp{};                           // warm-start network (device)
     uint32_t mlp_step = 0;                        // Adam steps taken
+    // online training of the network (sd_engine_set_gjk_training): every
+    // train_every steps the step logs max-margin targets, then train_iters
+    // Adam steps of rate train_lr run on them
+    int32_t train_every = 0, train_iters = 0;
+    float train_lr = 0.0f;
+    uint32_t* teach_flag = nullptr;               // [0] on (read by the step), [1] = 0, [2] = 1
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int parity = 0;
     int seed_mode = 0;                            // SD_GJK_SEED_*

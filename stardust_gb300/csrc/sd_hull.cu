@@ -25,6 +25,9 @@ namespace {
 
 constexpr int kHullThreads = 128;
 constexpr int kGjkMaxIt = 64;
+// support evaluations a seeded GJK run gets to certify separation before the
+// plain run takes over
+constexpr int kSeedMaxIt = 2;
 constexpr int kEpaMaxV = 48;
 constexpr int kEpaMaxF = 96;
 constexpr int kEpaMaxIt = 48;
@@ -240,7 +243,7 @@ __device__ int closest_simplex(Simplex* S, v3* v) {
  * -v, and the reference's test dot(w, d) < 0 ends it as separated.  Returns
  * the status, the number of support evaluations in *iters and, for a
  * separated pair, the separating search direction in *dir. */
-__device__ int gjk(const HPair& P, v3 d0, Simplex* S, int* iters, v3* dir) {
+__device__ int gjk(const HPair& P, v3 d0, Simplex* S, int* iters, v3* dir, int max_it = kGjkMaxIt) {
     v3 d = d0;
     if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
     Cso p = cso(P, d);
@@ -261,7 +264,7 @@ __device__ int gjk(const HPair& P, v3 d0, Simplex* S, int* iters, v3* dir) {
             *iters = it;
             return kTouch;
         }
-        if (it >= kGjkMaxIt) {
+        if (it >= max_it) {
             *iters = it;
             return kNoConv;
         }
@@ -291,6 +294,36 @@ __device__ int gjk(const HPair& P, v3 d0, Simplex* S, int* iters, v3* dir) {
         }
         vv = vdot(v, v);
     }
+}
+
+/* The separating direction of largest margin, for training the warm-start
+ * network: distance-form GJK run to convergence (|v|^2 - v.w <= 1e-5 |v|^2,
+ * at most kGjkMaxIt supports) from d0; returns false when the pair is not
+ * cleanly separated.  *out = -v / |v|, the direction of the closest points. */
+__device__ bool gjk_margin_dir(const HPair& P, v3 d0, v3* out) {
+    Simplex S;
+    v3 d = vzero(d0) ? mk(1.0f, 0.0f, 0.0f) : d0;
+    Cso p = cso(P, d);
+    S.s[0] = p;
+    S.n = 1;
+    v3 v = p.w;
+    for (int it = 1; it < kGjkMaxIt; ++it) {
+        const float vv = vdot(v, v);
+        if (!(vv > 0.0f)) return false;
+        d = vneg(v);
+        p = cso(P, d);
+        if (vv - vdot(v, p.w) <= 1e-5f * vv) break;  // converged: v is (nearly) the closest point
+        if (S.n >= 4) return false;  // (closest_simplex keeps at most 3 points unless it reports a hit)
+        for (int k = S.n; k > 0; --k) S.s[k] = S.s[k - 1];
+        S.s[0] = p;
+        S.n += 1;
+        if (closest_simplex(&S, &v)) return false;
+    }
+    const float vv = vdot(v, v);
+    if (!(vv > 0.0f)) return false;
+    const float inv = 1.0f / sqrtf(vv);
+    *out = mk(-v.x * inv, -v.y * inv, -v.z * inv);
+    return true;
 }
 
 struct Face {
@@ -584,8 +617,11 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     Simplex S;
     int iters = 0;
     v3 dir;
-    int st = gjk(P, d0, &S, &iters, &dir);
-    if (seeded && st != kSep) {  // only a separation certificate is taken from a seeded run
+    // a seeded run gets kSeedMaxIt support evaluations to certify separation;
+    // only that certificate is taken from it -- any other outcome is the
+    // plain run's, so contact sets, forces and states do not depend on seeds
+    int st = gjk(P, d0, &S, &iters, &dir, seeded ? kSeedMaxIt : kGjkMaxIt);
+    if (seeded && st != kSep) {
         int it2 = 0;
         st = gjk(P, vneg(P.off), &S, &it2, &dir);
         iters += it2;
@@ -621,6 +657,15 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     H.et[e] = make_float4(ta.x, ta.y, ta.z, 0.f);
     H.info[e] = info;
     H.dir[e] = d4;
+    if (H.teach && *H.teach_on) {
+        // a training step: the max-margin direction of a separated pair the
+        // network seeds (one seen in the previous step)
+        v3 m;
+        const bool ok = st == kSep && H.feat && H.feat[16 * (size_t)e + 7] == 1.0f && gjk_margin_dir(P, dir, &m);
+        const v3 mA = rotT(P.A.R, m);
+        H.teach[e] = ok ? make_float4(mA.x, mA.y, mA.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (em < H.off[B + 1]) H.teach[em] = make_float4(0.f, 0.f, 0.f, 0.f);  // one sample per pair
+    }
     if (em < H.off[B + 1]) {  // always true for consistent lists
         H.ef[em] = make_float4(fbv.x, fbv.y, fbv.z, 0.f);
         H.et[em] = make_float4(tb.x, tb.y, tb.z, 0.f);

@@ -203,8 +203,10 @@ sd_status hull_prepare(sd_engine* h) {
         (s = halloc(h, &H.self, cap)) || (s = halloc(h, &H.ef, cap)) || (s = halloc(h, &H.et, cap)) ||
         (s = halloc(h, &H.info, cap)) || (s = halloc(h, &H.seeds, cap)) || (s = halloc(h, &H.feat, 16 * cap)) ||
         (s = halloc(h, &S.stats, 4)) || (s = halloc(h, &H.ucount, nb)) || (s = halloc(h, &H.upos, (size_t)nb + 1)) ||
-        (s = halloc(h, &H.ulist, cap / 2 + 1)) || (s = halloc(h, &H.uscan, sd::scan_scratch_words(nb) + 1)))
+        (s = halloc(h, &H.ulist, cap / 2 + 1)) || (s = halloc(h, &H.uscan, sd::scan_scratch_words(nb) + 1)) ||
+        (s = halloc(h, &H.teach, cap)) || (s = halloc(h, &S.teach_flag, 4)))
         return s;
+    H.teach_on = S.teach_flag;
     for (int k = 0; k < 2; ++k)
         if ((s = halloc(h, &S.off[k], (size_t)nb + 1)) || (s = halloc(h, &S.partners[k], cap)) ||
             (s = halloc(h, &S.dir[k], cap)))
@@ -232,6 +234,10 @@ sd_status hull_prepare(sd_engine* h) {
     HULL_CUDA(h, cudaMemsetAsync(S.tree.status, 0, 16, st));
     HULL_CUDA(h, cudaMemsetAsync(S.stats, 0, 32, st));
     HULL_CUDA(h, cudaMemsetAsync(S.mlp.status, 0, 16, st));
+    {
+        const uint32_t flags[4] = {0u, 0u, 1u, 0u};  // training off; the constants 0 and 1 to copy from
+        HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, flags, sizeof flags, cudaMemcpyHostToDevice, st));
+    }
     {
         // network initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) for
         // the hidden layers from a fixed SplitMix64 stream; the last layer
@@ -268,8 +274,25 @@ sd_status hull_step(sd_engine* h, float dt, int32_t n_steps) {
         sd_status s = build_hull_graphs(h, dt);
         if (s) return s;
     }
+    const bool online = S.train_every > 0 && S.seed_mode == SD_GJK_SEED_LEARNED;
     for (int32_t k = 0; k < n_steps; ++k) {
+        const uint64_t step = h->steps + (uint64_t)k;
+        const bool train = online && step % (uint64_t)S.train_every == 0;
+        if (train)  // this step logs the max-margin targets of its separated pairs
+            HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, S.teach_flag + 2, 4, cudaMemcpyDeviceToDevice, h->stream));
         HULL_CUDA(h, cudaGraphLaunch(S.graph[S.parity], h->stream));
+        if (train) {
+            HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, S.teach_flag + 1, 4, cudaMemcpyDeviceToDevice, h->stream));
+            // Adam on the step's entries (features, targets), on the GPU
+            // between steps; the entry count stays on the device.  Adam is
+            // invariant to the loss scale, so the mean's divisor is nominal
+            const uint32_t* count = S.off[S.parity] + S.H.nb;
+            for (int32_t it = 0; it < S.train_iters; ++it) {
+                S.mlp_step += 1;
+                HULL_CUDA(h, sd::mlp_train_async(S.mlp, S.H.feat, S.H.teach, (uint32_t)S.H.cap, S.H.nb, S.train_lr,
+                                                 S.mlp_step, true, h->stream, count));
+            }
+        }
         S.parity ^= 1;
     }
     h->steps += (uint64_t)n_steps;
@@ -435,6 +458,16 @@ sd_status sd_engine_set_gjk_seed(sd_engine* h, int32_t mode) {
         return sd_fail(h, SD_ERR_INVALID_ARG, "unknown GJK seed mode");
     h->hull.seed_mode = mode;
     h->hull.graph_valid = false;
+    return SD_OK;
+}
+
+sd_status sd_engine_set_gjk_training(sd_engine* h, int32_t every, int32_t iters, float lr) {
+    if (!h) return sd_fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
+    if (every < 0 || iters < 0 || !(lr >= 0.0f) || !std::isfinite(lr))
+        return sd_fail(h, SD_ERR_INVALID_ARG, "every >= 0, iters >= 0 and a finite lr >= 0");
+    h->hull.train_every = every;
+    h->hull.train_iters = iters;
+    h->hull.train_lr = lr;
     return SD_OK;
 }
 

@@ -139,6 +139,11 @@ struct HullBuffers {
     float4* dir;                           // per entry: final search direction in A's frame, w = 1 if separated
     float4* seeds;                         // per entry: seed in A's frame, w = 1 to use (may be null)
     float* feat;                           // per entry: 16 MLP inputs (may be null)
+    // training targets of the warm-start network (may be null): when
+    // *teach_on, per unique entry the converged closest-point direction of
+    // a separated pair in A's frame (w = 1), else w = 0
+    float4* teach;
+    const uint32_t* teach_on;
     const uint32_t *prev_off, *prev_partners;  // the previous step's lists
     const float4* prev_dir;
     float4 *force, *torque;                // optional per body totals
@@ -167,9 +172,10 @@ cudaError_t mlp_set_params_async(MlpState& s, const float* host_params, cudaStre
 cudaError_t mlp_forward_async(const MlpState& s, const float* feat, float4* out, const uint32_t* d_count, uint64_t n,
                               bool seeds, cudaStream_t st);
 // one full-batch gradient of the cosine loss (grad[] = its value) and, when
-// update, an Adam step (adam_step counts from 1)
+// update, an Adam step (adam_step counts from 1); d_count (may be null): a
+// device word capping the rows below n
 cudaError_t mlp_train_async(MlpState& s, const float* feat, const float4* tgt, uint32_t n, uint32_t n_valid, float lr,
-                            uint32_t adam_step, bool update, cudaStream_t st);
+                            uint32_t adam_step, bool update, cudaStream_t st, const uint32_t* d_count = nullptr);
 
 // ---- physics pipeline (sd_dem.cu)
 struct DemParams {

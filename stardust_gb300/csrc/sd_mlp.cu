@@ -311,10 +311,12 @@ __global__ void __launch_bounds__(kRows) mlp_train_kernel(const uint8_t* __restr
                                                          const float* __restrict__ params,
                                                          const float* __restrict__ feat, const float4* __restrict__ tgt,
                                                          uint32_t n, float inv_batch, float* __restrict__ part,
-                                                         uint32_t* __restrict__ status) {
+                                                         uint32_t* __restrict__ status,
+                                                         const uint32_t* __restrict__ d_count) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(aligned_smem(smem_raw));
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    if (d_count) n = min(n, *d_count);  // rows: the step's entry count, read on the device
     const uint32_t tiles = (n + kRows - 1) / kRows;
     copy_img(S.w1, img + kImgW1, sizeof S.w1);
     copy_img(S.w2, img + kImgW2, sizeof S.w2);
@@ -596,13 +598,13 @@ cudaError_t mlp_forward_async(const MlpState& s, const float* feat, float4* out,
 }
 
 cudaError_t mlp_train_async(MlpState& s, const float* feat, const float4* tgt, uint32_t n, uint32_t n_valid, float lr,
-                            uint32_t adam_step, bool update, cudaStream_t st) {
+                            uint32_t adam_step, bool update, cudaStream_t st, const uint32_t* d_count) {
     if (n == 0) return cudaSuccess;
     const uint32_t tiles = grid_for(n, kRows);
     const uint32_t ctas = tiles < kMaxTrainCtas ? tiles : kMaxTrainCtas;
     const float inv = n_valid ? 1.0f / (float)n_valid : 0.0f;
     mlp_train_kernel<<<ctas, kRows, sizeof(TrainSmem) + 1024, st>>>(s.img, s.params, feat, tgt, n, inv, s.part,
-                                                                     s.status);
+                                                                     s.status, d_count);
     const float c1 = update ? (float)(1.0 / (1.0 - std::pow(0.9, (double)adam_step))) : 0.f;
     const float c2 = update ? (float)(1.0 / (1.0 - std::pow(0.999, (double)adam_step))) : 0.f;
     mlp_reduce_kernel<<<grid_for(kParams, 256), 256, 0, st>>>(s.part, ctas, s.grad, s.params, s.m1, s.m2,

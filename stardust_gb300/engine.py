@@ -221,6 +221,10 @@ class DEMEngine:
     def set_gjk_seed(self, mode: int) -> None:
         self._call("sd_engine_set_gjk_seed", mode)
 
+    def set_gjk_training(self, every: int, iters: int, lr: float = 1e-3) -> None:
+        """Online training of the warm-start network (sd_engine_set_gjk_training)."""
+        self._call("sd_engine_set_gjk_training", every, iters, lr)
+
     def hull_entries(self) -> dict:
         """The last step's candidate entries (CSR) with status, iterations,
         final directions, seeds and network inputs."""
