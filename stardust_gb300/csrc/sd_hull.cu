@@ -621,6 +621,7 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     // only that certificate is taken from it -- any other outcome is the
     // plain run's, so contact sets, forces and states do not depend on seeds
     int st = gjk(P, d0, &S, &iters, &dir, seeded ? kSeedMaxIt : kGjkMaxIt);
+    const bool certified_by_seed = seeded && st == kSep;
     if (seeded && st != kSep) {
         int it2 = 0;
         st = gjk(P, vneg(P.off), &S, &it2, &dir);
@@ -628,7 +629,11 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     }
     v3 fa = mk(0.f, 0.f, 0.f), ta = mk(0.f, 0.f, 0.f), fbv = mk(0.f, 0.f, 0.f), tb = mk(0.f, 0.f, 0.f);
     int epa_it = 0;
-    const v3 dA = rotT(P.A.R, dir);  // final direction in A's frame (seed of the next step)
+    // final direction in A's frame (seed of the next step); with learned
+    // seeds a seed's certificate keeps the anchor it was predicted from
+    const v3 dA = (certified_by_seed && H.keep_anchor && H.feat)
+                      ? mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9], H.feat[16 * (size_t)e + 10])
+                      : rotT(P.A.R, dir);
     if (st == kHit) {
         Contact c;
         epa(P, S, (H.iinv[A].w + H.iinv[B].w) * 1e-7f, &c);

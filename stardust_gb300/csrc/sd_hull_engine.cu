@@ -124,6 +124,7 @@ sd_status build_hull_graphs(sd_engine* h, float dt) {
         H.prev_off = S.off[par ^ 1];
         H.prev_partners = S.partners[par ^ 1];
         H.prev_dir = S.dir[par ^ 1];
+        H.keep_anchor = S.seed_mode == SD_GJK_SEED_LEARNED;
         cudaGraph_t g = nullptr;
         HULL_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = sd::hull_aabb_async(H, h->stream);

@@ -144,6 +144,10 @@ struct HullBuffers {
     // a separated pair in A's frame (w = 1), else w = 0
     float4* teach;
     const uint32_t* teach_on;
+    // learned seeds: a pair whose seeded run certified separation keeps its
+    // previous direction (inputs 8..10, the anchor) as the next step's, so
+    // the network is never fed its own outputs
+    bool keep_anchor;
     const uint32_t *prev_off, *prev_partners;  // the previous step's lists
     const float4* prev_dir;
     float4 *force, *torque;                // optional per body totals
