@@ -619,9 +619,28 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     v3 dir;
     // a seeded run gets kSeedMaxIt support evaluations to certify separation;
     // only that certificate is taken from it -- any other outcome is the
-    // plain run's, so contact sets, forces and states do not depend on seeds
-    int st = gjk(P, d0, &S, &iters, &dir, seeded ? kSeedMaxIt : kGjkMaxIt);
-    const bool certified_by_seed = seeded && st == kSep;
+    // plain run's, so contact sets, forces and states do not depend on seeds.
+    // Learned seeds (keep_anchor): the pair's anchor direction (its last
+    // certificate, inputs 8..10) is tried first with one support, and the
+    // network's direction -- trained on the pairs whose anchor failed -- with
+    // one more only when the anchor fails.
+    const bool learned = seeded && H.keep_anchor && H.feat;
+    bool anchor_failed = false, certified_by_anchor = false;
+    int st;
+    if (learned) {
+        const v3 anchor = rot(P.A.R, mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9],
+                                        H.feat[16 * (size_t)e + 10]));
+        st = gjk(P, anchor, &S, &iters, &dir, 1);
+        certified_by_anchor = st == kSep;
+        if (!certified_by_anchor) {
+            anchor_failed = true;
+            int it1 = 0;
+            st = gjk(P, d0, &S, &it1, &dir, 1);
+            iters += it1;
+        }
+    } else {
+        st = gjk(P, d0, &S, &iters, &dir, seeded ? kSeedMaxIt : kGjkMaxIt);
+    }
     if (seeded && st != kSep) {
         int it2 = 0;
         st = gjk(P, vneg(P.off), &S, &it2, &dir);
@@ -631,7 +650,7 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     int epa_it = 0;
     // final direction in A's frame (seed of the next step); with learned
     // seeds a seed's certificate keeps the anchor it was predicted from
-    const v3 dA = (certified_by_seed && H.keep_anchor && H.feat)
+    const v3 dA = certified_by_anchor
                       ? mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9], H.feat[16 * (size_t)e + 10])
                       : rotT(P.A.R, dir);
     if (st == kHit) {
@@ -663,10 +682,10 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     H.info[e] = info;
     H.dir[e] = d4;
     if (H.teach && *H.teach_on) {
-        // a training step: the max-margin direction of a separated pair the
-        // network seeds (one seen in the previous step)
+        // a training step: the max-margin direction of a separated pair
+        // whose anchor failed (the cases the network's seed is tried on)
         v3 m;
-        const bool ok = st == kSep && H.feat && H.feat[16 * (size_t)e + 7] == 1.0f && gjk_margin_dir(P, dir, &m);
+        const bool ok = st == kSep && anchor_failed && gjk_margin_dir(P, dir, &m);
         const v3 mA = rotT(P.A.R, m);
         H.teach[e] = ok ? make_float4(mA.x, mA.y, mA.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
         if (em < H.off[B + 1]) H.teach[em] = make_float4(0.f, 0.f, 0.f, 0.f);  // one sample per pair
