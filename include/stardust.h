@@ -47,9 +47,15 @@ typedef enum sd_status {
 } sd_status;
 
 /* Collision engine selector; mirrors STARDUST::CollisionEngine
- * (src/engine/engine.hpp:21-24).  SD_ENGINE_SAP is accepted for source
- * compatibility and runs the spatial-hash pipeline (the reference's SAP
- * step is not a correct broad phase). */
+ * (src/engine/engine.hpp:21-24).  SD_ENGINE_SAP: sphere-triangle candidates
+ * of a mesh come from sweep and prune along one axis (the rotation axis of
+ * a rotating mesh, else the mesh's longest extent: triangle boxes sorted by
+ * their lower bound, each sphere sweeps the window its box can meet);
+ * SD_ENGINE_SHP: from a static grid in the mesh frame.  Sphere-sphere
+ * candidates come from the spatial hash under both (the reference's SAP
+ * step keeps at most 9 partners per sorted box in a window of 64 and is not
+ * a correct broad phase; sd_sap_pairs is the exact SAP operator).  Both
+ * engines give the same contacts in the same order, so the same bits. */
 typedef enum sd_collision_engine {
     SD_ENGINE_SAP = 0,
     SD_ENGINE_SHP = 1 /* spatial hash */

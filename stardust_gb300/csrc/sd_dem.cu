@@ -306,8 +306,35 @@ __device__ __forceinline__ float3 closest_on_triangle(float3 p, float3 a, float3
 // listed in its cell of the mesh grid, ascending; per patch the deepest
 // contact (the first of equal depth) is kept; each kept contact applies the
 // sphere law against the moving wall (velocity omega axis x (q - c)).
+// Triangle tr as a contact candidate of the sphere at q (mesh frame):
+// updates the deepest contact of its patch (the first of equal depth).
+__device__ __forceinline__ void mesh_candidate(const MeshView& m, uint32_t tr, float3 q, float r2, int32_t* pid,
+                                               float* pd2, float3* pv, float3* pq, int& np) {
+    const float3 a = f3v(__ldg(m.tri + 3 * tr)), b = f3v(__ldg(m.tri + 3 * tr + 1)), cc = f3v(__ldg(m.tri + 3 * tr + 2));
+    const float3 cl = closest_on_triangle(q, a, b, cc);
+    const float3 v = sub3(q, cl);
+    const float d2 = dot3(v, v);
+    if (!(d2 < r2) || d2 == 0.0f) return;
+    const int32_t pa = __ldg(m.patch + tr);
+    int k = 0;
+    while (k < np && pid[k] != pa) ++k;
+    if (k < np) {
+        if (d2 < pd2[k]) {
+            pd2[k] = d2;
+            pv[k] = v;
+            pq[k] = cl;
+        }
+    } else if (np < kMeshPatches) {
+        pid[np] = pa;
+        pd2[np] = d2;
+        pv[np] = v;
+        pq[np] = cl;
+        ++np;
+    }
+}
+
 __device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView& m, float4 pi, float4 vi, float4 wi,
-                                              float3& f, float3& t) {
+                                              float3& f, float3& t, uint32_t* status) {
     const float* S = m.state;
     float R[9];
 #pragma unroll
@@ -318,41 +345,55 @@ __device__ __forceinline__ void mesh_contacts(const DemParams& p, const MeshView
     const float3 d = sub3(make_float3(pi.x, pi.y, pi.z), c);
     const float3 q = make_float3((R[0] * d.x + R[3] * d.y) + R[6] * d.z, (R[1] * d.x + R[4] * d.y) + R[7] * d.z,
                                  (R[2] * d.x + R[5] * d.y) + R[8] * d.z);  // R^T d: mesh frame
-    const int32_t ix = axis_cell(q.x, m.lo[0], m.h, m.nx);
-    const int32_t iy = axis_cell(q.y, m.lo[1], m.h, m.ny);
-    const int32_t iz = axis_cell(q.z, m.lo[2], m.h, m.nz);
-    const uint32_t cell = (uint32_t)((ix * m.ny + iy) * m.nz + iz);
-    const uint32_t e0 = __ldg(m.cell_off + cell), e1 = __ldg(m.cell_off + cell + 1);
-    if (e0 == e1) return;
     const float r2 = pi.w * pi.w;
     int32_t pid[kMeshPatches];
     float pd2[kMeshPatches];
     float3 pv[kMeshPatches], pq[kMeshPatches];
     int np = 0;
-    for (uint32_t e = e0; e < e1; ++e) {
-        const uint32_t tr = __ldg(m.cell_tri + e);
-        const float3 a = f3v(__ldg(m.tri + 3 * tr)), b = f3v(__ldg(m.tri + 3 * tr + 1)),
-                     cc = f3v(__ldg(m.tri + 3 * tr + 2));
-        const float3 cl = closest_on_triangle(q, a, b, cc);
-        const float3 v = sub3(q, cl);
-        const float d2 = dot3(v, v);
-        if (!(d2 < r2) || d2 == 0.0f) continue;
-        const int32_t pa = __ldg(m.patch + tr);
-        int k = 0;
-        while (k < np && pid[k] != pa) ++k;
-        if (k < np) {
-            if (d2 < pd2[k]) {
-                pd2[k] = d2;
-                pv[k] = v;
-                pq[k] = cl;
-            }
-        } else if (np < kMeshPatches) {
-            pid[np] = pa;
-            pd2[np] = d2;
-            pv[np] = v;
-            pq[np] = cl;
-            ++np;
+    if (m.sap_n) {
+        // sweep and prune along sap_axis: triangles whose box starts within
+        // [x - r - longest extent, x + r] (sorted lower bounds, binary
+        // search); those whose box meets the sphere's are tested, the ones in
+        // contact are taken in ascending id order -- the grid's order -- so the
+        // patch choices, and the force sums, are the same bits
+        const float qs[3] = {q.x, q.y, q.z};
+        const float xa = qs[m.sap_axis], r = pi.w;
+        const float from = (xa - r) - m.sap_len, to = xa + r;
+        uint32_t lo = 0, hi = m.sap_n;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(m.sap_lo + mid) < from) lo = mid + 1;
+            else hi = mid;
         }
+        uint32_t hits[kSapHits];
+        uint32_t nh = 0;
+        for (uint32_t k = lo; k < m.sap_n && __ldg(m.sap_lo + k) <= to; ++k) {
+            const float4 bl = __ldg(m.sap_box + 2 * k), bh = __ldg(m.sap_box + 2 * k + 1);
+            if (bl.x > q.x + r || bh.x < q.x - r || bl.y > q.y + r || bh.y < q.y - r || bl.z > q.z + r ||
+                bh.z < q.z - r)
+                continue;
+            const uint32_t tr = __float_as_uint(bh.w);
+            const float3 a = f3v(__ldg(m.tri + 3 * tr)), b = f3v(__ldg(m.tri + 3 * tr + 1)),
+                         cc = f3v(__ldg(m.tri + 3 * tr + 2));
+            const float3 v = sub3(q, closest_on_triangle(q, a, b, cc));
+            const float d2 = dot3(v, v);
+            if (!(d2 < r2) || d2 == 0.0f) continue;
+            if (nh == kSapHits) {  // more contacts than the sweep can order
+                if (status) atomicOr(status, kErrPairOverflow);
+                break;
+            }
+            uint32_t j = nh++;
+            for (; j > 0 && hits[j - 1] > tr; --j) hits[j] = hits[j - 1];
+            hits[j] = tr;
+        }
+        for (uint32_t k = 0; k < nh; ++k) mesh_candidate(m, hits[k], q, r2, pid, pd2, pv, pq, np);
+    } else {
+        const int32_t ix = axis_cell(q.x, m.lo[0], m.h, m.nx);
+        const int32_t iy = axis_cell(q.y, m.lo[1], m.h, m.ny);
+        const int32_t iz = axis_cell(q.z, m.lo[2], m.h, m.nz);
+        const uint32_t cell = (uint32_t)((ix * m.ny + iy) * m.nz + iz);
+        const uint32_t e0 = __ldg(m.cell_off + cell), e1 = __ldg(m.cell_off + cell + 1);
+        for (uint32_t e = e0; e < e1; ++e) mesh_candidate(m, __ldg(m.cell_tri + e), q, r2, pid, pd2, pv, pq, np);
     }
     for (int k = 0; k < np; ++k) {
         const float dist = sqrtf(pd2[k]);
@@ -403,7 +444,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                                                   float4* __restrict__ torque, uint32_t& contacts,
                                                   const ClumpCtx& cc, bool* has_key, const Batch& bt = Batch{},
                                                   const MeshView* mesh = nullptr, const NbrLists* nl = nullptr,
-                                                  const SkinLists* sk = nullptr) {
+                                                  const SkinLists* sk = nullptr, uint32_t* status = nullptr) {
     const Grid g = BATCHED ? grid_of_slot(bt.scenes, bt.first, bt.n, i) : grid_of(p);
     const float4 pi = pos[i], vi = vel[i], wi = omg[i];
     const float ri = pi.w, mi = vi.w;
@@ -620,7 +661,7 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
             }
         }
     }
-    if (MESH) mesh_contacts(p, *mesh, pi, vi, wi, f, t);
+    if (MESH) mesh_contacts(p, *mesh, pi, vi, wi, f, t, status);
     if (p.walls) {
         const float wsx = ri * wi.x, wsy = ri * wi.y, wsz = ri * wi.z;
         const float xs[3] = {pi.x, pi.y, pi.z};
@@ -827,7 +868,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
     if (i < n)
         key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, LISTED, SKIN>(
             p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
-            contacts, cc, &has_key, bt, &mesh, &nl, &sk);
+            contacts, cc, &has_key, bt, &mesh, &nl, &sk, status);
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();

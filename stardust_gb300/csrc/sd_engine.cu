@@ -386,6 +386,62 @@ sd_status build_mesh(sd_engine* h) {
     V.cell_off = coff;
     V.cell_tri = ctri;
     V.state = state;
+    V.sap_n = 0;
+    if (h->cfg.collision_engine == SD_ENGINE_SAP && nt) {
+        // sweep and prune of the triangles: along the rotation axis of a
+        // rotating mesh (its triangles' extents along it never change), else
+        // along the mesh's longest extent; boxes sorted by lower bound (ties
+        // by triangle id)
+        int axis = 0;
+        if (M.omega != 0.0f) {
+            for (int a = 1; a < 3; ++a)
+                if (std::fabs(M.axis[a]) > std::fabs(M.axis[axis])) axis = a;
+        } else {
+            for (int a = 1; a < 3; ++a)
+                if (hi[a] - lo[a] > hi[axis] - lo[axis]) axis = a;
+        }
+        std::vector<float4> box(2 * (size_t)nt);
+        std::vector<uint32_t> order(nt);
+        float len = 0.0f;
+        for (uint32_t t = 0; t < nt; ++t) {
+            float tl[3] = {INFINITY, INFINITY, INFINITY}, th[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int k = 0; k < 3; ++k) {
+                const float4 v = M.tri[3 * (size_t)t + k];
+                const float cc[3] = {v.x, v.y, v.z};
+                for (int a = 0; a < 3; ++a) {
+                    tl[a] = std::min(tl[a], cc[a]);
+                    th[a] = std::max(th[a], cc[a]);
+                }
+            }
+            uint32_t id_bits = t;
+            float id_f;
+            std::memcpy(&id_f, &id_bits, 4);
+            box[2 * (size_t)t] = make_float4(tl[0], tl[1], tl[2], tl[axis]);
+            box[2 * (size_t)t + 1] = make_float4(th[0], th[1], th[2], id_f);
+            len = std::max(len, th[axis] - tl[axis]);
+            order[t] = t;
+        }
+        std::stable_sort(order.begin(), order.end(),
+                         [&](uint32_t a, uint32_t b) { return box[2 * (size_t)a].w < box[2 * (size_t)b].w; });
+        std::vector<float4> sbox(2 * (size_t)nt);
+        std::vector<float> slo(nt);
+        for (uint32_t k = 0; k < nt; ++k) {
+            sbox[2 * (size_t)k] = box[2 * (size_t)order[k]];
+            sbox[2 * (size_t)k + 1] = box[2 * (size_t)order[k] + 1];
+            slo[k] = box[2 * (size_t)order[k]].w;
+        }
+        float4* dbox = nullptr;
+        float* dlo = nullptr;
+        if ((s = dev_alloc(h, &dbox, 2 * (size_t)nt)) || (s = dev_alloc(h, &dlo, nt))) return s;
+        SD_CUDA(h, cudaMemcpyAsync(dbox, sbox.data(), 32 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaMemcpyAsync(dlo, slo.data(), 4 * (size_t)nt, cudaMemcpyHostToDevice, h->stream));
+        SD_CUDA(h, cudaStreamSynchronize(h->stream));
+        V.sap_n = nt;
+        V.sap_box = dbox;
+        V.sap_lo = dlo;
+        V.sap_axis = axis;
+        V.sap_len = len;
+    }
     M.dt = 0.0f;
     SD_CUDA(h, sd::mesh_advance_async(V, 0, h->stream));
     return SD_OK;

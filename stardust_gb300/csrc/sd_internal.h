@@ -225,8 +225,19 @@ struct MeshView {
     float h;
     int32_t nx, ny, nz;
     float* state;
+    // sweep and prune of the triangles (collision engine SD_ENGINE_SAP): the
+    // triangles' boxes (mesh frame) sorted by their lower bound along axis
+    // sap_axis -- sap_box[2k] = (lo, lower bound), sap_box[2k+1] = (hi,
+    // triangle id as float bits) -- and the largest box extent along it;
+    // sap_n == 0: the static grid above gives the candidates
+    uint32_t sap_n;
+    const float4* sap_box;
+    const float* sap_lo;      // sorted lower bounds (the binary search's array)
+    int32_t sap_axis;
+    float sap_len;
 };
 constexpr int kMeshPatches = 4;  // deepest contact kept per patch, up to this many patches per sphere
+constexpr int kSapHits = 32;     // triangles in contact with one sphere the sweep can order (more: error bit)
 
 struct DemBuffers {
     uint32_t n;

@@ -12,10 +12,12 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
-def small_drum(sd, omega=20.0, seed=0):
+def small_drum(sd, omega=20.0, seed=0, engine=None):
     from stardust_gb300 import scenes
     d = scenes.drum_scene(n_spheres=650, radius=0.04, length=0.04, n_around=24, n_along=6, n_rings=3,
                           r_range=(0.002, 0.0028), omega=omega, seed=seed)
+    if engine is not None:
+        d["cfg"].collision_engine = engine
     eng = sd.DEMEngine(d["cfg"])
     scenes.add_drum_scene(eng, d)
     eng.prepare()
@@ -39,9 +41,12 @@ def body_tables(d, n):
 
 
 @pytest.mark.parametrize("steps", [1, 50, 400])
-def test_drum_bit_exact(sdlib, orc, steps):
+@pytest.mark.parametrize("engine", ["SHP", "SAP"])
+def test_drum_bit_exact(sdlib, orc, steps, engine):
+    """Either collision engine: sphere-triangle candidates from the mesh's
+    static grid (SHP) or from sweep and prune along the drum axis (SAP)."""
     from stardust_gb300 import _abi
-    eng, d = small_drum(sdlib)
+    eng, d = small_drum(sdlib, engine=getattr(_abi, "SD_ENGINE_" + engine))
     n = eng.n
     body_of, r0, first, count = body_tables(d, n)
     pos, vel, omg = eng.positions(), eng.velocities(), eng.omegas()

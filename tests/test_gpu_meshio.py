@@ -33,7 +33,7 @@ def test_drum_from_stl_is_the_drum(sdlib, tmp_path):
     assert np.array_equal(bits(a[4][0]), bits(b[4][0])) and np.array_equal(a[4][1], b[4][1])
 
 
-def hopper_engine(sd, tmp_path, n_side=9):
+def hopper_engine(sd, tmp_path, n_side=9, engine=None):
     from stardust_gb300 import scenes
     funnel, tray = scenes.hopper_meshes()
     sd.write_stl(tmp_path / "funnel.stl", funnel, binary=False)
@@ -53,6 +53,8 @@ def hopper_engine(sd, tmp_path, n_side=9):
     vel[:, 3] = 2500 * 4 / 3 * np.pi * r ** 3
     cfg = sd.EngineConfig(box_lo=(-0.1, -0.1, -0.02), box_hi=(0.1, 0.1, 0.2), walls=0x3F, cell=2 * r, kn=1e4,
                           restitution=0.4, mu=0.3, gravity=(0.0, 0.0, -9.81))
+    if engine is not None:
+        cfg.collision_engine = engine
     eng = sd.DEMEngine(cfg)
     eng.add_spheres(pos, vel)
     eng.add_mesh_stl(tmp_path / "funnel.stl")
@@ -60,8 +62,12 @@ def hopper_engine(sd, tmp_path, n_side=9):
     return eng, pos, vel, 2e-5, funnel, tray
 
 
-def test_stl_hopper_bit_exact_vs_oracle(sdlib, orc, tmp_path):
-    eng, pos, vel, dt, funnel, tray = hopper_engine(sdlib, tmp_path)
+@pytest.mark.parametrize("engine", ["SHP", "SAP"])
+def test_stl_hopper_bit_exact_vs_oracle(sdlib, orc, tmp_path, engine):
+    """Two static STL meshes; sphere-triangle candidates from the static grid
+    (SHP) or from sweep and prune along the meshes' longest extent (SAP)."""
+    from stardust_gb300 import _abi
+    eng, pos, vel, dt, funnel, tray = hopper_engine(sdlib, tmp_path, engine=getattr(_abi, "SD_ENGINE_" + engine))
     t, pa, c = eng.mesh()
     assert len(t) == 18 and len(np.unique(pa)) == 9
     assert np.allclose(t + np.float32(c), np.concatenate([funnel, tray]), atol=1e-6)  # the tray is back in place
