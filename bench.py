@@ -30,6 +30,9 @@ the settling run rather than right after the packing.  Timings:
              on a bounded sample of the same scene;
   dense_bed  the same spheres with radii x1.2 (~2.5M contact pairs), after
              1,000 steps;
+  reference_gpu  the reference's own GPU step (its kernels compiled
+             unchanged from its sources, oracle/time_ref_step.py) on the same
+             scene and GPU, beside this step's time (a baseline leg);
   drum       the rotating drum: 2.1M spheres and clumps against a turning
              20,480-triangle cylinder (bench_drum);
   batch      512 independent scenes (~2.9M spheres) stepped together, one
@@ -458,7 +461,27 @@ def bench_drum(steps: int, warmup: int, local: int):
     stt = eng.stats()
     n = eng.n
     eng.close()
-    return {"workload": f"rotating drum, {n} spheres ({len(d['clumps'])} 4-sphere clumps), "
+    # the same drum with the triangles' sweep and prune along the drum axis
+    # (collision engine SAP) in place of the mesh grid
+    from stardust_gb300 import _abi
+    d["cfg"].collision_engine = _abi.SD_ENGINE_SAP
+    eng = sd.DEMEngine(d["cfg"])
+    scenes.add_drum_scene(eng, d)
+    eng.prepare()
+    eng.step(dt, 3)
+    eng.sync()
+    st2 = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    k = 5
+    a2, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a2.record(st2)
+    eng.step(dt, k)
+    b2.record(st2)
+    torch.cuda.synchronize()
+    sap_ms = a2.elapsed_time(b2) / k
+    sap_err = eng.stats()["device_errors"]
+    eng.close()
+    return {"ms_per_step_sap_triangles": sap_ms, "device_errors_sap": sap_err,
+            "workload": f"rotating drum, {n} spheres ({len(d['clumps'])} 4-sphere clumps), "
                         f"{len(d['tris'])} triangles loaded from a binary STL, R 0.5 m, L 0.5 m, 2 rad/s, dt 2e-6 s",
             "spheres": n, "bodies": int(stt["n_bodies"]), "triangles": int(len(d["tris"])), "ms_per_step": ms,
             "particle_steps_per_s": n / (ms * 1e-3), "device_errors": stt["device_errors"],
@@ -759,6 +782,19 @@ def run_ours(args, rank, world, local):
                "sample": f"{csteps} steps of the {n_cpu}-sphere scene in {cel:.1f}s, CPU restatement of the step "
                          f"(oracle/, OpenMP, {used} threads)"}
 
+    # ---- the reference's own GPU step (its kernels, compiled unchanged from
+    # its sources) on the same scene and GPU (rank 0, N = 1): a baseline leg
+    ref_gpu = None
+    if rank == 0 and world == 1 and not args.no_ref_gpu:
+        try:
+            from oracle import time_ref_step
+            ref_gpu = time_ref_step.measure(5, 2, n, scene=(pos, vel, dt))
+        except BaseException as e:  # noqa: BLE001 -- a baseline leg never fails the bench
+            ref_gpu = {"impl": "reference-gpu", "unavailable": f"{type(e).__name__}: {e}"}
+        if ref_gpu.get("ms_per_step"):
+            ref_gpu["ours_speedup"] = ref_gpu["ms_per_step"] / (total_ms / args.steps)
+        log(f"reference GPU step: {ref_gpu}")
+
     if rank == 0:
         sm_mhz = clocks_mhz(clocks)
         line = {
@@ -799,6 +835,7 @@ def run_ours(args, rank, world, local):
             "step_bytes_per_sphere": STEP_BYTES_PER_SPHERE,
             "step_hbm_frac": (n * STEP_BYTES_PER_SPHERE / (total_ms / args.steps * 1e-3) / 1e9) / peak,
             "cpu_baseline": cpu,
+            "reference_gpu": ref_gpu,
             "clocks": clocks,
             "gpu_launches": st["step_kernels"] * args.steps,
             "contacts": st["contacts"],
@@ -829,6 +866,7 @@ def main():
     ap.add_argument("--advance", type=int, default=1000,
                     help="untimed steps of the settling run before tuning and timing (the timed window's start)")
     ap.add_argument("--no-dense", action="store_true", help="skip the dense contact network (radii x1.2)")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference's own GPU step")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-hulls", action="store_true")
     ap.add_argument("--only-hulls", action="store_true", help="run only the convex-hull GJK section")

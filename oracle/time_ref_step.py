@@ -40,33 +40,37 @@ class RefStep(C.Structure):
             "bquat", "bmass", "lin", "ang", "inertia", "start", "length")] + [("dt", C.c_float)]
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--n", type=int, default=1 << 20)
-    args = ap.parse_args()
-
+def measure(steps: int = 10, warmup: int = 3, n: int = 1 << 20, scene=None) -> dict:
+    """Times the reference's GPU step (see the module docstring); returns the
+    JSON-able result, or {"unavailable": why} when its kernels are not built.
+    scene: (pos4, vel4, dt) of the settling box when already generated."""
+    import types
+    args = types.SimpleNamespace(steps=steps, warmup=warmup, n=n)
     import torch
     from oracle import ref_build
     from stardust_gb300 import scenes
 
     cub = ROOT / "oracle" / "_ref"
     if not all((cub / f"{s}.cubin").exists() for s in ref_build.SOURCES):
-        print(json.dumps({"impl": "reference-gpu", "unavailable": "reference cubins not built (oracle/ref_build.py)"}))
-        return 0
+        return {"impl": "reference-gpu", "unavailable": "reference kernels not built (oracle/ref_build.py)"}
     lib_path = ref_build.build_harness()
+    if lib_path is None:
+        return {"impl": "reference-gpu", "unavailable": "the launch harness did not compile"}
     lib = C.CDLL(str(lib_path))
     lib.ref_last_error.restype = C.c_char_p
     torch.zeros(1, device="cuda")
     if lib.ref_init(str(cub).encode()) != 0:
-        raise SystemExit(lib.ref_last_error().decode())
+        return {"impl": "reference-gpu", "unavailable": lib.ref_last_error().decode()}
 
     n = args.n
-    box = (1.0, 1.0, 2.0) if n == 1 << 20 else scenes.scaled_box(n)
-    t0 = time.time()
-    pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=box, seed=0)
-    print(f"scene: {n} spheres in {time.time() - t0:.1f}s", file=sys.stderr)
+    if scene is not None:
+        pos, vel, dt = scene
+        n = len(pos)
+    else:
+        box = (1.0, 1.0, 2.0) if n == 1 << 20 else scenes.scaled_box(n)
+        t0 = time.time()
+        pos, vel, cfg, dt, phi = scenes.settling_rsa(n, box=box, seed=0)
+        print(f"scene: {n} spheres in {time.time() - t0:.1f}s", file=sys.stderr)
     dev = torch.device("cuda")
     f4 = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev)
     p = pos.copy()
@@ -147,14 +151,23 @@ def main():
     st_rigid = timed(8)
     med = lambda x: sorted(x)[len(x) // 2]
     staged = med(st_construct) + med(st_sort) + med(st_traverse) + med(st_rigid)
-    print(json.dumps({
+    return {
         "impl": "reference-gpu", "metric": "particle-steps/s @1M spheres", "n_spheres": n, "steps": args.steps,
         "ms_per_step": staged, "value": n / (staged * 1e-3), "unit": "particle-steps/s",
         "ms_stages_median": {"construct": med(st_construct), "sort_as_written": med(st_sort),
                              "traverse_sorted_input": med(st_traverse), "rigid_body": med(st_rigid)},
         "as_written_step_ms": {"median": med(whole), "min": min(whole), "max": max(whole)},
         "kernels": "constructCollisionList + 4x(Tabulate, Sum, Reorder) over 9n entries + "
-                   "tranverseCollisionList + computeForcesAndTorques + advect + updateSphereData"}))
+                   "tranverseCollisionList + computeForcesAndTorques + advect + updateSphereData"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=1 << 20)
+    args = ap.parse_args()
+    print(json.dumps(measure(args.steps, args.warmup, args.n)))
     return 0
 
 
