@@ -12,8 +12,9 @@
 //      per warp that has any (the list's order does not matter);
 //   2. resort_plan_kernel, one block: publishes the count M and, in shared
 //      memory, sorts the list by (key, slot) and the moved slots alone
-//      (bitonic); moved entry r (rank r in (key, slot) order) goes to r plus
-//      the unmoved slots that sort before it -- the previous step's cell
+//      (each entry placed by counting the smaller ones); moved entry r
+//      (rank r in (key, slot) order) goes to r plus the unmoved slots that
+//      sort before it -- the previous step's cell
 //      table bounds the slots of its key, so that count is its slot clamped
 //      to that range minus the moved slots below it.  Only positions between
 //      a moved entry's old slot and its new position change hands, so it also
@@ -41,30 +42,7 @@ namespace {
 
 // one block of 1024 threads: one thread per moved entry of a full list
 constexpr int kRsThreads = 1024;
-// lists up to this long are sorted by counting ranks (M^2 / 1024 shared
-// reads per thread), longer ones by a bitonic sort
-constexpr uint32_t kRankSortMax = 256;
 static_assert(kResortMaxCap <= (uint32_t)kRsThreads, "one thread per moved entry");
-
-// Sorts v[0, P) ascending in shared memory (P a power of two; every thread
-// of the block calls it).
-__device__ void bitonic_sort(unsigned long long* v, uint32_t P) {
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-                const uint32_t l = i ^ j;
-                if (l > i) {
-                    const unsigned long long a = v[i], b = v[l];
-                    if ((a > b) == ((i & k) == 0)) {
-                        v[i] = b;
-                        v[l] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
 
 // scratch (u32): [0] moved count (appended to during the step, zero again
 // when this kernel ends), [1] M of the step, [3] total length T of the
@@ -100,36 +78,35 @@ resort_plan_kernel(unsigned long long* __restrict__ list, uint32_t* __restrict__
         if (threadIdx.x == 0) scratch[3] = 0u;
         return;
     }
-    if (M <= kRankSortMax) {
-        // few entries: each thread places its own by counting the smaller
-        // ones (entries and slots are distinct), two barriers in all
-        const uint32_t r = threadIdx.x;
-        unsigned long long c = 0;
-        if (r < M) s_b[r] = list[r];
+    {
+        // each entry is placed by counting the smaller ones (entries and
+        // slots are distinct): G threads per entry, G the largest power of two
+        // up to 32 with G * M <= 1024, each counting a G-th of the list, then
+        // summed across the G lanes; two barriers in all
+        uint32_t G = 32;
+        while (G > 1 && G * M > (uint32_t)kRsThreads) G >>= 1;
+        if (threadIdx.x < M) s_b[threadIdx.x] = list[threadIdx.x];
         __syncthreads();
+        const uint32_t r = threadIdx.x / G, g = threadIdx.x % G;
+        const unsigned long long c = r < M ? s_b[r] : 0ull;
+        uint32_t ra = 0, rs = 0;
         if (r < M) {
-            c = s_b[r];
-            uint32_t ra = 0, rs = 0;
-            for (uint32_t j = 0; j < M; ++j) {
+            for (uint32_t j = g; j < M; j += G) {
                 const unsigned long long o = s_b[j];
                 ra += o < c;
                 rs += (o & 0xffffffffull) < (c & 0xffffffffull);
             }
-            s_a[ra] = c;
-            c = (c & 0xffffffffull) | ((unsigned long long)rs << 32);  // slot, its rank among the slots
+        }
+        for (uint32_t o = G >> 1; o > 0; o >>= 1) {
+            ra += __shfl_xor_sync(0xffffffffu, ra, (int)o);
+            rs += __shfl_xor_sync(0xffffffffu, rs, (int)o);
         }
         __syncthreads();
-        if (r < M) s_b[(uint32_t)(c >> 32)] = c & 0xffffffffull;
+        if (r < M && g == 0) {
+            s_a[ra] = c;
+            s_b[rs] = c & 0xffffffffull;  // the moved slots, ascending
+        }
         __syncthreads();
-    } else {
-        uint32_t P = 2;
-        while (P < M) P <<= 1;
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_a[i] = i < M ? list[i] : ~0ull;
-        __syncthreads();
-        bitonic_sort(s_a, P);
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_b[i] = i < M ? (s_a[i] & 0xffffffffull) : ~0ull;
-        __syncthreads();
-        bitonic_sort(s_b, P);
     }
     // one moved entry per thread (M <= kResortMaxCap = blockDim.x)
     const uint32_t r = threadIdx.x;
