@@ -485,6 +485,8 @@ __device__ __forceinline__ uint32_t particle_step(const DemParams& p, uint32_t n
                         const float ax = pi.x - pa.x, ay = pi.y - pa.y, az = pi.z - pa.z;
                         const float da = dist2(ax, ay, az);
                         if (s == i) continue;  // the sphere itself; a coincident partner is listed
+                        // a sphere of the same rigid body is never a contact: not listed
+                        if (clump_i && same_body(cc, idb, omg, s)) continue;
                         const float rl = ri + pa.w + sk->skin;
                         if (da < rl * rl) {
                             if (c < kVlCap)
@@ -887,23 +889,22 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
 // blocks of 256 per SM (4: 64 registers; 5: 48, with spills in the build
 // scan; knob "listed_blocks", default 5).  It never builds radix histograms (the lists
 // run only with the incremental re-sort).
-template <bool RECORD, int MINB, bool BATCHED>
+template <bool RECORD, int MINB, bool BATCHED, bool CLUMPS = false, bool MESH = false>
 __global__ void __launch_bounds__(256, MINB)
 dem_contact_listed_kernel(DemParams p, uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ vel,
                           const float4* __restrict__ omg, const uint32_t* __restrict__ cell_start,
                           float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
                           uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, float4* __restrict__ force,
                           float4* __restrict__ torque, uint32_t* __restrict__ status, SkinLists sk, MoveSink ms,
-                          Batch bt) {
+                          Batch bt, ClumpCtx cc = ClumpCtx{}, MeshView mesh = MeshView{}) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t contacts = 0, key = 0;
     bool has_key = false;
     const uint32_t kprev = ms.list && i < n ? __ldg(ms.keys_prev + i) : 0u;
-    const ClumpCtx cc{nullptr, nullptr, nullptr};
     if (i < n)
-        key = particle_step<RECORD, false, GlobalSource, BATCHED, false, false, true>(
+        key = particle_step<RECORD, CLUMPS, GlobalSource, BATCHED, MESH, false, true>(
             p, n, i, GlobalSource{pos}, pos, vel, omg, cell_start, pos_n, vel_n, omg_n, keys, vals, force, torque,
-            contacts, cc, &has_key, bt, nullptr, nullptr, &sk);
+            contacts, cc, &has_key, bt, &mesh, nullptr, &sk, status);
     if (ms.list) move_append_warp(ms, i, key, has_key, kprev);
     if (RECORD) count_contacts(status, contacts);
 }
@@ -1076,7 +1077,7 @@ __device__ __forceinline__ void body_step(
     const float4* __restrict__ omg, const float4* __restrict__ sf, const float4* __restrict__ st,
     float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n, uint32_t hist_spec,
-    uint32_t* s_hist, const MoveSink& ms) {
+    uint32_t* s_hist, const MoveSink& ms, const SkinLists& sk) {
     const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
     const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
     const uint32_t first = bfirst[b], cnt = bcount[b];
@@ -1137,6 +1138,10 @@ __device__ __forceinline__ void body_step(
         const float rz = (R[6] * o.x + R[7] * o.y) + R[8] * o.z;
         const float4 po = make_float4(nxp + rx, nyp + ry, nzp + rz, pos[s].w);
         pos_n[s] = po;
+        if (sk.ref) {  // contact lists: a clump sphere that left 0.45 skin of its build position
+            const float4 r = sk.ref[s];
+            if (dist2(po.x - r.x, po.y - r.y, po.z - r.z) > sk.thr2) atomicOr(sk.next, 1u);
+        }
         vel_n[s] = make_float4(vx + (wy * rz - wz * ry), vy + (wz * rx - wx * rz), vz + (wx * ry - wy * rx), m);
         omg_n[s] = make_float4(wx, wy, wz, omg[s].w);
         const uint32_t key = cell_key(p, po.x, po.y, po.z);
@@ -1171,7 +1176,7 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
                 const float4* __restrict__ pos, const float4* __restrict__ omg, const float4* __restrict__ sf,
                 const float4* __restrict__ st, float4* __restrict__ pos_n, float4* __restrict__ vel_n,
                 float4* __restrict__ omg_n, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
-                uint32_t hist_spec, uint32_t* __restrict__ ghist, MoveSink ms) {
+                uint32_t hist_spec, uint32_t* __restrict__ ghist, MoveSink ms, SkinLists sk) {
     __shared__ uint32_t s_hist[kHistWords];
     if (ghist) {
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
@@ -1180,7 +1185,7 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nb)
         body_step(p, b, bpos, bvel, bquat, bomg, bang, binv, bfirst, bcount, r0, slot_of, pos, omg, sf, st, pos_n,
-                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr, ms);
+                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr, ms, sk);
     if (ghist) {
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
@@ -1740,7 +1745,7 @@ cudaError_t dem_sort_async(DemBuffers& b, cudaStream_t st) {
 
 // The slot table covers every sphere when the skin lists use it, else only
 // clump spheres (null without clumps or lists).
-static bool slot_all_of(const DemBuffers& b) { return b.vl_skin > 0.0f && b.vl_cnt && !b.nb; }
+static bool slot_all_of(const DemBuffers& b) { return b.vl_skin > 0.0f && b.vl_cnt; }
 
 cudaError_t dem_reorder_async(DemBuffers& b, cudaStream_t st) {
     if (b.n == 0) return cudaMemsetAsync(b.cell_start, 0, sizeof(uint32_t) * (b.ncells + 1), st);
@@ -1802,16 +1807,7 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
     const unsigned grid = grid_for(b.n, cb);
     // the re-sort step needs no slot identity (its radix fallback writes it)
     uint32_t* const vals = ms.list ? nullptr : b.vals;
-    if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
-        if (b.nb)
-            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, cb, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
-        else
-            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, cb, 0, st>>>(
-                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
-                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
-    } else if (skin) {  // free spheres, one scene or a batch, contact lists
+    if (skin) {  // one scene or a batch, contact lists (clumps and meshes: one scene)
         const float thr = 0.45f * b.vl_skin;
         const SkinLists sk{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin, thr * thr};
         const Batch bt{b.scenes, b.scene_first, b.nscenes};
@@ -1824,6 +1820,18 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
                 dem_contact_listed_kernel<RECORD, 4, true><<<grid, cb, 0, st>>>(
                     p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                     b.dev_status, sk, ms, bt);
+        } else if (b.nb && b.mesh.ntri) {
+            dem_contact_listed_kernel<RECORD, 5, false, true, true><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{}, cc, b.mesh);
+        } else if (b.nb) {
+            dem_contact_listed_kernel<RECORD, 5, false, true, false><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{}, cc);
+        } else if (b.mesh.ntri) {
+            dem_contact_listed_kernel<RECORD, 5, false, false, true><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{}, ClumpCtx{}, b.mesh);
         } else if (g_listed_blocks == 5) {
             dem_contact_listed_kernel<RECORD, 5, false><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
@@ -1833,6 +1841,15 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, sk, ms, Batch{});
         }
+    } else if (b.mesh.ntri) {  // mesh walls (one scene; clumps allowed; per-slot kernel)
+        if (b.nb)
+            dem_contact_integrate_kernel<RECORD, true, false, true><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
+        else
+            dem_contact_integrate_kernel<RECORD, false, false, true><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, spec, ghist, cc, Batch{}, b.mesh, NbrLists{}, SkinLists{}, ms);
     } else if (b.nscenes > 1) {  // a batch: scene grids per slot (clumps are not batched)
         const Batch bt{b.scenes, b.scene_first, b.nscenes};
         if (g_pair_lists != 0 && b.nbr_cnt) {
@@ -1890,7 +1907,10 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
     if (b.nb) {
         dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
             p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
-            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, ms.list ? nullptr : b.vals, b.n, spec, ghist, ms);
+            b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, ms.list ? nullptr : b.vals, b.n, spec, ghist, ms,
+            skin ? SkinLists{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin,
+                             (0.45f * b.vl_skin) * (0.45f * b.vl_skin)}
+                 : SkinLists{});
     }
     return cudaGetLastError();
 }
@@ -1957,7 +1977,7 @@ cudaError_t dem_step_async(const DemParams& p, DemBuffers& b, bool record, cudaS
 }
 
 bool dem_step_skin(const DemBuffers& b) {
-    return b.vl_skin > 0.0f && b.vl_cnt && b.slot_of && !b.nb && !b.mesh.ntri &&
+    return b.vl_skin > 0.0f && b.vl_cnt && b.slot_of &&
            g_contact_mode == 0 && dem_step_swaps(b);
 }
 

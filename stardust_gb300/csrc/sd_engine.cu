@@ -568,7 +568,7 @@ static void swap_state(sd::DemBuffers& B) {
 static sd_status ensure_contact_lists(sd_engine* h) {
     sd::DemBuffers& B = h->B;
     const uint32_t n = B.n;
-    if (!(g_skin_um > 0 && h->hb_pos.empty() && h->mesh.tri.empty() && n)) {
+    if (!(g_skin_um > 0 && n)) {
         B.vl_skin = 0.0f;
         return SD_OK;
     }
@@ -617,7 +617,7 @@ sd_status build_graph(sd_engine* h, float dt) {
         h->mesh.dt = dt;
     }
     h->B.rs_max = sd::dem_resort_max();
-    if (!h->B.nb) {  // free-sphere scenes: the contact lists follow the skin knob
+    {  // the contact lists follow the skin knob
         sd_status s = ensure_contact_lists(h);
         if (s) return s;
     }
