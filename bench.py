@@ -352,9 +352,57 @@ def bench_hulls(n_hulls: int, steps: int, warmup: int, local: int):
     out["ratio_plain_over_online"] = out["iters_per_pair_plain"] / out["iters_per_pair_online"]
     out["ratio_previous_over_online"] = out["iters_per_pair_previous"] / out["iters_per_pair_online"]
     out["hull_steps_per_s_learned"] = n_hulls / (out["ms_per_step_learned"] * 1e-3)
+    for k in ("plain", "learned"):
+        out[f"narrow_roofline_{k}"] = narrow_roofline(engines[k], local)
     for e in engines.values():
         e.close()
     return out
+
+
+# Compulsory HBM bytes of one unique hull pair in the narrow phase besides its
+# vertices: the unique-list entry, its self and partner ids (12); per body
+# position and quaternion (2 x 32) and its vertex range (2 x 8); the seed
+# (16); written for the entry and its mirror: direction, force, torque, info
+# (2 x 52).
+NARROW_BYTES_PER_PAIR = 12 + 64 + 16 + 16 + 104
+
+
+def narrow_roofline(eng, local: int, reps: int = 10):
+    """The narrow phase (GJK, EPA on the hits, contact forces) launched alone
+    on the last step's lists, timed with CUDA events after a 256 MB write;
+    algorithmic bytes per unique pair = one read of both hulls' vertices
+    (16 B each) + NARROW_BYTES_PER_PAIR.  Also the vertex bytes the support
+    evaluations load (iterations x both hulls), the re-read factor."""
+    import torch
+    from stardust_gb300 import _abi
+    ent = eng.hull_entries()
+    _, vc, _ = eng.hull_shapes()
+    selfs = np.repeat(np.arange(len(ent["off"]) - 1), np.diff(ent["off"]))
+    u = ent["partners"] > selfs
+    nv = vc[selfs[u]].astype(np.int64) + vc[ent["partners"][u]].astype(np.int64)
+    pairs = int(u.sum())
+    min_bytes = 16 * int(nv.sum()) + NARROW_BYTES_PER_PAIR * pairs
+    loaded_vertex_bytes = 16 * int((nv * ent["iters"][u]).sum())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    st = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+    a = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    b = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    for i in range(reps):
+        with torch.cuda.stream(st):
+            flush.fill_(i & 0xFF)
+        a[i].record(st)
+        _abi.call("sd_engine_launch_stage", eng._h, _abi.SD_STAGE_CONTACT, 0.0, h=eng._h)
+        b[i].record(st)
+    torch.cuda.synchronize()
+    eng.sync()
+    ms = sum(x.elapsed_time(y) for x, y in zip(a, b)) / reps
+    peak, kind = measured_peak()
+    achieved = min_bytes / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "unique_pairs": pairs, "hits": int((ent["status"][u] == 1).sum()),
+            "bytes_per_pair": min_bytes / max(pairs, 1), "vertex_bytes_per_pair": 16 * float(nv.mean()) if pairs else 0,
+            "loaded_vertex_bytes_per_pair": loaded_vertex_bytes / max(pairs, 1), "ms": ms,
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind,
+            "pairs_per_s": pairs / (ms * 1e-3)}
 
 
 def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
@@ -495,11 +543,12 @@ def bench_sap(n: int, steps: int, warmup: int, local: int):
     lower x, windowed sweep) and the exact pair set (sd_sap_pairs).  The
     reference records 6.8-8.6 ms per "blocksweep"/"serialweep" run
     (profiling/*.txt) for testSAP.cu, whose setup is 2,000,000 objects but
-    whose hardware and initialisation are not recorded.  The exact one-axis
-    sweep is slow on a uniform 3D field (each box sweeps every box whose
-    lower x lies within its x extent); the LBVH operator (sd_lbvh_pairs) gives
-    the same pair set quickly.  CUDA events on the current stream, mean over
-    `steps` calls after `warmup`."""
+    whose hardware and initialisation are not recorded.  The exact sweep is
+    binned into y-z columns (each box sweeps only the boxes of its own
+    columns); the LBVH operator (sd_lbvh_pairs) gives the same pair set.
+    CUDA events on the current stream, mean over `steps` calls after
+    `warmup` (each call includes its scratch allocation from torch's cache
+    and the read of the pair count)."""
     import torch
     import stardust_gb300 as sd
     g = torch.Generator(device="cpu").manual_seed(7)

@@ -296,7 +296,10 @@ sd_status sd_engine_update(sd_engine* h, float dt);
 
 /* Stages of one step, for profiling: launching CONTACT, SORT, REORDER in
  * that order is one step.  CONTACT alone is idempotent (it reads the
- * current state and writes the next-state buffers). */
+ * current state and writes the next-state buffers).  In a convex-hull scene
+ * CONTACT is the narrow phase (GJK, EPA, contact forces) of the last step's
+ * candidate lists at the current bodies, and the only stage: it changes no
+ * body, and the entry results it rewrites are rewritten by the next step. */
 #define SD_STAGE_CONTACT 0
 #define SD_STAGE_SORT 1
 #define SD_STAGE_REORDER 2
@@ -501,7 +504,9 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   for: 4 (64 registers) or 5 (48 registers, the default)
  *   "contact_block" threads per block of the per-sphere contact kernels: 64, 128 or 256
  *                   (default)
- *   "fix_blocks"    blocks per SM of the in-place reorder's fixed grid: 2, 4 or 8 (default) */
+ *   "fix_blocks"    blocks per SM of the in-place reorder's fixed grid: 2, 4 or 8 (default)
+ *   "hull_blocks"   convex-hull scenes: resident 128-thread blocks per SM the GJK kernel is
+ *                   compiled for: 3 (168 registers) or 4 (128, the default) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

@@ -1403,6 +1403,9 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
     } else if (k == "listed_blocks") {
         if (value != 4 && value != 5) return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4 or 5");
         sd::dem_set_listed_blocks(value);
+    } else if (k == "hull_blocks") {
+        if (value != 3 && value != 4) return fail(nullptr, SD_ERR_INVALID_ARG, "hull_blocks must be 3 or 4");
+        sd::hull_set_blocks(value);
     } else if (k == "skin_um") {
         if (value < 0 || value > 100000) return fail(nullptr, SD_ERR_INVALID_ARG, "skin_um must be in [0, 100000]");
         g_skin_um = value;
@@ -1432,6 +1435,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "listed_blocks") *value = sd::dem_listed_blocks();
     else if (k == "contact_block") *value = sd::dem_contact_block();
     else if (k == "fix_blocks") *value = sd::dem_fix_blocks();
+    else if (k == "hull_blocks") *value = sd::hull_blocks();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }
@@ -1547,7 +1551,10 @@ sd_status sd_engine_set_state(sd_engine* h, int32_t field, const void* host_src,
 sd_status sd_engine_launch_stage(sd_engine* h, int32_t stage, float dt) {
     if (!h) return fail(nullptr, SD_ERR_INVALID_ARG, "NULL engine");
     if (!h->prepared) return fail(h, SD_ERR_STATE, "call sd_engine_prepare first");
-    if (h->hull_mode()) return fail(h, SD_ERR_UNSUPPORTED, "not available for convex-hull scenes (use sd_engine_get_bodies)");
+    if (h->hull_mode()) {
+        if (stage != SD_STAGE_CONTACT) return fail(h, SD_ERR_UNSUPPORTED, "convex-hull scenes have the contact stage only");
+        return hull_launch_narrow(h);
+    }
     SD_CUDA(h, cudaSetDevice(h->device));
     sd_status s = resort_if_needed(h);
     if (s) return s;

@@ -115,6 +115,7 @@ uint64_t sd_tune_epoch();
 // hull mode (sd_hull_engine.cu)
 sd_status hull_prepare(sd_engine* h);
 sd_status hull_step(sd_engine* h, float dt, int32_t n_steps);
+sd_status hull_launch_narrow(sd_engine* h);
 sd_status hull_stats(sd_engine* h, sd_stats* out);
 sd_status hull_get_bodies(sd_engine* h, int32_t field, void* host_dst, size_t bytes);
 sd_status hull_get_state(sd_engine* h, int32_t field, void* host_dst, size_t bytes);

@@ -24,6 +24,7 @@ namespace sd {
 namespace {
 
 constexpr int kHullThreads = 128;
+constexpr int kEpaWarps = 4;  // warps per block of the EPA kernel
 constexpr int kGjkMaxIt = 64;
 // support evaluations a seeded GJK run gets to certify separation before the
 // plain run takes over
@@ -45,7 +46,6 @@ __device__ __forceinline__ float vdot(v3 a, v3 b) { return (a.x * b.x + a.y * b.
 __device__ __forceinline__ v3 vcross(v3 a, v3 b) {
     return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-__device__ __forceinline__ v3 vtriple(v3 a, v3 b, v3 c) { return vcross(vcross(a, b), c); }
 __device__ __forceinline__ bool vzero(v3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
 __device__ __forceinline__ v3 f3(float4 a) { return mk(a.x, a.y, a.z); }
 
@@ -238,61 +238,87 @@ __device__ int closest_simplex(Simplex* S, v3* v) {
     return 0;
 }
 
-/* GJK (distance form) on B - A from seed direction d0: v is the closest
+/* GJK (distance form) on B - A from a seed direction d0: v is the closest
  * point of the current simplex to the origin, the next support is taken in
- * -v, and the reference's test dot(w, d) < 0 ends it as separated.  Returns
- * the status, the number of support evaluations in *iters and, for a
- * separated pair, the separating search direction in *dir. */
-__device__ int gjk(const HPair& P, v3 d0, Simplex* S, int* iters, v3* dir, int max_it = kGjkMaxIt) {
-    v3 d = d0;
-    if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
-    Cso p = cso(P, d);
-    int it = 1;
-    *dir = d;
-    if (vdot(p.w, d) < 0.0f) {
-        *iters = it;
-        return kSep;
+ * -v, and the reference's test dot(w, d) < 0 ends it as separated; a
+ * support point seen before in the run ends it as touching (no further
+ * progress is possible: the origin is on the boundary of B - A within
+ * rounding); a simplex that encloses the origin ends it as a hit; a zero
+ * |v| as touching; max_it supports without an end as not converged.
+ *
+ * Run over a sequence of attempts: attempt a starts from d0[a] and may take
+ * max_it[a] supports; the first attempt that certifies separation, or the
+ * last attempt, decides.  Each attempt is a whole GJK run from its seed
+ * (its own simplex and seen supports), but all attempts run in one loop
+ * with one support call per pass, so the threads of a warp in different
+ * attempts still share that call.  Returns the status; *iters =
+ * supports over all attempts run, *which = the deciding attempt, *dir and
+ * *S of the deciding attempt. */
+struct GjkAttempts {
+    v3 d0[3];
+    int max_it[3];
+    int n;
+    // selects, not indexing, so that the attempts stay in registers
+    __device__ __forceinline__ v3 seed(int a) const { return a == 0 ? d0[0] : (a == 1 ? d0[1] : d0[2]); }
+    __device__ __forceinline__ int limit(int a) const {
+        return a == 0 ? max_it[0] : (a == 1 ? max_it[1] : max_it[2]);
     }
-    S->s[0] = p;
-    S->n = 1;
+};
+
+__device__ int gjk_attempts(const HPair& P, const GjkAttempts& at, Simplex* S, int* iters, v3* dir, int* which) {
+    int a = 0, it = 0, total = 0;
+    bool first = true;
     uint32_t seen[kGjkMaxIt];
-    seen[0] = p.key;
-    v3 v = p.w;
-    float vv = vdot(v, v);
+    v3 v = mk(0.f, 0.f, 0.f);
+    float vv = 0.0f;
     for (;;) {
-        if (vv == 0.0f) {
-            *iters = it;
-            return kTouch;
+        v3 d;
+        if (first) {
+            d = at.seed(a);
+            if (vzero(d)) d = mk(1.0f, 0.0f, 0.0f);
+            it = 0;
+        } else {
+            d = vneg(v);
         }
-        if (it >= max_it) {
-            *iters = it;
-            return kNoConv;
-        }
-        d = vneg(v);
         *dir = d;
-        p = cso(P, d);
+        const Cso p = cso(P, d);
         ++it;
+        int st = -1;
         if (vdot(p.w, d) < 0.0f) {
-            *iters = it;
-            return kSep;
-        }
-        /* a support point seen before in this run: no further progress is
-         * possible (the origin is on the boundary of B - A within rounding) */
-        for (int k = 0; k < it - 1; ++k) {
-            if (seen[k] == p.key) {
-                *iters = it;
-                return kTouch;
+            st = kSep;
+        } else if (first) {
+            S->s[0] = p;
+            S->n = 1;
+            seen[0] = p.key;
+            v = p.w;
+            vv = vdot(v, v);
+            first = false;
+        } else {
+            for (int k = 0; k < it - 1; ++k)
+                if (seen[k] == p.key) st = kTouch;
+            if (st < 0) {
+                seen[it - 1] = p.key;
+                for (int k = S->n; k > 0; --k) S->s[k] = S->s[k - 1];
+                S->s[0] = p;
+                S->n += 1;
+                if (closest_simplex(S, &v)) st = kHit;
+                else vv = vdot(v, v);
             }
         }
-        seen[it - 1] = p.key;
-        for (int k = S->n; k > 0; --k) S->s[k] = S->s[k - 1];
-        S->s[0] = p;
-        S->n += 1;
-        if (closest_simplex(S, &v)) {
-            *iters = it;
-            return kHit;
+        if (st < 0) {  // the tests made before the next support
+            if (vv == 0.0f) st = kTouch;
+            else if (it >= at.limit(a)) st = kNoConv;
         }
-        vv = vdot(v, v);
+        if (st >= 0) {
+            total += it;
+            if (st == kSep || a + 1 >= at.n) {
+                *iters = total;
+                *which = a;
+                return st;
+            }
+            ++a;
+            first = true;
+        }
     }
 }
 
@@ -351,16 +377,119 @@ struct Contact {
     bool ok;
 };
 
-__device__ void epa(const HPair& P, const Simplex& S, float tol, Contact* out) {
+// ---------------------------------------------------------------- EPA
+// One warp per intersecting pair; the polytope lives in shared memory.  The
+// warp splits the scans (faces, vertices of the support calls, duplicate
+// keys, face visibility, new faces) and keeps the sequential algorithm's
+// choices exactly: the first face of least distance, the first vertex of
+// largest dot product, kept faces and new faces in list order; lane 0 alone
+// builds the horizon edge list (its order decides the new faces' order).
+
+constexpr uint32_t kFull = 0xffffffffu;
+
+struct EpaShared {
     Cso V[kEpaMaxV];
     Face F[kEpaMaxF];
     uint8_t E[3 * kEpaMaxF][2];
+};
+
+// support() by a warp: the first vertex (lowest index) of largest dot
+// product, as the sequential scan's strict '>' from vertex 0 picks (a NaN
+// product never wins, and a NaN at vertex 0 keeps vertex 0).
+__device__ __forceinline__ uint32_t support_warp(const HBody& h, v3 d, v3* out) {
+    const uint32_t lane = threadIdx.x & 31;
+    const v3 db = rotT(h.R, d);
+    float bd = 0.0f;
+    uint32_t best = 0xffffffffu;
+    for (uint32_t k = lane; k < h.nv; k += 32) {
+        const float t = vdot(db, f3(__ldg(h.V + k)));
+        if (t != t) continue;
+        if (best == 0xffffffffu || t > bd) {
+            bd = t;
+            best = k;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, bd, o);
+        const uint32_t oi = __shfl_xor_sync(kFull, best, o);
+        if (oi != 0xffffffffu && (best == 0xffffffffu || ob > bd || (ob == bd && oi < best))) {
+            bd = ob;
+            best = oi;
+        }
+    }
+    const float t0 = vdot(db, f3(__ldg(h.V)));
+    if (t0 != t0 || best == 0xffffffffu) best = 0;
+    *out = rot(h.R, f3(__ldg(h.V + best)));
+    return best;
+}
+
+__device__ __forceinline__ Cso cso_warp(const HPair& P, v3 d) {
+    Cso r;
+    const uint32_t ia = support_warp(P.A, vneg(d), &r.a);
+    v3 bb;
+    const uint32_t ib = support_warp(P.B, d, &bb);
+    r.b = vadd(bb, P.off);
+    r.w = vsub(r.b, r.a);
+    r.key = ia * 1024u + ib;
+    return r;
+}
+
+// The support point a key names (key = ia * 1024 + ib): the same arithmetic
+// as cso(), so the same bits.
+__device__ __forceinline__ Cso cso_of_key(const HPair& P, uint32_t key) {
+    Cso r;
+    r.a = rot(P.A.R, f3(__ldg(P.A.V + (key >> 10))));
+    const v3 bb = rot(P.B.R, f3(__ldg(P.B.V + (key & 1023u))));
+    r.b = vadd(bb, P.off);
+    r.w = vsub(r.b, r.a);
+    r.key = key;
+    return r;
+}
+
+// The sequential "best = 0; if (F[k].dist < F[best].dist) best = k" by a
+// warp: the first face of least distance (NaN never wins; NaN at face 0
+// keeps face 0).
+__device__ __forceinline__ int closest_face_warp(const Face* F, int nf) {
+    const int lane = threadIdx.x & 31;
+    float bd = 0.0f;
+    int best = -1;
+    for (int k = lane; k < nf; k += 32) {
+        const float t = F[k].dist;
+        if (t != t) continue;
+        if (best < 0 || t < bd) {
+            bd = t;
+            best = k;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, bd, o);
+        const int oi = __shfl_xor_sync(kFull, best, o);
+        if (oi >= 0 && (best < 0 || ob < bd || (ob == bd && oi < best))) {
+            bd = ob;
+            best = oi;
+        }
+    }
+    const float d0 = F[0].dist;
+    return (d0 != d0 || best < 0) ? 0 : best;
+}
+
+/* EPA from GJK's enclosing tetrahedron s[0..3] (every lane holds it):
+ * expands the polytope of B - A towards the origin's closest face until the
+ * support gains at most tol (or repeats a vertex, or a capacity is reached);
+ * the contact is that face's plane (normal -n, depth) and the midpoint of
+ * the witness points at the origin's projection.  Every lane returns the
+ * same *out. */
+__device__ void epa_warp(const HPair& P, const Cso* s, float tol, EpaShared& sh, Contact* out) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
     int nv = 4, nf = 0;
-    for (int k = 0; k < 4; ++k) V[k] = S.s[k];
+    __syncwarp();  // the previous pair's reads of the polytope are done
+    if (lane < 4) sh.V[lane] = s[lane];
+    __syncwarp();
     const uint8_t init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
     for (int k = 0; k < 4; ++k) {
         Face f;
-        if (!face_make(V, init[k][0], init[k][1], init[k][2], &f)) continue;
+        if (!face_make(sh.V, init[k][0], init[k][1], init[k][2], &f)) continue;
         if (f.dist < 0.0f) {
             const uint8_t t = f.i[1];
             f.i[1] = f.i[2];
@@ -368,64 +497,99 @@ __device__ void epa(const HPair& P, const Simplex& S, float tol, Contact* out) {
             f.n = vneg(f.n);
             f.dist = -f.dist;
         }
-        F[nf++] = f;
+        if (lane == 0) sh.F[nf] = f;
+        ++nf;
     }
     out->ok = false;
     out->epa_iters = 0;
+    __syncwarp();
     if (nf == 0) return;
     int best = 0;
     for (int it = 0;; ++it) {
-        best = 0;
-        for (int k = 1; k < nf; ++k)
-            if (F[k].dist < F[best].dist) best = k;
+        best = closest_face_warp(sh.F, nf);
         out->epa_iters = it + 1;
         if (it >= kEpaMaxIt || nv >= kEpaMaxV) break;
-        const Cso p = cso(P, F[best].n);
+        const Face fb = sh.F[best];
+        const Cso p = cso_warp(P, fb.n);
         bool dup = false;
-        for (int k = 0; k < nv; ++k) dup |= V[k].key == p.key;
-        if (dup || vdot(p.w, F[best].n) - F[best].dist <= tol) break;
+        for (int k = lane; k < nv; k += 32) dup |= sh.V[k].key == p.key;
+        if (__any_sync(kFull, dup) || vdot(p.w, fb.n) - fb.dist <= tol) break;
         const uint8_t q = (uint8_t)nv;
-        V[nv++] = p;
-        int ne = 0, keep = 0;
-        for (int k = 0; k < nf; ++k) {
-            if (vdot(F[k].n, vsub(p.w, V[F[k].i[0]].w)) > 0.0f) {
+        // faces that see p (before any face moves)
+        uint32_t vis[(kEpaMaxF + 31) / 32];
+        for (int c = 0; c < (kEpaMaxF + 31) / 32; ++c) {
+            const int k = 32 * c + lane;
+            bool v = false;
+            if (k < nf) v = vdot(sh.F[k].n, vsub(p.w, sh.V[sh.F[k].i[0]].w)) > 0.0f;
+            vis[c] = __ballot_sync(kFull, v);
+        }
+        __syncwarp();
+        if (lane == 0) sh.V[nv] = p;
+        ++nv;
+        // horizon: edges of the visible faces in face order, an edge met
+        // again reversed cancels (the last edge moves into its place)
+        int ne = 0;
+        if (lane == 0) {
+            for (int k = 0; k < nf; ++k) {
+                if (!((vis[k >> 5] >> (k & 31)) & 1u)) continue;
                 for (int e = 0; e < 3; ++e) {
-                    const uint8_t a = F[k].i[e], b = F[k].i[(e + 1) % 3];
+                    const uint8_t a = sh.F[k].i[e], b = sh.F[k].i[(e + 1) % 3];
                     int found = -1;
                     for (int m = 0; m < ne; ++m)
-                        if (E[m][0] == b && E[m][1] == a) {
+                        if (sh.E[m][0] == b && sh.E[m][1] == a) {
                             found = m;
                             break;
                         }
                     if (found >= 0) {
-                        E[found][0] = E[ne - 1][0];
-                        E[found][1] = E[ne - 1][1];
+                        sh.E[found][0] = sh.E[ne - 1][0];
+                        sh.E[found][1] = sh.E[ne - 1][1];
                         --ne;
                     } else {
-                        E[ne][0] = a;
-                        E[ne][1] = b;
+                        sh.E[ne][0] = a;
+                        sh.E[ne][1] = b;
                         ++ne;
                     }
                 }
-            } else {
-                F[keep++] = F[k];
             }
+        }
+        ne = __shfl_sync(kFull, ne, 0);
+        __syncwarp();
+        // the faces that do not see p, compacted in order (a face moves to
+        // an index at or below its own: read a chunk, then write it)
+        int keep = 0;
+        for (int c = 0; 32 * c < nf; ++c) {
+            const int k = 32 * c + lane;
+            const bool kept = k < nf && !((vis[c] >> lane) & 1u);
+            Face f;
+            if (kept) f = sh.F[k];
+            const uint32_t m = __ballot_sync(kFull, kept);
+            __syncwarp();
+            if (kept) sh.F[keep + __popc(m & lt)] = f;
+            keep += __popc(m);
+            __syncwarp();
         }
         nf = keep;
         if (nf + ne > kEpaMaxF) break;
-        for (int m = 0; m < ne; ++m) {
+        // new faces (edge, p) in edge order; degenerate ones are dropped
+        for (int c = 0; 32 * c < ne; ++c) {
+            const int m = 32 * c + lane;
             Face f;
-            if (face_make(V, E[m][0], E[m][1], q, &f)) F[nf++] = f;
+            const bool ok = m < ne && face_make(sh.V, sh.E[m][0], sh.E[m][1], q, &f);
+            const uint32_t mk_ = __ballot_sync(kFull, ok);
+            if (ok) sh.F[nf + __popc(mk_ & lt)] = f;
+            nf += __popc(mk_);
         }
+        __syncwarp();
         if (nf == 0) return;
     }
-    Cso t[3] = {V[F[best].i[0]], V[F[best].i[1]], V[F[best].i[2]]};
+    Cso t[3] = {sh.V[sh.F[best].i[0]], sh.V[sh.F[best].i[1]], sh.V[sh.F[best].i[2]]};
+    __syncwarp();  // the polytope is read: the next pair may overwrite it
     for (int a = 0; a < 2; ++a)
         for (int b = 0; b < 2 - a; ++b)
             if (t[b].key > t[b + 1].key) {
-                const Cso s = t[b];
+                const Cso s2 = t[b];
                 t[b] = t[b + 1];
-                t[b + 1] = s;
+                t[b + 1] = s2;
             }
     const v3 e0 = vsub(t[1].w, t[0].w), e1 = vsub(t[2].w, t[0].w);
     const v3 nn = vcross(e0, e1);
@@ -591,23 +755,33 @@ __global__ void hull_unique_fill_kernel(HullBuffers H) {
         if (H.partners[e] > b) H.ulist[w++] = e;
 }
 
-// Narrow phase of one pair (A, B), A < B, from its entry in A's list: GJK
-// (seeded or plain), EPA on a hit, contact force; the entry of A and its
-// mirror in B's list (binary search: lists are ascending) receive the
-// force and torque on their own body, the same status and direction.
-__global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, HullBuffers H) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t total = H.off[H.nb];
-    if ((uint64_t)total > H.cap || u >= H.upos[H.nb]) return;  // an overflowed step is reported, not evaluated
-    const uint32_t e = H.ulist[u];
-    const uint32_t A = H.self[e], B = H.partners[e];
+// The mirror entry (B, A) of the unique entry e = (A, B): binary search in
+// B's ascending partner list.
+__device__ __forceinline__ uint32_t mirror_entry(const HullBuffers& H, uint32_t A, uint32_t B) {
     uint32_t lo = H.off[B], hi = H.off[B + 1];
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (H.partners[mid] < A) lo = mid + 1;
         else hi = mid;
     }
-    const uint32_t em = lo;  // the mirror entry (B, A)
+    return lo;
+}
+
+// Narrow phase, part 1, one thread per unique pair (A, B), A < B, from its
+// entry in A's list: GJK (seeded or plain).  A separated or touching pair is
+// finished here -- its entry and its mirror in B's list get the status, the
+// direction and zero force; a pair GJK found intersecting goes to the hit
+// list for hull_epa_kernel.  Split so that GJK, which every pair runs, does
+// not carry EPA's registers and polytope (the hits are a few per cent).
+// MINB: resident blocks per SM it is compiled for (knob "hull_blocks").
+template <int MINB>
+__global__ void __launch_bounds__(kHullThreads, MINB) hull_gjk_kernel(HullBuffers H) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t total = H.off[H.nb];
+    if ((uint64_t)total > H.cap || u >= H.upos[H.nb]) return;  // an overflowed step is reported, not evaluated
+    const uint32_t e = H.ulist[u];
+    const uint32_t A = H.self[e], B = H.partners[e];
+    const uint32_t em = mirror_entry(H, A, B);
     HPair P;
     make_pair(H, A, B, &P);
     v3 d0 = vneg(P.off);
@@ -625,38 +799,82 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
     // network's direction -- trained on the pairs whose anchor failed -- with
     // one more only when the anchor fails.
     const bool learned = seeded && H.keep_anchor && H.feat;
-    bool anchor_failed = false, certified_by_anchor = false;
-    int st;
+    // the plain run decides whenever no seed certifies
+    GjkAttempts at;
     if (learned) {
-        const v3 anchor = rot(P.A.R, mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9],
-                                        H.feat[16 * (size_t)e + 10]));
-        st = gjk(P, anchor, &S, &iters, &dir, 1);
-        certified_by_anchor = st == kSep;
-        if (!certified_by_anchor) {
-            anchor_failed = true;
-            int it1 = 0;
-            st = gjk(P, d0, &S, &it1, &dir, 1);
-            iters += it1;
-        }
+        at = {{rot(P.A.R, mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9], H.feat[16 * (size_t)e + 10])),
+               d0, vneg(P.off)},
+              {1, 1, kGjkMaxIt},
+              3};
+    } else if (seeded) {
+        at = {{d0, vneg(P.off), vneg(P.off)}, {kSeedMaxIt, kGjkMaxIt, kGjkMaxIt}, 2};
     } else {
-        st = gjk(P, d0, &S, &iters, &dir, seeded ? kSeedMaxIt : kGjkMaxIt);
+        at = {{vneg(P.off), vneg(P.off), vneg(P.off)}, {kGjkMaxIt, kGjkMaxIt, kGjkMaxIt}, 1};
     }
-    if (seeded && st != kSep) {
-        int it2 = 0;
-        st = gjk(P, vneg(P.off), &S, &it2, &dir);
-        iters += it2;
-    }
-    v3 fa = mk(0.f, 0.f, 0.f), ta = mk(0.f, 0.f, 0.f), fbv = mk(0.f, 0.f, 0.f), tb = mk(0.f, 0.f, 0.f);
-    int epa_it = 0;
+    int which = 0;
+    const int st = gjk_attempts(P, at, &S, &iters, &dir, &which);
+    const bool certified_by_anchor = learned && which == 0;
+    const bool anchor_failed = learned && which > 0;
     // final direction in A's frame (seed of the next step); with learned
     // seeds a seed's certificate keeps the anchor it was predicted from
     const v3 dA = certified_by_anchor
                       ? mk(H.feat[16 * (size_t)e + 8], H.feat[16 * (size_t)e + 9], H.feat[16 * (size_t)e + 10])
                       : rotT(P.A.R, dir);
-    if (st == kHit) {
+    const float4 d4 = make_float4(dA.x, dA.y, dA.z, st == kSep ? 1.0f : 0.0f);
+    const bool mirror = em < H.off[B + 1];  // always true for consistent lists
+    H.dir[e] = d4;
+    if (mirror) H.dir[em] = d4;
+    if (H.teach && *H.teach_on) {
+        // a training step: the max-margin direction of a separated pair
+        // whose anchor failed (the cases the network's seed is tried on)
+        v3 m;
+        const bool ok = st == kSep && anchor_failed && gjk_margin_dir(P, dir, &m);
+        const v3 mA = rotT(P.A.R, m);
+        H.teach[e] = ok ? make_float4(mA.x, mA.y, mA.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mirror) H.teach[em] = make_float4(0.f, 0.f, 0.f, 0.f);  // one sample per pair
+    }
+    if (st == kHit) {  // EPA and the contact force in hull_epa_kernel
+        const uint32_t k = atomicAdd(H.hit_count, 1u);  // k < unique pairs <= cap / 2 + 1
+        H.hits[k] = make_uint2(u, (uint32_t)iters);
+        H.hit_keys[k] = make_uint4(S.s[0].key, S.s[1].key, S.s[2].key, S.s[3].key);
+        return;
+    }
+    const uint32_t info = (uint32_t)st | ((uint32_t)iters << 8);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    H.ef[e] = z;
+    H.et[e] = z;
+    H.info[e] = info;
+    if (mirror) {
+        H.ef[em] = z;
+        H.et[em] = z;
+        H.info[em] = info;
+    }
+}
+
+// Narrow phase, part 2, one warp per pair GJK found intersecting: EPA from
+// GJK's enclosing tetrahedron (rebuilt from its support keys), the contact
+// force at the EPA point; A's entry and B's mirror get forces of opposite
+// sign -- exact action = reaction, no atomics.  Warps stride over the hit
+// count.
+__global__ void __launch_bounds__(kEpaWarps * 32) hull_epa_kernel(HullParams p, HullBuffers H) {
+    __shared__ EpaShared polytope[kEpaWarps];
+    EpaShared& sh = polytope[threadIdx.x >> 5];
+    const uint32_t n_hits = *H.hit_count;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_hits; k += nwarps) {
+        const uint2 hit = H.hits[k];
+        const uint4 keys = H.hit_keys[k];
+        const uint32_t e = H.ulist[hit.x];
+        const uint32_t A = H.self[e], B = H.partners[e];
+        const uint32_t em = mirror_entry(H, A, B);
+        HPair P;
+        make_pair(H, A, B, &P);
+        const Cso s[4] = {cso_of_key(P, keys.x), cso_of_key(P, keys.y), cso_of_key(P, keys.z), cso_of_key(P, keys.w)};
+        int st = kHit;
+        v3 fa = mk(0.f, 0.f, 0.f), ta = mk(0.f, 0.f, 0.f), fbv = mk(0.f, 0.f, 0.f), tb = mk(0.f, 0.f, 0.f);
         Contact c;
-        epa(P, S, (H.iinv[A].w + H.iinv[B].w) * 1e-7f, &c);
-        epa_it = c.epa_iters;
+        epa_warp(P, s, (H.iinv[A].w + H.iinv[B].w) * 1e-7f, sh, &c);
         // contact skin: overlaps within it (float GJK cannot resolve them
         // reliably) carry no force and the spring acts on depth - skin
         const float skin = (H.iinv[A].w + H.iinv[B].w) * 1e-4f;
@@ -674,27 +892,17 @@ __global__ void __launch_bounds__(kHullThreads) hull_pair_kernel(HullParams p, H
             fa = vneg(fbv);
             ta = vcross(rA, fa);
         }
-    }
-    const uint32_t info = (uint32_t)st | ((uint32_t)iters << 8) | ((uint32_t)epa_it << 16);
-    const float4 d4 = make_float4(dA.x, dA.y, dA.z, st == kSep ? 1.0f : 0.0f);
-    H.ef[e] = make_float4(fa.x, fa.y, fa.z, 0.f);
-    H.et[e] = make_float4(ta.x, ta.y, ta.z, 0.f);
-    H.info[e] = info;
-    H.dir[e] = d4;
-    if (H.teach && *H.teach_on) {
-        // a training step: the max-margin direction of a separated pair
-        // whose anchor failed (the cases the network's seed is tried on)
-        v3 m;
-        const bool ok = st == kSep && anchor_failed && gjk_margin_dir(P, dir, &m);
-        const v3 mA = rotT(P.A.R, m);
-        H.teach[e] = ok ? make_float4(mA.x, mA.y, mA.z, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (em < H.off[B + 1]) H.teach[em] = make_float4(0.f, 0.f, 0.f, 0.f);  // one sample per pair
-    }
-    if (em < H.off[B + 1]) {  // always true for consistent lists
-        H.ef[em] = make_float4(fbv.x, fbv.y, fbv.z, 0.f);
-        H.et[em] = make_float4(tb.x, tb.y, tb.z, 0.f);
-        H.info[em] = info;
-        H.dir[em] = d4;
+        if (lane == 0) {
+            const uint32_t info = (uint32_t)st | (hit.y << 8) | ((uint32_t)c.epa_iters << 16);
+            H.ef[e] = make_float4(fa.x, fa.y, fa.z, 0.f);
+            H.et[e] = make_float4(ta.x, ta.y, ta.z, 0.f);
+            H.info[e] = info;
+            if (em < H.off[B + 1]) {
+                H.ef[em] = make_float4(fbv.x, fbv.y, fbv.z, 0.f);
+                H.et[em] = make_float4(tb.x, tb.y, tb.z, 0.f);
+                H.info[em] = info;
+            }
+        }
     }
 }
 
@@ -808,13 +1016,22 @@ cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st) {
 // Each pair is evaluated once, by one thread, into both of its entries.
 // The grid covers the largest possible pair count (cap / 2); threads past
 // the step's count return at once.
+static int g_hull_blocks = 4;
+void hull_set_blocks(int b) { g_hull_blocks = b == 3 ? 3 : 4; }
+int hull_blocks() { return g_hull_blocks; }
+
 cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st) {
     if (H.nb == 0 || H.cap == 0) return cudaSuccess;
     hull_unique_count_kernel<<<grid_for(H.nb, 256), 256, 0, st>>>(H);
     cudaError_t e = scan_exclusive_async(H.ucount, H.upos, H.nb, H.uscan, st);
     if (e != cudaSuccess) return e;
     hull_unique_fill_kernel<<<grid_for(H.nb, 256), 256, 0, st>>>(H);
-    hull_pair_kernel<<<grid_for(H.cap / 2 + 1, kHullThreads), kHullThreads, 0, st>>>(p, H);
+    if ((e = cudaMemsetAsync(H.hit_count, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+    if (g_hull_blocks == 3)
+        hull_gjk_kernel<3><<<grid_for(H.cap / 2 + 1, kHullThreads), kHullThreads, 0, st>>>(H);
+    else
+        hull_gjk_kernel<4><<<grid_for(H.cap / 2 + 1, kHullThreads), kHullThreads, 0, st>>>(H);
+    hull_epa_kernel<<<152 * 4, kEpaWarps * 32, 0, st>>>(p, H);
     return cudaGetLastError();
 }
 

@@ -205,7 +205,9 @@ sd_status hull_prepare(sd_engine* h) {
         (s = halloc(h, &H.info, cap)) || (s = halloc(h, &H.seeds, cap)) || (s = halloc(h, &H.feat, 16 * cap)) ||
         (s = halloc(h, &S.stats, 4)) || (s = halloc(h, &H.ucount, nb)) || (s = halloc(h, &H.upos, (size_t)nb + 1)) ||
         (s = halloc(h, &H.ulist, cap / 2 + 1)) || (s = halloc(h, &H.uscan, sd::scan_scratch_words(nb) + 1)) ||
-        (s = halloc(h, &H.teach, cap)) || (s = halloc(h, &S.teach_flag, 4)))
+        (s = halloc(h, &H.teach, cap)) || (s = halloc(h, &S.teach_flag, 4)) ||
+        (s = halloc(h, &H.hit_count, 1)) || (s = halloc(h, &H.hits, cap / 2 + 1)) ||
+        (s = halloc(h, &H.hit_keys, cap / 2 + 1)))
         return s;
     H.teach_on = S.teach_flag;
     for (int k = 0; k < 2; ++k)
@@ -297,6 +299,29 @@ sd_status hull_step(sd_engine* h, float dt, int32_t n_steps) {
         S.parity ^= 1;
     }
     h->steps += (uint64_t)n_steps;
+    return SD_OK;
+}
+
+// The narrow phase alone, for timing between steps: GJK, EPA and the
+// contact forces of the last step's candidate lists at the current bodies,
+// into the entry buffers.  No body changes; the entry results it rewrites
+// (status, forces, directions) are rewritten by the next step, and its
+// directions only seed that step's GJK where seeding is on (seeds move
+// iteration counts, never the state).
+sd_status hull_launch_narrow(sd_engine* h) {
+    HullScene& S = h->hull;
+    if (!S.graph_valid || h->steps == 0) return sd_fail(h, SD_ERR_STATE, "step the hull scene once first");
+    HULL_CUDA(h, cudaSetDevice(h->device));
+    const int par = S.parity ^ 1;  // the buffers of the last step
+    sd::HullBuffers H = S.H;
+    H.off = S.off[par];
+    H.partners = S.partners[par];
+    H.dir = S.dir[par];
+    H.prev_off = S.off[par ^ 1];
+    H.prev_partners = S.partners[par ^ 1];
+    H.prev_dir = S.dir[par ^ 1];
+    H.keep_anchor = S.seed_mode == SD_GJK_SEED_LEARNED;
+    HULL_CUDA(h, sd::hull_narrow_async(S.P, H, h->stream));
     return SD_OK;
 }
 

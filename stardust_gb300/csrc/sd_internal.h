@@ -83,9 +83,11 @@ struct Lbvh {
     uint32_t* visit;                     // refit arrival counters
     float4 *node_lo, *node_hi, *leaf_lo, *leaf_hi;
     uint32_t* counts;                    // per box id
+    uint32_t* first;                     // per leaf: its first kLbvhFirst partners found (counting pass)
     uint32_t* scan_scratch;
     uint32_t* status;                    // device error bits
 };
+constexpr int kLbvhFirst = 16;
 uint64_t lbvh_scratch_bytes(uint32_t n);
 void lbvh_carve(void* scratch, uint32_t n, Lbvh* t);
 cudaError_t lbvh_morton_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
@@ -148,6 +150,12 @@ struct HullBuffers {
     // previous direction (inputs 8..10, the anchor) as the next step's, so
     // the network is never fed its own outputs
     bool keep_anchor;
+    // the pairs GJK found intersecting, for the EPA kernel: count, and per
+    // hit the unique-pair index and the GJK support evaluations spent, and
+    // the support keys of the enclosing tetrahedron
+    uint32_t* hit_count;
+    uint2* hits;
+    uint4* hit_keys;
     const uint32_t *prev_off, *prev_partners;  // the previous step's lists
     const float4* prev_dir;
     float4 *force, *torque;                // optional per body totals
@@ -156,6 +164,8 @@ struct HullBuffers {
 cudaError_t hull_aabb_async(HullBuffers& H, cudaStream_t st);
 cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st);
 cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
+void hull_set_blocks(int b);
+int hull_blocks();
 cudaError_t hull_integrate_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
 cudaError_t hull_stats_async(HullBuffers& H, unsigned long long* out, cudaStream_t st);
 

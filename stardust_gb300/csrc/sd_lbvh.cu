@@ -239,22 +239,53 @@ __global__ void refit_kernel(int n, const uint32_t* __restrict__ vals, const flo
 }
 
 // Traversal of leaf k (sorted position) against the tree.  WRITE == false:
-// count[id] = number of partners.  WRITE == true: partners of body id at
-// [off[id], off[id+1]), ascending, and self[] of each entry.
+// count[id] = number of partners, and the first kLbvhFirst partners found
+// into first[k * kLbvhFirst ...].  WRITE == true: partners of body id at
+// [off[id], off[id+1]), ascending, and self[] of each entry -- sorted from
+// first[] when the counting pass kept them all, else found by a second
+// traversal.
 template <bool WRITE>
 __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const float4* __restrict__ leaf_lo,
                              const float4* __restrict__ leaf_hi, const float4* __restrict__ node_lo,
                              const float4* __restrict__ node_hi, const int2* __restrict__ children,
                              uint32_t* __restrict__ count, const uint32_t* __restrict__ off,
                              uint32_t* __restrict__ partners, uint32_t* __restrict__ self, uint64_t cap,
-                             uint32_t* __restrict__ status) {
+                             uint32_t* __restrict__ first, uint32_t* __restrict__ status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t id = vals[k];
-    const float4 qlo = leaf_lo[k], qhi = leaf_hi[k];
     uint32_t c = 0;
     const uint32_t base = WRITE ? off[id] : 0u;
     const uint32_t lim = WRITE ? off[id + 1] : 0u;
+    if (WRITE && lim - base <= (uint32_t)kLbvhFirst) {
+        if ((uint64_t)lim > cap) {
+            atomicOr(status, kErrPairOverflow);
+            return;
+        }
+        // the partners the counting pass kept: sorted in registers (a
+        // network over kLbvhFirst values; ids are distinct, so the order
+        // is the ascending one)
+        uint32_t v[kLbvhFirst];
+#pragma unroll
+        for (int i = 0; i < kLbvhFirst; ++i) v[i] = (uint32_t)i < lim - base ? first[(size_t)k * kLbvhFirst + i] : 0xffffffffu;
+#pragma unroll
+        for (int a = 0; a < kLbvhFirst; ++a)
+#pragma unroll
+            for (int b = (a & 1); b + 1 < kLbvhFirst; b += 2)
+                if (v[b] > v[b + 1]) {
+                    const uint32_t t = v[b];
+                    v[b] = v[b + 1];
+                    v[b + 1] = t;
+                }
+#pragma unroll
+        for (int i = 0; i < kLbvhFirst; ++i)
+            if ((uint32_t)i < lim - base) {
+                partners[base + i] = v[i];
+                self[base + i] = id;
+            }
+        return;
+    }
+    const float4 qlo = leaf_lo[k], qhi = leaf_hi[k];
     if (n > 1) {
         int stack[kStack];
         int sp = 0;
@@ -276,6 +307,8 @@ __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const flo
                     if (WRITE) {
                         const uint32_t e = base + c;
                         if (e < lim && (uint64_t)e < cap) partners[e] = vals[j];
+                    } else if (c < (uint32_t)kLbvhFirst) {
+                        first[(size_t)k * kLbvhFirst + c] = vals[j];
                     }
                     ++c;
                 } else if (box_overlap(qlo, qhi, node_lo[x], node_hi[x])) {
@@ -367,6 +400,7 @@ uint64_t lbvh_scratch_bytes(uint32_t n) {
     b += align256(8 * m) + align256(4 * (2 * m)) + align256(4 * m); // children, parent, visit
     b += 4 * align256(16 * m);                                     // node lo/hi, leaf lo/hi
     b += align256(4 * (m + 1)) + align256(4 * scan_scratch_words((uint32_t)m + 1));
+    b += align256(4 * kLbvhFirst * m);                             // first partners per leaf
     b += align256(4 * 4);                                          // status
     return b;
 }
@@ -396,6 +430,7 @@ void lbvh_carve(void* scratch, uint32_t n, Lbvh* t) {
     t->leaf_hi = (float4*)take(16 * m);
     t->counts = (uint32_t*)take(4 * (m + 1));
     t->scan_scratch = (uint32_t*)take(4 * scan_scratch_words((uint32_t)m + 1));
+    t->first = (uint32_t*)take(4 * kLbvhFirst * m);
     t->status = (uint32_t*)take(16);
     t->skeys = t->keys;
     t->svals = t->vals;
@@ -440,12 +475,12 @@ cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint
     if (n == 0) return cudaMemsetAsync(off, 0, 4, st);
     query_kernel<false><<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(
         (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.node_lo, t.node_hi, t.children, t.counts, nullptr, nullptr, nullptr,
-        0, t.status);
+        0, t.first, t.status);
     cudaError_t e = scan_exclusive_async(t.counts, off, n, t.scan_scratch, st);
     if (e != cudaSuccess) return e;
     query_kernel<true><<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(
         (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.node_lo, t.node_hi, t.children, nullptr, off, partners, self, cap,
-        t.status);
+        t.first, t.status);
     return cudaGetLastError();
 }
 

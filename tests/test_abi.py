@@ -347,3 +347,17 @@ def test_skin_knob(sdlib):
                 _abi.tune_set("skin_um", v)
     finally:
         _abi.tune_set("skin_um", old)
+
+
+def test_hull_blocks_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("hull_blocks")
+    assert old == 4
+    try:
+        _abi.tune_set("hull_blocks", 3)
+        assert _abi.tune_get("hull_blocks") == 3
+        for v in (0, 2, 5):
+            with pytest.raises(Exception):
+                _abi.tune_set("hull_blocks", v)
+    finally:
+        _abi.tune_set("hull_blocks", old)

@@ -86,16 +86,21 @@ def oracle_params(orc, cfg, dt):
                            cfg.gravity, dt, cfg.walls)
 
 
-@pytest.mark.parametrize("steps", [1, 5, 40])
-def test_hull_steps_bit_exact(sdlib, orc, steps):
+@pytest.mark.parametrize("steps,hull_blocks", [(1, 4), (5, 4), (40, 4), (40, 3)])
+def test_hull_steps_bit_exact(sdlib, orc, steps, hull_blocks):
     from stardust_gb300 import _abi
     eng, cfg, dt = hull_engine(sdlib)
     H = oracle_hulls(orc, eng)
     p = oracle_params(orc, cfg, dt)
     for _ in range(steps):
         out = H.step(p, record=True)
-    eng.step(dt, steps)
-    eng.sync()
+    old = _abi.tune_get("hull_blocks")
+    try:
+        _abi.tune_set("hull_blocks", hull_blocks)
+        eng.step(dt, steps)
+        eng.sync()
+    finally:
+        _abi.tune_set("hull_blocks", old)
     st = eng.stats()
     assert st["device_errors"] == 0
     for k, f in (("pos", _abi.SD_BODY_POSITION), ("vel", _abi.SD_BODY_VELOCITY), ("quat", _abi.SD_BODY_QUATERNION),
@@ -143,3 +148,35 @@ def test_previous_direction_seed_cuts_iterations(sdlib, orc):
     mean_plain = plain[0]["gjk_iters"] / plain[0]["gjk_pairs"]
     mean_prev = prev[0]["gjk_iters"] / prev[0]["gjk_pairs"]
     assert mean_prev < 0.6 * mean_plain, (mean_plain, mean_prev)
+
+
+@pytest.mark.parametrize("seed_mode", [0, 2])
+def test_narrow_stage_alone_changes_nothing(sdlib, seed_mode):
+    """The contact stage of a hull scene (the narrow phase of the last
+    step's lists at the current bodies, launched alone for timing) changes
+    no body: interleaving it leaves the bodies bit-identical, and with plain
+    GJK the next steps' entries too (with seeds it moves the next step's
+    seeds, so only iteration counts may differ)."""
+    from stardust_gb300 import _abi
+    runs = []
+    for extra in (0, 3):
+        eng, cfg, dt = hull_engine(sdlib, seed_mode=seed_mode)
+        eng.step(dt, 5)
+        for _ in range(extra):
+            _abi.call("sd_engine_launch_stage", eng._h, _abi.SD_STAGE_CONTACT, 0.0, h=eng._h)
+        e = eng.hull_entries()
+        eng.step(dt, 5)
+        eng.sync()
+        assert eng.stats()["device_errors"] == 0
+        runs.append((e, eng.hull_entries(), eng.bodies(_abi.SD_BODY_POSITION), eng.bodies(_abi.SD_BODY_OMEGA)))
+        with pytest.raises(Exception):
+            _abi.call("sd_engine_launch_stage", eng._h, _abi.SD_STAGE_SORT, 0.0, h=eng._h)
+        eng.close()
+    (e0, f0, p0, w0), (e1, f1, p1, w1) = runs
+    assert np.array_equal(e0["off"], e1["off"]) and np.array_equal(e0["partners"], e1["partners"])
+    assert np.array_equal(f0["status"] == 1, f1["status"] == 1)
+    if seed_mode == 0:
+        for k in ("status", "iters", "epa_iters"):
+            assert np.array_equal(f0[k], f1[k]), k
+        assert np.array_equal(bits(f0["dir"]), bits(f1["dir"]))
+    assert np.array_equal(bits(p0), bits(p1)) and np.array_equal(bits(w0), bits(w1))

@@ -60,3 +60,47 @@ def test_sap_pairs_overflow_is_reported(sdlib):
     H[:, :3] = c + 0.05
     got, cnt, err = sdlib.SweepAndPrune.pairs(torch.from_numpy(L).cuda(), torch.from_numpy(H).cuda(), 10)
     assert err & sdlib._abi.SD_DEVERR_PAIR_OVERFLOW
+
+
+def _scene(kind, n, seed):
+    """Boxes that stress the binned sweep's column grid: mixed sizes with a
+    few boxes spanning the domain, corners on column boundaries, a flat
+    scene (no y-z extent at all), y/z-inverted boxes, large coordinates."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-0.7, 1.3, (n, 3)).astype(np.float32)
+    h = np.exp(rng.normal(np.log(0.006), 0.6, (n, 3))).astype(np.float32)
+    if kind == "mixed":
+        h[rng.random(n) < 0.01] = 0.0
+        big = rng.random(n) < 0.002
+        h[big] = rng.uniform(0.2, 0.9, (int(big.sum()), 3))
+    elif kind == "aligned":
+        c = (rng.integers(0, 96, (n, 3)) / 64.0).astype(np.float32)
+        h = (rng.integers(0, 3, (n, 3)) / 128.0).astype(np.float32)
+    elif kind == "flat":
+        c[:, 1:] = 0.5
+        h[:, 1:] = 0.0
+    elif kind == "large":
+        c = (c * 1000.0 + 1.0e6).astype(np.float32)
+        h = (h * 1000.0).astype(np.float32)
+    L = np.zeros((n, 4), np.float32)
+    H = np.zeros((n, 4), np.float32)
+    L[:, :3] = c - h
+    H[:, :3] = c + h
+    if kind == "inverted_yz":
+        flip = rng.random(n) < 0.1
+        L[flip, 1], H[flip, 1] = H[flip, 1].copy(), L[flip, 1].copy()
+        flip = rng.random(n) < 0.1
+        L[flip, 2], H[flip, 2] = H[flip, 2].copy(), L[flip, 2].copy()
+    return L, H
+
+
+@pytest.mark.parametrize("kind", ["mixed", "aligned", "flat", "inverted_yz", "large"])
+def test_sap_pairs_binned_edge_cases(sdlib, orc, kind):
+    """The binned sweep (columns, one report per pair in the column of the
+    overlap's lower y-z corner) finds exactly the oracle's pair set."""
+    import torch
+    L, H = _scene(kind, 20_000 if kind != "flat" else 4000, seed=len(kind))
+    want = orc.aabb_pairs(L, H)
+    got, cnt, err = sdlib.SweepAndPrune.pairs(torch.from_numpy(L).cuda(), torch.from_numpy(H).cuda(), len(want) + 8)
+    assert err == 0 and cnt == len(want), (kind, cnt, len(want), err)
+    assert np.array_equal(got.cpu().numpy().view(np.uint64), want)
