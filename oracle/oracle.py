@@ -614,13 +614,43 @@ def bf16(x):
     return b.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def mlp_forward_backward(params, X, T, round_bf16=True):
+def mlp_forward_bound(params, X, acc_eps=2.0 ** -23):
+    """The forward pass of mlp_forward_backward with a per-element bound on
+    how far a correct FP32-accumulating kernel can land from it: each
+    pre-activation sums K exact BF16 x BF16 products and a bias in FP32, so
+    it is off by at most (K + 1) * acc_eps * (sum of |terms|) (acc_eps =
+    2^-23 admits truncating adds) plus what the previous layer's deviations
+    carry through |W|; a BF16 rounding of relu(z) is monotone in z, so the
+    activation can move at most to the roundings of the interval's ends.
+    Returns (y (n, 3), bound (n, 3))."""
+    P = mlp_unpack(params)
+    W = [bf16(P["W1"]), bf16(P["W2"]), bf16(P["W3"])]
+    b = [P["b1"], P["b2"], P["b3"]]
+    H = bf16(X)
+    dH = np.zeros_like(H)
+    for layer in range(3):
+        Wa = np.abs(W[layer])
+        Z = H @ W[layer].T + b[layer]
+        e = dH @ Wa.T + (W[layer].shape[1] + 1) * acc_eps * ((np.abs(H) + dH) @ Wa.T + np.abs(b[layer]))
+        if layer == 2:
+            break
+        H = bf16(np.maximum(Z, 0))
+        dH = np.maximum(np.abs(bf16(np.maximum(Z - e, 0)) - H), np.abs(bf16(np.maximum(Z + e, 0)) - H))
+    skip = np.asarray(X, np.float64)[:, 8:11]
+    Y = Z[:, :3] + skip
+    # the residual add in FP32, rounded to nearest
+    bound = e[:, :3] + 2.0 ** -24 * (np.abs(Z[:, :3]) + e[:, :3] + np.abs(skip))
+    return Y, bound
+
+
+def mlp_forward_backward(params, X, T, round_bf16=True, with_abs=False):
     """The network of sd_mlp.cu restated in float64: forward (rows of 16
     inputs; the output adds inputs 8..10, a residual over the previous
     direction) and the gradient of mean over rows of valid * (1 - y.t/|y|),
     with BF16 rounding where the tensor-core kernels round (inputs, hidden
     activations, output gradient and activation gradients).  Returns
-    (y (n, 3), loss, grad (6288,))."""
+    (y (n, 3), loss, grad (6288,)); with_abs adds the gradient's sums of
+    |terms| per element (same packing), the scale of its rounding errors."""
     r = bf16 if round_bf16 else (lambda a: np.asarray(a, np.float64))
     P = mlp_unpack(params)
     W1, W2, W3 = r(P["W1"]), r(P["W2"]), r(P["W3"])
@@ -645,7 +675,14 @@ def mlp_forward_backward(params, X, T, round_bf16=True):
     g = {"W3": dY.T @ H2, "b3": dY.sum(0), "W2": dZ2.T @ H1, "b2": dZ2.sum(0), "W1": dZ1.T @ Xb, "b1": dZ1.sum(0)}
     g["W3"][3:] = 0
     g["b3"][3:] = 0
-    return Y, loss, mlp_pack(g)
+    if not with_abs:
+        return Y, loss, mlp_pack(g)
+    a = np.abs
+    ga = {"W3": a(dY).T @ a(H2), "b3": a(dY).sum(0), "W2": a(dZ2).T @ a(H1), "b2": a(dZ2).sum(0),
+          "W1": a(dZ1).T @ a(Xb), "b1": a(dZ1).sum(0)}
+    ga["W3"][3:] = 0
+    ga["b3"][3:] = 0
+    return Y, loss, mlp_pack(g), mlp_pack(ga)
 
 
 def sap_sweep_ref(upperx, lowerx_sorted, uppery, lowery, idx_sorted):

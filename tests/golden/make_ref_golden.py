@@ -16,9 +16,16 @@ them on seeded inputs:
 * ``ref_sap_<case>.npz`` -- sweepAndPruneCUDA
   (src/engine/cuda/collisions/SAP/sap_detection.cu:385-440) over sphere AABBs
   whose lower x extents are stably sorted as uint32 float bits -> 16-entry
-  rows per sorted position (cleared to -1 before the launch).
+  rows per sorted position (cleared to -1 before the launch);
+* ``ref_morton_<case>.npz`` -- computeSpaceFillingCurveCUDA
+  (sandbox/testLBVH.cu:113-151): boxes and a domain -> 30-bit Morton codes;
+* ``ref_gjk.npz`` -- STARDUST::gjkCUDA (sandbox/testGJK.cu:237-315): convex
+  point sets (world vertices) placed clearly apart or clearly overlapping
+  by construction -> the kernel's verdict per pair (it prints a line for a
+  hit and stores nothing, so each pair runs in its own launch and the
+  printed lines are counted).
 
-Usage:  python tests/golden/make_ref_golden.py OUT_DIR
+Usage:  python tests/golden/make_ref_golden.py OUT_DIR [hash rigid sap morton gjk]
 """
 from __future__ import annotations
 
@@ -218,6 +225,136 @@ def run_sap(lib, out: Path):
         print(f"sap {name}: {n} boxes, {(res >= 0).sum()} row entries")
 
 
+def run_morton(lib, out: Path):
+    for name, n, seed, span in (("a", 5000, 31, 1.0), ("b", 3000, 32, 0.25)):
+        rng = np.random.default_rng(seed)
+        # a domain around the origin; some box centres outside it (clamped
+        # codes) and on both sides of its centre (the floor of negatives)
+        glo = np.array([-1.0, -0.5, -2.0, 0.0], np.float32) * span
+        ghi = np.array([1.5, 0.75, 1.0, 0.0], np.float32) * span
+        c = rng.uniform(glo[:3] - 0.1 * span, ghi[:3] + 0.1 * span, (n, 3)).astype(np.float32)
+        h = rng.uniform(0.0, 0.01 * span, (n, 3)).astype(np.float32)
+        L = np.zeros((n, 4), np.float32)
+        H = np.zeros((n, 4), np.float32)
+        L[:, :3] = c - h
+        H[:, :3] = c + h
+        if name == "b":  # the domain as the LBVH builds it: the boxes' bounds (testLBVH.cu:61-77)
+            glo = np.concatenate([L[:, :3].min(0), [0.0]]).astype(np.float32)
+            ghi = np.concatenate([H[:, :3].max(0), [0.0]]).astype(np.float32)
+        rows = np.concatenate([H, L], 1)  # the sandbox AABB: upper extent, then lower extent
+        d_rows, d_codes, d_idx = dev(rows), dev(np.zeros(n, np.uint32)), dev(np.zeros(n, np.int32))
+        import torch
+        torch.cuda.synchronize()
+        check(lib, lib.ref_morton(n, ghi.ctypes.data_as(C.c_void_p), glo.ctypes.data_as(C.c_void_p), ptr(d_rows),
+                                  ptr(d_codes), ptr(d_idx), C.c_void_p(0)), "morton")
+        codes = host(d_codes, np.uint32, (n,))
+        np.savez_compressed(out / f"ref_morton_{name}.npz", lo=L, hi=H, glo=glo, ghi=ghi, codes=codes)
+        print(f"morton {name}: {n} boxes, {len(np.unique(codes))} distinct codes")
+
+
+HULL_DTYPE = np.dtype({"names": ["type", "group_owner", "is_active", "is_visible", "vertex_idx", "n_vertices",
+                                 "mass", "radius", "position", "force", "torque"],
+                       "formats": ["<u4", "<u4", "u1", "u1", "<i4", "<i4", "<f4", "<f4", ("<f4", 4), ("<f4", 4),
+                                   ("<f4", 4)],
+                       "offsets": [0, 4, 8, 9, 12, 16, 20, 24, 32, 48, 64], "itemsize": 80})  # primitives.hpp
+
+
+def gjk_cases(n_pairs: int, seed: int):
+    """Pairs of convex point sets (8-32 points on a jittered sphere around
+    their centre), placed along a random direction u either apart by a gap
+    beyond their support extents along u (separated by construction) or
+    closer than the sum of their inscribed-ball radii (overlapping by
+    construction); gaps and overlaps of 30 %, 5 % and 1 % of the size."""
+    from scipy.spatial import ConvexHull
+    rng = np.random.default_rng(seed)
+
+    def shape():
+        while True:
+            k = int(rng.integers(8, 33))
+            d = rng.normal(size=(k, 3))
+            pts = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(0.85, 1.0, (k, 1))
+            pts *= rng.uniform(0.5, 1.5)
+            rin = float(np.min(-ConvexHull(pts).equations[:, 3]))
+            if rin > 0.1 * np.abs(pts).max():
+                return pts, rin
+
+    cen, pts_all, pairs, truth = [], [], [], []
+    for i in range(n_pairs):
+        (pa, ra), (pb, rb) = shape(), shape()
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        ca = rng.uniform(-5.0, 5.0, 3)
+        frac = (0.3, 0.05, 0.01)[(i // 2) % 3]
+        if i % 2 == 0:
+            gap = frac * min(np.abs(pa).max(), np.abs(pb).max())
+            cb = ca + u * ((pa @ u).max() + (pb @ -u).max() + gap)
+        else:
+            cb = ca + u * (ra + rb - frac * min(ra, rb))
+        for c, p in ((ca, pa), (cb, pb)):
+            cen.append(c)
+            pts_all.append(p)
+        pairs.append((2 * i, 2 * i + 1))
+        truth.append(i % 2 == 1)
+    return cen, pts_all, np.array(pairs, np.int32), np.array(truth)
+
+
+class StdoutCapture:
+    """Collects what the process writes to file descriptor 1 (device printf
+    output is written there at synchronisation)."""
+
+    def __enter__(self):
+        import os
+        import tempfile
+        self.libc = C.CDLL(None)
+        self.libc.fflush(None)
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.tmp = tempfile.TemporaryFile()
+        os.dup2(self.tmp.fileno(), 1)
+        return self
+
+    def __exit__(self, *exc):
+        import os
+        self.libc.fflush(None)
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        self.tmp.seek(0)
+        self.text = self.tmp.read().decode(errors="replace")
+        self.tmp.close()
+
+
+def run_gjk(lib, out: Path):
+    import torch
+    cen, pts, pairs, truth = gjk_cases(600, 41)
+    counts = np.array([len(p) for p in pts], np.int32)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int32)
+    verts = np.zeros((counts.sum(), 4), np.float32)
+    hulls = np.zeros(len(pts), HULL_DTYPE)
+    for k, (c, p) in enumerate(zip(cen, pts)):
+        w = (np.asarray(c)[None, :] + p).astype(np.float32)
+        verts[starts[k]:starts[k] + counts[k], :3] = w
+        hulls[k]["type"] = 2  # POLYHEDRA
+        hulls[k]["is_active"] = 1
+        hulls[k]["vertex_idx"] = starts[k]
+        hulls[k]["n_vertices"] = counts[k]
+        hulls[k]["mass"] = 1.0
+        hulls[k]["radius"] = -1.0
+        hulls[k]["position"][:3] = np.asarray(c, np.float32)
+    d_h, d_v = dev(hulls.view(np.uint8)), dev(verts)
+    verdict = np.zeros(len(pairs), bool)
+    for i, (a, b) in enumerate(pairs):
+        d_p = dev(np.array([a, b, -1, -1], np.int32))
+        torch.cuda.synchronize()
+        with StdoutCapture() as cap:
+            check(lib, lib.ref_gjk_one(len(pts), ptr(d_p), ptr(d_h), ptr(d_v), C.c_void_p(0)), "gjk")
+        verdict[i] = "collided" in cap.text
+    np.savez_compressed(out / f"ref_gjk.npz", verts=verts, starts=starts, counts=counts,
+                        centres=np.asarray(cen, np.float32), pairs=pairs, truth=truth, verdict=verdict)
+    print(f"gjk: {len(pairs)} pairs, reference verdicts agree with the construction on "
+          f"{int((verdict == truth).sum())} (separated {int((~verdict & ~truth).sum())}/{int((~truth).sum())}, "
+          f"overlapping {int((verdict & truth).sum())}/{int(truth.sum())})")
+
+
 def main():
     out = Path(sys.argv[1] if len(sys.argv) > 1 else ".")
     out.mkdir(parents=True, exist_ok=True)
@@ -226,10 +363,18 @@ def main():
     torch.zeros(1, device="cuda")  # make the primary context current
     lib = harness()
     check(lib, lib.ref_init(str(ROOT / "oracle" / "_ref").encode()), "init")
-    hashed = run_hash(lib, out)
-    run_traverse(lib, out, hashed)
-    run_rigid(lib, out)
-    run_sap(lib, out)
+    parts = sys.argv[2:] or ["hash", "rigid", "sap", "morton", "gjk"]
+    if "hash" in parts:
+        hashed = run_hash(lib, out)
+        run_traverse(lib, out, hashed)
+    if "rigid" in parts:
+        run_rigid(lib, out)
+    if "sap" in parts:
+        run_sap(lib, out)
+    if "morton" in parts:
+        run_morton(lib, out)
+    if "gjk" in parts:
+        run_gjk(lib, out)
 
 
 if __name__ == "__main__":

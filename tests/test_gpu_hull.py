@@ -180,3 +180,45 @@ def test_narrow_stage_alone_changes_nothing(sdlib, seed_mode):
             assert np.array_equal(f0[k], f1[k]), k
         assert np.array_equal(bits(f0["dir"]), bits(f1["dir"]))
     assert np.array_equal(bits(p0), bits(p1)) and np.array_equal(bits(w0), bits(w1))
+
+
+def test_lbvh_morton_matches_reference_kernel(sdlib):
+    """The LBVH's Morton codes against computeSpaceFillingCurveCUDA itself
+    (sandbox/testLBVH.cu:113-151, golden ref_morton_b.npz: the domain is the
+    boxes' bounds, as the LBVH builds it)."""
+    import torch
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref_morton_b.npz")
+    got = sdlib.BoundingVolumes.morton(torch.from_numpy(g["lo"]).cuda(), torch.from_numpy(g["hi"]).cuda())
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), g["codes"])
+
+
+def test_hull_gjk_verdicts_match_reference_kernel(sdlib):
+    """The engine's narrow phase against STARDUST::gjkCUDA's verdicts
+    (sandbox/testGJK.cu:237-315, golden ref_gjk.npz): 600 constructed pairs
+    of convex point sets, apart or overlapping by 1-30 % of their size, added
+    as hulls; after one step each pair is in contact (status 1) exactly when
+    the reference kernel reported a collision."""
+    from pathlib import Path
+    from stardust_gb300 import EngineConfig
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref_gjk.npz")
+    cfg = EngineConfig(box_lo=(-20.0, -20.0, -20.0), box_hi=(20.0, 20.0, 20.0), walls=0, cell=4.0, kn=1e5,
+                       restitution=0.5, mu=0.3, gravity=(0.0, 0.0, 0.0), pair_capacity=1 << 16)
+    eng = sdlib.DEMEngine(cfg)
+    for k in range(len(g["counts"])):
+        s, c = int(g["starts"][k]), int(g["counts"][k])
+        centre = g["centres"][k]
+        eng.add_hull(g["verts"][s:s + c, :3] - centre, 1.0, tuple(float(x) for x in centre))
+    eng.prepare()
+    eng.step(1e-6, 1)
+    eng.sync()
+    assert eng.stats()["device_errors"] == 0
+    e = eng.hull_entries()
+    contact = set()
+    for a in range(len(e["off"]) - 1):
+        for q in range(e["off"][a], e["off"][a + 1]):
+            if e["status"][q] == 1:
+                contact.add((a, int(e["partners"][q])))
+    got = np.array([(int(a), int(b)) in contact for a, b in g["pairs"]])
+    assert np.array_equal(got, g["verdict"])
+    eng.close()
