@@ -84,6 +84,7 @@ struct Lbvh {
     float4 *node_lo, *node_hi, *leaf_lo, *leaf_hi;
     uint32_t* counts;                    // per box id
     uint32_t* first;                     // per leaf: its first kLbvhFirst partners found (counting pass)
+    float4* rec;                         // per internal node: both children's boxes (lo.w = child ref)
     uint32_t* scan_scratch;
     uint32_t* status;                    // device error bits
 };

@@ -203,10 +203,15 @@ __device__ __forceinline__ bool child_ok(int c, int n) {
     return (c & kLeaf) ? (c & ~kLeaf) < n : (c >= 0 && c < n - 1);
 }
 
+// Bottom-up boxes: the last of a node's two children to finish computes
+// the node's box and writes the node's record -- both children's boxes,
+// each lower corner's w lane holding the child reference -- which the
+// traversal reads in one 64-byte piece instead of the children's indices
+// and then their boxes.
 __global__ void refit_kernel(int n, const uint32_t* __restrict__ vals, const float4* __restrict__ lo,
                              const float4* __restrict__ hi, float4* leaf_lo, float4* leaf_hi, float4* node_lo,
                              float4* node_hi, const int2* __restrict__ children, const int32_t* __restrict__ parent,
-                             uint32_t* visit, uint32_t* __restrict__ status) {
+                             uint32_t* visit, float4* __restrict__ rec, uint32_t* __restrict__ status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t id = vals[k];
@@ -233,6 +238,10 @@ __global__ void refit_kernel(int n, const uint32_t* __restrict__ vals, const flo
         else { b0 = ldcg4(node_lo + c.y); b1 = ldcg4(node_hi + c.y); }
         node_lo[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.f);
         node_hi[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f);
+        rec[4 * (size_t)p + 0] = make_float4(a0.x, a0.y, a0.z, __int_as_float(c.x));
+        rec[4 * (size_t)p + 1] = a1;
+        rec[4 * (size_t)p + 2] = make_float4(b0.x, b0.y, b0.z, __int_as_float(c.y));
+        rec[4 * (size_t)p + 3] = b1;
         __threadfence();
         p = parent[p];
     }
@@ -246,8 +255,7 @@ __global__ void refit_kernel(int n, const uint32_t* __restrict__ vals, const flo
 // traversal.
 template <bool WRITE>
 __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const float4* __restrict__ leaf_lo,
-                             const float4* __restrict__ leaf_hi, const float4* __restrict__ node_lo,
-                             const float4* __restrict__ node_hi, const int2* __restrict__ children,
+                             const float4* __restrict__ leaf_hi, const float4* __restrict__ rec,
                              uint32_t* __restrict__ count, const uint32_t* __restrict__ off,
                              uint32_t* __restrict__ partners, uint32_t* __restrict__ self, uint64_t cap,
                              uint32_t* __restrict__ first, uint32_t* __restrict__ status) {
@@ -257,7 +265,8 @@ __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const flo
     uint32_t c = 0;
     const uint32_t base = WRITE ? off[id] : 0u;
     const uint32_t lim = WRITE ? off[id + 1] : 0u;
-    if (WRITE && lim - base <= (uint32_t)kLbvhFirst) {
+    if constexpr (WRITE) {
+      if (lim - base <= (uint32_t)kLbvhFirst) {
         if ((uint64_t)lim > cap) {
             atomicOr(status, kErrPairOverflow);
             return;
@@ -284,6 +293,7 @@ __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const flo
                 self[base + i] = id;
             }
         return;
+      }
     }
     const float4 qlo = leaf_lo[k], qhi = leaf_hi[k];
     if (n > 1) {
@@ -292,51 +302,54 @@ __global__ void query_kernel(int n, const uint32_t* __restrict__ vals, const flo
         stack[sp++] = 0;
         while (sp > 0) {
             const int node = stack[--sp];
-            const int2 ch = children[node];
-            if (!child_ok(ch.x, n) || !child_ok(ch.y, n)) {
+            // the node's record: both children's boxes and references
+            const float4 r0 = rec[4 * (size_t)node + 0], r1 = rec[4 * (size_t)node + 1];
+            const float4 r2 = rec[4 * (size_t)node + 2], r3 = rec[4 * (size_t)node + 3];
+            const int cx = __float_as_int(r0.w), cy = __float_as_int(r2.w);
+            if (!child_ok(cx, n) || !child_ok(cy, n)) {
                 atomicOr(status, kErrBadInput);
                 continue;
             }
-            const int cc[2] = {ch.x, ch.y};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int x = cc[h];
+                const int x = h ? cy : cx;
+                const float4 blo = h ? r2 : r0, bhi = h ? r3 : r1;
                 if (x & kLeaf) {
                     const int j = x & ~kLeaf;
-                    if (j == k || !box_overlap(qlo, qhi, leaf_lo[j], leaf_hi[j])) continue;
-                    if (WRITE) {
+                    if (j == k || !box_overlap(qlo, qhi, blo, bhi)) continue;
+                    if constexpr (WRITE) {
                         const uint32_t e = base + c;
                         if (e < lim && (uint64_t)e < cap) partners[e] = vals[j];
                     } else if (c < (uint32_t)kLbvhFirst) {
                         first[(size_t)k * kLbvhFirst + c] = vals[j];
                     }
                     ++c;
-                } else if (box_overlap(qlo, qhi, node_lo[x], node_hi[x])) {
+                } else if (box_overlap(qlo, qhi, blo, bhi)) {
                     if (sp < kStack) stack[sp++] = x;
                     else atomicOr(status, kErrPairOverflow);
                 }
             }
         }
     }
-    if (!WRITE) {
+    if constexpr (!WRITE) {
         count[id] = c;
-        return;
-    }
-    if ((uint64_t)lim > cap) {
-        atomicOr(status, kErrPairOverflow);
-        return;
-    }
-    // sort the body's partner list ascending (insertion sort: lists are short)
-    for (uint32_t e = base + 1; e < lim; ++e) {
-        const uint32_t x = partners[e];
-        uint32_t m = e;
-        while (m > base && partners[m - 1] > x) {
-            partners[m] = partners[m - 1];
-            --m;
+    } else {
+        if ((uint64_t)lim > cap) {
+            atomicOr(status, kErrPairOverflow);
+            return;
         }
-        partners[m] = x;
+        // sort the body's partner list ascending (insertion sort: lists are short)
+        for (uint32_t e = base + 1; e < lim; ++e) {
+            const uint32_t x = partners[e];
+            uint32_t m = e;
+            while (m > base && partners[m - 1] > x) {
+                partners[m] = partners[m - 1];
+                --m;
+            }
+            partners[m] = x;
+        }
+        for (uint32_t e = base; e < lim; ++e) self[e] = id;
     }
-    for (uint32_t e = base; e < lim; ++e) self[e] = id;
 }
 
 // Unique pairs (i < j) of the partner lists, ascending u64.
@@ -401,6 +414,7 @@ uint64_t lbvh_scratch_bytes(uint32_t n) {
     b += 4 * align256(16 * m);                                     // node lo/hi, leaf lo/hi
     b += align256(4 * (m + 1)) + align256(4 * scan_scratch_words((uint32_t)m + 1));
     b += align256(4 * kLbvhFirst * m);                             // first partners per leaf
+    b += align256(64 * m);                                         // node records
     b += align256(4 * 4);                                          // status
     return b;
 }
@@ -431,6 +445,7 @@ void lbvh_carve(void* scratch, uint32_t n, Lbvh* t) {
     t->counts = (uint32_t*)take(4 * (m + 1));
     t->scan_scratch = (uint32_t*)take(4 * scan_scratch_words((uint32_t)m + 1));
     t->first = (uint32_t*)take(4 * kLbvhFirst * m);
+    t->rec = (float4*)take(64 * m);
     t->status = (uint32_t*)take(16);
     t->skeys = t->keys;
     t->svals = t->vals;
@@ -465,7 +480,7 @@ cudaError_t lbvh_build_async(Lbvh& t, const float4* lo, const float4* hi, cudaSt
     }
     refit_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>((int)n, t.svals, lo, hi, t.leaf_lo, t.leaf_hi,
                                                                        t.node_lo, t.node_hi, t.children, t.parent,
-                                                                       t.visit, t.status);
+                                                                       t.visit, t.rec, t.status);
     return cudaGetLastError();
 }
 
@@ -474,13 +489,11 @@ cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint
     const uint32_t n = t.n;
     if (n == 0) return cudaMemsetAsync(off, 0, 4, st);
     query_kernel<false><<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(
-        (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.node_lo, t.node_hi, t.children, t.counts, nullptr, nullptr, nullptr,
-        0, t.first, t.status);
+        (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.rec, t.counts, nullptr, nullptr, nullptr, 0, t.first, t.status);
     cudaError_t e = scan_exclusive_async(t.counts, off, n, t.scan_scratch, st);
     if (e != cudaSuccess) return e;
     query_kernel<true><<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>(
-        (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.node_lo, t.node_hi, t.children, nullptr, off, partners, self, cap,
-        t.first, t.status);
+        (int)n, t.svals, t.leaf_lo, t.leaf_hi, t.rec, nullptr, off, partners, self, cap, t.first, t.status);
     return cudaGetLastError();
 }
 
