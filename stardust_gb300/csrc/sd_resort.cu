@@ -42,6 +42,8 @@ namespace {
 
 // one block of 1024 threads: one thread per moved entry of a full list
 constexpr int kRsThreads = 1024;
+// above this many moved entries the ranks are counted against sorted chunks
+constexpr uint32_t kChunkedRankM = 256;
 static_assert(kResortMaxCap <= (uint32_t)kRsThreads, "one thread per moved entry");
 
 // scratch (u32): [0] moved count (appended to during the step, zero again
@@ -55,6 +57,7 @@ resort_plan_kernel(unsigned long long* __restrict__ list, uint32_t* __restrict__
                    uint32_t ncells, uint32_t n, uint32_t* __restrict__ vl_flags, uint32_t* __restrict__ sort_clear,
                    uint32_t sort_clear_words) {
     __shared__ unsigned long long s_a[kResortMaxCap], s_b[kResortMaxCap];
+    __shared__ uint32_t s_c[kResortMaxCap];
     __shared__ uint32_t s_M, ws[33];
     if (threadIdx.x == 0) {
         const uint32_t M = scratch[0];
@@ -78,7 +81,51 @@ resort_plan_kernel(unsigned long long* __restrict__ list, uint32_t* __restrict__
         if (threadIdx.x == 0) scratch[3] = 0u;
         return;
     }
-    {
+    if (M > kChunkedRankM) {
+        // each entry is placed by counting the smaller ones (entries and
+        // slots are distinct), chunk by chunk: every warp sorts 32 entries
+        // by (key, slot) and their slots alone (bitonic network over the
+        // lanes), then each entry adds up, over the chunks, the number of
+        // smaller elements (binary search): M/32 chunks x 6 probes per
+        // order instead of M comparisons
+        const uint32_t lane = threadIdx.x & 31u, t = threadIdx.x;
+        unsigned long long v = t < M ? list[t] : ~0ull;
+        uint32_t sv = t < M ? (uint32_t)v : 0xffffffffu;
+        const unsigned long long c = v;
+        for (uint32_t k = 2; k <= 32; k <<= 1)
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, (int)j);
+                const uint32_t os = __shfl_xor_sync(0xffffffffu, sv, (int)j);
+                const bool take_min = ((lane & j) == 0) == ((lane & k) == 0);
+                v = take_min ? (o < v ? o : v) : (o < v ? v : o);
+                sv = take_min ? min(os, sv) : max(os, sv);
+            }
+        s_b[t] = v;  // chunks of 32, each ascending (padding last)
+        s_c[t] = sv;
+        __syncthreads();
+        uint32_t ra = 0, rs = 0;
+        if (t < M) {
+            const uint32_t cs = (uint32_t)c, nch = (M + 31u) >> 5;
+            for (uint32_t q = 0; q < nch; ++q) {
+                const unsigned long long* A = s_b + 32u * q;
+                const uint32_t* S = s_c + 32u * q;
+                uint32_t pa = 0, ps = 0;  // elements of the chunk below c, below cs
+#pragma unroll
+                for (uint32_t step = 32; step > 0; step >>= 1) {
+                    if (pa + step <= 32u && A[pa + step - 1u] < c) pa += step;
+                    if (ps + step <= 32u && S[ps + step - 1u] < cs) ps += step;
+                }
+                ra += pa;
+                rs += ps;
+            }
+        }
+        __syncthreads();
+        if (t < M) {
+            s_a[ra] = c;
+            s_b[rs] = c & 0xffffffffull;  // the moved slots, ascending
+        }
+        __syncthreads();
+    } else {
         // each entry is placed by counting the smaller ones (entries and
         // slots are distinct): G threads per entry, G the largest power of two
         // up to 32 with G * M <= 1024, each counting a G-th of the list, then
