@@ -1062,15 +1062,22 @@ __device__ __forceinline__ void quat_rot(float qs, float qx, float qy, float qz,
     R[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
 }
 
-// One thread per rigid body (replaces computeForcesAndTorquesCUDA +
+// A rigid body's step (replaces computeForcesAndTorquesCUDA +
 // advectParticlesCUDA + updateSphereDataCUDA, physics_update.cu:26-310):
 // gather the body's sphere forces and torques in sphere-id order (the
 // segmented reduction, no atomics), add gravity, integrate momentum and
 // angular momentum, w = R I0^-1 R^T L, normalised first-order quaternion
 // update, then write every sphere's next state and cell key (and its
 // digits to the block's shared sort histograms when s_hist is given).
+// One body per quad of lanes (q = lane & 3): lane q loads and writes the
+// body's spheres q, q + 4, ...; the sums over the spheres are formed in
+// sphere-id order in every lane of the quad from the values the lanes
+// exchange, so every lane holds the same body state (the same bits as one
+// thread walking the spheres in order) and integrates it.  Loops run to the
+// warp's largest sphere count so that every lane takes part in the
+// exchanges.
 __device__ __forceinline__ void body_step(
-    const DemParams& p, uint32_t b, float4* __restrict__ bpos, float4* __restrict__ bvel,
+    const DemParams& p, uint32_t b, bool valid, uint32_t q, float4* __restrict__ bpos, float4* __restrict__ bvel,
     float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
     const float4* __restrict__ binv, const uint32_t* __restrict__ bfirst, const uint32_t* __restrict__ bcount,
     const float4* __restrict__ r0, const uint32_t* __restrict__ slot_of, const float4* __restrict__ pos,
@@ -1078,25 +1085,53 @@ __device__ __forceinline__ void body_step(
     float4* __restrict__ pos_n, float4* __restrict__ vel_n, float4* __restrict__ omg_n,
     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n, uint32_t hist_spec,
     uint32_t* s_hist, const MoveSink& ms, const SkinLists& sk) {
-    const float4 bp = bpos[b], bv = bvel[b], bq = bquat[b], bl = bang[b];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 bp = valid ? bpos[b] : z4, bv = valid ? bvel[b] : z4, bq = valid ? bquat[b] : z4,
+                 bl = valid ? bang[b] : z4;
     const float x = bp.x, y = bp.y, z = bp.z, m = bp.w;
-    const uint32_t first = bfirst[b], cnt = bcount[b];
+    const uint32_t first = valid ? bfirst[b] : 0u, cnt = valid ? bcount[b] : 0u;
+    const uint32_t kmax = __reduce_max_sync(0xffffffffu, cnt);
     float Fx = 0, Fy = 0, Fz = 0, Tx = 0, Ty = 0, Tz = 0;
-    for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t s = slot_of[first + k];
-        if (s >= n) continue;  // a consistent slot table never trips this
-        const float4 ps = pos[s], fs = sf[s], ts = st[s];
-        const float rx = ps.x - x, ry = ps.y - y, rz = ps.z - z;
-        Fx = Fx + fs.x;
-        Fy = Fy + fs.y;
-        Fz = Fz + fs.z;
-        Tx = Tx + (ry * fs.z - rz * fs.y);
-        Ty = Ty + (rz * fs.x - rx * fs.z);
-        Tz = Tz + (rx * fs.y - ry * fs.x);
-        Tx = Tx + ts.x;
-        Ty = Ty + ts.y;
-        Tz = Tz + ts.z;
+    for (uint32_t k0 = 0; k0 < kmax; k0 += 4) {
+        const uint32_t k = k0 + q;
+        float4 fs = z4, ts = z4;
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        bool has = false;
+        if (k < cnt) {
+            const uint32_t s = slot_of[first + k];
+            if (s < n) {  // a consistent slot table never fails this
+                const float4 ps = pos[s];
+                fs = sf[s];
+                ts = st[s];
+                const float rx = ps.x - x, ry = ps.y - y, rz = ps.z - z;
+                cx = ry * fs.z - rz * fs.y;
+                cy = rz * fs.x - rx * fs.z;
+                cz = rx * fs.y - ry * fs.x;
+                has = true;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {  // spheres k0 .. k0 + 3, in order
+            const float fx = __shfl_sync(0xffffffffu, fs.x, u, 4), fy = __shfl_sync(0xffffffffu, fs.y, u, 4),
+                        fz = __shfl_sync(0xffffffffu, fs.z, u, 4);
+            const float ux = __shfl_sync(0xffffffffu, cx, u, 4), uy = __shfl_sync(0xffffffffu, cy, u, 4),
+                        uz = __shfl_sync(0xffffffffu, cz, u, 4);
+            const float tx = __shfl_sync(0xffffffffu, ts.x, u, 4), ty = __shfl_sync(0xffffffffu, ts.y, u, 4),
+                        tz = __shfl_sync(0xffffffffu, ts.z, u, 4);
+            if (__shfl_sync(0xffffffffu, has ? 1 : 0, u, 4)) {
+                Fx = Fx + fx;
+                Fy = Fy + fy;
+                Fz = Fz + fz;
+                Tx = Tx + ux;
+                Ty = Ty + uy;
+                Tz = Tz + uz;
+                Tx = Tx + tx;
+                Ty = Ty + ty;
+                Tz = Tz + tz;
+            }
+        }
     }
+    if (!valid) return;
     const float dt = p.dt;
     const float vx = bv.x + dt * (Fx / m + p.g[0]);
     const float vy = bv.y + dt * (Fy / m + p.g[1]);
@@ -1129,7 +1164,7 @@ __device__ __forceinline__ void body_step(
     const float nrm = sqrtf((ns * ns + nx * nx) + (ny * ny + nz * nz));
     const float q0 = ns / nrm, q1 = nx / nrm, q2 = ny / nrm, q3 = nz / nrm;
     quat_rot(q0, q1, q2, q3, R);
-    for (uint32_t k = 0; k < cnt; ++k) {
+    for (uint32_t k = q; k < cnt; k += 4) {
         const uint32_t id = first + k, s = slot_of[id];
         if (s >= n) continue;
         const float4 o = r0[id];
@@ -1151,23 +1186,25 @@ __device__ __forceinline__ void body_step(
         if (s_hist) {
             const int passes = (int)(hist_spec & 3u);
             const uint32_t stride = spec_stride(hist_spec);
-            for (int q = 0; q < passes; ++q) {
-                const uint32_t shift = (hist_spec >> (2 + 9 * q)) & 31u, bits = (hist_spec >> (7 + 9 * q)) & 15u;
-                atomicAdd(&s_hist[q * stride + ((key >> shift) & ((1u << bits) - 1u))], 1u);
+            for (int pq = 0; pq < passes; ++pq) {
+                const uint32_t shift = (hist_spec >> (2 + 9 * pq)) & 31u, bits = (hist_spec >> (7 + 9 * pq)) & 15u;
+                atomicAdd(&s_hist[pq * stride + ((key >> shift) & ((1u << bits) - 1u))], 1u);
             }
         }
     }
-    bpos[b] = make_float4(nxp, nyp, nzp, m);
-    bvel[b] = make_float4(vx, vy, vz, bv.w);
-    bang[b] = make_float4(Lx, Ly, Lz, bl.w);
-    bquat[b] = make_float4(q0, q1, q2, q3);
-    bomg[b] = make_float4(wx, wy, wz, 0.0f);
+    if (q == 0) {
+        bpos[b] = make_float4(nxp, nyp, nzp, m);
+        bvel[b] = make_float4(vx, vy, vz, bv.w);
+        bang[b] = make_float4(Lx, Ly, Lz, bl.w);
+        bquat[b] = make_float4(q0, q1, q2, q3);
+        bomg[b] = make_float4(wx, wy, wz, 0.0f);
+    }
 }
 
-// One thread per body.  The clump spheres' key digits are counted in shared
-// memory and added to the global histograms once per block: a global atomic
-// per sphere piles onto the few bins of the high digits (one L2 slice) and
-// stalls the whole kernel behind it.
+// Four lanes per body (see body_step).  The clump spheres' key digits are
+// counted in shared memory and added to the global histograms once per
+// block: a global atomic per sphere piles onto the few bins of the high
+// digits (one L2 slice) and stalls the whole kernel behind it.
 __global__ void __launch_bounds__(128)
 dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __restrict__ bvel,
                 float4* __restrict__ bquat, float4* __restrict__ bomg, float4* __restrict__ bang,
@@ -1182,10 +1219,10 @@ dem_body_kernel(DemParams p, uint32_t nb, float4* __restrict__ bpos, float4* __r
         for (int q = threadIdx.x; q < kHistWords; q += blockDim.x) s_hist[q] = 0;
         __syncthreads();
     }
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nb)
-        body_step(p, b, bpos, bvel, bquat, bomg, bang, binv, bfirst, bcount, r0, slot_of, pos, omg, sf, st, pos_n,
-                  vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr, ms, sk);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t b = t >> 2;
+    body_step(p, b, b < nb, t & 3u, bpos, bvel, bquat, bomg, bang, binv, bfirst, bcount, r0, slot_of, pos, omg, sf,
+              st, pos_n, vel_n, omg_n, keys, vals, n, hist_spec, ghist ? s_hist : nullptr, ms, sk);
     if (ghist) {
         __syncthreads();
         hist_flush(s_hist, hist_spec, ghist);
@@ -1905,7 +1942,7 @@ static cudaError_t launch_contact(const DemParams& p, DemBuffers& b, bool record
         launch_contact_t<false>(p, b, spec, ghist, st, skin, ms);
     }
     if (b.nb) {
-        dem_body_kernel<<<grid_for(b.nb, 128), 128, 0, st>>>(
+        dem_body_kernel<<<grid_for(4u * b.nb, 128), 128, 0, st>>>(
             p, b.nb, b.bpos, b.bvel, b.bquat, b.bomg, b.bang, b.binv, b.bfirst, b.bcount, b.r0, b.slot_of, b.pos,
             b.omg, b.sf, b.st, b.pos_n, b.vel_n, b.omg_n, b.keys, ms.list ? nullptr : b.vals, b.n, spec, ghist, ms,
             skin ? SkinLists{b.vl_cnt, b.vl_nbr, b.vl_ref, b.vl_flags, b.vl_flags + 1, b.slot_of, b.vl_skin,
