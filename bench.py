@@ -471,15 +471,18 @@ def bench_batch(n_scenes: int, steps: int, warmup: int, local: int, tune: bool):
             "device_errors": st["device_errors"], "moved_keys_last_step": st["moved_keys"], "autotune": tuned}
 
 
-def bench_drum(steps: int, warmup: int, local: int):
+def bench_drum(steps: int, warmup: int, local: int, tune: bool = True):
     """The rotating drum (drum_scene): 2,097,152 spheres -- 10 % of the bodies
     4-sphere clumps -- in a closed cylinder of radius 0.5 m and length 0.5 m
     meshed with 20,480 triangles, turning at 2 rad/s, dt 2e-6 s; radii
     U[1.2, 2.4] mm (the specified U[2, 4] mm would fill 67 % of the drum's
     volume, beyond random close packing).  The mesh is written to a binary
     STL file and loaded from it (sd_engine_add_mesh_stl: the smooth-face rule
-    recovers the wall and the two caps).  Device time per step, CUDA events,
-    a 256 MB write before every timed step."""
+    recovers the wall and the two caps).  Unless `tune` is off, the
+    autotuner picks the contact-list skin on the warmed-up drum, timing each
+    by the mean over 24 steps (the turning wall moves spheres out of their
+    skins, so list builds recur and must count).  Device time per step, CUDA
+    events, a 256 MB write before every timed step."""
     import torch
     import stardust_gb300 as sd
     from stardust_gb300 import scenes
@@ -494,6 +497,13 @@ def bench_drum(steps: int, warmup: int, local: int):
     dt = d["dt"]
     eng.step(dt, warmup)
     eng.sync()
+    tuned = None
+    from stardust_gb300 import _abi
+    skin_before = _abi.tune_get("skin_um")
+    if tune:  # the contact-list skin, timed by the mean over 24 steps (the turning wall makes builds recur)
+        from stardust_gb300 import autotune
+        tuned = autotune.tune_engine(eng, dt, reps=24, knobs={"skin_um": (50, 100, 200, 400, 800, 1600)},
+                                     rounds=1, label="drum", stat="mean")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     st = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
     a = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
@@ -511,7 +521,6 @@ def bench_drum(steps: int, warmup: int, local: int):
     eng.close()
     # the same drum with the triangles' sweep and prune along the drum axis
     # (collision engine SAP) in place of the mesh grid
-    from stardust_gb300 import _abi
     d["cfg"].collision_engine = _abi.SD_ENGINE_SAP
     eng = sd.DEMEngine(d["cfg"])
     scenes.add_drum_scene(eng, d)
@@ -528,12 +537,14 @@ def bench_drum(steps: int, warmup: int, local: int):
     sap_ms = a2.elapsed_time(b2) / k
     sap_err = eng.stats()["device_errors"]
     eng.close()
+    _abi.tune_set("skin_um", skin_before)
     return {"ms_per_step_sap_triangles": sap_ms, "device_errors_sap": sap_err,
             "workload": f"rotating drum, {n} spheres ({len(d['clumps'])} 4-sphere clumps), "
                         f"{len(d['tris'])} triangles loaded from a binary STL, R 0.5 m, L 0.5 m, 2 rad/s, dt 2e-6 s",
             "spheres": n, "bodies": int(stt["n_bodies"]), "triangles": int(len(d["tris"])), "ms_per_step": ms,
             "particle_steps_per_s": n / (ms * 1e-3), "device_errors": stt["device_errors"],
-            "moved_keys_last_step": stt["moved_keys"], "scene_generation_s": gen_s}
+            "moved_keys_last_step": stt["moved_keys"], "list_builds": stt["list_builds"],
+            "listed_steps": stt["listed_steps"], "scene_generation_s": gen_s, "autotune": tuned}
 
 
 def bench_sap(n: int, steps: int, warmup: int, local: int):
@@ -809,7 +820,7 @@ def run_ours(args, rank, world, local):
     # ---- rotating drum (rank 0, N = 1)
     drum = None
     if rank == 0 and world == 1 and not args.no_drum:
-        drum = bench_drum(args.steps, args.warmup, local)
+        drum = bench_drum(args.steps, args.warmup, local, not args.no_tune)
         log(f"drum: {drum}")
 
     # ---- sweep and prune on 2,000,000 boxes (rank 0, N = 1)
@@ -951,7 +962,7 @@ def main():
     if args.only_drum:
         import torch
         torch.cuda.set_device(local)
-        print(json.dumps({"drum": bench_drum(args.steps, args.warmup, local)}), flush=True)
+        print(json.dumps({"drum": bench_drum(args.steps, args.warmup, local, not args.no_tune)}), flush=True)
         return 0
     if args.only_batch:
         import torch

@@ -55,7 +55,7 @@ def _redundant(c: dict) -> bool:
     return False
 
 
-def _time(eng, dt: float, reps: int, stream, flush) -> float:
+def _time(eng, dt: float, reps: int, stream, flush, stat: str = "median") -> float:
     import torch
     eng.step(dt, 2)  # re-capture + warm
     eng.sync()
@@ -68,15 +68,18 @@ def _time(eng, dt: float, reps: int, stream, flush) -> float:
         b.record(stream)
     torch.cuda.synchronize()
     ms = sorted(a.elapsed_time(b) for a, b in ev)
-    return ms[len(ms) // 2]
+    return sum(ms) / len(ms) if stat == "mean" else ms[len(ms) // 2]
 
 
 def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, rounds: int = 2,
-                flush_bytes: int = 256 << 20, label: str | None = None) -> dict:
+                flush_bytes: int = 256 << 20, label: str | None = None, stat: str = "median") -> dict:
     """Coordinate descent over `knobs` (default: the bucket kind's set) on
     the live engine; sets the best and records it for the engine's bucket
     (or under `label`, for a regime of one bucket tuned apart, e.g. a dense
-    bed).  Returns {"bucket", "choice", "ms", "table"}: every timed setting."""
+    bed).  Each setting is timed over `reps` steps by their median, or by
+    their mean (stat "mean": for scenes whose contact-list builds recur
+    within a few steps, e.g. a turning drum, so that the builds count).
+    Returns {"bucket", "choice", "ms", "table"}: every timed setting."""
     import torch
 
     bucket = label or bucket_of(eng)
@@ -94,8 +97,8 @@ def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, rounds
         if key not in seen:
             for k, v in c.items():
                 _abi.tune_set(k, v)
-            seen[key] = _time(eng, dt, reps, stream, flush)
-            table.append({"knobs": dict(c), "ms_median": seen[key]})
+            seen[key] = _time(eng, dt, reps, stream, flush, stat)
+            table.append({"knobs": dict(c), f"ms_{stat}": seen[key]})
         return seen[key]
 
     best_ms = run(cur)
