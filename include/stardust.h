@@ -506,7 +506,10 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   (default)
  *   "fix_blocks"    blocks per SM of the in-place reorder's fixed grid: 2, 4 or 8 (default)
  *   "hull_blocks"   convex-hull scenes: resident 128-thread blocks per SM the GJK kernel is
- *                   compiled for: 3 (168 registers) or 4 (128, the default) */
+ *                   compiled for: 3 (168 registers) or 4 (128, the default)
+ *   "lbvh_rebuild"  convex-hull scenes: steps between full LBVH builds (1..4096, default 16);
+ *                   the steps between refit the last build's tree (exact bounds, so the
+ *                   same candidate pairs) */
 sd_status sd_tune_set(const char* knob, int32_t value);
 sd_status sd_tune_get(const char* knob, int32_t* value);
 

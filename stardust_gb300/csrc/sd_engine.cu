@@ -1403,6 +1403,9 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
     } else if (k == "listed_blocks") {
         if (value != 4 && value != 5) return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4 or 5");
         sd::dem_set_listed_blocks(value);
+    } else if (k == "lbvh_rebuild") {
+        if (value < 1 || value > 4096) return fail(nullptr, SD_ERR_INVALID_ARG, "lbvh_rebuild must be in [1, 4096]");
+        sd::lbvh_set_rebuild_every(value);
     } else if (k == "hull_blocks") {
         if (value != 3 && value != 4) return fail(nullptr, SD_ERR_INVALID_ARG, "hull_blocks must be 3 or 4");
         sd::hull_set_blocks(value);
@@ -1436,6 +1439,7 @@ sd_status sd_tune_get(const char* knob, int32_t* value) {
     else if (k == "contact_block") *value = sd::dem_contact_block();
     else if (k == "fix_blocks") *value = sd::dem_fix_blocks();
     else if (k == "hull_blocks") *value = sd::hull_blocks();
+    else if (k == "lbvh_rebuild") *value = sd::lbvh_rebuild_every();
     else return fail(nullptr, SD_ERR_INVALID_ARG, "unknown knob " + k);
     return SD_OK;
 }

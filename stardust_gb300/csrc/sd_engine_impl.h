@@ -32,7 +32,9 @@ struct HullScene {
     int32_t train_every = 0, train_iters = 0;
     float train_lr = 0.0f;
     uint32_t* teach_flag = nullptr;               // [0] on (read by the step), [1] = 0, [2] = 1
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};        // full LBVH build
+    cudaGraphExec_t graph_refit[2] = {nullptr, nullptr};  // refit of the last build's tree
+    bool tree_built = false;                              // a full build ran since prepare
     int parity = 0;
     int seed_mode = 0;                            // SD_GJK_SEED_*
     float graph_dt = 0.0f;

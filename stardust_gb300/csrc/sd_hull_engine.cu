@@ -110,13 +110,20 @@ void mat_to_quat(const double* R, double* q) {
 
 sd_status build_hull_graphs(sd_engine* h, float dt) {
     HullScene& S = h->hull;
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < 2; ++k) {
         if (S.graph[k]) {
             cudaGraphExecDestroy(S.graph[k]);
             S.graph[k] = nullptr;
         }
+        if (S.graph_refit[k]) {
+            cudaGraphExecDestroy(S.graph_refit[k]);
+            S.graph_refit[k] = nullptr;
+        }
+    }
     S.P.dt = dt;
-    for (int par = 0; par < 2; ++par) {
+    for (int g2 = 0; g2 < 4; ++g2) {
+        const int par = g2 & 1;
+        const bool full = g2 < 2;
         sd::HullBuffers H = S.H;
         H.off = S.off[par];
         H.partners = S.partners[par];
@@ -128,7 +135,9 @@ sd_status build_hull_graphs(sd_engine* h, float dt) {
         cudaGraph_t g = nullptr;
         HULL_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = sd::hull_aabb_async(H, h->stream);
-        if (e == cudaSuccess) e = sd::lbvh_build_async(S.tree, H.lo, H.hi, h->stream);
+        if (e == cudaSuccess)
+            e = full ? sd::lbvh_build_async(S.tree, H.lo, H.hi, h->stream)
+                     : sd::lbvh_refit_async(S.tree, H.lo, H.hi, h->stream);
         if (e == cudaSuccess) e = sd::lbvh_partners_async(S.tree, H.off, H.partners, H.self, H.cap, h->stream);
         if (e == cudaSuccess) e = sd::hull_seed_async(H, (uint32_t)S.seed_mode, h->stream);
         if (e == cudaSuccess && S.seed_mode == SD_GJK_SEED_LEARNED)
@@ -139,8 +148,8 @@ sd_status build_hull_graphs(sd_engine* h, float dt) {
         cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
         if (e != cudaSuccess) return sd_cuda_fail(h, e, "capturing the hull step");
         if (e2 != cudaSuccess) return sd_cuda_fail(h, e2, "cudaStreamEndCapture");
-        cudaError_t e3 = cudaGraphInstantiate(&S.graph[par], g, 0);
-        S.graph_kernels = graph_kernel_nodes(g);
+        cudaError_t e3 = cudaGraphInstantiate(full ? &S.graph[par] : &S.graph_refit[par], g, 0);
+        if (full) S.graph_kernels = graph_kernel_nodes(g);
         cudaGraphDestroy(g);
         if (e3 != cudaSuccess) return sd_cuda_fail(h, e3, "cudaGraphInstantiate");
     }
@@ -157,8 +166,11 @@ void hull_release(sd_engine* h) {
     for (int k = 0; k < 2; ++k) {
         if (S.graph[k]) cudaGraphExecDestroy(S.graph[k]);
         S.graph[k] = nullptr;
+        if (S.graph_refit[k]) cudaGraphExecDestroy(S.graph_refit[k]);
+        S.graph_refit[k] = nullptr;
     }
     S.graph_valid = false;
+    S.tree_built = false;
     S.H = sd::HullBuffers{};
     S.tree = sd::Lbvh{};
     for (int k = 0; k < 2; ++k) {
@@ -265,6 +277,7 @@ sd_status hull_prepare(sd_engine* h) {
     }
     S.parity = 0;
     S.graph_valid = false;
+    S.tree_built = false;
     h->prepared = true;
     h->steps = 0;
     return SD_OK;
@@ -283,7 +296,11 @@ sd_status hull_step(sd_engine* h, float dt, int32_t n_steps) {
         const bool train = online && step % (uint64_t)S.train_every == 0;
         if (train)  // this step logs the max-margin targets of its separated pairs
             HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, S.teach_flag + 2, 4, cudaMemcpyDeviceToDevice, h->stream));
-        HULL_CUDA(h, cudaGraphLaunch(S.graph[S.parity], h->stream));
+        // the tree is built again every lbvh_rebuild steps and refitted in
+        // between: the pair sets are exact either way
+        const bool full = !S.tree_built || step % (uint64_t)sd::lbvh_rebuild_every() == 0;
+        HULL_CUDA(h, cudaGraphLaunch(full ? S.graph[S.parity] : S.graph_refit[S.parity], h->stream));
+        S.tree_built = true;
         if (train) {
             HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, S.teach_flag + 1, 4, cudaMemcpyDeviceToDevice, h->stream));
             // Adam on the step's entries (features, targets), on the GPU

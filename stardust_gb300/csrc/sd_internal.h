@@ -93,6 +93,12 @@ uint64_t lbvh_scratch_bytes(uint32_t n);
 void lbvh_carve(void* scratch, uint32_t n, Lbvh* t);
 cudaError_t lbvh_morton_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
 cudaError_t lbvh_build_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
+// new boxes in the tree the last build made (its leaf order and topology):
+// bounds stay exact, so the pair sets do too; only the tree's quality ages
+cudaError_t lbvh_refit_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st);
+// steps between full LBVH builds of a moving scene (knob "lbvh_rebuild")
+void lbvh_set_rebuild_every(int k);
+int lbvh_rebuild_every();
 // per box id: partners at [off[id], off[id+1]) ascending, self[] = id; off has n+1
 cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint32_t* self, uint64_t cap,
                                 cudaStream_t st);

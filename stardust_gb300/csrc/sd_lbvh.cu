@@ -484,6 +484,21 @@ cudaError_t lbvh_build_async(Lbvh& t, const float4* lo, const float4* hi, cudaSt
     return cudaGetLastError();
 }
 
+cudaError_t lbvh_refit_async(Lbvh& t, const float4* lo, const float4* hi, cudaStream_t st) {
+    const uint32_t n = t.n;
+    if (n == 0) return cudaSuccess;
+    cudaError_t e;
+    if (n > 1 && (e = cudaMemsetAsync(t.visit, 0, 4 * ((size_t)n - 1), st)) != cudaSuccess) return e;
+    refit_kernel<<<grid_for(n, kLbvhThreads), kLbvhThreads, 0, st>>>((int)n, t.svals, lo, hi, t.leaf_lo, t.leaf_hi,
+                                                                       t.node_lo, t.node_hi, t.children, t.parent,
+                                                                       t.visit, t.rec, t.status);
+    return cudaGetLastError();
+}
+
+static int g_lbvh_rebuild = 16;
+void lbvh_set_rebuild_every(int k) { g_lbvh_rebuild = k < 1 ? 1 : k; }
+int lbvh_rebuild_every() { return g_lbvh_rebuild; }
+
 cudaError_t lbvh_partners_async(Lbvh& t, uint32_t* off, uint32_t* partners, uint32_t* self, uint64_t cap,
                                 cudaStream_t st) {
     const uint32_t n = t.n;

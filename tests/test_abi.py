@@ -361,3 +361,18 @@ def test_hull_blocks_knob(sdlib):
                 _abi.tune_set("hull_blocks", v)
     finally:
         _abi.tune_set("hull_blocks", old)
+
+
+def test_lbvh_rebuild_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("lbvh_rebuild")
+    assert old == 16
+    try:
+        for v in (1, 7, 4096):
+            _abi.tune_set("lbvh_rebuild", v)
+            assert _abi.tune_get("lbvh_rebuild") == v
+        for v in (0, -1, 4097):
+            with pytest.raises(Exception):
+                _abi.tune_set("lbvh_rebuild", v)
+    finally:
+        _abi.tune_set("lbvh_rebuild", old)

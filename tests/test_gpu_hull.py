@@ -86,21 +86,26 @@ def oracle_params(orc, cfg, dt):
                            cfg.gravity, dt, cfg.walls)
 
 
-@pytest.mark.parametrize("steps,hull_blocks", [(1, 4), (5, 4), (40, 4), (40, 3)])
-def test_hull_steps_bit_exact(sdlib, orc, steps, hull_blocks):
+@pytest.mark.parametrize("steps,hull_blocks,rebuild", [(1, 4, 16), (5, 4, 16), (40, 4, 16), (40, 3, 16), (40, 4, 1),
+                                                       (40, 4, 4096)])
+def test_hull_steps_bit_exact(sdlib, orc, steps, hull_blocks, rebuild):
+    """The hull step against the oracle; the LBVH built every step, every
+    16 steps (refitted between) or once: the same pair sets and bits."""
     from stardust_gb300 import _abi
     eng, cfg, dt = hull_engine(sdlib)
     H = oracle_hulls(orc, eng)
     p = oracle_params(orc, cfg, dt)
     for _ in range(steps):
         out = H.step(p, record=True)
-    old = _abi.tune_get("hull_blocks")
+    old = (_abi.tune_get("hull_blocks"), _abi.tune_get("lbvh_rebuild"))
     try:
         _abi.tune_set("hull_blocks", hull_blocks)
+        _abi.tune_set("lbvh_rebuild", rebuild)
         eng.step(dt, steps)
         eng.sync()
     finally:
-        _abi.tune_set("hull_blocks", old)
+        _abi.tune_set("hull_blocks", old[0])
+        _abi.tune_set("lbvh_rebuild", old[1])
     st = eng.stats()
     assert st["device_errors"] == 0
     for k, f in (("pos", _abi.SD_BODY_POSITION), ("vel", _abi.SD_BODY_VELOCITY), ("quat", _abi.SD_BODY_QUATERNION),
