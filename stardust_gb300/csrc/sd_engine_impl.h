@@ -32,6 +32,10 @@ struct HullScene {
     int32_t train_every = 0, train_iters = 0;
     float train_lr = 0.0f;
     uint32_t* teach_flag = nullptr;               // [0] on (read by the step), [1] = 0, [2] = 1
+    // a training step's samples gathered for the Adam iterations
+    float* teach_feat = nullptr;
+    float4* teach_tgt = nullptr;
+    uint32_t *teach_flags = nullptr, *teach_pos = nullptr, *teach_scan = nullptr, *teach_total = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};        // full LBVH build
     cudaGraphExec_t graph_refit[2] = {nullptr, nullptr};  // refit of the last build's tree
     bool tree_built = false;                              // a full build ran since prepare

@@ -1016,9 +1016,46 @@ cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st) {
 // Each pair is evaluated once, by one thread, into both of its entries.
 // The grid covers the largest possible pair count (cap / 2); threads past
 // the step's count return at once.
+__global__ void hull_teach_flags_kernel(const float4* __restrict__ teach, const uint32_t* __restrict__ d_count,
+                                        uint32_t cap, uint32_t* __restrict__ flags) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= cap) return;
+    const uint32_t n = min(*d_count, cap);
+    flags[e] = e < n && teach[e].w == 1.0f ? 1u : 0u;
+}
+
+__global__ void hull_teach_gather_kernel(const float* __restrict__ feat, const float4* __restrict__ teach,
+                                         const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos,
+                                         uint32_t cap, float* __restrict__ feat_c, float4* __restrict__ teach_c,
+                                         uint32_t* __restrict__ d_total) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= cap) return;
+    if (e == cap - 1) *d_total = pos[e] + flags[e];
+    if (!flags[e]) return;
+    const uint32_t r = pos[e];
+    const float4* src = reinterpret_cast<const float4*>(feat + 16 * (size_t)e);
+    float4* dst = reinterpret_cast<float4*>(feat_c + 16 * (size_t)r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dst[k] = src[k];
+    teach_c[r] = teach[e];
+}
+
 static int g_hull_blocks = 4;
 void hull_set_blocks(int b) { g_hull_blocks = b == 3 ? 3 : 4; }
 int hull_blocks() { return g_hull_blocks; }
+
+cudaError_t hull_teach_compact_async(const HullBuffers& H, const uint32_t* d_count, float* feat_c, float4* teach_c,
+                                     uint32_t* flags, uint32_t* pos, uint32_t* scan, uint32_t* d_total,
+                                     cudaStream_t st) {
+    const uint32_t cap = (uint32_t)H.cap;
+    if (cap == 0) return cudaMemsetAsync(d_total, 0, 4, st);
+    hull_teach_flags_kernel<<<grid_for(cap, 256), 256, 0, st>>>(H.teach, d_count, cap, flags);
+    cudaError_t e = scan_exclusive_async(flags, pos, cap, scan, st);
+    if (e != cudaSuccess) return e;
+    hull_teach_gather_kernel<<<grid_for(cap, 256), 256, 0, st>>>(H.feat, H.teach, flags, pos, cap, feat_c, teach_c,
+                                                                 d_total);
+    return cudaGetLastError();
+}
 
 cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st) {
     if (H.nb == 0 || H.cap == 0) return cudaSuccess;

@@ -218,6 +218,10 @@ sd_status hull_prepare(sd_engine* h) {
         (s = halloc(h, &S.stats, 4)) || (s = halloc(h, &H.ucount, nb)) || (s = halloc(h, &H.upos, (size_t)nb + 1)) ||
         (s = halloc(h, &H.ulist, cap / 2 + 1)) || (s = halloc(h, &H.uscan, sd::scan_scratch_words(nb) + 1)) ||
         (s = halloc(h, &H.teach, cap)) || (s = halloc(h, &S.teach_flag, 4)) ||
+        (s = halloc(h, &S.teach_feat, 16 * (cap / 2 + 1))) || (s = halloc(h, &S.teach_tgt, cap / 2 + 1)) ||
+        (s = halloc(h, &S.teach_flags, cap)) || (s = halloc(h, &S.teach_pos, cap)) ||
+        (s = halloc(h, &S.teach_scan, sd::scan_scratch_words((uint32_t)cap) + 1)) ||
+        (s = halloc(h, &S.teach_total, 1)) ||
         (s = halloc(h, &H.hit_count, 1)) || (s = halloc(h, &H.hits, cap / 2 + 1)) ||
         (s = halloc(h, &H.hit_keys, cap / 2 + 1)))
         return s;
@@ -303,14 +307,17 @@ sd_status hull_step(sd_engine* h, float dt, int32_t n_steps) {
         S.tree_built = true;
         if (train) {
             HULL_CUDA(h, cudaMemcpyAsync(S.teach_flag, S.teach_flag + 1, 4, cudaMemcpyDeviceToDevice, h->stream));
-            // Adam on the step's entries (features, targets), on the GPU
-            // between steps; the entry count stays on the device.  Adam is
-            // invariant to the loss scale, so the mean's divisor is nominal
-            const uint32_t* count = S.off[S.parity] + S.H.nb;
+            // Adam on the step's samples (features, targets) gathered in entry
+            // order, on the GPU between steps; their count stays on the
+            // device.  Adam is invariant to the loss scale, so the mean's
+            // divisor is nominal
+            HULL_CUDA(h, sd::hull_teach_compact_async(S.H, S.off[S.parity] + S.H.nb, S.teach_feat, S.teach_tgt,
+                                                      S.teach_flags, S.teach_pos, S.teach_scan, S.teach_total,
+                                                      h->stream));
             for (int32_t it = 0; it < S.train_iters; ++it) {
                 S.mlp_step += 1;
-                HULL_CUDA(h, sd::mlp_train_async(S.mlp, S.H.feat, S.H.teach, (uint32_t)S.H.cap, S.H.nb, S.train_lr,
-                                                 S.mlp_step, true, h->stream, count));
+                HULL_CUDA(h, sd::mlp_train_async(S.mlp, S.teach_feat, S.teach_tgt, (uint32_t)(S.H.cap / 2 + 1),
+                                                 S.H.nb, S.train_lr, S.mlp_step, true, h->stream, S.teach_total));
             }
         }
         S.parity ^= 1;

@@ -173,6 +173,13 @@ cudaError_t hull_seed_async(HullBuffers& H, uint32_t mode, cudaStream_t st);
 cudaError_t hull_narrow_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
 void hull_set_blocks(int b);
 int hull_blocks();
+// The training samples of a step (teach[e].w == 1 among the d_count[0]
+// entries), gathered in entry order into feat_c (16 floats per row) and
+// teach_c; *d_total = their number.  flags and pos hold cap words, scan the
+// scan scratch of cap words.
+cudaError_t hull_teach_compact_async(const HullBuffers& H, const uint32_t* d_count, float* feat_c, float4* teach_c,
+                                     uint32_t* flags, uint32_t* pos, uint32_t* scan, uint32_t* d_total,
+                                     cudaStream_t st);
 cudaError_t hull_integrate_async(const HullParams& p, HullBuffers& H, cudaStream_t st);
 cudaError_t hull_stats_async(HullBuffers& H, unsigned long long* out, cudaStream_t st);
 
