@@ -2,7 +2,7 @@
  * its engine headers (which pull Eigen and OpenGL): the include guards of
  * src/engine/engine.hpp and src/engine/types.hpp are pre-defined on the
  * command line, and the few names the kernels use from them are declared
- * here.  Written for this build; layouts follow types.hpp:33-43. */
+ * here (own declarations; their layouts follow types.hpp:33-43). */
 #pragma once
 #include <cuda_runtime.h>
 namespace STARDUST {
