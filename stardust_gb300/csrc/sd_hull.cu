@@ -122,7 +122,11 @@ struct Simplex {
     Cso s[4];
     int n;
     v3 d;
+    float pad;  // 45 words: one thread's simplex per bank offset when kept in shared memory
 };
+
+// A support key (ia * 1024 + ib, both indices below 256) in 16 bits.
+__device__ __forceinline__ uint16_t key16(uint32_t key) { return (uint16_t)(((key >> 10) << 8) | (key & 1023u)); }
 
 /* Closest point to the origin of the simplex S->s[0..n) (Ericson, Real-Time
  * Collision Detection, 5.1.2, 5.1.5, 5.1.6: Voronoi-region tests of the
@@ -265,10 +269,10 @@ struct GjkAttempts {
     }
 };
 
-__device__ int gjk_attempts(const HPair& P, const GjkAttempts& at, Simplex* S, int* iters, v3* dir, int* which) {
+__device__ int gjk_attempts(const HPair& P, const GjkAttempts& at, Simplex* S, int* iters, v3* dir, int* which,
+                            uint16_t* seen, uint32_t seen_stride) {
     int a = 0, it = 0, total = 0;
     bool first = true;
-    uint32_t seen[kGjkMaxIt];
     v3 v = mk(0.f, 0.f, 0.f);
     float vv = 0.0f;
     for (;;) {
@@ -289,15 +293,15 @@ __device__ int gjk_attempts(const HPair& P, const GjkAttempts& at, Simplex* S, i
         } else if (first) {
             S->s[0] = p;
             S->n = 1;
-            seen[0] = p.key;
+            seen[0] = key16(p.key);
             v = p.w;
             vv = vdot(v, v);
             first = false;
         } else {
             for (int k = 0; k < it - 1; ++k)
-                if (seen[k] == p.key) st = kTouch;
+                if (seen[(size_t)k * seen_stride] == key16(p.key)) st = kTouch;
             if (st < 0) {
-                seen[it - 1] = p.key;
+                seen[(size_t)(it - 1) * seen_stride] = key16(p.key);
                 for (int k = S->n; k > 0; --k) S->s[k] = S->s[k - 1];
                 S->s[0] = p;
                 S->n += 1;
@@ -788,7 +792,11 @@ __global__ void __launch_bounds__(kHullThreads, MINB) hull_gjk_kernel(HullBuffer
     const float4 sd = H.seeds ? H.seeds[e] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool seeded = sd.w == 1.0f;
     if (seeded) d0 = rot(P.A.R, f3(sd));
-    Simplex S;
+    // the simplex and the supports seen, per thread in shared memory (in
+    // local memory they missed L1 at this occupancy)
+    __shared__ Simplex s_simplex[kHullThreads];
+    __shared__ uint16_t s_seen[kGjkMaxIt * kHullThreads];
+    Simplex& S = s_simplex[threadIdx.x];
     int iters = 0;
     v3 dir;
     // a seeded run gets kSeedMaxIt support evaluations to certify separation;
@@ -812,7 +820,7 @@ __global__ void __launch_bounds__(kHullThreads, MINB) hull_gjk_kernel(HullBuffer
         at = {{vneg(P.off), vneg(P.off), vneg(P.off)}, {kGjkMaxIt, kGjkMaxIt, kGjkMaxIt}, 1};
     }
     int which = 0;
-    const int st = gjk_attempts(P, at, &S, &iters, &dir, &which);
+    const int st = gjk_attempts(P, at, &S, &iters, &dir, &which, s_seen + threadIdx.x, kHullThreads);
     const bool certified_by_anchor = learned && which == 0;
     const bool anchor_failed = learned && which > 0;
     // final direction in A's frame (seed of the next step); with learned
