@@ -501,7 +501,8 @@ sd_status sd_engine_load_checkpoint(sd_engine* h, const char* path);
  *                   within r_i + r_j + skin; other steps test only the listed neighbours.
  *                   Same contact set and order as the scan, so the same bits
  *   "listed_blocks" resident 256-thread blocks per SM the contact-list kernel is compiled
- *                   for: 4 (64 registers) or 5 (48 registers, the default)
+ *                   for: 4 (64 registers) or 5 (48 registers, the default); single scenes
+ *                   without clumps or meshes also 6 (40) or 8 (32 registers, more spills)
  *   "contact_block" threads per block of the per-sphere contact kernels: 64, 128 or 256
  *                   (default)
  *   "fix_blocks"    blocks per SM of the in-place reorder's fixed grid: 2, 4 or 8 (default)

@@ -26,7 +26,7 @@ import math
 
 from . import _abi
 
-SCENE_KNOBS = {"skin_um": (0, 20, 50, 100, 200), "listed_blocks": (4, 5), "contact_block": (128, 256),
+SCENE_KNOBS = {"skin_um": (0, 20, 50, 100, 200), "listed_blocks": (4, 5, 6), "contact_block": (128, 256),
                "contact_mode": (0, 1), "sort_items": (8, 16), "resort_max": (256, 1024), "fix_blocks": (4, 8)}
 BATCH_KNOBS = {"skin_um": (0, 20, 50, 100), "listed_blocks": (4, 5), "contact_block": (128, 256),
                "pair_lists": (0, 2), "sort_items": (8, 16), "resort_max": (256, 1024), "fix_blocks": (4, 8)}

@@ -887,7 +887,7 @@ dem_contact_integrate_kernel(DemParams p, uint32_t n, const float4* __restrict__
 // at a build.  Its own kernel so that the registers are capped for the
 // listed steps' occupancy (they are bound by load latency): MINB resident
 // blocks of 256 per SM (4: 64 registers; 5: 48, with spills in the build
-// scan; knob "listed_blocks", default 5).  It never builds radix histograms (the lists
+// scan; 6: 40; 8: 32; knob "listed_blocks", default 5).  It never builds radix histograms (the lists
 // run only with the incremental re-sort).
 template <bool RECORD, int MINB, bool BATCHED, bool CLUMPS = false, bool MESH = false>
 __global__ void __launch_bounds__(256, MINB)
@@ -1825,7 +1825,7 @@ int dem_fix_blocks() { return g_fix_blocks; }
 // (48 registers, spills only in the build scan) measured 0.0632 ms per
 // step at 1,048,576 spheres against 0.0668 ms with four (64 registers)
 static int g_listed_blocks = 5;
-void dem_set_listed_blocks(int b) { g_listed_blocks = b == 5 ? 5 : 4; }
+void dem_set_listed_blocks(int b) { g_listed_blocks = (b == 5 || b == 6 || b == 8) ? b : 4; }
 int dem_listed_blocks() { return g_listed_blocks; }
 int dem_pair_lists() { return g_pair_lists; }
 
@@ -1869,6 +1869,14 @@ static void launch_contact_t(const DemParams& p, DemBuffers& b, uint32_t spec, u
             dem_contact_listed_kernel<RECORD, 5, false, false, true><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
                 b.dev_status, sk, ms, Batch{}, ClumpCtx{}, b.mesh);
+        } else if (g_listed_blocks == 6) {
+            dem_contact_listed_kernel<RECORD, 6, false><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{});
+        } else if (g_listed_blocks == 8) {
+            dem_contact_listed_kernel<RECORD, 8, false><<<grid, cb, 0, st>>>(
+                p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,
+                b.dev_status, sk, ms, Batch{});
         } else if (g_listed_blocks == 5) {
             dem_contact_listed_kernel<RECORD, 5, false><<<grid, cb, 0, st>>>(
                 p, b.n, b.pos, b.vel, b.omg, b.cell_start, b.pos_n, b.vel_n, b.omg_n, b.keys, vals, f, t,

@@ -1401,7 +1401,8 @@ sd_status sd_tune_set(const char* knob, int32_t value) {
         if (value != 2 && value != 4 && value != 8) return fail(nullptr, SD_ERR_INVALID_ARG, "fix_blocks must be 2, 4 or 8");
         sd::dem_set_fix_blocks(value);
     } else if (k == "listed_blocks") {
-        if (value != 4 && value != 5) return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4 or 5");
+        if (value != 4 && value != 5 && value != 6 && value != 8)
+            return fail(nullptr, SD_ERR_INVALID_ARG, "listed_blocks must be 4, 5, 6 or 8");
         sd::dem_set_listed_blocks(value);
     } else if (k == "lbvh_rebuild") {
         if (value < 1 || value > 4096) return fail(nullptr, SD_ERR_INVALID_ARG, "lbvh_rebuild must be in [1, 4096]");

@@ -376,3 +376,18 @@ def test_lbvh_rebuild_knob(sdlib):
                 _abi.tune_set("lbvh_rebuild", v)
     finally:
         _abi.tune_set("lbvh_rebuild", old)
+
+
+def test_listed_blocks_knob(sdlib):
+    from stardust_gb300 import _abi
+    old = _abi.tune_get("listed_blocks")
+    assert old == 5
+    try:
+        for v in (4, 5, 6, 8):
+            _abi.tune_set("listed_blocks", v)
+            assert _abi.tune_get("listed_blocks") == v
+        for v in (0, 3, 7, 9):
+            with pytest.raises(Exception):
+                _abi.tune_set("listed_blocks", v)
+    finally:
+        _abi.tune_set("listed_blocks", old)

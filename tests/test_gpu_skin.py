@@ -24,13 +24,18 @@ def scene(n, inflate, speed, seed):
     return pos, vel, cfg, dt
 
 
-@pytest.mark.parametrize("skin_um,inflate,speed", [(50, 1.0, 2.0), (1000, 1.0, 0.5), (200, 1.3, 5.0),
-                                                   (2000, 1.8, 1.0), (20, 1.2, 20.0)])
-def test_skin_lists_bit_exact(sdlib, orc, skin_um, inflate, speed):
+@pytest.mark.parametrize("skin_um,inflate,speed,blocks", [(50, 1.0, 2.0, 5), (1000, 1.0, 0.5, 5), (200, 1.3, 5.0, 5),
+                                                          (2000, 1.8, 1.0, 5), (20, 1.2, 20.0, 5), (200, 1.3, 5.0, 4),
+                                                          (200, 1.3, 5.0, 6), (200, 1.3, 5.0, 8)])
+def test_skin_lists_bit_exact(sdlib, orc, skin_um, inflate, speed, blocks):
+    """Contact lists against the oracle, over skins, speeds and the list
+    kernel's register budgets (knob listed_blocks)."""
     from stardust_gb300 import _abi
     old = _abi.tune_get("skin_um")
+    old_blocks = _abi.tune_get("listed_blocks")
     try:
         _abi.tune_set("skin_um", skin_um)
+        _abi.tune_set("listed_blocks", blocks)
         n = 20_000
         pos, vel, cfg, dt = scene(n, inflate, speed, seed=skin_um)
         eng = sdlib.DEMEngine(cfg)
@@ -54,6 +59,7 @@ def test_skin_lists_bit_exact(sdlib, orc, skin_um, inflate, speed):
         eng.close()
     finally:
         _abi.tune_set("skin_um", old)
+        _abi.tune_set("listed_blocks", old_blocks)
 
 
 def test_skin_lists_after_set_state(sdlib):
