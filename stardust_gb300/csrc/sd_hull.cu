@@ -1034,13 +1034,14 @@ __global__ void hull_teach_flags_kernel(const float4* __restrict__ teach, const 
 
 __global__ void hull_teach_gather_kernel(const float* __restrict__ feat, const float4* __restrict__ teach,
                                          const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos,
-                                         uint32_t cap, float* __restrict__ feat_c, float4* __restrict__ teach_c,
-                                         uint32_t* __restrict__ d_total) {
+                                         uint32_t cap, uint32_t rows_cap, float* __restrict__ feat_c,
+                                         float4* __restrict__ teach_c, uint32_t* __restrict__ d_total) {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= cap) return;
-    if (e == cap - 1) *d_total = pos[e] + flags[e];
+    if (e == cap - 1) *d_total = min(pos[e] + flags[e], rows_cap);
     if (!flags[e]) return;
     const uint32_t r = pos[e];
+    if (r >= rows_cap) return;  // one sample per unique pair fits; inconsistent lists could exceed it
     const float4* src = reinterpret_cast<const float4*>(feat + 16 * (size_t)e);
     float4* dst = reinterpret_cast<float4*>(feat_c + 16 * (size_t)r);
 #pragma unroll
@@ -1060,8 +1061,8 @@ cudaError_t hull_teach_compact_async(const HullBuffers& H, const uint32_t* d_cou
     hull_teach_flags_kernel<<<grid_for(cap, 256), 256, 0, st>>>(H.teach, d_count, cap, flags);
     cudaError_t e = scan_exclusive_async(flags, pos, cap, scan, st);
     if (e != cudaSuccess) return e;
-    hull_teach_gather_kernel<<<grid_for(cap, 256), 256, 0, st>>>(H.feat, H.teach, flags, pos, cap, feat_c, teach_c,
-                                                                 d_total);
+    hull_teach_gather_kernel<<<grid_for(cap, 256), 256, 0, st>>>(H.feat, H.teach, flags, pos, cap, cap / 2 + 1,
+                                                                 feat_c, teach_c, d_total);
     return cudaGetLastError();
 }
 

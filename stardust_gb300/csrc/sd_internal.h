@@ -175,8 +175,8 @@ void hull_set_blocks(int b);
 int hull_blocks();
 // The training samples of a step (teach[e].w == 1 among the d_count[0]
 // entries), gathered in entry order into feat_c (16 floats per row) and
-// teach_c; *d_total = their number.  flags and pos hold cap words, scan the
-// scan scratch of cap words.
+// teach_c (cap / 2 + 1 rows each); *d_total = their number.  flags and pos
+// hold cap words, scan the scan scratch of cap words.
 cudaError_t hull_teach_compact_async(const HullBuffers& H, const uint32_t* d_count, float* feat_c, float4* teach_c,
                                      uint32_t* flags, uint32_t* pos, uint32_t* scan, uint32_t* d_total,
                                      cudaStream_t st);
