@@ -72,22 +72,29 @@ def _time(eng, dt: float, reps: int, stream, flush, stat: str = "median") -> flo
 
 
 def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, rounds: int = 2,
-                flush_bytes: int = 256 << 20, label: str | None = None, stat: str = "median") -> dict:
+                flush_bytes: int = 256 << 20, label: str | None = None, stat: str = "median",
+                timer=None) -> dict:
     """Coordinate descent over `knobs` (default: the bucket kind's set) on
     the live engine; sets the best and records it for the engine's bucket
     (or under `label`, for a regime of one bucket tuned apart, e.g. a dense
     bed).  Each setting is timed over `reps` steps by their median, or by
     their mean (stat "mean": for scenes whose contact-list builds recur
     within a few steps, e.g. a turning drum, so that the builds count).
-    Returns {"bucket", "choice", "ms", "table"}: every timed setting."""
-    import torch
-
+    `timer` (tests): a function of no arguments that times the current
+    settings in its place.  Returns {"bucket", "choice", "ms", "table"}:
+    every timed setting."""
     bucket = label or bucket_of(eng)
     if knobs is None:
         knobs = BATCH_KNOBS if bucket.startswith("batch") else SCENE_KNOBS
-    dev = torch.device("cuda", torch.cuda.current_device())
-    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
-    flush = torch.empty(flush_bytes, dtype=torch.uint8, device=dev)
+    if timer is None:
+        import torch
+
+        dev = torch.device("cuda", torch.cuda.current_device())
+        stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+        flush = torch.empty(flush_bytes, dtype=torch.uint8, device=dev)
+
+        def timer():
+            return _time(eng, dt, reps, stream, flush, stat)
     cur = {k: _abi.tune_get(k) for k in knobs}
     seen: dict[tuple, float] = {}
     table = []
@@ -97,7 +104,7 @@ def tune_engine(eng, dt: float, reps: int = 5, knobs: dict | None = None, rounds
         if key not in seen:
             for k, v in c.items():
                 _abi.tune_set(k, v)
-            seen[key] = _time(eng, dt, reps, stream, flush, stat)
+            seen[key] = timer()
             table.append({"knobs": dict(c), f"ms_{stat}": seen[key]})
         return seen[key]
 

@@ -61,3 +61,39 @@ def test_table_round_trip(tmp_path, sdlib):
         for k, v in old.items():
             _abi.tune_set(k, v)
         autotune._TABLE.clear()
+
+
+def test_coordinate_descent_finds_the_best_setting(sdlib):
+    """The search on a stand-in timer (a cost of the current knobs): it
+    reaches the best combination, skips equivalent settings, records every
+    timed setting under the statistic's name, sets the choice and keeps it
+    for the bucket or label."""
+    from stardust_gb300 import _abi, autotune
+
+    class Eng(FakeEngine):
+        def step(self, dt, k):
+            pass
+
+        def sync(self):
+            pass
+
+    knobs = {"skin_um": (0, 20, 50, 100), "listed_blocks": (4, 5, 6)}
+    best = {"skin_um": 50, "listed_blocks": 6}
+
+    def cost():
+        c = {k: _abi.tune_get(k) for k in knobs}
+        return 1.0 + sum(abs(c[k] - best[k]) for k in knobs) / 100.0
+
+    old = {k: _abi.tune_get(k) for k in knobs}
+    try:
+        r = autotune.tune_engine(Eng(1 << 20), 1e-5, knobs=knobs, label="test:cost", stat="mean", timer=cost)
+        assert r["choice"] == best and r["ms"] == 1.0
+        assert {k: _abi.tune_get(k) for k in knobs} == best
+        assert autotune.table()["test:cost"] == best
+        assert all("ms_mean" in t for t in r["table"])
+        # skin 0 takes no list kernel: its register budget is not timed apart
+        assert not any(t["knobs"]["skin_um"] == 0 and t["knobs"]["listed_blocks"] != 5 for t in r["table"])
+    finally:
+        for k, v in old.items():
+            _abi.tune_set(k, v)
+        autotune._TABLE.pop("test:cost", None)
